@@ -1,0 +1,325 @@
+#!/usr/bin/env python
+"""Benchmark: MH chain-steps/s and point-evals/s of the sampler on one GB300.
+
+Workload (default "plain-mh-131k"): 131072 chains, PROGRAM_LENGTH 63 (max
+postfix length 64), ops {+,-,*,/,exp,log,pow,x,const}, Gaussian random-walk
+constant proposals sd 0.1, 250 float32 points of y = b1*exp(-b2*x)+b3 with
+x ~ U[0,50] and noise N(0, 0.05 std(y)); blocks of 1000 MH steps, chains more
+than 20 log-units below the block's MAP re-drawn from the prior between
+blocks.  One bench "step" = one block (1000 MH steps of every chain).
+
+value     : chain-steps/s of the device-resident block loop (kernel time from
+            CUDA events on the library's stream, L2 flushed between blocks).
+e2e       : the same through the C ABI with host buffers: each block uploads
+            the state from pinned memory, runs, downloads state and scores,
+            and re-draws chains on the host (the reference's loop,
+            main.cu:1156-1239).
+cpu_baseline / --impl reference : the reference's own per-chain code
+            (main.cu:679-813) compiled for the host cores, OpenMP over chains,
+            on a bounded sample of the same chains.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from tests import helpers as H  # noqa: E402  (seeded synthetic inputs)
+
+WORKLOADS = {
+    "plain-mh-131k": dict(N=131072, PL=63, nd=250, data="expdecay", ops="basic", rw_sd=0.1,
+                          mh_steps=1000, map_delta=20.0, blocks=20),
+    "plain-mh-1k": dict(N=1024, PL=31, nd=101, data="quad", ops="basic", rw_sd=0.1,
+                        mh_steps=1000, map_delta=20.0, blocks=10),
+}
+METRIC = "MH chain-steps/s & point-evals/s (1 GB300); ESS/s gradient vs random-walk MH"
+
+
+def dataset(w):
+    if w["data"] == "expdecay":
+        return H.expdecay_data(w["nd"], seed=2024)
+    return H.quad_data(w["nd"], seed=2024)
+
+
+def initial_state(w, seed=99):
+    ops = H.OPSET_BASIC if w["ops"] == "basic" else None
+    return H.random_programs(w["N"], w["PL"], ops=ops, seed=seed, shallow_frac=0.0)
+
+
+def resample_host(P, C, prior, lik, delta, ops, rng):
+    """Re-draw chains whose posterior is below max - delta from the prior-draw
+    distribution of the reference's initialisation (main.cu:1133-1137)."""
+    post = prior + lik
+    fin = np.isfinite(post)
+    if not fin.any():
+        return 0
+    cut = post[fin].max() - delta
+    bad = np.where(post < cut)[0]
+    if bad.size:
+        opsa = np.asarray(ops)
+        P[:, bad] = opsa[rng.integers(0, len(opsa) - 1, size=(P.shape[0], bad.size))]
+        C[:, bad] = (10.0 ** rng.integers(-4, 4, size=(P.shape[0], bad.size)) *
+                     rng.normal(size=(P.shape[0], bad.size))).astype(np.float32)
+    return bad.size
+
+
+class ClockSampler:
+    def __init__(self, path):
+        self.path = path
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self, device_index=0):
+        try:
+            rows = [r.split(", ") for r in open(self.path).read().strip().splitlines()]
+        except OSError:
+            return None
+        rows = [r for r in rows if len(r) >= 9 and r[0].strip() == str(device_index)]
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for n, v in zip(names, r[5:9]):
+                if v.strip() == "Active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(rows[0][2]),
+                "samples": len(rows), "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return {}
+
+
+def cpu_reference_rate(w, P, C, x, y, sd, target_s=12.0, threads=0, chains=None):
+    """chain-steps/s of the reference's own code on the host cores, measured on
+    chains [0, S) of the given state, S sized to about target_s seconds."""
+    from oracle import ref as oref
+    o = oref.get(pl=w["PL"], opset=1 if w["ops"] == "basic" else 0, project_math=0,
+                 rw_sd=w["rw_sd"])
+    ncores = threads or os.cpu_count()
+    steps = w["mh_steps"]
+    if chains is None:
+        S = min(w["N"], 4 * ncores)
+        Ps, Cs = np.ascontiguousarray(P[:, :S]), np.ascontiguousarray(C[:, :S])
+        t0 = time.perf_counter()
+        o.run_kernel(Ps, Cs, x, y, sd, steps, 12345, nthreads=ncores)
+        dt = max(time.perf_counter() - t0, 1e-3)
+        chains = int(min(w["N"], max(S, S * target_s / dt)))
+    Ps, Cs = np.ascontiguousarray(P[:, :chains]), np.ascontiguousarray(C[:, :chains])
+    t0 = time.perf_counter()
+    o.run_kernel(Ps, Cs, x, y, sd, steps, 12345, nthreads=ncores)
+    dt = time.perf_counter() - t0
+    return chains * steps / dt, ncores, chains, dt
+
+
+def run_reference(args, w):
+    """--impl reference: the reference's CPU code on a bounded sample per step."""
+    x, y, sd = dataset(w)
+    P, C = initial_state(w)
+    ncores = os.cpu_count()
+    rates = []
+    chains = None
+    for i in range(args.warmup + args.steps):
+        rate, cores, chains, dt = cpu_reference_rate(w, P, C, x, y, sd, chains=chains)
+        if i >= args.warmup:
+            rates.append(rate)
+    value = float(np.mean(rates))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "chain-steps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * w["N"] * w["mh_steps"] / value,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)",
+        "point_evals_per_s": value * w["nd"],
+        "config": {"workload": args.workload, **{k: w[k] for k in ("N", "PL", "nd", "mh_steps")}},
+        "cpu_baseline": {"value": value, "unit": "chain-steps/s", "cores": ncores, "kind": "reference",
+                         "sample": "%d chains x %d MH steps per step, from the seeded initial state"
+                                   % (chains, w["mh_steps"])},
+        "e2e": {"value": value, "unit": "chain-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_gpu(args, w):
+    import torch
+    import gpuropolis_gb300 as g
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+
+    x, y, sd = dataset(w)
+    P0, C0 = initial_state(w, seed=99 + rank)
+    ops = H.OPSET_BASIC if w["ops"] == "basic" else list(range(27))
+    s = g.Sampler(w["N"], program_length=w["PL"], ops=ops, rng=g.RNG_LCG,
+                  const_proposal=g.CONST_RANDOM_WALK, rw_sd=w["rw_sd"], device=local,
+                  stream=stream.cuda_stream)
+    s.set_data(x, y, sd)
+    s.set_state(P0, C0)
+    hostrng = np.random.default_rng(7 + rank)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def block(i):
+        s.run_block(w["mh_steps"], 1000003 * (i + 1) + rank)
+
+    def resample():
+        P, C, prior, lik = s.get_state()
+        resample_host(P, C, prior, lik, w["map_delta"], ops, hostrng)
+        s.set_state(P, C)
+
+    # warm-up blocks (untimed)
+    for i in range(args.warmup):
+        block(i)
+        resample()
+    torch.cuda.synchronize()
+    s.reset_stats()
+    launches0 = s.launch_count()
+
+    # device-resident timed loop: per block CUDA events around the kernel
+    evs = []
+    clk = ClockSampler(os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")
+                       if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp/gpr_clocks.csv")
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with clk:
+        for i in range(args.steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            block(args.warmup + i)
+            e1.record(stream)
+            evs.append((e0, e1))
+            resample()   # state stays resident; the re-draw is outside the events
+        torch.cuda.synchronize()
+    kernel_ms = float(sum(a.elapsed_time(b) for a, b in evs))
+    launches = s.launch_count() - launches0
+    st = s.stats()
+    if world > 1:
+        t = torch.tensor([kernel_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        kernel_ms = float(t.item())
+    chain_steps = w["N"] * w["mh_steps"] * args.steps
+    value = world * chain_steps / (kernel_ms / 1e3)
+
+    # end-to-end through the C ABI with pinned host buffers
+    Ph = torch.empty((w["PL"], w["N"]), dtype=torch.int32, pin_memory=True).numpy()
+    Ch = torch.empty((w["PL"], w["N"]), dtype=torch.float32, pin_memory=True).numpy()
+    prh = torch.empty(w["N"], dtype=torch.float64, pin_memory=True).numpy()
+    lih = torch.empty(w["N"], dtype=torch.float64, pin_memory=True).numpy()
+    lib = s.lib
+    ptr = lambda a: a.ctypes.data_as(g.ctypes.c_void_p)  # noqa: E731
+    lib.gpr_get_state(s.h, ptr(Ph), ptr(Ch), ptr(prh), ptr(lih))
+    e2e_blocks = max(1, min(args.steps, 5))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(e2e_blocks):
+        lib.gpr_set_state(s.h, ptr(Ph), ptr(Ch))
+        lib.gpr_run_block(s.h, w["mh_steps"], 7919 * (i + 1))
+        lib.gpr_get_state(s.h, ptr(Ph), ptr(Ch), ptr(prh), ptr(lih))
+        resample_host(Ph, Ch, prh, lih, w["map_delta"], ops, hostrng)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = world * w["N"] * w["mh_steps"] * e2e_blocks / e2e_s
+    h2d = Ph.nbytes + Ch.nbytes
+    d2h = Ph.nbytes + Ch.nbytes + prh.nbytes + lih.nbytes
+
+    if rank != 0:
+        return
+    peaks = measured_peaks()
+    clocks = clk.summary(local)
+    sm_mhz = (clocks or {}).get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+    # FP32 issue roofline: 152 SMs x 128 FP32 lanes per clock, one op per lane
+    props = torch.cuda.get_device_properties(dev)
+    nsm = props.multi_processor_count
+    peak_tops = nsm * 128 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+    alg_ops = st["eval_node_points"]
+    achieved_tops = alg_ops / (kernel_ms / 1e3) / 1e12
+    geo = s.launch_geometry()
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        Pw, Cw, _, _ = s.get_state()
+        rate, cores, chains, dt = cpu_reference_rate(w, Pw, Cw, x, y, sd)
+        cpu = {"value": rate, "unit": "chain-steps/s", "cores": cores, "kind": "reference",
+               "sample": "%d chains x %d MH steps of the warmed-up state (%.1f s)"
+                         % (chains, w["mh_steps"], dt)}
+    line = {
+        "metric": METRIC, "value": value, "unit": "chain-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": kernel_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)",
+        "point_evals_per_s": value * w["nd"],
+        "config": {"workload": args.workload, **{k: w[k] for k in ("N", "PL", "nd", "mh_steps", "map_delta")},
+                   "ops": w["ops"], "const_proposal": "rw:%g" % w["rw_sd"], "rng": "lcg",
+                   "l2": "flushed between blocks (256 MB write)", "parallelism": "replicas" if world > 1 else "1 GPU",
+                   "launch": geo},
+        "e2e": {"value": e2e_value, "unit": "chain-steps/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "blocks": e2e_blocks},
+        "gpu_launches": launches,
+        "roofline": {"bound": "fp32-issue", "achieved": achieved_tops, "peak": peak_tops,
+                     "unit": "T-ops/s", "frac": achieved_tops / peak_tops, "traffic": None,
+                     "note": "algorithmic FP32 ops = (node count + 4) per point evaluated; peak = "
+                             "SMs x 128 lanes x max SM clock (nominal, no measured FP32 peak)"},
+        "stats": st,
+        "acceptance": {"structure": st["struct_accepted"] / max(1, st["struct_proposed"]),
+                       "constant": st["const_accepted"] / max(1, st["const_proposed"])},
+        "clocks": clocks,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="plain-mh-131k", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    w = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        if int(os.environ.get("RANK", "0")) != 0:
+            return
+        run_reference(args, w)
+    else:
+        run_gpu(args, w)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,424 @@
+/*
+ * gpr_capi.cu -- the C ABI of include/gpuropolis.h: handle lifetime, device
+ * state, dataset upload, launch geometry, error reporting.
+ *
+ * It owns what the reference's main() does around its kernel launch: the
+ * device allocations and copies of P, C, D, prior, likelihood
+ * (main.cu:1123-1147, 1163-1167, 1233-1234) and the launch itself
+ * (main.cu:1160).  Nothing here calls exit(); every failure becomes a status
+ * code and a message (the reference prints and continues, main.cu:162-168).
+ */
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <string>
+#include <vector>
+
+#include "../../include/gpuropolis.h"
+#include "gpr_common.h"
+#include "gpr_kernels.cuh"
+#include "gpr_rngmath.h"
+
+#define GPR_VERSION_STRING "gpuropolis-gb300 0.1 (sm_103a)"
+
+struct gpr_handle {
+    gpr_config cfg;
+    int N = 0;
+    int PL = 0;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int num_sms = 0;
+
+    int32_t* dP = nullptr;
+    float* dC = nullptr;
+    double* dprior = nullptr;
+    double* dlik = nullptr;
+    float* dlogcount = nullptr;
+    int* dcounter = nullptr;   /* [0] next chain, [1] error flags */
+    unsigned long long* dstats = nullptr;
+    float* ddata = nullptr;    /* x | y | w | sd, each nd_pad floats */
+    int nd = -1;
+    int nd_pad = 0;
+    double normsum = 0.0;
+
+    gpr::KParams kp;
+    gpr::LaunchCfg lc;
+    int64_t launches = 0;
+    std::string err;
+};
+
+static std::string g_create_error;
+
+static int fail(gpr_handle* h, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (h) h->err = buf; else g_create_error = buf;
+    return code;
+}
+
+#define CUDA_TRY(h, call)                                                                     \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess)                                                                \
+            return fail((h), GPR_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));  \
+    } while (0)
+
+static gpr::Magic magic_for(uint32_t d) {
+    int l = 0;
+    while ((1ull << l) < (unsigned long long)d) ++l;
+    unsigned long long m = ((1ull << (31 + l)) + d - 1) / d;
+    gpr::Magic r;
+    r.m = (uint32_t)m;
+    r.s = (uint32_t)(31 + l);
+    return r;
+}
+
+/* divisor of random_int(n), main.cu:220 */
+static uint32_t divisor_for(int n) { return (uint32_t)(2147483647 / (n + 1)); }
+
+extern "C" {
+
+void gpr_default_config(gpr_config* cfg) {
+    if (!cfg) return;
+    memset(cfg, 0, sizeof *cfg);
+    cfg->program_length = 31;           /* PROGRAM_LENGTH, main.cu:26 */
+    cfg->n_ops = OP_NREF;               /* NOPS, main.cu:53 */
+    for (int i = 0; i < OP_NREF; ++i) cfg->ops[i] = i;
+    cfg->rng = GPR_RNG_LCG;
+    cfg->const_proposal = GPR_CONST_REFERENCE;
+    cfg->rw_sd = 0.1f;
+    cfg->device = 0;
+    cfg->stream = nullptr;
+}
+
+const char* gpr_version(void) { return GPR_VERSION_STRING; }
+
+const char* gpr_last_error(gpr_handle* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+int64_t gpr_launch_count(gpr_handle* h) { return h ? h->launches : 0; }
+
+static void free_all(gpr_handle* h) {
+    cudaFree(h->dP); cudaFree(h->dC); cudaFree(h->dprior); cudaFree(h->dlik);
+    cudaFree(h->dlogcount); cudaFree(h->dcounter); cudaFree(h->ddata); cudaFree(h->dstats);
+    if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+}
+
+int gpr_create(const gpr_config* cfg, int n_chains, gpr_handle** out) {
+    if (!out) return fail(nullptr, GPR_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    if (!cfg) return fail(nullptr, GPR_ERR_ARG, "cfg is NULL");
+    if (n_chains <= 0) return fail(nullptr, GPR_ERR_ARG, "n_chains must be > 0 (got %d)", n_chains);
+    const int PL = cfg->program_length;
+    if (PL < 1 || PL > GPR_MAX_PROGRAM_LENGTH || (PL % 2) == 0)
+        return fail(nullptr, GPR_ERR_ARG, "program_length must be odd and in [1, %d] (got %d)",
+                    GPR_MAX_PROGRAM_LENGTH, PL);
+    if (cfg->n_ops < 1 || cfg->n_ops > GPR_MAX_OPS)
+        return fail(nullptr, GPR_ERR_ARG, "n_ops must be in [1, %d] (got %d)", GPR_MAX_OPS, cfg->n_ops);
+    for (int i = 0; i < cfg->n_ops; ++i)
+        if (cfg->ops[i] < 0 || cfg->ops[i] >= OP_NREF)
+            return fail(nullptr, GPR_ERR_ARG, "ops[%d] = %d is not an op code", i, cfg->ops[i]);
+    if (cfg->rng != GPR_RNG_LCG && cfg->rng != GPR_RNG_PHILOX)
+        return fail(nullptr, GPR_ERR_ARG, "unknown rng mode %d", cfg->rng);
+    if (cfg->const_proposal != GPR_CONST_REFERENCE && cfg->const_proposal != GPR_CONST_RANDOM_WALK)
+        return fail(nullptr, GPR_ERR_ARG, "unknown constant proposal %d", cfg->const_proposal);
+    if ((long long)n_chains * PL > (1ll << 31) - 1)
+        return fail(nullptr, GPR_ERR_ARG, "n_chains * program_length exceeds 2^31-1");
+
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess) return fail(nullptr, GPR_ERR_CUDA, "cudaGetDeviceCount: %s", cudaGetErrorString(e));
+    if (cfg->device < 0 || cfg->device >= ndev)
+        return fail(nullptr, GPR_ERR_ARG, "invalid GPU device %d (%d present)", cfg->device, ndev);
+
+    gpr_handle* h = new gpr_handle();
+    h->cfg = *cfg;
+    h->N = n_chains;
+    h->PL = PL;
+    h->device = cfg->device;
+    auto bail = [&](int code) { free_all(h); std::string m = h->err; delete h; g_create_error = m; return code; };
+#define CREATE_TRY(call)                                                                       \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess) {                                                               \
+            fail(h, GPR_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));            \
+            return bail(GPR_ERR_CUDA);                                                         \
+        }                                                                                      \
+    } while (0)
+    CREATE_TRY(cudaSetDevice(h->device));
+    CREATE_TRY(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device));
+    if (cfg->stream) {
+        h->stream = (cudaStream_t)cfg->stream;
+    } else {
+        CREATE_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+        h->own_stream = true;
+    }
+    const size_t n = (size_t)n_chains;
+    CREATE_TRY(cudaMalloc(&h->dP, n * PL * sizeof(int32_t)));
+    CREATE_TRY(cudaMalloc(&h->dC, n * PL * sizeof(float)));
+    CREATE_TRY(cudaMalloc(&h->dprior, n * sizeof(double)));
+    CREATE_TRY(cudaMalloc(&h->dlik, n * sizeof(double)));
+    CREATE_TRY(cudaMalloc(&h->dlogcount, (PL + 2) * sizeof(float)));
+    CREATE_TRY(cudaMalloc(&h->dcounter, 2 * sizeof(int)));
+    CREATE_TRY(cudaMalloc(&h->dstats, GPR_NSTATS * sizeof(unsigned long long)));
+    CREATE_TRY(cudaMemsetAsync(h->dstats, 0, GPR_NSTATS * sizeof(unsigned long long), h->stream));
+    CREATE_TRY(cudaMemsetAsync(h->dP, 0, n * PL * sizeof(int32_t), h->stream));
+    CREATE_TRY(cudaMemsetAsync(h->dC, 0, n * PL * sizeof(float), h->stream));
+    CREATE_TRY(cudaMemsetAsync(h->dprior, 0, n * sizeof(double), h->stream));
+    CREATE_TRY(cudaMemsetAsync(h->dlik, 0, n * sizeof(double), h->stream));
+    CREATE_TRY(cudaMemsetAsync(h->dcounter, 0, 2 * sizeof(int), h->stream));
+
+    /* Hastings term table: logf((float)k) (main.cu:702,723) */
+    std::vector<float> lc(PL + 2);
+    for (int k = 0; k < PL + 2; ++k) lc[k] = logf((float)k);
+    CREATE_TRY(cudaMemcpyAsync(h->dlogcount, lc.data(), lc.size() * sizeof(float),
+                               cudaMemcpyHostToDevice, h->stream));
+    CREATE_TRY(cudaStreamSynchronize(h->stream));
+
+    gpr::KParams& kp = h->kp;
+    memset(&kp, 0, sizeof kp);
+    kp.P = h->dP; kp.C = h->dC; kp.prior = h->dprior; kp.lik = h->dlik;
+    kp.N = n_chains; kp.PL = PL;
+    kp.rng_mode = cfg->rng;
+    kp.const_mode = cfg->const_proposal;
+    kp.rw_sd = cfg->rw_sd;
+    kp.nops = cfg->n_ops;
+    for (int i = 0; i < cfg->n_ops; ++i) kp.opmap[i] = (int8_t)cfg->ops[i];
+    kp.mag_pl = magic_for(divisor_for(PL));
+    kp.mag_nops = magic_for(divisor_for(cfg->n_ops));
+    kp.mag_1e6 = magic_for(divisor_for(1000000));
+    kp.log_nops1 = log((double)cfg->n_ops + 1);                  /* main.cu:536 */
+    const double PIf = 3.141592653589;                             /* main.cu:194 */
+    kp.lpi_f = logf((float)PIf);                                   /* main.cu:304 */
+    kp.lnorm1_f = (float)(0.5 * ((double)logf((float)(2.0 * PIf)) + 2.0 * (double)logf(1.0f)));
+    const float R = 0.1f, PI_INT = 0.15f;                          /* main.cu:32,34 */
+    kp.logf_r = logf(R);
+    kp.log1mr_f = (float)log(1.0 - (double)R);
+    kp.log2_f = (float)log(2.0);
+    kp.logpi_f = (float)log((double)PI_INT);
+    kp.log1mpi_f = (float)log(1.0 - (double)PI_INT);
+    kp.geom_logr = gpr_rng_logf(R);
+    kp.logcount = h->dlogcount;
+    kp.next_chain = h->dcounter;
+    kp.err = h->dcounter + 1;
+    kp.stats = h->dstats;
+    kp.max_instr = GPR_MAX_INSTR(PL);
+    int lev = 1;
+    while ((1 << lev) <= PL) ++lev;   /* heap levels: pending pushes never exceed this */
+    kp.levels = lev;
+    gpr::fill_lcg_jump_table(kp);
+    *out = h;
+    return GPR_OK;
+#undef CREATE_TRY
+}
+
+int gpr_destroy(gpr_handle* h) {
+    if (!h) return GPR_OK;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    free_all(h);
+    delete h;
+    return GPR_OK;
+}
+
+static int choose_launch(gpr_handle* h) {
+    gpr::KParams& kp = h->kp;
+    gpr::LaunchCfg lc;
+    if (kp.nd <= 128) { lc.K = 4; lc.onepass = 1; }
+    else if (kp.nd <= 256) { lc.K = 8; lc.onepass = 1; }
+    else { lc.K = 8; lc.onepass = 0; }
+    int wpc = 8;
+    size_t smem = gpr::mh_smem_bytes(kp, lc.K, wpc);
+    while (smem > 227 * 1024 && wpc > 1) {
+        wpc /= 2;
+        smem = gpr::mh_smem_bytes(kp, lc.K, wpc);
+    }
+    if (smem > 227 * 1024)
+        return fail(h, GPR_ERR_ARG, "dataset of %d points does not fit in shared memory", kp.nd);
+    int per_sm = 0;
+    CUDA_TRY(h, gpr::mh_occupancy(kp, lc.K, lc.onepass, wpc, smem, &per_sm));
+    if (per_sm < 1) return fail(h, GPR_ERR_ARG, "kernel cannot be resident (smem %zu)", smem);
+    long long ctas = (long long)h->num_sms * per_sm;
+    long long need = (h->N + wpc - 1) / wpc;
+    if (ctas > need) ctas = need;
+    lc.warps_per_cta = wpc;
+    lc.ctas = (int)ctas;
+    lc.smem_bytes = smem;
+    h->lc = lc;
+    return GPR_OK;
+}
+
+int gpr_set_data(gpr_handle* h, const float* x, const float* y, const float* sd, int n) {
+    if (!h) return GPR_ERR_ARG;
+    if (n < 0) return fail(h, GPR_ERR_ARG, "n must be >= 0");
+    if (n > 0 && (!x || !y || !sd)) return fail(h, GPR_ERR_ARG, "x, y, sd must be non-NULL");
+    for (int i = 0; i < n; ++i)
+        if (!(sd[i] > 0.0f)) return fail(h, GPR_ERR_ARG, "sd[%d] = %g is not > 0", i, (double)sd[i]);
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    const int nd_pad = (n + 3) & ~3;
+    std::vector<float> host((size_t)4 * nd_pad, 0.0f);
+    double normsum = 0.0;
+    const double PIf = 3.141592653589;
+    for (int i = 0; i < n; ++i) {
+        host[i] = x[i];
+        host[nd_pad + i] = y[i];
+        double s = (double)sd[i];
+        host[2 * (size_t)nd_pad + i] = (float)(1.0 / (2.0 * s * s));
+        host[3 * (size_t)nd_pad + i] = sd[i];
+        /* the constant part of lnormalpdf (main.cu:300), per point */
+        normsum += 0.5 * ((double)logf((float)(2.0 * PIf)) + 2.0 * (double)logf(sd[i]));
+    }
+    if (h->ddata) { CUDA_TRY(h, cudaStreamSynchronize(h->stream)); cudaFree(h->ddata); h->ddata = nullptr; }
+    if (nd_pad > 0) {
+        CUDA_TRY(h, cudaMalloc(&h->ddata, host.size() * sizeof(float)));
+        CUDA_TRY(h, cudaMemcpyAsync(h->ddata, host.data(), host.size() * sizeof(float),
+                                    cudaMemcpyHostToDevice, h->stream));
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    }
+    h->nd = n;
+    h->nd_pad = nd_pad;
+    h->normsum = normsum;
+    gpr::KParams& kp = h->kp;
+    kp.nd = n; kp.nd_pad = nd_pad; kp.normsum = normsum;
+    kp.dx = h->ddata;
+    kp.dy = h->ddata ? h->ddata + nd_pad : nullptr;
+    kp.dw = h->ddata ? h->ddata + 2 * (size_t)nd_pad : nullptr;
+    kp.dsd = h->ddata ? h->ddata + 3 * (size_t)nd_pad : nullptr;
+    return choose_launch(h);
+}
+
+int gpr_set_state(gpr_handle* h, const int32_t* P, const float* C) {
+    if (!h) return GPR_ERR_ARG;
+    if (!P || !C) return fail(h, GPR_ERR_ARG, "P and C must be non-NULL");
+    const size_t cnt = (size_t)h->N * h->PL;
+    for (size_t i = 0; i < cnt; ++i)
+        if (P[i] < 0 || P[i] >= OP_NREF)
+            return fail(h, GPR_ERR_ARG, "P[%zu] = %d is not an op code", i, P[i]);
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    CUDA_TRY(h, cudaMemcpyAsync(h->dP, P, cnt * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(h->dC, C, cnt * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return GPR_OK;
+}
+
+int gpr_get_state(gpr_handle* h, int32_t* P, float* C, double* prior, double* likelihood) {
+    if (!h) return GPR_ERR_ARG;
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    const size_t cnt = (size_t)h->N * h->PL;
+    if (P) CUDA_TRY(h, cudaMemcpyAsync(P, h->dP, cnt * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+    if (C) CUDA_TRY(h, cudaMemcpyAsync(C, h->dC, cnt * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+    if (prior) CUDA_TRY(h, cudaMemcpyAsync(prior, h->dprior, h->N * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    if (likelihood)
+        CUDA_TRY(h, cudaMemcpyAsync(likelihood, h->dlik, h->N * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    return gpr_sync(h);
+}
+
+static int run(gpr_handle* h, int steps, int seed) {
+    if (h->nd < 0) return fail(h, GPR_ERR_STATE, "gpr_set_data has not been called");
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    h->kp.steps = steps;
+    h->kp.seed = (uint32_t)seed;
+    CUDA_TRY(h, cudaMemsetAsync(h->dcounter, 0, sizeof(int), h->stream));
+    CUDA_TRY(h, gpr::launch_mh_block(h->kp, h->lc, h->stream));
+    h->launches++;
+    return GPR_OK;
+}
+
+int gpr_run_block(gpr_handle* h, int steps, int random_seed) {
+    if (!h) return GPR_ERR_ARG;
+    if (steps < 0) return fail(h, GPR_ERR_ARG, "steps must be >= 0 (got %d)", steps);
+    return run(h, steps, random_seed);
+}
+
+int gpr_evaluate(gpr_handle* h) {
+    if (!h) return GPR_ERR_ARG;
+    return run(h, 0, 0);
+}
+
+int gpr_sync(gpr_handle* h) {
+    if (!h) return GPR_ERR_ARG;
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    int flags = 0;
+    CUDA_TRY(h, cudaMemcpy(&flags, h->dcounter + 1, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flags) {
+        cudaMemset(h->dcounter + 1, 0, sizeof(int));
+        return fail(h, GPR_ERR_DEVICE, "kernel error flags 0x%x (1: dataset staging timed out, "
+                    "2: constant-proposal offsets did not converge)", flags);
+    }
+    return GPR_OK;
+}
+
+int gpr_device_state(gpr_handle* h, int32_t** P, float** C, double** prior, double** likelihood) {
+    if (!h) return GPR_ERR_ARG;
+    if (P) *P = h->dP;
+    if (C) *C = h->dC;
+    if (prior) *prior = h->dprior;
+    if (likelihood) *likelihood = h->dlik;
+    return GPR_OK;
+}
+
+int gpr_debug_eval_values(gpr_handle* h, const float* xs, int nx, float* out, float* length,
+                          int* count) {
+    if (!h) return GPR_ERR_ARG;
+    if (nx < 0 || (nx > 0 && (!xs || !out)) || !length || !count)
+        return fail(h, GPR_ERR_ARG, "bad arguments");
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    float *dxs = nullptr, *dout = nullptr, *dlen = nullptr;
+    int* dcnt = nullptr;
+    const size_t no = (size_t)h->N * (size_t)nx;
+    int rc = GPR_OK;
+    cudaError_t e = cudaSuccess;
+    if ((e = cudaMalloc(&dxs, (nx + 1) * sizeof(float))) != cudaSuccess) goto done;
+    if ((e = cudaMalloc(&dout, (no + 1) * sizeof(float))) != cudaSuccess) goto done;
+    if ((e = cudaMalloc(&dlen, h->N * sizeof(float))) != cudaSuccess) goto done;
+    if ((e = cudaMalloc(&dcnt, h->N * sizeof(int))) != cudaSuccess) goto done;
+    if (nx > 0 && (e = cudaMemcpyAsync(dxs, xs, nx * sizeof(float), cudaMemcpyHostToDevice, h->stream)) != cudaSuccess) goto done;
+    if ((e = gpr::launch_eval_values(h->kp, dxs, nx, dout, dlen, dcnt, h->stream)) != cudaSuccess) goto done;
+    h->launches++;
+    if (nx > 0 && (e = cudaMemcpyAsync(out, dout, no * sizeof(float), cudaMemcpyDeviceToHost, h->stream)) != cudaSuccess) goto done;
+    if ((e = cudaMemcpyAsync(length, dlen, h->N * sizeof(float), cudaMemcpyDeviceToHost, h->stream)) != cudaSuccess) goto done;
+    if ((e = cudaMemcpyAsync(count, dcnt, h->N * sizeof(int), cudaMemcpyDeviceToHost, h->stream)) != cudaSuccess) goto done;
+    e = cudaStreamSynchronize(h->stream);
+done:
+    if (e != cudaSuccess) rc = fail(h, GPR_ERR_CUDA, "gpr_debug_eval_values: %s", cudaGetErrorString(e));
+    cudaFree(dxs); cudaFree(dout); cudaFree(dlen); cudaFree(dcnt);
+    return rc;
+}
+
+int gpr_launch_geometry(gpr_handle* h, int* K, int* onepass, int* warps_per_cta, int* ctas, int64_t* smem) {
+    if (!h) return GPR_ERR_ARG;
+    if (K) *K = h->lc.K;
+    if (onepass) *onepass = h->lc.onepass;
+    if (warps_per_cta) *warps_per_cta = h->lc.warps_per_cta;
+    if (ctas) *ctas = h->lc.ctas;
+    if (smem) *smem = (int64_t)h->lc.smem_bytes;
+    return GPR_OK;
+}
+
+void* gpr_stream(gpr_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+int gpr_get_stats(gpr_handle* h, uint64_t* out, int n) {
+    if (!h || !out || n < 0) return GPR_ERR_ARG;
+    unsigned long long tmp[GPR_NSTATS];
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    CUDA_TRY(h, cudaMemcpyAsync(tmp, h->dstats, sizeof tmp, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    for (int i = 0; i < n && i < GPR_NSTATS; ++i) out[i] = tmp[i];
+    return GPR_OK;
+}
+
+int gpr_reset_stats(gpr_handle* h) {
+    if (!h) return GPR_ERR_ARG;
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    CUDA_TRY(h, cudaMemsetAsync(h->dstats, 0, GPR_NSTATS * sizeof(unsigned long long), h->stream));
+    return GPR_OK;
+}
+
+}  /* extern "C" */

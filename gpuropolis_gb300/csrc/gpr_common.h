@@ -1,0 +1,90 @@
+/*
+ * gpr_common.h -- op codes, op classes and the compiled-program instruction
+ * encoding shared by the host library and the kernels.
+ *
+ * Op codes keep the reference's numbering (enum OPS, main.cu:53) so chain
+ * state moves between the reference layout and this library unchanged.
+ * Each op's arity, description-length cost (dispatch_length, main.cu:477-526)
+ * and node count (dispatch_countnodes, main.cu:553-601) is a property of its
+ * class below.
+ */
+#ifndef GPR_COMMON_H
+#define GPR_COMMON_H
+
+#include <stdint.h>
+
+enum gpr_op {
+    OP_ONE = 0, OP_CONST, OP_INV, OP_A, OP_B, OP_PLUS, OP_MINUS, OP_RMINUS, OP_CPLUS,
+    OP_TIMES, OP_CTIMES, OP_DIV, OP_RDIV, OP_LOG, OP_EXP, OP_POW, OP_CPOW, OP_RPOW,
+    OP_CRPOW, OP_SQRT, OP_SIN, OP_ASIN, OP_COS, OP_ACOS, OP_TAN, OP_ATAN, OP_ABS,
+    OP_NREF /* 27 = NOPS of the reference's default op set */
+};
+
+/* PROGRAM_CODE, main.cu:55: one character per op, used in samples.txt. */
+#define GPR_PROGRAM_CODE "1CIab+-_#*@/|LE^pVPRSsCcTtA"
+
+enum gpr_opclass {
+    CLS_LEAF0 = 0,   /* ONE, CONST: no children                                  */
+    CLS_PASS_A,      /* A: value of the left child                               */
+    CLS_PASS_B,      /* B: value of the right child                              */
+    CLS_UNARY,       /* f(a): length 1+a, count 1+a                              */
+    CLS_CUNARY,      /* f(a, C): length CONST_LENGTH_PRIOR+a+1, count a+1        */
+    CLS_BINARY,      /* g(a, b): length 1+a+b, count 1+a+b                       */
+    CLS_INVALID
+};
+
+#if defined(__CUDACC__)
+#define GPR_HDI __host__ __device__ __forceinline__
+#else
+#define GPR_HDI static inline
+#endif
+
+GPR_HDI int gpr_op_class(int o) {
+    switch (o) {
+        case OP_ONE: case OP_CONST: return CLS_LEAF0;
+        case OP_A: return CLS_PASS_A;
+        case OP_B: return CLS_PASS_B;
+        case OP_INV: case OP_LOG: case OP_EXP: case OP_SQRT: case OP_SIN: case OP_ASIN:
+        case OP_COS: case OP_ACOS: case OP_TAN: case OP_ATAN: case OP_ABS: return CLS_UNARY;
+        case OP_CPLUS: case OP_CTIMES: case OP_CPOW: case OP_CRPOW: return CLS_CUNARY;
+        case OP_PLUS: case OP_MINUS: case OP_RMINUS: case OP_TIMES: case OP_DIV: case OP_RDIV:
+        case OP_POW: case OP_RPOW: return CLS_BINARY;
+        default: return CLS_INVALID;
+    }
+}
+
+/* ---- compiled program: a reachable-only postfix form of the heap tree ----
+ * One 32-bit word per instruction: bits 0-7 code, bits 8-15 heap node (the
+ * constant C[node] an instruction reads).  The evaluator keeps the running
+ * value in an accumulator; leaf operands (x, 1, a constant) are folded into
+ * the instruction that consumes them, so the value stack is touched only
+ * where both children of a binary node are subtrees. */
+enum gpr_icode {
+    I_END = 0,
+    I_LDX = 1, I_LDC = 2, I_LD1 = 3, I_PUSH = 4, I_LDNAN = 5,
+    U_INV = 8, U_LOG, U_EXP, U_SQRT, U_SIN, U_ASIN, U_COS, U_ACOS, U_TAN, U_ATAN, U_ABS,
+    U_CPLUS, U_CTIMES, U_CPOW, U_CRPOW,
+    I_BIN0 = 32   /* 32 + bop*8 + accleft*4 + src */
+};
+enum gpr_bop { BOP_ADD = 0, BOP_SUB = 1, BOP_MUL = 2, BOP_DIV = 3, BOP_POW = 4 };
+enum gpr_src { SRC_X = 0, SRC_C = 1, SRC_ONE = 2, SRC_POP = 3 };
+
+#define GPR_BIN(bop, accleft, src) (I_BIN0 + (bop) * 8 + (accleft) * 4 + (src))
+
+/* Counters the MH kernel accumulates (gpr_get_stats). */
+enum gpr_stat {
+    GPR_STAT_EVALS = 0,        /* likelihood evaluations (one per proposal + one per chain) */
+    GPR_STAT_EVAL_NODES,       /* sum over evaluations of the program's node count          */
+    GPR_STAT_EVAL_POINTS,      /* data points actually evaluated (early exit on invalid)   */
+    GPR_STAT_EVAL_NODE_POINTS, /* sum over evaluations of (node count + 4) * points        */
+    GPR_STAT_STRUCT_PROPOSED,
+    GPR_STAT_STRUCT_ACCEPTED,
+    GPR_STAT_CONST_PROPOSED,
+    GPR_STAT_CONST_ACCEPTED,
+    GPR_NSTATS
+};
+
+/* Maximum compiled length for a program of PL heap nodes. */
+#define GPR_MAX_INSTR(PL) (2 * (PL) + 4)
+
+#endif /* GPR_COMMON_H */

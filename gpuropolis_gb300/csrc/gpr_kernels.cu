@@ -1,0 +1,93 @@
+/*
+ * gpr_kernels.cu -- host-side launch helpers of the MH block kernels
+ * (gpr_mh.cuh, instantiated in gpr_mh_k*.cu) and the diagnostics kernel that
+ * evaluates compiled programs point by point for the parity tests.
+ */
+#include "gpr_mh.cuh"
+
+namespace gpr {
+
+/* ------------------------------------------------------------------------ */
+size_t mh_smem_bytes(const KParams& p, int K, int warps_per_cta) {
+    return 16 + align16((size_t)3 * p.nd_pad * 4) +
+           (size_t)warps_per_cta * warp_smem_bytes(p.PL, p.max_instr, p.levels, K);
+}
+
+static const void* pick_kernel(int K, int onepass, int rng) {
+    if (K == 4 && onepass) return mh_kernel_k4(rng);
+    if (K == 8 && onepass) return mh_kernel_k8(rng);
+    if (K == 8 && !onepass) return mh_kernel_k8m(rng);
+    return nullptr;
+}
+
+void fill_lcg_jump_table(KParams& p) {
+    uint32_t a = 1103515245u, c = 12345u;
+    for (int b = 0; b < 20; ++b) {
+        p.lcgA[b] = a; p.lcgC[b] = c;
+        c = a * c + c;   /* the map composed with itself: 2^(b+1) steps */
+        a = a * a;
+    }
+}
+
+cudaError_t mh_occupancy(const KParams& p, int K, int onepass, int warps_per_cta, size_t smem,
+                         int* ctas_per_sm) {
+    const void* f = pick_kernel(K, onepass, p.rng_mode);
+    if (!f) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, f, warps_per_cta * 32, smem);
+}
+
+cudaError_t launch_mh_block(const KParams& p, const LaunchCfg& lc, cudaStream_t st) {
+    const void* f = pick_kernel(lc.K, lc.onepass, p.rng_mode);
+    if (!f) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lc.smem_bytes);
+    if (e != cudaSuccess) return e;
+    KParams pp = p;
+    void* args[] = {(void*)&pp};
+    return cudaLaunchKernel(f, dim3(lc.ctas), dim3(lc.warps_per_cta * 32), args, lc.smem_bytes, st);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Diagnostics kernel: one warp per chain, values of the compiled program at
+ * nx points, plus its length and node count. */
+__global__ void __launch_bounds__(128) eval_values_kernel(const KParams p, const float* xs, int nx,
+                                                          float* out, float* length, int* count) {
+    extern __shared__ __align__(128) uint8_t smem[];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const size_t wbytes = warp_smem_bytes(p.PL, p.max_instr, p.levels, 1);
+    WarpSmem ws = carve_warp(smem + (size_t)warp * wbytes, p.PL, p.max_instr);
+    const int chain = blockIdx.x * (blockDim.x >> 5) + warp;
+    if (chain >= p.N) return;
+    for (int i = lane; i < p.PL; i += 32) {
+        int o = p.P[(size_t)i * p.N + chain];
+        ws.ops[0][i] = (uint8_t)((o >= 0 && o < OP_NREF) ? o : 255);
+        ws.Cs[0][i] = p.C[(size_t)i * p.N + chain];
+    }
+    __syncwarp();
+    CompileOut co = compile_program(ws.ops[0], p.PL, ws.prog[0], lane);
+    __syncwarp();
+    if (lane == 0) { length[chain] = co.length; count[chain] = co.count; }
+    for (int b = 0; b < nx; b += 32) {
+        float x[1], acc[1];
+        int i = b + lane;
+        x[0] = i < nx ? xs[i] : 0.0f;
+        run_program<1>(ws.prog[0], ws.Cs[0], x, acc, ws.stk, lane);
+        if (i < nx) out[(size_t)chain * nx + i] = acc[0];
+    }
+}
+
+cudaError_t launch_eval_values(const KParams& p, const float* xs, int nx, float* out,
+                               float* length, int* count, cudaStream_t st) {
+    const int wpc = 4;
+    size_t smem = (size_t)wpc * warp_smem_bytes(p.PL, p.max_instr, p.levels, 1);
+    cudaError_t e = cudaFuncSetAttribute((const void*)eval_values_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int blocks = (p.N + wpc - 1) / wpc;
+    eval_values_kernel<<<blocks, wpc * 32, smem, st>>>(p, xs, nx, out, length, count);
+    return cudaGetLastError();
+}
+
+}  // namespace gpr

@@ -1,0 +1,105 @@
+/*
+ * gpr_kernels.cuh -- launch parameters shared by the kernels (gpr_kernels.cu)
+ * and the host library (gpr_capi.cu).
+ */
+#ifndef GPR_KERNELS_CUH
+#define GPR_KERNELS_CUH
+
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+namespace gpr {
+
+/* Exact 31-bit division by a run-time constant: x / d == (x * m) >> s for
+ * every 0 <= x < 2^31 (Granlund-Montgomery, m = ceil(2^(31+l)/d), s = 31+l,
+ * l = ceil(log2 d)). */
+struct Magic {
+    uint32_t m;
+    uint32_t s;
+};
+
+/* Everything one launch of the MH block kernel needs.  Passed by value. */
+struct KParams {
+    /* chain state, reference layout (main.cu:387-389) */
+    int32_t* P;
+    float* C;
+    double* prior;
+    double* lik;
+    int N;            /* chains                                              */
+    int PL;           /* heap nodes per program (= NCONSTANTS)               */
+    int steps;        /* MH steps this block (0 = evaluate only)             */
+    uint32_t seed;    /* random_seed argument of MH_simple_kernel            */
+
+    /* dataset, staged per CTA into shared memory; arrays padded to 4 floats */
+    const float* dx;
+    const float* dy;
+    const float* dw;   /* 1 / (2 sd^2) as float                               */
+    const float* dsd;  /* sd, for the double-precision fallback               */
+    int nd;
+    int nd_pad;        /* multiple of 4                                       */
+    double normsum;    /* sum over points of 0.5*(logf(2 PIf) + 2 logf(sd))    */
+
+    /* proposals */
+    int rng_mode;      /* 0 LCG, 1 Philox                                     */
+    int const_mode;    /* 0 reference independence proposal, 1 random walk    */
+    float rw_sd;
+    int nops;
+    int8_t opmap[32];  /* draw index -> op code                               */
+    Magic mag_pl, mag_nops, mag_1e6;   /* divisors of random_int(n) (main.cu:220) */
+    double log_nops1;  /* log((double)NOPS + 1), main.cu:536                  */
+
+    /* float constants the reference computes with libm on the host side of
+     * the oracle; the host library computes them the same way once */
+    float lpi_f;       /* logf(PIf)                        lcauchypdf, main.cu:304 */
+    float lnorm1_f;    /* 0.5*(logf(2 PIf) + 2 logf(1.0f)) lnormalpdf(.,1), main.cu:300 */
+    float logf_r;      /* logf(PROPOSE_GEOM_R) as a float   lgeometricpdf, main.cu:308 */
+    float log1mr_f;    /* log(1.0 - (double)PROPOSE_GEOM_R)                     */
+    float log2_f;      /* log(2.0)                                              */
+    float logpi_f;     /* log((double)PROPOSE_INT)                              */
+    float log1mpi_f;   /* log(1.0 - (double)PROPOSE_INT)                        */
+    float geom_logr;   /* gpr_rng_logf(PROPOSE_GEOM_R), random_geometric        */
+    const float* logcount;  /* logf((float)k), k = 0..PL: Hastings term, main.cu:702,723 */
+
+    /* work distribution and error reporting */
+    int* next_chain;   /* dynamic chain counter (zeroed before launch)          */
+    int* err;          /* device error flags                                    */
+    unsigned long long* stats;  /* GPR_STAT_* counters, accumulated per launch  */
+    int levels;        /* value-stack slots per lane                            */
+    int max_instr;     /* instruction buffer length per program                 */
+
+    /* the reference LCG (main.cu:215) advanced 2^b steps is the affine map
+     * x -> lcgA[b]*x + lcgC[b] (mod 2^32, then masked to 31 bits) */
+    uint32_t lcgA[20];
+    uint32_t lcgC[20];
+};
+
+/* Fill p.lcgA / p.lcgC. */
+void fill_lcg_jump_table(KParams& p);
+
+/* Kernel entry points of the translation units gpr_mh_k*.cu. */
+const void* mh_kernel_k4(int rng);
+const void* mh_kernel_k8(int rng);
+const void* mh_kernel_k8m(int rng);
+
+/* Launch geometry picked by the host (persistent grid). */
+struct LaunchCfg {
+    int K;             /* points per lane per pass: 1, 2, 4 or 8                */
+    int onepass;       /* nd <= 32*K: data kept in registers                    */
+    int warps_per_cta;
+    int ctas;
+    size_t smem_bytes;
+};
+
+size_t mh_smem_bytes(const KParams& p, int K, int warps_per_cta);
+cudaError_t launch_mh_block(const KParams& p, const LaunchCfg& lc, cudaStream_t st);
+cudaError_t mh_occupancy(const KParams& p, int K, int onepass, int warps_per_cta, size_t smem,
+                         int* ctas_per_sm);
+
+/* Diagnostics: evaluate every chain's program at nx points, and report the
+ * compiled length / node count (used by the parity tests). */
+cudaError_t launch_eval_values(const KParams& p, const float* xs, int nx, float* out,
+                               float* length, int* count, cudaStream_t st);
+
+}  // namespace gpr
+
+#endif /* GPR_KERNELS_CUH */

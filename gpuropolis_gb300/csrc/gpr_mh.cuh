@@ -1,0 +1,910 @@
+/*
+ * gpr_mh.cuh -- the GB300 (sm_103a) hot path of the sampler.
+ *
+ * One warp owns one chain at a time (the reference runs one thread per chain,
+ * MH_simple_kernel, main.cu:679-813).  For each MH step the warp
+ *   1. proposes: a structure move every 5th step (main.cu:699-742) or a move
+ *      of every constant (main.cu:743-806), the constants spread over the 32
+ *      lanes with a speculative jump-ahead of the chain's random stream;
+ *   2. compiles the heap tree (main.cu:371-393) into a reachable-only postfix
+ *      program (only after structure moves: constant moves keep the program);
+ *   3. evaluates the program with data points strided across lanes, K points
+ *      per lane per pass, every opcode warp-uniform (no divergence), value
+ *      stack in shared memory, FP32 arithmetic (main.cu:397-444);
+ *   4. forms the Gaussian log-likelihood from a warp-shuffle reduction
+ *      (main.cu:454-468) and the description-length + Cauchy prior
+ *      (main.cu:529-544), then applies the reference's accept rule
+ *      (main.cu:728-740, 790-802) with its exact short-circuit order of draws.
+ * The grid is persistent (a few CTAs per SM); warps fetch the next chain from
+ * a global counter, which balances chains of very different program sizes.
+ * Each CTA stages the dataset into shared memory with one bulk TMA copy
+ * (cp.async.bulk + mbarrier) before any warp starts.
+ */
+#ifndef GPR_MH_CUH
+#define GPR_MH_CUH
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <float.h>
+#include <math.h>
+
+#include "gpr_common.h"
+#include "gpr_rngmath.h"
+#include "gpr_philox.h"
+#include "gpr_kernels.cuh"
+
+namespace gpr {
+
+#define FULLMASK 0xffffffffu
+
+/* ------------------------------------------------------------------------ */
+/* Random stream of one chain.  LCG: s is the 31-bit state.  Philox: s is the
+ * index of the next draw; a 4-word block is cached. */
+struct Rng {
+    uint32_t s;
+    uint32_t key0, key1;
+    uint32_t blk;
+    uint32_t w0, w1, w2, w3;
+    uint32_t drawn;      /* draws consumed since the last reset */
+};
+
+__device__ __forceinline__ uint32_t magic_div(uint32_t x, Magic m) {
+    return (uint32_t)(((uint64_t)x * (uint64_t)m.m) >> m.s);
+}
+
+template <int RNG>
+__device__ __forceinline__ uint32_t rng_next(Rng& r) {
+    r.drawn++;
+    if (RNG == 0) {
+        r.s = (r.s * 1103515245u + 12345u) & 0x7fffffffu;
+        return r.s;
+    } else {
+        uint32_t b = r.s >> 2;
+        if (b != r.blk) {
+            uint32_t c[4] = {b, 0u, 0u, 0u};
+            gpr_philox4x32_10(c, r.key0, r.key1);
+            r.w0 = c[0]; r.w1 = c[1]; r.w2 = c[2]; r.w3 = c[3];
+            r.blk = b;
+        }
+        uint32_t i = r.s & 3u;
+        uint32_t v = (i == 0) ? r.w0 : (i == 1) ? r.w1 : (i == 2) ? r.w2 : r.w3;
+        r.s++;
+        return v >> 1;
+    }
+}
+
+/* Advance by k draws without producing them. */
+template <int RNG>
+__device__ __forceinline__ void rng_jump(Rng& r, uint32_t k, const KParams& p) {
+    if (RNG == 0) {
+        uint32_t x = r.s;
+#pragma unroll 1
+        for (int b = 0; k != 0u; ++b, k >>= 1)
+            if (k & 1u) x = p.lcgA[b] * x + p.lcgC[b];
+        r.s = x & 0x7fffffffu;
+    } else {
+        r.s += k;
+    }
+}
+
+/* random_int (main.cu:218-228): divisor = MY_RAND_MAX/(n+1), reject >= n. */
+template <int RNG>
+__device__ __forceinline__ int random_int(Rng& r, int n, Magic m) {
+    uint32_t v;
+    do { v = magic_div(rng_next<RNG>(r), m); } while (v >= (uint32_t)n);
+    return (int)v;
+}
+
+/* random_float (main.cu:230-232). */
+template <int RNG>
+__device__ __forceinline__ float random_float(Rng& r, const KParams& p) {
+    return gpr_rng_k_over_1e6(random_int<RNG>(r, 1000000, p.mag_1e6));
+}
+
+/* random_normal (main.cu:237-241), Box-Muller with the project log/sin. */
+template <int RNG>
+__device__ __forceinline__ float random_normal(Rng& r, const KParams& p) {
+    float u = random_float<RNG>(r, p);
+    float v = random_float<RNG>(r, p);
+    float a = __fsqrt_rn(__fmul_rn(-2.0f, gpr_rng_logf(u)));
+    return __fmul_rn(a, gpr_rng_sinf(gpr_rng_twopi_times(v)));
+}
+
+/* random_geometric (main.cu:251-254). */
+template <int RNG>
+__device__ __forceinline__ float random_geometric(Rng& r, const KParams& p) {
+    return ceilf(__fdiv_rn(gpr_rng_logf(random_float<RNG>(r, p)), p.geom_logr));
+}
+
+/* ------------------------------------------------------------------------ */
+/* Heap-tree compiler.  Node j is 1-based, children 2j and 2j+1; a child index
+ * beyond PL is the leaf x (main.cu:374-385). */
+#define LEAF_X (-1)
+#define LEAF_ONE (-2)
+#define LEAF_NAN (-3)
+#define LEAF_C0 (-16) /* LEAF_C0 - i : the constant of node i (0-based) */
+
+__device__ __forceinline__ int resolve_leaf(const uint8_t* ops, int PL, int j) {
+    while (j <= PL) {
+        int o = ops[j - 1];
+        if (o == OP_A) j = 2 * j;
+        else if (o == OP_B) j = 2 * j + 1;
+        else break;
+    }
+    if (j > PL) return LEAF_X;
+    int o = ops[j - 1];
+    if (o == OP_ONE) return LEAF_ONE;
+    if (o == OP_CONST) return LEAF_C0 - (j - 1);
+    if (gpr_op_class(o) == CLS_INVALID) return LEAF_NAN;
+    return j;
+}
+
+struct CompileOut {
+    int ninstr;
+    float length;   /* dispatch_length fold, main.cu:477-526 (X_LENGTH_PRIOR = 1) */
+    int count;      /* dispatch_countnodes fold, main.cu:553-601                 */
+};
+
+__device__ __forceinline__ uint32_t load_leaf_instr(int leaf) {
+    if (leaf == LEAF_X) return I_LDX;
+    if (leaf == LEAF_ONE) return I_LD1;
+    if (leaf == LEAF_NAN) return I_LDNAN;
+    return I_LDC | ((uint32_t)(LEAF_C0 - leaf) << 8);
+}
+__device__ __forceinline__ uint32_t bin_instr(int bop, int accleft, int leaf_or_pop) {
+    if (leaf_or_pop == 0) return GPR_BIN(bop, accleft, SRC_POP);
+    if (leaf_or_pop == LEAF_X) return GPR_BIN(bop, accleft, SRC_X);
+    if (leaf_or_pop == LEAF_ONE) return GPR_BIN(bop, accleft, SRC_ONE);
+    if (leaf_or_pop == LEAF_NAN) return GPR_BIN(bop, accleft, SRC_C) | (255u << 8);
+    return GPR_BIN(bop, accleft, SRC_C) | ((uint32_t)(LEAF_C0 - leaf_or_pop) << 8);
+}
+__device__ __forceinline__ void leaf_cost(int leaf, float& len, int& cnt) {
+    /* X: X_LENGTH_PRIOR, count 0; ONE/CONST: 1, count 1 (main.cu:481-482,556-557) */
+    if (leaf == LEAF_X) { len += 1.0f; }
+    else if (leaf == LEAF_NAN) { len = __int_as_float(0x7fc00000); }
+    else { len += 1.0f; cnt += 1; }
+}
+__device__ __forceinline__ int unary_code(int o) {
+    switch (o) {
+        case OP_INV: return U_INV;   case OP_LOG: return U_LOG;   case OP_EXP: return U_EXP;
+        case OP_SQRT: return U_SQRT; case OP_SIN: return U_SIN;   case OP_ASIN: return U_ASIN;
+        case OP_COS: return U_COS;   case OP_ACOS: return U_ACOS; case OP_TAN: return U_TAN;
+        case OP_ATAN: return U_ATAN; case OP_ABS: return U_ABS;   case OP_CPLUS: return U_CPLUS;
+        case OP_CTIMES: return U_CTIMES; case OP_CPOW: return U_CPOW; default: return U_CRPOW;
+    }
+}
+/* base op and operand order of a binary heap op: value = bop(u, v) with
+ * u, v the (left, right) child values or (right, left) for the R-variants */
+__device__ __forceinline__ int binary_bop(int o, int& swapped) {
+    swapped = (o == OP_RMINUS || o == OP_RDIV || o == OP_RPOW);
+    switch (o) {
+        case OP_PLUS: return BOP_ADD;
+        case OP_MINUS: case OP_RMINUS: return BOP_SUB;
+        case OP_TIMES: return BOP_MUL;
+        case OP_DIV: case OP_RDIV: return BOP_DIV;
+        default: return BOP_POW;
+    }
+}
+
+/* Executed identically by every lane of the warp (all inputs are shared
+ * memory broadcasts); lane 0 alone writes the program. */
+static __device__ CompileOut compile_program(const uint8_t* ops, int PL, uint32_t* prog, int lane) {
+    CompileOut out;
+    out.ninstr = 0; out.length = 0.0f; out.count = 0;
+    int fs_node[12], fs_phase[12], fs_aux[12];
+    int fp = 0;
+#define EMIT(w) do { if (lane == 0) prog[out.ninstr] = (w); out.ninstr++; } while (0)
+    int r0 = resolve_leaf(ops, PL, 1);
+    if (r0 < 0) {
+        EMIT(load_leaf_instr(r0));
+        leaf_cost(r0, out.length, out.count);
+    } else {
+        fs_node[0] = r0; fs_phase[0] = 0; fp = 1;
+    }
+    while (fp > 0) {
+        int j = fs_node[fp - 1];
+        int ph = fs_phase[fp - 1];
+        int o = ops[j - 1];
+        int cls = gpr_op_class(o);
+        if (cls == CLS_UNARY || cls == CLS_CUNARY) {
+            uint32_t ui = (uint32_t)unary_code(o) | ((uint32_t)(j - 1) << 8);
+            if (ph == 0) {
+                out.count += 1;
+                out.length += (cls == CLS_CUNARY) ? 2.0f : 1.0f;
+                int L = resolve_leaf(ops, PL, 2 * j);
+                if (L < 0) {
+                    leaf_cost(L, out.length, out.count);
+                    EMIT(load_leaf_instr(L));
+                    EMIT(ui);
+                    --fp;
+                } else {
+                    fs_phase[fp - 1] = 1;
+                    fs_node[fp] = L; fs_phase[fp] = 0; ++fp;
+                }
+            } else {
+                EMIT(ui);
+                --fp;
+            }
+        } else { /* binary */
+            int sw;
+            int bop = binary_bop(o, sw);
+            if (ph == 0) {
+                out.count += 1;
+                out.length += 1.0f;
+                int U = resolve_leaf(ops, PL, sw ? 2 * j + 1 : 2 * j);
+                int V = resolve_leaf(ops, PL, sw ? 2 * j : 2 * j + 1);
+                if (U < 0 && V < 0) {
+                    leaf_cost(U, out.length, out.count);
+                    leaf_cost(V, out.length, out.count);
+                    EMIT(load_leaf_instr(U));
+                    EMIT(bin_instr(bop, 1, V));
+                    --fp;
+                } else if (U >= 0 && V < 0) {
+                    leaf_cost(V, out.length, out.count);
+                    fs_phase[fp - 1] = 1; fs_aux[fp - 1] = V;
+                    fs_node[fp] = U; fs_phase[fp] = 0; ++fp;
+                } else if (U < 0 && V >= 0) {
+                    leaf_cost(U, out.length, out.count);
+                    fs_phase[fp - 1] = 2; fs_aux[fp - 1] = U;
+                    fs_node[fp] = V; fs_phase[fp] = 0; ++fp;
+                } else {
+                    fs_phase[fp - 1] = 3; fs_aux[fp - 1] = V;
+                    fs_node[fp] = U; fs_phase[fp] = 0; ++fp;
+                }
+            } else if (ph == 1) {
+                EMIT(bin_instr(bop, 1, fs_aux[fp - 1]));
+                --fp;
+            } else if (ph == 2) {
+                EMIT(bin_instr(bop, 0, fs_aux[fp - 1]));
+                --fp;
+            } else if (ph == 3) {
+                EMIT(I_PUSH);
+                int V = fs_aux[fp - 1];
+                fs_phase[fp - 1] = 4;
+                fs_node[fp] = V; fs_phase[fp] = 0; ++fp;
+            } else {
+                EMIT(bin_instr(bop, 0, 0));
+                --fp;
+            }
+        }
+    }
+    EMIT(I_END);
+#undef EMIT
+    return out;
+}
+
+/* ------------------------------------------------------------------------ */
+/* The evaluator: acc[k] = f(x[k]) for this lane's K points. */
+template <int K>
+__device__ __forceinline__ void run_program(const uint32_t* __restrict__ prog,
+                                            const float* __restrict__ Cs,
+                                            const float (&x)[K], float (&acc)[K],
+                                            float* __restrict__ stk, int lane) {
+    int sp = 0;
+#pragma unroll 1
+    for (int pc = 0;; ++pc) {
+        const uint32_t ins = prog[pc];
+        const uint32_t code = ins & 0xffu;
+        if (code == I_END) break;
+        const uint32_t node = (ins >> 8) & 0xffu;
+        const float c = (node == 255u) ? __int_as_float(0x7fc00000) : Cs[node];
+        switch (code) {
+            case I_LDX:
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = x[k];
+                break;
+            case I_LDC:
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = c;
+                break;
+            case I_LD1:
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = 1.0f;
+                break;
+            case I_LDNAN:
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = __int_as_float(0x7fc00000);
+                break;
+            case I_PUSH:
+#pragma unroll
+                for (int k = 0; k < K; ++k) stk[(sp * K + k) * 32 + lane] = acc[k];
+                ++sp;
+                break;
+            case U_INV:
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = __fdiv_rn(1.0f, acc[k]);
+                break;
+            case U_LOG:
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = logf(acc[k]);
+                break;
+            case U_EXP:
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = expf(acc[k]);
+                break;
+            case U_SQRT:
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = __fsqrt_rn(acc[k]);
+                break;
+            case U_SIN:
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = sinf(acc[k]);
+                break;
+            case U_ASIN:
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = asinf(acc[k]);
+                break;
+            case U_COS:
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = cosf(acc[k]);
+                break;
+            case U_ACOS:
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = acosf(acc[k]);
+                break;
+            case U_TAN:
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = tanf(acc[k]);
+                break;
+            case U_ATAN:
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = atanf(acc[k]);
+                break;
+            case U_ABS:
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = fabsf(acc[k]);
+                break;
+            case U_CPLUS:
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = __fadd_rn(acc[k], c);
+                break;
+            case U_CTIMES:
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = __fmul_rn(c, acc[k]);
+                break;
+            case U_CPOW:
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = powf(acc[k], c);
+                break;
+            case U_CRPOW:
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = powf(c, acc[k]);
+                break;
+            /* the common fused binary forms, no operand moves */
+            case GPR_BIN(BOP_ADD, 1, SRC_X):
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = __fadd_rn(acc[k], x[k]);
+                break;
+            case GPR_BIN(BOP_ADD, 1, SRC_C):
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = __fadd_rn(acc[k], c);
+                break;
+            case GPR_BIN(BOP_MUL, 1, SRC_X):
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = __fmul_rn(acc[k], x[k]);
+                break;
+            case GPR_BIN(BOP_MUL, 1, SRC_C):
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = __fmul_rn(acc[k], c);
+                break;
+            case GPR_BIN(BOP_SUB, 1, SRC_X):
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = __fsub_rn(acc[k], x[k]);
+                break;
+            case GPR_BIN(BOP_SUB, 1, SRC_C):
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = __fsub_rn(acc[k], c);
+                break;
+            case GPR_BIN(BOP_SUB, 0, SRC_X):
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = __fsub_rn(x[k], acc[k]);
+                break;
+            case GPR_BIN(BOP_SUB, 0, SRC_C):
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = __fsub_rn(c, acc[k]);
+                break;
+            default: {
+                if (code < I_BIN0) break;   /* unknown code: leave acc (cannot be emitted) */
+                const uint32_t bop = (code - I_BIN0) >> 3;
+                const uint32_t accleft = (code >> 2) & 1u;
+                const uint32_t src = code & 3u;
+                float v[K];
+                if (src == SRC_X) {
+#pragma unroll
+                    for (int k = 0; k < K; ++k) v[k] = x[k];
+                } else if (src == SRC_C) {
+#pragma unroll
+                    for (int k = 0; k < K; ++k) v[k] = c;
+                } else if (src == SRC_ONE) {
+#pragma unroll
+                    for (int k = 0; k < K; ++k) v[k] = 1.0f;
+                } else {
+                    --sp;
+#pragma unroll
+                    for (int k = 0; k < K; ++k) v[k] = stk[(sp * K + k) * 32 + lane];
+                }
+                float a[K], b[K];
+#pragma unroll
+                for (int k = 0; k < K; ++k) {
+                    a[k] = accleft ? acc[k] : v[k];
+                    b[k] = accleft ? v[k] : acc[k];
+                }
+                switch (bop) {
+                    case BOP_ADD:
+#pragma unroll
+                        for (int k = 0; k < K; ++k) acc[k] = __fadd_rn(a[k], b[k]);
+                        break;
+                    case BOP_SUB:
+#pragma unroll
+                        for (int k = 0; k < K; ++k) acc[k] = __fsub_rn(a[k], b[k]);
+                        break;
+                    case BOP_MUL:
+#pragma unroll
+                        for (int k = 0; k < K; ++k) acc[k] = __fmul_rn(a[k], b[k]);
+                        break;
+                    case BOP_DIV:
+#pragma unroll
+                        for (int k = 0; k < K; ++k) acc[k] = __fdiv_rn(a[k], b[k]);
+                        break;
+                    default:
+#pragma unroll
+                        for (int k = 0; k < K; ++k) acc[k] = powf(a[k], b[k]);
+                        break;
+                }
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULLMASK, v, o);
+    return v;
+}
+
+/* Shared-memory pointers of one warp. */
+struct WarpSmem {
+    uint8_t* ops[2];
+    float* Cs[2];
+    uint32_t* prog[2];
+    int* off;        /* per constant: offset of its first draw   */
+    int* ndr;        /* per constant: draws used                 */
+    float* fw;       /* per constant: forward log-density term   */
+    float* bw;       /* per constant: backward log-density term  */
+    float* stk;      /* value stack: [levels][K][32]             */
+};
+
+__host__ __device__ __forceinline__ size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
+
+__host__ __device__ __forceinline__ size_t warp_smem_bytes(int PL, int max_instr, int levels, int K) {
+    size_t plp = align16((size_t)PL);
+    size_t b = 0;
+    b += 2 * plp;                                /* ops */
+    b += align16(2 * plp * 4);                   /* Cs */
+    b += align16(2 * (size_t)max_instr * 4);     /* prog */
+    b += 4 * plp * 4;                            /* off, ndr, fw, bw */
+    b += (size_t)levels * K * 32 * 4;            /* stack */
+    return align16(b);
+}
+
+__device__ __forceinline__ WarpSmem carve_warp(uint8_t* base, int PL, int max_instr) {
+    WarpSmem w;
+    size_t plp = align16((size_t)PL);
+    uint8_t* p = base;
+    w.ops[0] = p; w.ops[1] = p + plp; p += 2 * plp;
+    w.Cs[0] = (float*)p; w.Cs[1] = (float*)p + plp; p += align16(2 * plp * 4);
+    w.prog[0] = (uint32_t*)p; w.prog[1] = (uint32_t*)p + max_instr; p += align16(2 * (size_t)max_instr * 4);
+    w.off = (int*)p; p += plp * 4;
+    w.ndr = (int*)p; p += plp * 4;
+    w.fw = (float*)p; p += plp * 4;
+    w.bw = (float*)p; p += plp * 4;
+    w.stk = (float*)p;
+    return w;
+}
+
+/* Per-lane data of the single-pass layout (nd <= 32*K). */
+template <int K>
+struct LaneData {
+    float x[K], y[K], w[K];
+    uint32_t valid;  /* bit k: point lane + 32k exists */
+};
+
+/* log-likelihood of one program: returns -inf when any point is invalid
+ * (main.cu:459,462).  On FP32 overflow of the residual sum the warp recomputes
+ * the sum in FP64 (the reference accumulates in double). */
+template <int K, bool ONEPASS>
+__device__ double eval_loglik(const uint32_t* prog, const float* Cs, float* stk,
+                              const LaneData<K>& ld, const float* sx, const float* sy,
+                              const float* sw, const KParams& p, int lane, int& pts) {
+    float s = 0.0f;
+    bool bad = false;
+    const int npass = ONEPASS ? 1 : (p.nd + 32 * K - 1) / (32 * K);
+#pragma unroll 1
+    for (int pass = 0; pass < npass; ++pass) {
+        float x[K], acc[K];
+        float yv[K], wv[K];
+        uint32_t valid;
+        if (ONEPASS) {
+#pragma unroll
+            for (int k = 0; k < K; ++k) { x[k] = ld.x[k]; yv[k] = ld.y[k]; wv[k] = ld.w[k]; }
+            valid = ld.valid;
+        } else {
+            valid = 0u;
+            const int base = pass * 32 * K + lane;
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                int i = base + 32 * k;
+                bool v = i < p.nd;
+                x[k] = v ? sx[i] : 0.0f;
+                yv[k] = v ? sy[i] : 0.0f;
+                wv[k] = v ? sw[i] : 0.0f;
+                valid |= (v ? 1u : 0u) << k;
+            }
+        }
+        run_program<K>(prog, Cs, x, acc, stk, lane);
+        pts += ONEPASS ? p.nd : min(32 * K, p.nd - pass * 32 * K);
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            if (valid & (1u << k)) {
+                float r = __fsub_rn(acc[k], yv[k]);
+                float q = __fmul_rn(r, r);
+                bad |= !(q <= FLT_MAX);
+                s = fmaf(q, wv[k], s);
+            }
+        }
+        if (__any_sync(FULLMASK, bad)) return -INFINITY;
+    }
+    float S = warp_sum(s);
+    if (S <= FLT_MAX) return -(double)S - p.normsum;
+    /* rare: the FP32 sum overflowed while every term is finite */
+    double sd = 0.0;
+#pragma unroll 1
+    for (int pass = 0; pass < (p.nd + 32 * K - 1) / (32 * K); ++pass) {
+        float x[K], acc[K];
+        const int base = pass * 32 * K + lane;
+#pragma unroll
+        for (int k = 0; k < K; ++k) { int i = base + 32 * k; x[k] = i < p.nd ? sx[i] : 0.0f; }
+        run_program<K>(prog, Cs, x, acc, stk, lane);
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            int i = base + 32 * k;
+            if (i < p.nd) {
+                float r = __fsub_rn(acc[k], sy[i]);
+                float q = __fmul_rn(r, r);
+                double sdv = (double)p.dsd[i];
+                sd += (double)q / (2.0 * sdv * sdv);
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sd += __shfl_xor_sync(FULLMASK, sd, o);
+    return -sd - p.normsum;
+}
+
+/* Sum over all constants of lcauchypdf(C, 1) (main.cu:303-305, 537-540). */
+__device__ __forceinline__ float cauchy_sum(const float* Cs, const KParams& p, int lane) {
+    float s = 0.0f;
+    for (int c = lane; c < p.PL; c += 32) {
+        float x = Cs[c];
+        float a = __fadd_rn(1.0f, __fmul_rn(x, x));
+        s += __fsub_rn(-p.lpi_f, logf(a));
+    }
+    return warp_sum(s);
+}
+
+__device__ __forceinline__ bool is_invalid_d(double v) { return isnan(v) || !isfinite(v); }
+
+/* lnormalpdf(x, 1.0) (main.cu:299-301) */
+__device__ __forceinline__ float lnormal1(float x, const KParams& p) {
+    return __fsub_rn(__fmul_rn(-__fmul_rn(x, x), 0.5f), p.lnorm1_f);
+}
+/* lgeometricpdf(n, r) (main.cu:307-309) with n = v + 1 */
+__device__ __forceinline__ float lgeom_plus1(float v, const KParams& p) {
+    float n = __fadd_rn(v, 1.0f);
+    return __fadd_rn(__fmul_rn(__fsub_rn(n, 1.0f), p.logf_r), p.log1mr_f);
+}
+/* is_int (main.cu:192): |x - lroundf(x)| < 1e-6 */
+__device__ __forceinline__ bool is_int_ref(float x) {
+    if (!(fabsf(x) < 9.2233720368547758e18f)) return false;
+    float d = __fsub_rn(x, roundf(x));
+    return fabsf(d) <= 9.99999997e-07f;
+}
+
+/* One constant's proposal (main.cu:746-785) starting at the stream position
+ * held in r.  Writes the new value and the forward/backward terms. */
+template <int RNG>
+__device__ __forceinline__ void propose_constant(Rng& r, float old, float& nc, float& dfw,
+                                                 float& dbw, const KParams& p) {
+    dfw = 0.0f; dbw = 0.0f;
+    float u0 = random_float<RNG>(r, p);
+    const float p_geom = (p.const_mode == 0) ? 1.0f : 0.0f;   /* P_PROPOSE_C_GEOMETRIC */
+    if (u0 < p_geom) {
+        float u1 = random_float<RNG>(r, p);
+        if (u1 < 0.15f) {                                     /* PROPOSE_INT */
+            float u2 = random_float<RNG>(r, p);
+            float sgn = (u2 < 0.5f) ? -1.0f : 1.0f;
+            float g = random_geometric<RNG>(r, p);
+            nc = __fsub_rn(__fmul_rn(sgn, g), 1.0f);
+            dfw = __fadd_rn(__fadd_rn(lgeom_plus1(nc, p), (nc == 0.0f) ? 0.0f : p.log2_f), p.logpi_f);
+        } else {
+            nc = random_normal<RNG>(r, p);
+            dfw = __fadd_rn(lnormal1(nc, p), p.log1mpi_f);
+        }
+        float bn = __fadd_rn(lnormal1(old, p), p.log1mpi_f);
+        if (is_int_ref(old)) {
+            float bg = __fadd_rn(__fadd_rn(lgeom_plus1(old, p), (nc == 0.0f) ? 0.0f : p.log2_f), p.logpi_f);
+            float m = fmaxf(bg, bn);
+            dbw = logf(expf(bg - m) + expf(bn - m)) + m;
+        } else {
+            dbw = bn;
+        }
+    } else {
+        float z = random_normal<RNG>(r, p);
+        nc = __fadd_rn(old, __fmul_rn(p.rw_sd, z));
+    }
+}
+
+/* Constant move of one chain, lanes in parallel.  Draw counts vary (rejection
+ * in random_int), so each constant first assumes the nominal count for all
+ * earlier constants; a warp prefix sum then gives the true offsets and the
+ * constants whose offset changed are redone, until nothing changes. */
+template <int RNG>
+__device__ void constant_move(Rng& r, const WarpSmem& w, const float* Cold, float* Cnew,
+                              float& fw_sum, float& bw_sum, const KParams& p, int lane) {
+    const int PL = p.PL;
+    const int nominal = (p.const_mode == 0) ? 4 : 3;
+    for (int c = lane; c < PL; c += 32) { w.off[c] = nominal * c; w.ndr[c] = -1; }
+    __syncwarp();
+    bool converged = false;
+#pragma unroll 1
+    for (int iter = 0; iter <= PL && !converged; ++iter) {
+        /* (re)do the constants marked dirty (ndr < 0) at their current offset */
+        for (int c = lane; c < PL; c += 32) {
+            if (w.ndr[c] >= 0) continue;
+            Rng rc = r;
+            rng_jump<RNG>(rc, (uint32_t)w.off[c], p);
+            rc.drawn = 0;
+            float nc, dfw, dbw;
+            propose_constant<RNG>(rc, Cold[c], nc, dfw, dbw, p);
+            Cnew[c] = nc; w.fw[c] = dfw; w.bw[c] = dbw; w.ndr[c] = (int)rc.drawn;
+        }
+        __syncwarp();
+        /* exclusive prefix sum of draw counts, 32 constants at a time */
+        bool changed = false;
+        int base = 0;
+        for (int c0 = 0; c0 < PL; c0 += 32) {
+            int c = c0 + lane;
+            int v = (c < PL) ? w.ndr[c] : 0;
+            int incl = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int t = __shfl_up_sync(FULLMASK, incl, o);
+                if (lane >= o) incl += t;
+            }
+            int excl = base + incl - v;
+            if (c < PL && w.off[c] != excl) { changed = true; w.off[c] = excl; w.ndr[c] = -1; }
+            base += __shfl_sync(FULLMASK, incl, 31);
+        }
+        __syncwarp();
+        if (!__any_sync(FULLMASK, changed)) {
+            rng_jump<RNG>(r, (uint32_t)base, p);
+            converged = true;
+        }
+    }
+    if (!converged && lane == 0) atomicOr(p.err, 2);
+    __syncwarp();
+    float f = 0.0f, b = 0.0f;
+    for (int c = lane; c < PL; c += 32) { f += w.fw[c]; b += w.bw[c]; }
+    fw_sum = warp_sum(f);
+    bw_sum = warp_sum(b);
+}
+
+/* ------------------------------------------------------------------------ */
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+/* Stage the dataset with one bulk TMA copy per array; bounded wait. */
+static __device__ void stage_dataset(float* sx, float* sy, float* sw, uint64_t* bar, const KParams& p) {
+    const uint32_t bytes = (uint32_t)p.nd_pad * 4u;
+    if (bytes == 0) return;
+    if (threadIdx.x == 0) {
+        uint32_t b = smem_u32(bar);
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(3u * bytes) : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     ::"r"(smem_u32(sx)), "l"(p.dx), "r"(bytes), "r"(b) : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     ::"r"(smem_u32(sy)), "l"(p.dy), "r"(bytes), "r"(b) : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     ::"r"(smem_u32(sw)), "l"(p.dw), "r"(bytes), "r"(b) : "memory");
+    }
+    __syncthreads();
+    uint32_t b = smem_u32(bar);
+    uint32_t done = 0;
+    for (int it = 0; it < (1 << 22) && !done; ++it) {
+        asm volatile("{\n\t.reg .pred P1;\n\t"
+                     "mbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\n\t"
+                     "selp.b32 %0, 1, 0, P1;\n\t}"
+                     : "=r"(done) : "r"(b), "r"(0u) : "memory");
+    }
+    if (!done) atomicOr(p.err, 1);
+}
+
+template <int K, bool ONEPASS, int RNG>
+__global__ void __launch_bounds__(256) mh_block_kernel(const KParams p) {
+    extern __shared__ __align__(128) uint8_t smem[];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+
+    /* CTA-shared dataset */
+    uint64_t* bar = (uint64_t*)smem;
+    float* sx = (float*)(smem + 16);
+    float* sy = sx + p.nd_pad;
+    float* sw = sy + p.nd_pad;
+    uint8_t* wbase = smem + 16 + align16((size_t)3 * p.nd_pad * 4);
+    const size_t wbytes = warp_smem_bytes(p.PL, p.max_instr, p.levels, K);
+    WarpSmem ws = carve_warp(wbase + (size_t)warp * wbytes, p.PL, p.max_instr);
+
+    stage_dataset(sx, sy, sw, bar, p);
+
+    LaneData<K> ld;
+    if (ONEPASS) {
+        ld.valid = 0u;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            int i = lane + 32 * k;
+            bool v = i < p.nd;
+            ld.x[k] = v ? sx[i] : 0.0f;
+            ld.y[k] = v ? sy[i] : 0.0f;
+            ld.w[k] = v ? sw[i] : 0.0f;
+            ld.valid |= (v ? 1u : 0u) << k;
+        }
+    }
+    const int PL = p.PL;
+
+#pragma unroll 1
+    for (;;) {
+        int chain = 0;
+        if (lane == 0) chain = atomicAdd(p.next_chain, 1);
+        chain = __shfl_sync(FULLMASK, chain, 0);
+        if (chain >= p.N) break;
+
+        /* load the chain (reference layout) */
+        for (int i = lane; i < PL; i += 32) {
+            int o = p.P[(size_t)i * p.N + chain];
+            ws.ops[0][i] = (uint8_t)((o >= 0 && o < OP_NREF) ? o : 255);
+            ws.Cs[0][i] = p.C[(size_t)i * p.N + chain];
+        }
+        __syncwarp();
+        int cur = 0;       /* which ops/prog buffer is current */
+        int ccur = 0;      /* which constants buffer is current */
+        CompileOut co = compile_program(ws.ops[0], PL, ws.prog[0], lane);
+        __syncwarp();
+        float cs = cauchy_sum(ws.Cs[0], p, lane);
+        double prior_len = (double)(-co.length) * p.log_nops1;
+        double cur_prior = prior_len + (double)cs;
+        int pts0 = 0;
+        double cur_lik = eval_loglik<K, ONEPASS>(ws.prog[0], ws.Cs[0], ws.stk, ld, sx, sy, sw, p, lane, pts0);
+        double cur_post = cur_prior + cur_lik;
+        int cur_count = co.count;
+        float cur_cs = cs;
+        unsigned long long st_pts = (unsigned long long)pts0;
+
+        Rng r;
+        r.key0 = p.seed; r.key1 = (uint32_t)chain; r.blk = 0xffffffffu; r.drawn = 0;
+        r.w0 = r.w1 = r.w2 = r.w3 = 0u;
+        if (RNG == 0) r.s = (p.seed + (uint32_t)chain) & 0x7fffffffu;   /* rx = random_seed + idx */
+        else r.s = 0u;
+
+        double forward = 0.0, backward = 0.0;
+        unsigned long long st_nodes = 0, st_np = 0;
+        int st_evals = 1, st_sp = 0, st_sa = 0, st_cp = 0, st_ca = 0;
+        {
+            st_nodes += (unsigned long long)cur_count;
+            st_np += (unsigned long long)(cur_count + 4) * (unsigned long long)pts0;
+        }
+
+#pragma unroll 1
+        for (int step = 0; step < p.steps; ++step) {
+            if (step % 5 == 0) {
+                /* ---- structure move (main.cu:699-742) ---- */
+                forward = -(double)p.logcount[cur_count];
+                int n = is_invalid_d(cur_post) ? 0 : random_int<RNG>(r, PL, p.mag_pl);
+                const uint8_t* oc = ws.ops[cur];
+                uint8_t* opn = ws.ops[cur ^ 1];
+                for (int i = lane; i < PL; i += 32) opn[i] = oc[i];
+                __syncwarp();
+                const int m = n + 1;
+#pragma unroll 1
+                for (int d = 0;; ++d) {
+                    int lo = m << d;
+                    if (lo > PL) break;
+                    int hi = min(lo + (1 << d) - 1, PL);
+#pragma unroll 1
+                    for (int j = lo; j <= hi; ++j) {
+                        int k = random_int<RNG>(r, p.nops, p.mag_nops);
+                        if (lane == 0) opn[j - 1] = (uint8_t)p.opmap[k];
+                    }
+                }
+                __syncwarp();
+                CompileOut cp = compile_program(opn, PL, ws.prog[cur ^ 1], lane);
+                __syncwarp();
+                backward = -(double)p.logcount[cp.count];
+                double pprior = (double)(-cp.length) * p.log_nops1 + (double)cur_cs;
+                int pts = 0;
+                double plik = eval_loglik<K, ONEPASS>(ws.prog[cur ^ 1], ws.Cs[ccur], ws.stk, ld, sx, sy, sw, p, lane, pts);
+                st_evals++; st_sp++; st_pts += (unsigned)pts; st_nodes += (unsigned)cp.count;
+                st_np += (unsigned long long)(cp.count + 4) * (unsigned)pts;
+                double ppost = pprior + plik;
+                double acc = ppost - cur_post + backward - forward;
+                bool accept = false;
+                if (!is_invalid_d(ppost)) {
+                    if (acc > 0.0) accept = true;
+                    else accept = random_float<RNG>(r, p) < expf((float)acc);
+                }
+                if (is_invalid_d(cur_post)) accept = true;
+                if (accept) {
+                    st_sa++;
+                    cur ^= 1;
+                    cur_post = ppost; cur_lik = plik; cur_prior = pprior;
+                    cur_count = cp.count;
+                    co = cp;
+                }
+            } else {
+                /* ---- constant move (main.cu:743-806) ---- */
+                float fws, bws;
+                constant_move<RNG>(r, ws, ws.Cs[ccur], ws.Cs[ccur ^ 1], fws, bws, p, lane);
+                if (p.const_mode == 0) { forward += (double)fws; backward += (double)bws; }
+                __syncwarp();
+                float ncs = cauchy_sum(ws.Cs[ccur ^ 1], p, lane);
+                double pprior = (double)(-co.length) * p.log_nops1 + (double)ncs;
+                int pts = 0;
+                double plik = eval_loglik<K, ONEPASS>(ws.prog[cur], ws.Cs[ccur ^ 1], ws.stk, ld, sx, sy, sw, p, lane, pts);
+                st_evals++; st_cp++; st_pts += (unsigned)pts; st_nodes += (unsigned)co.count;
+                st_np += (unsigned long long)(co.count + 4) * (unsigned)pts;
+                double ppost = pprior + plik;
+                double acc = ppost - cur_post + backward - forward;
+                bool accept = false;
+                if (!is_invalid_d(ppost)) {
+                    if (acc > 0.0) accept = true;
+                    else accept = random_float<RNG>(r, p) < expf((float)acc);
+                }
+                if (is_invalid_d(cur_post)) accept = true;
+                if (accept) {
+                    st_ca++;
+                    ccur ^= 1;
+                    cur_post = ppost; cur_lik = plik; cur_prior = pprior;
+                    cur_cs = ncs;
+                }
+            }
+            __syncwarp();
+        }
+
+        /* write back (main.cu:811-812 and the in-place P, C) */
+        for (int i = lane; i < PL; i += 32) {
+            uint8_t o = ws.ops[cur][i];
+            if (o != 255) p.P[(size_t)i * p.N + chain] = (int32_t)o;
+            p.C[(size_t)i * p.N + chain] = ws.Cs[ccur][i];
+        }
+        if (lane == 0) {
+            p.prior[chain] = cur_prior; p.lik[chain] = cur_lik;
+            if (p.stats) {
+                atomicAdd(&p.stats[GPR_STAT_EVALS], (unsigned long long)st_evals);
+                atomicAdd(&p.stats[GPR_STAT_EVAL_NODES], st_nodes);
+                atomicAdd(&p.stats[GPR_STAT_EVAL_POINTS], st_pts);
+                atomicAdd(&p.stats[GPR_STAT_EVAL_NODE_POINTS], st_np);
+                atomicAdd(&p.stats[GPR_STAT_STRUCT_PROPOSED], (unsigned long long)st_sp);
+                atomicAdd(&p.stats[GPR_STAT_STRUCT_ACCEPTED], (unsigned long long)st_sa);
+                atomicAdd(&p.stats[GPR_STAT_CONST_PROPOSED], (unsigned long long)st_cp);
+                atomicAdd(&p.stats[GPR_STAT_CONST_ACCEPTED], (unsigned long long)st_ca);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+}  // namespace gpr
+
+#endif /* GPR_MH_CUH */

@@ -1,0 +1,11 @@
+/* Instantiations of the MH block kernel for K = 8 points per lane, dataset held in registers (one pass)
+ * (a translation unit of its own so the kernels compile in parallel). */
+#include "gpr_mh.cuh"
+
+namespace gpr {
+template __global__ void mh_block_kernel<8, true, 0>(const KParams p);
+template __global__ void mh_block_kernel<8, true, 1>(const KParams p);
+const void* mh_kernel_k8(int rng) {
+    return rng ? (const void*)mh_block_kernel<8, true, 1> : (const void*)mh_block_kernel<8, true, 0>;
+}
+}  // namespace gpr

@@ -1,0 +1,143 @@
+/*
+ * gpuropolis.h -- C ABI of the GB300 Metropolis-Hastings sampler over
+ * arithmetic expressions (libgpuropolis.so).
+ *
+ * The reference has no library interface: its sampling loop lives in main()
+ * (main.cu:1011-1257) and talks to one CUDA kernel,
+ *     MH_simple_kernel(int N, op* P, data_t* C, datum* D, int ndata, int steps,
+ *                      bayes_t* prior, bayes_t* likelihood, int random_seed)
+ * (main.cu:679), launched once per block of steps (main.cu:1160), with
+ * synchronous copies of the chain state either side (main.cu:1143-1147,
+ * 1163-1167, 1233-1234).  Each entry point below replaces one of those steps;
+ * the comment on each names the reference lines.  Plain pointers and sizes
+ * only; every call returns a status code (GPR_OK == 0) and never exits the
+ * process; gpr_last_error() describes the last failure of a handle.
+ *
+ * State layout (unchanged from the reference, main.cu:387-389):
+ *   P[i*N + chain]  int32   op code of heap node i (0-based) of a chain
+ *   C[i*N + chain]  float   constant of heap node i
+ *   prior[chain], likelihood[chain]  double
+ * Op codes use the reference numbering (main.cu:53): ONE=0, CONST=1, INV=2,
+ * A=3, B=4, PLUS=5, MINUS=6, RMINUS=7, CPLUS=8, TIMES=9, CTIMES=10, DIV=11,
+ * RDIV=12, LOG=13, EXP=14, POW=15, CPOW=16, RPOW=17, CRPOW=18, SQRT=19,
+ * SIN=20, ASIN=21, COS=22, ACOS=23, TAN=24, ATAN=25, ABS=26.
+ *
+ * A handle is not thread-safe; all of its work runs on one CUDA stream.
+ */
+#ifndef GPUROPOLIS_H
+#define GPUROPOLIS_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    GPR_OK = 0,
+    GPR_ERR_ARG = 1,       /* invalid argument (size, pointer, option)       */
+    GPR_ERR_CUDA = 2,      /* a CUDA call failed; see gpr_last_error         */
+    GPR_ERR_STATE = 3,     /* call out of order (e.g. no data set)           */
+    GPR_ERR_DEVICE = 4,    /* the kernel reported an error flag              */
+    GPR_ERR_NOMEM = 5
+};
+
+enum { GPR_RNG_LCG = 0, GPR_RNG_PHILOX = 1 };
+enum { GPR_CONST_REFERENCE = 0, GPR_CONST_RANDOM_WALK = 1 };
+
+#define GPR_MAX_PROGRAM_LENGTH 255
+#define GPR_MAX_OPS 32
+
+typedef struct gpr_config {
+    int program_length;      /* heap nodes per program (PROGRAM_LENGTH, main.cu:26); odd, 1..255 */
+    int n_ops;               /* size of the op set drawn by proposals                         */
+    int ops[GPR_MAX_OPS];    /* op codes of the set, in draw order (reference: 0..NOPS-1)     */
+    int rng;                 /* GPR_RNG_LCG (main.cu:213-216) or GPR_RNG_PHILOX               */
+    int const_proposal;      /* GPR_CONST_REFERENCE (main.cu:746-785) or GPR_CONST_RANDOM_WALK */
+    float rw_sd;             /* random-walk sd for GPR_CONST_RANDOM_WALK                      */
+    int device;              /* CUDA device ordinal (--gpu, main.cu:104)                      */
+    void* stream;            /* cudaStream_t to run on, or NULL to let the handle create one  */
+    int reserved[8];
+} gpr_config;
+
+typedef struct gpr_handle gpr_handle;
+
+/* Fill *cfg with the reference's defaults: PROGRAM_LENGTH 31, the 27-op set
+ * in enum order, LCG, independence constant proposals (main.cu:21-53). */
+void gpr_default_config(gpr_config* cfg);
+
+/* Create a sampler for n_chains chains (N, main.cu:97).  Allocates the device
+ * state (replaces the DEVARRAY allocations, main.cu:1143-1147). */
+int gpr_create(const gpr_config* cfg, int n_chains, gpr_handle** out);
+
+/* Release everything the handle owns (main.cu:1251-1254). */
+int gpr_destroy(gpr_handle* h);
+
+/* Upload the dataset: n points of (x, y, sd), host arrays (the datum array D,
+ * main.cu:48,1143).  sd must be > 0 (main.cu:332). */
+int gpr_set_data(gpr_handle* h, const float* x, const float* y, const float* sd, int n);
+
+/* Upload chain state in the reference layout (main.cu:1144-1145, 1233-1234).
+ * P holds program_length*N ints, C program_length*N floats (host memory). */
+int gpr_set_state(gpr_handle* h, const int32_t* P, const float* C);
+
+/* Download chain state (main.cu:1163-1166).  Any pointer may be NULL. */
+int gpr_get_state(gpr_handle* h, int32_t* P, float* C, double* prior, double* likelihood);
+
+/* Run `steps` Metropolis-Hastings steps on every chain, the block the
+ * reference launches at main.cu:1160 with random_seed = host rand().  Queued on
+ * the handle's stream; returns once queued (gpr_sync waits). */
+int gpr_run_block(gpr_handle* h, int steps, int random_seed);
+
+/* Recompute prior and likelihood of the current state without stepping
+ * (compute_prior / compute_likelihood, main.cu:529-544, 454-468); results land
+ * in the handle's device prior/likelihood arrays. */
+int gpr_evaluate(gpr_handle* h);
+
+/* Wait for the handle's stream; reports device-side error flags. */
+int gpr_sync(gpr_handle* h);
+
+/* Device pointers of the handle's state (for callers that keep data on the
+ * GPU); valid until gpr_destroy. */
+int gpr_device_state(gpr_handle* h, int32_t** P, float** C, double** prior, double** likelihood);
+
+/* Kernel launches issued by this handle since creation (evidence counter). */
+int64_t gpr_launch_count(gpr_handle* h);
+
+/* Human-readable description of the last error on h (or of the last failed
+ * gpr_create when h is NULL). */
+const char* gpr_last_error(gpr_handle* h);
+
+/* Library version string. */
+const char* gpr_version(void);
+
+/* ---- diagnostics (no reference counterpart; used by the parity tests) ---- */
+
+/* Evaluate every chain's current program at nx points xs (host array) with
+ * the device evaluator: out[chain*nx + i] = f_chain(xs[i]) (the reference's
+ * call(), main.cu:446-448), plus the description length (main.cu:532) and
+ * node count (main.cu:604-608) of each program. */
+int gpr_debug_eval_values(gpr_handle* h, const float* xs, int nx, float* out, float* length,
+                          int* count);
+
+/* Launch geometry chosen for the current dataset: points per lane K, whether
+ * the data stay in registers (onepass), warps per CTA, CTAs, shared bytes. */
+int gpr_launch_geometry(gpr_handle* h, int* K, int* onepass, int* warps_per_cta, int* ctas,
+                        int64_t* smem_bytes);
+
+/* The cudaStream_t the handle runs on. */
+void* gpr_stream(gpr_handle* h);
+
+/* Counters accumulated by the MH kernel since the last reset (no reference
+ * counterpart): [0] likelihood evaluations, [1] sum of evaluated node counts,
+ * [2] data points evaluated, [3] sum of (node count + 4) * points (the
+ * algorithmic FP32 work), [4]/[5] structure moves proposed/accepted,
+ * [6]/[7] constant moves proposed/accepted.  Copies min(n, 8) values. */
+int gpr_get_stats(gpr_handle* h, uint64_t* out, int n);
+int gpr_reset_stats(gpr_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GPUROPOLIS_H */
