@@ -84,6 +84,20 @@ def library():
     lib.gpr_stream.restype = vp
     lib.gpr_get_stats.argtypes = [vp, vp, ip]
     lib.gpr_reset_stats.argtypes = [vp]
+    # host side (include/gpuropolis_host.h)
+    lib.gpr_load_data_file.argtypes = [ctypes.c_char_p, fp, ip, ip, P(vp), P(vp), P(vp), P(ip)]
+    lib.gpr_free.argtypes = [vp]
+    lib.gpr_host_last_error.restype = ctypes.c_char_p
+    lib.gpr_format_expression.argtypes = [vp, vp, ip, ip, ip, ctypes.c_char_p, ip, ctypes.c_char_p, ip]
+    lib.gpr_program_length_of.argtypes = [vp, vp, ip, ip, ip]
+    lib.gpr_program_length_of.restype = fp
+    lib.gpr_polynomial_degree.argtypes = [vp, vp, ip, ip, ip]
+    lib.gpr_polynomial_degree.restype = fp
+    lib.gpr_format_samples.argtypes = [vp, vp, vp, vp, ip, ip, ip, ip, ip, P(vp)]
+    lib.gpr_format_samples.restype = ctypes.c_int64
+    lib.gpr_host_srand.argtypes = [ctypes.c_uint]
+    lib.gpr_host_init_chains.argtypes = [vp, vp, ip, ip, vp, ip]
+    lib.gpr_host_resample.argtypes = [vp, vp, vp, vp, ip, ip, vp, ip, ip, ctypes.c_double]
     _lib = lib
     return lib
 
@@ -200,3 +214,82 @@ class Sampler:
 
     def stream(self):
         return self.lib.gpr_stream(self.h)
+
+
+# ---- host-side helpers (CPU only; no GPU needed) ---------------------------
+
+def load_data_file(path, sdscale=1.0, first_half=False, even_half=False):
+    """The reference's data loader (main.cu:319-363); raises on errors."""
+    lib = library()
+    px, py, ps = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+    n = ctypes.c_int()
+    rc = lib.gpr_load_data_file(path.encode(), sdscale, int(first_half), int(even_half),
+                                ctypes.byref(px), ctypes.byref(py), ctypes.byref(ps), ctypes.byref(n))
+    if rc != 0:
+        raise GprError(rc, lib.gpr_host_last_error().decode(errors="replace"))
+    out = []
+    for p in (px, py, ps):
+        a = np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ctypes.c_float)), shape=(max(n.value, 1),))
+        out.append(a[:n.value].copy())
+        lib.gpr_free(p)
+    return tuple(out)
+
+
+def format_expression(P, C, idx, cfmt="C", latex=False):
+    lib = library()
+    P = np.ascontiguousarray(P, np.int32)
+    C = np.ascontiguousarray(C, np.float32)
+    PL, N = P.shape
+    n = lib.gpr_format_expression(_ptr(P), _ptr(C), N, PL, idx, cfmt.encode(), int(latex), None, 0)
+    buf = ctypes.create_string_buffer(n + 1)
+    lib.gpr_format_expression(_ptr(P), _ptr(C), N, PL, idx, cfmt.encode(), int(latex), buf, n + 1)
+    return buf.value.decode("latin-1")
+
+
+def program_length_of(P, C, idx):
+    P = np.ascontiguousarray(P, np.int32)
+    C = np.ascontiguousarray(C, np.float32)
+    return library().gpr_program_length_of(_ptr(P), _ptr(C), P.shape[1], P.shape[0], idx)
+
+
+def polynomial_degree(P, C, idx):
+    P = np.ascontiguousarray(P, np.int32)
+    C = np.ascontiguousarray(C, np.float32)
+    return library().gpr_polynomial_degree(_ptr(P), _ptr(C), P.shape[1], P.shape[0], idx)
+
+
+def format_samples(P, C, prior, lik, block, show_constants=False, nthreads=0):
+    lib = library()
+    P = np.ascontiguousarray(P, np.int32)
+    C = np.ascontiguousarray(C, np.float32)
+    prior = np.ascontiguousarray(prior, np.float64)
+    lik = np.ascontiguousarray(lik, np.float64)
+    out = ctypes.c_void_p()
+    n = lib.gpr_format_samples(_ptr(P), _ptr(C), _ptr(prior), _ptr(lik), P.shape[1], P.shape[0],
+                               block, int(show_constants), nthreads, ctypes.byref(out))
+    if n < 0:
+        raise GprError(1, "gpr_format_samples failed")
+    s = ctypes.string_at(out, n).decode("latin-1")
+    lib.gpr_free(out)
+    return s
+
+
+def host_init_chains(N, PL, seed, ops=None):
+    """srand(seed) then the reference's initial state (main.cu:1107,1133-1137)."""
+    lib = library()
+    ops = np.ascontiguousarray(OPSET_REFERENCE if ops is None else ops, np.int32)
+    P = np.empty((PL, N), np.int32)
+    C = np.empty((PL, N), np.float32)
+    lib.gpr_host_srand(seed)
+    lib.gpr_host_init_chains(_ptr(P), _ptr(C), N, PL, _ptr(ops), len(ops))
+    return P, C
+
+
+def host_resample(P, C, prior, lik, ops=None, mode=0, param=0.5):
+    """In-place resampling (main.cu:1216-1231); continues the current rand() stream."""
+    lib = library()
+    ops = np.ascontiguousarray(OPSET_REFERENCE if ops is None else ops, np.int32)
+    prior = np.ascontiguousarray(prior, np.float64)
+    lik = np.ascontiguousarray(lik, np.float64)
+    return lib.gpr_host_resample(_ptr(P), _ptr(C), _ptr(prior), _ptr(lik), P.shape[1], P.shape[0],
+                                 _ptr(ops), len(ops), mode, param)

@@ -201,7 +201,7 @@ int gpr_create(const gpr_config* cfg, int n_chains, gpr_handle** out) {
     kp.logf_r = logf(R);
     kp.log1mr_f = (float)log(1.0 - (double)R);
     kp.log2_f = (float)log(2.0);
-    kp.logpi_f = (float)log((double)PI_INT);
+    kp.logpi_f = logf(PI_INT);                 /* log(PROPOSE_INT) binds to the float overload */
     kp.log1mpi_f = (float)log(1.0 - (double)PI_INT);
     kp.geom_logr = gpr_rng_logf(R);
     kp.logcount = h->dlogcount;

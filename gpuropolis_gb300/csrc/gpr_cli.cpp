@@ -1,0 +1,265 @@
+/*
+ * gpr_cli.cpp -- the `gpuropolis` command-line tool: a drop-in for the
+ * reference's main() (main.cu:1011-1257) on top of libgpuropolis.so.
+ *
+ * Same options (main.cu:111-129) and defaults (main.cu:96-109), same
+ * samples.txt header and lines (main.cu:1087-1117, 1170-1213), same host
+ * random stream (srand(seed), one rand() per block as the kernel seed, rand()
+ * for the initial state and for resampling), same outer loop.  Differences:
+ * errors are reported and return 1 instead of aborting on assert; N may
+ * exceed the reference's 524,160-chain limit (main.cu:1059); log.txt (named
+ * in the reference's README but never written by it) receives the parameter
+ * block; the samples of a block are formatted on all host cores.
+ *
+ * Additional options (all off by default, so the defaults reproduce the
+ * reference): --program-length=PL (or --max-len=PL+1), --ops=reference|basic|
+ * <comma-separated op codes>, --rng=lcg|philox, --const-proposal=reference|
+ * rw:SD, --resample=quantile:Q|map-delta:D, --threads=T.
+ */
+#include <getopt.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/gpuropolis.h"
+#include "../../include/gpuropolis_host.h"
+
+static float sdscale = 1.0f;
+static int N = 1024, steps = 1000, outer = 100, thin = 1, seed = -1, burn = 0, QUIET = 0;
+static int WHICH_GPU = 0, FIRST_HALF_DATA = 0, EVEN_HALF_DATA = 0, SHOW_CONSTANTS = 0;
+static std::string in_file_path = "data.txt", out_path = "out/";
+static int PL = 31, rng_mode = GPR_RNG_LCG, const_mode = GPR_CONST_REFERENCE, threads = 0;
+static float rw_sd = 0.1f;
+static int resample_mode = GPR_RESAMPLE_QUANTILE;
+static double resample_param = 0.5;
+static std::vector<int> ops;
+
+enum { OPT_PL = 1000, OPT_MAXLEN, OPT_OPS, OPT_RNG, OPT_CONST, OPT_RESAMPLE, OPT_THREADS };
+
+static struct option long_options[] = {
+    {"in", required_argument, NULL, 'd'},
+    {"steps", required_argument, NULL, 'i'},
+    {"N", required_argument, NULL, 'N'},
+    {"out", required_argument, NULL, 'O'},
+    {"outer", required_argument, NULL, 'o'},
+    {"thin", required_argument, NULL, 't'},
+    {"seed", required_argument, NULL, 's'},
+    {"burn", required_argument, NULL, 'b'},
+    {"gpu", required_argument, NULL, 'g'},
+    {"sdscale", required_argument, NULL, 'r'},
+    {"first-half", no_argument, NULL, 'f'},
+    {"even-half", no_argument, NULL, 'e'},
+    {"show-constants", no_argument, NULL, 'C'},
+    {"quiet", no_argument, NULL, 'q'},
+    {"all", no_argument, NULL, '_'},
+    {"program-length", required_argument, NULL, OPT_PL},
+    {"max-len", required_argument, NULL, OPT_MAXLEN},
+    {"ops", required_argument, NULL, OPT_OPS},
+    {"rng", required_argument, NULL, OPT_RNG},
+    {"const-proposal", required_argument, NULL, OPT_CONST},
+    {"resample", required_argument, NULL, OPT_RESAMPLE},
+    {"threads", required_argument, NULL, OPT_THREADS},
+    {NULL, 0, 0, 0}};
+
+static int parse_ops(const char* s) {
+    ops.clear();
+    if (!strcmp(s, "reference")) { for (int i = 0; i < 27; ++i) ops.push_back(i); return 0; }
+    if (!strcmp(s, "basic")) { ops = {1, 3, 4, 5, 6, 9, 11, 13, 14, 15}; return 0; }
+    std::string t(s);
+    size_t p = 0;
+    while (p <= t.size()) {
+        size_t q = t.find(',', p);
+        std::string tok = t.substr(p, q == std::string::npos ? std::string::npos : q - p);
+        if (tok.empty()) return 1;
+        ops.push_back(atoi(tok.c_str()));
+        if (q == std::string::npos) break;
+        p = q + 1;
+    }
+    return ops.empty();
+}
+
+static int process_arguments(int argc, char** argv) {
+    int option_index = 0, opt = 0;
+    while ((opt = getopt_long(argc, argv, "bp", long_options, &option_index)) != -1) switch (opt) {
+            case 'd': in_file_path = optarg; break;
+            case 'i': steps = atoi(optarg); break;
+            case 'N': N = atoi(optarg); break;
+            case 'o': outer = atoi(optarg); break;
+            case 'O': out_path = optarg; break;
+            case 't': thin = atoi(optarg); break;
+            case 'b': burn = atoi(optarg); break;
+            case 'g': WHICH_GPU = atoi(optarg); break;
+            case 's': seed = atoi(optarg); break;
+            case 'r': sdscale = (float)atof(optarg); break;
+            case 'f': FIRST_HALF_DATA = 1; break;
+            case 'e': EVEN_HALF_DATA = 1; break;
+            case 'C': SHOW_CONSTANTS = 1; break;
+            case 'q': QUIET = 1; break;
+            case '_': break;
+            case OPT_PL: PL = atoi(optarg); break;
+            case OPT_MAXLEN: PL = atoi(optarg) - 1; break;
+            case OPT_OPS: if (parse_ops(optarg)) return 1; break;
+            case OPT_RNG:
+                if (!strcmp(optarg, "lcg")) rng_mode = GPR_RNG_LCG;
+                else if (!strcmp(optarg, "philox")) rng_mode = GPR_RNG_PHILOX;
+                else return 1;
+                break;
+            case OPT_CONST:
+                if (!strcmp(optarg, "reference")) const_mode = GPR_CONST_REFERENCE;
+                else if (!strncmp(optarg, "rw:", 3)) { const_mode = GPR_CONST_RANDOM_WALK; rw_sd = (float)atof(optarg + 3); }
+                else return 1;
+                break;
+            case OPT_RESAMPLE:
+                if (!strncmp(optarg, "quantile:", 9)) { resample_mode = GPR_RESAMPLE_QUANTILE; resample_param = atof(optarg + 9); }
+                else if (!strncmp(optarg, "map-delta:", 10)) { resample_mode = GPR_RESAMPLE_MAP_DELTA; resample_param = atof(optarg + 10); }
+                else return 1;
+                break;
+            case OPT_THREADS: threads = atoi(optarg); break;
+            default: return 1;
+        }
+    return 0;
+}
+
+static void progress_bar(float pct) {   /* main.cu:997-1008 */
+    fprintf(stderr, "\r[");
+    for (int p = 0; p < 70; p++) fprintf(stderr, p <= pct * 70 ? "=" : " ");
+    fprintf(stderr, "]");
+}
+
+static void write_params(FILE* fp, int ndata, int wgpu) {   /* main.cu:1090-1104 */
+    fprintf(fp, "# -----------------------------------------------------------------\n");
+    fprintf(fp, "# -- Parameters:\n");
+    fprintf(fp, "# -----------------------------------------------------------------\n");
+    fprintf(fp, "# \tInput data path: %s\n", in_file_path.c_str());
+    fprintf(fp, "# \tOutput path: %s\n", out_path.c_str());
+    fprintf(fp, "# \tMCMC Iterations (per block): %i\n", steps);
+    fprintf(fp, "# \tBlocks: %i\n", outer);
+    fprintf(fp, "# \tN chains: %i\n", N);
+    fprintf(fp, "# \tSeed: %i\n", seed);
+    fprintf(fp, "# \tMax program length: %i\n", PL);
+    fprintf(fp, "# \tN Constants: %i\n", PL);
+    fprintf(fp, "# \tGPU: %i\n", wgpu);
+    fprintf(fp, "# \tNumber of data points: %i\n", ndata);
+    fprintf(fp, "#\n#\n");
+}
+
+#define FAIL(...) do { fprintf(stderr, __VA_ARGS__); fprintf(stderr, "\n"); return 1; } while (0)
+
+int main(int argc, char** argv) {
+    for (int i = 0; i < 27; ++i) ops.push_back(i);
+    if (process_arguments(argc, argv) == 1) {
+        fprintf(stderr, "Invalid command line arguments.\n");
+        return 1;
+    }
+    if (!(steps > 0)) FAIL("steps must be > 0");          /* main.cu:1028-1031 */
+    if (!(N > 0)) FAIL("N must be > 0");
+    if (!(burn >= 0)) FAIL("burn must be >= 0");
+    if (!(thin >= 1)) FAIL("thin must be >= 1");
+
+    gpr_config cfg;
+    gpr_default_config(&cfg);
+    cfg.program_length = PL;
+    cfg.n_ops = (int)ops.size();
+    if (cfg.n_ops > GPR_MAX_OPS) FAIL("too many ops");
+    for (int i = 0; i < cfg.n_ops; ++i) cfg.ops[i] = ops[i];
+    cfg.rng = rng_mode;
+    cfg.const_proposal = const_mode;
+    cfg.rw_sd = rw_sd;
+    cfg.device = WHICH_GPU;
+    gpr_handle* h = nullptr;
+    if (gpr_create(&cfg, N, &h) != GPR_OK) {
+        fprintf(stderr, "%s\n", gpr_last_error(nullptr));
+        if (strstr(gpr_last_error(nullptr), "invalid GPU device"))
+            fprintf(stderr, "Invalid GPU device %d\n", WHICH_GPU);   /* main.cu:1045 */
+        return 1;
+    }
+    const int wgpu = WHICH_GPU;
+    std::string SAMPLE_PATH = out_path + "/samples.txt";
+    std::string LOG_PATH = out_path + "/log.txt";
+    if (seed == -1) seed = (int)time(NULL);
+
+    float *x = nullptr, *y = nullptr, *sd = nullptr;
+    int ndata = 0;
+    int rc = gpr_load_data_file(in_file_path.c_str(), sdscale, FIRST_HALF_DATA, EVEN_HALF_DATA, &x, &y, &sd, &ndata);
+    if (rc != GPR_HOST_OK) { fprintf(stderr, "*** ERROR: %s\n", gpr_host_last_error()); gpr_destroy(h); return 1; }
+
+    FILE* fp = fopen(SAMPLE_PATH.c_str(), "a");
+    if (!fp) { fprintf(stderr, "*** ERROR: Cannot open file:\t%s\n", SAMPLE_PATH.c_str()); gpr_destroy(h); return 1; }
+    write_params(fp, ndata, wgpu);
+    gpr_host_srand((unsigned)seed);                     /* main.cu:1107 */
+    fprintf(fp, "# -----------------------------------------------------------------\n");
+    fprintf(fp, "# -- Data:\n");
+    fprintf(fp, "# -----------------------------------------------------------------\n");
+    for (int i = 0; i < ndata; i++) fprintf(fp, "# \t%f\t%f\t%f\n", x[i], y[i], sd[i]);
+    fprintf(fp, "#\n#\n");
+    fclose(fp);
+
+    FILE* lg = fopen(LOG_PATH.c_str(), "a");
+    if (lg) {
+        write_params(lg, ndata, wgpu);
+        fprintf(lg, "# \tRNG: %s\n# \tConstant proposal: %s", rng_mode == GPR_RNG_PHILOX ? "philox" : "lcg",
+                const_mode == GPR_CONST_RANDOM_WALK ? "rw:" : "reference");
+        if (const_mode == GPR_CONST_RANDOM_WALK) fprintf(lg, "%g", rw_sd);
+        fprintf(lg, "\n# \tResample: %s:%g\n# \tOps:", resample_mode == GPR_RESAMPLE_MAP_DELTA ? "map-delta" : "quantile",
+                resample_param);
+        for (int o : ops) fprintf(lg, " %d", o);
+        fprintf(lg, "\n# \tLibrary: %s\n", gpr_version());
+    }
+
+    const size_t cnt = (size_t)N * PL;
+    std::vector<int32_t> P(cnt);
+    std::vector<float> C(cnt);
+    std::vector<double> prior(N), lik(N);
+    gpr_host_init_chains(P.data(), C.data(), N, PL, ops.data(), (int)ops.size());   /* main.cu:1133-1137 */
+
+    if (gpr_set_data(h, x, y, sd, ndata) != GPR_OK || gpr_set_state(h, P.data(), C.data()) != GPR_OK) {
+        fprintf(stderr, "%s\n", gpr_last_error(h));
+        gpr_destroy(h);
+        return 1;
+    }
+    if (!QUIET) progress_bar(0.0f);
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    for (int o = 0; o < outer; o++) {
+        int block_seed = gpr_host_rand();                /* main.cu:1160 */
+        if (gpr_run_block(h, steps, block_seed) != GPR_OK ||
+            gpr_get_state(h, P.data(), C.data(), prior.data(), lik.data()) != GPR_OK) {
+            fprintf(stderr, "CUDA error: %s\n", gpr_last_error(h));
+            gpr_destroy(h);
+            return 1;
+        }
+        if (o > burn && o % thin == 0) {                 /* main.cu:1170 */
+            char* buf = nullptr;
+            int64_t n = gpr_format_samples(P.data(), C.data(), prior.data(), lik.data(), N, PL, o,
+                                           SHOW_CONSTANTS, threads, &buf);
+            fp = fopen(SAMPLE_PATH.c_str(), "a");
+            if (fp && n > 0) fwrite(buf, 1, (size_t)n, fp);
+            if (fp) fclose(fp);
+            gpr_free(buf);
+        }
+        gpr_host_resample(P.data(), C.data(), prior.data(), lik.data(), N, PL, ops.data(), (int)ops.size(),
+                          resample_mode, resample_param);
+        if (gpr_set_state(h, P.data(), C.data()) != GPR_OK) {
+            fprintf(stderr, "CUDA error: %s\n", gpr_last_error(h));
+            gpr_destroy(h);
+            return 1;
+        }
+        if (!QUIET) progress_bar(float(o) / float(outer));
+    }
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    if (!QUIET) progress_bar(1.1f);
+    fprintf(stderr, " Completed. \n");
+    if (lg) {
+        double s = (t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec);
+        fprintf(lg, "# \tSampling wall time (s): %.3f\n# \tChain-steps/s: %.4g\n", s,
+                (double)N * steps * outer / (s > 0 ? s : 1e-9));
+        fclose(lg);
+    }
+    gpr_free(x); gpr_free(y); gpr_free(sd);
+    gpr_destroy(h);
+    return 0;
+}

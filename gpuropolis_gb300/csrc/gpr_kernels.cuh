@@ -55,7 +55,7 @@ struct KParams {
     float logf_r;      /* logf(PROPOSE_GEOM_R) as a float   lgeometricpdf, main.cu:308 */
     float log1mr_f;    /* log(1.0 - (double)PROPOSE_GEOM_R)                     */
     float log2_f;      /* log(2.0)                                              */
-    float logpi_f;     /* log((double)PROPOSE_INT)                              */
+    float logpi_f;     /* log(PROPOSE_INT), float overload (logf)               */
     float log1mpi_f;   /* log(1.0 - (double)PROPOSE_INT)                        */
     float geom_logr;   /* gpr_rng_logf(PROPOSE_GEOM_R), random_geometric        */
     const float* logcount;  /* logf((float)k), k = 0..PL: Hastings term, main.cu:702,723 */

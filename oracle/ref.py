@@ -67,6 +67,9 @@ class RefOracle:
         lib.gpr_ref_lcauchypdf.argtypes = [fp, fp]
         lib.gpr_ref_lcauchypdf.restype = ctypes.c_double
         lib.gpr_ref_is_descendant.argtypes = [ip, ip]
+        lib.gpr_ref_load_data.argtypes = [ctypes.c_char_p, fp, ip, ip, vp, ip]
+        lib.gpr_ref_host_random_int.restype = ip
+        lib.gpr_ref_host_init.argtypes = [vp, vp, ip, ctypes.c_uint]
         self.ops = [lib.gpr_ref_opmap(k) for k in range(self.nops)]
 
     @staticmethod
@@ -116,6 +119,20 @@ class RefOracle:
         buf = ctypes.create_string_buffer(n + 1)
         self.lib.gpr_ref_display(fmt.encode(), P.shape[1], idx, _p(P), _p(C), int(latex), buf, n + 1)
         return buf.value.decode("latin-1")
+
+
+    def load_data(self, path, sdscale=1.0, first_half=False, even_half=False):
+        out = np.empty((100000, 3), np.float32)
+        n = self.lib.gpr_ref_load_data(path.encode(), sdscale, int(first_half), int(even_half), _p(out),
+                                       out.shape[0])
+        return out[:n, 0].copy(), out[:n, 1].copy(), out[:n, 2].copy()
+
+    def host_init(self, N, seed):
+        """srand(seed) then main.cu:1133-1137, with the reference's host RNG."""
+        P = np.empty((self.PL, N), np.int32)
+        C = np.empty((self.PL, N), np.float32)
+        self.lib.gpr_ref_host_init(_p(P), _p(C), N, seed)
+        return P, C
 
 
 def get(**kw):

@@ -91,6 +91,32 @@ int gpr_ref_rand(void) { return rand(); }
 int gpr_ref_host_random_int(int limit) { return random_int(limit); }
 float gpr_ref_host_random_normal(void) { return random_normal(); }
 
+/* load_data_file (main.cu:319-363) with the global sdscale it reads; writes
+ * up to cap points as (x, y, sd) triples.  Exits the process on bad input,
+ * like the reference, so callers only pass valid files. */
+int gpr_ref_load_data(const char* path, float scale, int first_half, int even_half, float* out, int cap) {
+    sdscale = scale;
+    vector<datum>* d = load_data_file(path, first_half, even_half);
+    int n = (int)d->size();
+    for (int i = 0; i < n && i < cap; ++i) {
+        out[3 * i] = (*d)[i].x; out[3 * i + 1] = (*d)[i].y; out[3 * i + 2] = (*d)[i].sd;
+    }
+    delete d;
+    return n;
+}
+
+/* The initialisation statements of main() (main.cu:1133-1137) on caller
+ * buffers, after srand(seed) (main.cu:1107), using the reference's own host
+ * random_int / random_normal. */
+void gpr_ref_host_init(int* P, float* C, int N, unsigned seed) {
+    srand(seed);
+    for (int i = 0; i < PROGRAM_LENGTH * N; i++) P[i] = GPR_OPMAP(random_int(GPR_NOPS - 1));
+    for (int i = 0; i < NCONSTANTS * N; i++) {
+        int order = random_int(C_MAX_ORDER - C_MIN_ORDER) + C_MIN_ORDER;
+        C[i] = CONSTANT_SCALE * powf(10.0, order) * random_normal();
+    }
+}
+
 /* The reference's main() (main.cu:1011), renamed. */
 int gpr_ref_cli(int argc, char** argv) { optind = 1; return gpr_ref_main(argc, argv); }
 

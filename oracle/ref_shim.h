@@ -122,9 +122,9 @@ static inline int gpr_ref_philox_next(gpr_philox_stream& s) { return gpr_philox_
 /* ---- op sets: index drawn by random_int -> op code of the reference enum -- */
 #if GPR_REF_OPSET == 1
 /* CONST, A, B, PLUS, MINUS, TIMES, DIV, LOG, EXP, POW in main.cu:53 numbering */
-static const int gpr_ref_opmap[10] = {1, 3, 4, 5, 6, 9, 11, 13, 14, 15};
+static const int gpr_ref_opmap_table[10] = {1, 3, 4, 5, 6, 9, 11, 13, 14, 15};
 #define GPR_NOPS 10
-#define GPR_OPMAP(k) (gpr_ref_opmap[(k)])
+#define GPR_OPMAP(k) (gpr_ref_opmap_table[(k)])
 #else
 #define GPR_NOPS NOPS
 #define GPR_OPMAP(k) (k)
