@@ -178,7 +178,8 @@ def run_gpu(args, w):
     if world > 1:
         torch.distributed.init_process_group("nccl")
     dev = torch.device("cuda", local)
-    stream = torch.cuda.current_stream(dev)
+    stream = torch.cuda.Stream(dev)          # the library's stream; events are recorded on it
+    torch.cuda.set_stream(stream)
 
     x, y, sd = dataset(w)
     P0, C0 = initial_state(w, seed=99 + rank)

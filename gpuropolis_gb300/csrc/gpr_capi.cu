@@ -193,7 +193,11 @@ int gpr_create(const gpr_config* cfg, int n_chains, gpr_handle** out) {
     kp.mag_pl = magic_for(divisor_for(PL));
     kp.mag_nops = magic_for(divisor_for(cfg->n_ops));
     kp.mag_1e6 = magic_for(divisor_for(1000000));
-    kp.log_nops1 = log((double)cfg->n_ops + 1);                  /* main.cu:536 */
+    {
+        const double ln1 = log((double)cfg->n_ops + 1) * 0x1p-64;   /* main.cu:536, scaled */
+        kp.ln1_hi = (float)ln1;
+        kp.ln1_lo = (float)(ln1 - (double)kp.ln1_hi);
+    }
     const double PIf = 3.141592653589;                             /* main.cu:194 */
     kp.lpi_f = logf((float)PIf);                                   /* main.cu:304 */
     kp.lnorm1_f = (float)(0.5 * ((double)logf((float)(2.0 * PIf)) + 2.0 * (double)logf(1.0f)));
@@ -269,7 +273,7 @@ int gpr_set_data(gpr_handle* h, const float* x, const float* y, const float* sd,
         host[i] = x[i];
         host[nd_pad + i] = y[i];
         double s = (double)sd[i];
-        host[2 * (size_t)nd_pad + i] = (float)(1.0 / (2.0 * s * s));
+        host[2 * (size_t)nd_pad + i] = (float)(0x1p-64 / (2.0 * s * s));
         host[3 * (size_t)nd_pad + i] = sd[i];
         /* the constant part of lnormalpdf (main.cu:300), per point */
         normsum += 0.5 * ((double)logf((float)(2.0 * PIf)) + 2.0 * (double)logf(sd[i]));
@@ -285,11 +289,15 @@ int gpr_set_data(gpr_handle* h, const float* x, const float* y, const float* sd,
     h->nd_pad = nd_pad;
     h->normsum = normsum;
     gpr::KParams& kp = h->kp;
-    kp.nd = n; kp.nd_pad = nd_pad; kp.normsum = normsum;
+    kp.nd = n; kp.nd_pad = nd_pad;
+    {
+        const double ns = normsum * 0x1p-64;
+        kp.normsum_hi = (float)ns;
+        kp.normsum_lo = (float)(ns - (double)kp.normsum_hi);
+    }
     kp.dx = h->ddata;
     kp.dy = h->ddata ? h->ddata + nd_pad : nullptr;
     kp.dw = h->ddata ? h->ddata + 2 * (size_t)nd_pad : nullptr;
-    kp.dsd = h->ddata ? h->ddata + 3 * (size_t)nd_pad : nullptr;
     return choose_launch(h);
 }
 

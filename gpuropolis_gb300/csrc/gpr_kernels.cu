@@ -51,13 +51,13 @@ cudaError_t launch_mh_block(const KParams& p, const LaunchCfg& lc, cudaStream_t 
 /* ------------------------------------------------------------------------ */
 /* Diagnostics kernel: one warp per chain, values of the compiled program at
  * nx points, plus its length and node count. */
-__global__ void __launch_bounds__(128) eval_values_kernel(const KParams p, const float* xs, int nx,
+__global__ void __launch_bounds__(128) eval_values_kernel(const __grid_constant__ KParams p, const float* xs, int nx,
                                                           float* out, float* length, int* count) {
     extern __shared__ __align__(128) uint8_t smem[];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const size_t wbytes = warp_smem_bytes(p.PL, p.max_instr, p.levels, 1);
-    WarpSmem ws = carve_warp(smem + (size_t)warp * wbytes, p.PL, p.max_instr);
+    WarpSmem ws = carve_warp<1>(smem + (size_t)warp * wbytes, p.PL, p.max_instr, p.levels);
     const int chain = blockIdx.x * (blockDim.x >> 5) + warp;
     if (chain >= p.N) return;
     for (int i = lane; i < p.PL; i += 32) {
@@ -66,14 +66,17 @@ __global__ void __launch_bounds__(128) eval_values_kernel(const KParams p, const
         ws.Cs[0][i] = p.C[(size_t)i * p.N + chain];
     }
     __syncwarp();
-    CompileOut co = compile_program(ws.ops[0], p.PL, ws.prog[0], lane);
+    if (lane == 0) {
+        CompileOut co = compile_program(ws.ops[0], p.PL, ws.prog[0]);
+        length[chain] = co.length;
+        count[chain] = co.count;
+    }
     __syncwarp();
-    if (lane == 0) { length[chain] = co.length; count[chain] = co.count; }
     for (int b = 0; b < nx; b += 32) {
         float x[1], acc[1];
         int i = b + lane;
         x[0] = i < nx ? xs[i] : 0.0f;
-        run_program<1>(ws.prog[0], ws.Cs[0], x, acc, ws.stk, lane);
+        run_program<1>(ws.prog[0], ws.Cs[0], x, acc, ws.stk, ws.scr, lane);
         if (i < nx) out[(size_t)chain * nx + i] = acc[0];
     }
 }

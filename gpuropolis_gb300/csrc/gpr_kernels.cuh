@@ -33,11 +33,10 @@ struct KParams {
     /* dataset, staged per CTA into shared memory; arrays padded to 4 floats */
     const float* dx;
     const float* dy;
-    const float* dw;   /* 1 / (2 sd^2) as float                               */
-    const float* dsd;  /* sd, for the double-precision fallback               */
+    const float* dw;   /* 2^-64 / (2 sd^2) as float: weights at the bookkeeping scale */
     int nd;
     int nd_pad;        /* multiple of 4                                       */
-    double normsum;    /* sum over points of 0.5*(logf(2 PIf) + 2 logf(sd))    */
+    float normsum_hi, normsum_lo;  /* 2^-64 * sum_d 0.5*(logf(2 PIf) + 2 logf(sd_d)), double-float */
 
     /* proposals */
     int rng_mode;      /* 0 LCG, 1 Philox                                     */
@@ -46,7 +45,7 @@ struct KParams {
     int nops;
     int8_t opmap[32];  /* draw index -> op code                               */
     Magic mag_pl, mag_nops, mag_1e6;   /* divisors of random_int(n) (main.cu:220) */
-    double log_nops1;  /* log((double)NOPS + 1), main.cu:536                  */
+    float ln1_hi, ln1_lo;  /* 2^-64 * log((double)NOPS + 1) (main.cu:536), double-float */
 
     /* float constants the reference computes with libm on the host side of
      * the oracle; the host library computes them the same way once */

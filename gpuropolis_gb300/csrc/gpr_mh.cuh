@@ -37,6 +37,59 @@ namespace gpr {
 #define FULLMASK 0xffffffffu
 
 /* ------------------------------------------------------------------------ */
+/* Double-float ("df") numbers: value = hi + lo, |lo| <= ulp(hi)/2, built from
+ * error-free transforms (Knuth's TwoSum, Dekker's Fast2Sum).  Every Bayes
+ * quantity of a chain (prior, likelihood, posterior, the accumulated
+ * forward/backward proposal log-densities, the acceptance log-ratio) is a df
+ * times 2^64, i.e. stored at the scale 2^-64: FP32 exponents then cover the
+ * whole range the reference's doubles reach in practice (|x| < 6e57), while
+ * every operation stays on the FP32 pipes. */
+#define GPR_DF_SCALE 5.42101086242752217e-20f  /* 2^-64 */
+#define GPR_DF_UNSCALE 1.8446744073709552e19   /* 2^64  */
+
+struct df {
+    float hi, lo;
+};
+
+__device__ __forceinline__ df df_make(float hi, float lo) { df r; r.hi = hi; r.lo = lo; return r; }
+__device__ __forceinline__ df df_neg(df a) { return df_make(-a.hi, -a.lo); }
+__device__ __forceinline__ df df_add(df a, df b) {
+    const float s = __fadd_rn(a.hi, b.hi);
+    if (!isfinite(s)) return df_make(s, 0.0f);
+    const float v = __fsub_rn(s, a.hi);
+    float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, v)), __fsub_rn(b.hi, v));
+    e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+    const float h = __fadd_rn(s, e);
+    return df_make(h, __fsub_rn(e, __fsub_rn(h, s)));
+}
+__device__ __forceinline__ df df_sub(df a, df b) { return df_add(a, df_neg(b)); }
+__device__ __forceinline__ bool df_invalid(df a) { return !isfinite(a.hi); }
+__device__ __forceinline__ bool df_gt0(df a) { return a.hi > 0.0f || (a.hi == 0.0f && a.lo > 0.0f); }
+__device__ __forceinline__ double df_to_double_unscaled(df a) {
+    return ((double)a.hi + (double)a.lo) * GPR_DF_UNSCALE;
+}
+__device__ __forceinline__ df warp_sum_df(df a) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        df b = df_make(__shfl_xor_sync(FULLMASK, a.hi, o), __shfl_xor_sync(FULLMASK, a.lo, o));
+        a = df_add(a, b);
+    }
+    return a;
+}
+/* -PRIOR_MULTIPLIER * length * log(NOPS+1) (main.cu:536), exact product of the
+ * integer-valued length with the double-float constant. */
+__device__ __forceinline__ df length_prior(float length, const KParams& p) {
+    const float L = -length;
+    const float ph = __fmul_rn(L, p.ln1_hi);
+    float e = __fmaf_rn(L, p.ln1_hi, -ph);
+    e = __fmaf_rn(L, p.ln1_lo, e);
+    if (!isfinite(ph)) return df_make(ph, 0.0f);
+    const float h = __fadd_rn(ph, e);
+    return df_make(h, __fsub_rn(e, __fsub_rn(h, ph)));
+}
+
+
+/* ------------------------------------------------------------------------ */
 /* Random stream of one chain.  LCG: s is the 31-bit state.  Philox: s is the
  * index of the next draw; a 4-word block is cached. */
 struct Rng {
@@ -77,9 +130,9 @@ template <int RNG>
 __device__ __forceinline__ void rng_jump(Rng& r, uint32_t k, const KParams& p) {
     if (RNG == 0) {
         uint32_t x = r.s;
-#pragma unroll 1
-        for (int b = 0; k != 0u; ++b, k >>= 1)
-            if (k & 1u) x = p.lcgA[b] * x + p.lcgC[b];
+#pragma unroll
+        for (int b = 0; b < 20; ++b)
+            if ((k >> b) & 1u) x = p.lcgA[b] * x + p.lcgC[b];
         r.s = x & 0x7fffffffu;
     } else {
         r.s += k;
@@ -114,6 +167,7 @@ template <int RNG>
 __device__ __forceinline__ float random_geometric(Rng& r, const KParams& p) {
     return ceilf(__fdiv_rn(gpr_rng_logf(random_float<RNG>(r, p)), p.geom_logr));
 }
+
 
 /* ------------------------------------------------------------------------ */
 /* Heap-tree compiler.  Node j is 1-based, children 2j and 2j+1; a child index
@@ -185,14 +239,14 @@ __device__ __forceinline__ int binary_bop(int o, int& swapped) {
     }
 }
 
-/* Executed identically by every lane of the warp (all inputs are shared
- * memory broadcasts); lane 0 alone writes the program. */
-static __device__ CompileOut compile_program(const uint8_t* ops, int PL, uint32_t* prog, int lane) {
+/* Executed by lane 0 of the warp only (its DFS frames live in that lane's
+ * registers/stack); the caller broadcasts length and count. */
+static __device__ __noinline__ CompileOut compile_program(const uint8_t* ops, int PL, uint32_t* prog) {
     CompileOut out;
     out.ninstr = 0; out.length = 0.0f; out.count = 0;
     int fs_node[12], fs_phase[12], fs_aux[12];
     int fp = 0;
-#define EMIT(w) do { if (lane == 0) prog[out.ninstr] = (w); out.ninstr++; } while (0)
+#define EMIT(w) do { prog[out.ninstr] = (w); out.ninstr++; } while (0)
     int r0 = resolve_leaf(ops, PL, 1);
     if (r0 < 0) {
         EMIT(load_leaf_instr(r0));
@@ -273,12 +327,58 @@ static __device__ CompileOut compile_program(const uint8_t* ops, int PL, uint32_
 }
 
 /* ------------------------------------------------------------------------ */
-/* The evaluator: acc[k] = f(x[k]) for this lane's K points. */
+/* The evaluator: acc[k] = f(x[k]) for this lane's K points.
+ *
+ * Cheap ops (loads, push/pop, + - * /, abs, the C-ops + and *) run unrolled
+ * over the K values in registers.  Transcendental ops and pow run through one
+ * non-unrolled loop over the K values staged in the warp's shared scratch, so
+ * the kernel carries a single copy of each math routine: with every warp of an
+ * SM executing a different program, instruction-cache footprint, not FP32
+ * throughput, is what limits an unrolled interpreter. */
+enum gpr_xop { XOP_LOG, XOP_EXP, XOP_SQRT, XOP_SIN, XOP_ASIN, XOP_COS, XOP_ACOS, XOP_TAN, XOP_ATAN,
+               XOP_CPOW, XOP_CRPOW, XOP_POW };
+
+__device__ __forceinline__ int xop_of_unary(uint32_t code) {
+    switch (code) {
+        case U_LOG: return XOP_LOG;   case U_EXP: return XOP_EXP;   case U_SQRT: return XOP_SQRT;
+        case U_SIN: return XOP_SIN;   case U_ASIN: return XOP_ASIN; case U_COS: return XOP_COS;
+        case U_ACOS: return XOP_ACOS; case U_TAN: return XOP_TAN;   case U_ATAN: return XOP_ATAN;
+        case U_CPOW: return XOP_CPOW; case U_CRPOW: return XOP_CRPOW;
+        default: return -1;
+    }
+}
+
+/* scr[(k)*32 + lane] holds first operands, scr[(K+k)*32 + lane] second ones. */
+template <int K>
+__device__ __noinline__ void expensive_loop(float* __restrict__ scr, int xop, float c, int lane) {
+#pragma unroll 1
+    for (int k = 0; k < K; ++k) {
+        const float u = scr[k * 32 + lane];
+        float r;
+        switch (xop) {
+            case XOP_LOG: r = logf(u); break;
+            case XOP_EXP: r = expf(u); break;
+            case XOP_SQRT: r = __fsqrt_rn(u); break;
+            case XOP_SIN: r = sinf(u); break;
+            case XOP_ASIN: r = asinf(u); break;
+            case XOP_COS: r = cosf(u); break;
+            case XOP_ACOS: r = acosf(u); break;
+            case XOP_TAN: r = tanf(u); break;
+            case XOP_ATAN: r = atanf(u); break;
+            case XOP_CPOW: r = powf(u, c); break;
+            case XOP_CRPOW: r = powf(c, u); break;
+            default: r = powf(u, scr[(K + k) * 32 + lane]); break;
+        }
+        scr[k * 32 + lane] = r;
+    }
+}
+
 template <int K>
 __device__ __forceinline__ void run_program(const uint32_t* __restrict__ prog,
                                             const float* __restrict__ Cs,
                                             const float (&x)[K], float (&acc)[K],
-                                            float* __restrict__ stk, int lane) {
+                                            float* __restrict__ stk, float* __restrict__ scr,
+                                            int lane) {
     int sp = 0;
 #pragma unroll 1
     for (int pc = 0;; ++pc) {
@@ -287,6 +387,66 @@ __device__ __forceinline__ void run_program(const uint32_t* __restrict__ prog,
         if (code == I_END) break;
         const uint32_t node = (ins >> 8) & 0xffu;
         const float c = (node == 255u) ? __int_as_float(0x7fc00000) : Cs[node];
+        if (code >= I_BIN0) {
+            const uint32_t bop = (code - I_BIN0) >> 3;
+            const uint32_t accleft = (code >> 2) & 1u;
+            const uint32_t src = code & 3u;
+            float v[K];
+            if (src == SRC_X) {
+#pragma unroll
+                for (int k = 0; k < K; ++k) v[k] = x[k];
+            } else if (src == SRC_C) {
+#pragma unroll
+                for (int k = 0; k < K; ++k) v[k] = c;
+            } else if (src == SRC_ONE) {
+#pragma unroll
+                for (int k = 0; k < K; ++k) v[k] = 1.0f;
+            } else {
+                --sp;
+#pragma unroll
+                for (int k = 0; k < K; ++k) v[k] = stk[(sp * K + k) * 32 + lane];
+            }
+            if (bop == BOP_POW) {
+#pragma unroll
+                for (int k = 0; k < K; ++k) {
+                    scr[k * 32 + lane] = accleft ? acc[k] : v[k];
+                    scr[(K + k) * 32 + lane] = accleft ? v[k] : acc[k];
+                }
+                expensive_loop<K>(scr, XOP_POW, 0.0f, lane);
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = scr[k * 32 + lane];
+            } else {
+                float a[K], b[K];
+#pragma unroll
+                for (int k = 0; k < K; ++k) {
+                    a[k] = accleft ? acc[k] : v[k];
+                    b[k] = accleft ? v[k] : acc[k];
+                }
+                if (bop == BOP_ADD) {
+#pragma unroll
+                    for (int k = 0; k < K; ++k) acc[k] = __fadd_rn(a[k], b[k]);
+                } else if (bop == BOP_SUB) {
+#pragma unroll
+                    for (int k = 0; k < K; ++k) acc[k] = __fsub_rn(a[k], b[k]);
+                } else if (bop == BOP_MUL) {
+#pragma unroll
+                    for (int k = 0; k < K; ++k) acc[k] = __fmul_rn(a[k], b[k]);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < K; ++k) acc[k] = __fdiv_rn(a[k], b[k]);
+                }
+            }
+            continue;
+        }
+        const int xop = xop_of_unary(code);
+        if (xop >= 0) {
+#pragma unroll
+            for (int k = 0; k < K; ++k) scr[k * 32 + lane] = acc[k];
+            expensive_loop<K>(scr, xop, c, lane);
+#pragma unroll
+            for (int k = 0; k < K; ++k) acc[k] = scr[k * 32 + lane];
+            continue;
+        }
         switch (code) {
             case I_LDX:
 #pragma unroll
@@ -313,42 +473,6 @@ __device__ __forceinline__ void run_program(const uint32_t* __restrict__ prog,
 #pragma unroll
                 for (int k = 0; k < K; ++k) acc[k] = __fdiv_rn(1.0f, acc[k]);
                 break;
-            case U_LOG:
-#pragma unroll
-                for (int k = 0; k < K; ++k) acc[k] = logf(acc[k]);
-                break;
-            case U_EXP:
-#pragma unroll
-                for (int k = 0; k < K; ++k) acc[k] = expf(acc[k]);
-                break;
-            case U_SQRT:
-#pragma unroll
-                for (int k = 0; k < K; ++k) acc[k] = __fsqrt_rn(acc[k]);
-                break;
-            case U_SIN:
-#pragma unroll
-                for (int k = 0; k < K; ++k) acc[k] = sinf(acc[k]);
-                break;
-            case U_ASIN:
-#pragma unroll
-                for (int k = 0; k < K; ++k) acc[k] = asinf(acc[k]);
-                break;
-            case U_COS:
-#pragma unroll
-                for (int k = 0; k < K; ++k) acc[k] = cosf(acc[k]);
-                break;
-            case U_ACOS:
-#pragma unroll
-                for (int k = 0; k < K; ++k) acc[k] = acosf(acc[k]);
-                break;
-            case U_TAN:
-#pragma unroll
-                for (int k = 0; k < K; ++k) acc[k] = tanf(acc[k]);
-                break;
-            case U_ATAN:
-#pragma unroll
-                for (int k = 0; k < K; ++k) acc[k] = atanf(acc[k]);
-                break;
             case U_ABS:
 #pragma unroll
                 for (int k = 0; k < K; ++k) acc[k] = fabsf(acc[k]);
@@ -361,96 +485,8 @@ __device__ __forceinline__ void run_program(const uint32_t* __restrict__ prog,
 #pragma unroll
                 for (int k = 0; k < K; ++k) acc[k] = __fmul_rn(c, acc[k]);
                 break;
-            case U_CPOW:
-#pragma unroll
-                for (int k = 0; k < K; ++k) acc[k] = powf(acc[k], c);
+            default:
                 break;
-            case U_CRPOW:
-#pragma unroll
-                for (int k = 0; k < K; ++k) acc[k] = powf(c, acc[k]);
-                break;
-            /* the common fused binary forms, no operand moves */
-            case GPR_BIN(BOP_ADD, 1, SRC_X):
-#pragma unroll
-                for (int k = 0; k < K; ++k) acc[k] = __fadd_rn(acc[k], x[k]);
-                break;
-            case GPR_BIN(BOP_ADD, 1, SRC_C):
-#pragma unroll
-                for (int k = 0; k < K; ++k) acc[k] = __fadd_rn(acc[k], c);
-                break;
-            case GPR_BIN(BOP_MUL, 1, SRC_X):
-#pragma unroll
-                for (int k = 0; k < K; ++k) acc[k] = __fmul_rn(acc[k], x[k]);
-                break;
-            case GPR_BIN(BOP_MUL, 1, SRC_C):
-#pragma unroll
-                for (int k = 0; k < K; ++k) acc[k] = __fmul_rn(acc[k], c);
-                break;
-            case GPR_BIN(BOP_SUB, 1, SRC_X):
-#pragma unroll
-                for (int k = 0; k < K; ++k) acc[k] = __fsub_rn(acc[k], x[k]);
-                break;
-            case GPR_BIN(BOP_SUB, 1, SRC_C):
-#pragma unroll
-                for (int k = 0; k < K; ++k) acc[k] = __fsub_rn(acc[k], c);
-                break;
-            case GPR_BIN(BOP_SUB, 0, SRC_X):
-#pragma unroll
-                for (int k = 0; k < K; ++k) acc[k] = __fsub_rn(x[k], acc[k]);
-                break;
-            case GPR_BIN(BOP_SUB, 0, SRC_C):
-#pragma unroll
-                for (int k = 0; k < K; ++k) acc[k] = __fsub_rn(c, acc[k]);
-                break;
-            default: {
-                if (code < I_BIN0) break;   /* unknown code: leave acc (cannot be emitted) */
-                const uint32_t bop = (code - I_BIN0) >> 3;
-                const uint32_t accleft = (code >> 2) & 1u;
-                const uint32_t src = code & 3u;
-                float v[K];
-                if (src == SRC_X) {
-#pragma unroll
-                    for (int k = 0; k < K; ++k) v[k] = x[k];
-                } else if (src == SRC_C) {
-#pragma unroll
-                    for (int k = 0; k < K; ++k) v[k] = c;
-                } else if (src == SRC_ONE) {
-#pragma unroll
-                    for (int k = 0; k < K; ++k) v[k] = 1.0f;
-                } else {
-                    --sp;
-#pragma unroll
-                    for (int k = 0; k < K; ++k) v[k] = stk[(sp * K + k) * 32 + lane];
-                }
-                float a[K], b[K];
-#pragma unroll
-                for (int k = 0; k < K; ++k) {
-                    a[k] = accleft ? acc[k] : v[k];
-                    b[k] = accleft ? v[k] : acc[k];
-                }
-                switch (bop) {
-                    case BOP_ADD:
-#pragma unroll
-                        for (int k = 0; k < K; ++k) acc[k] = __fadd_rn(a[k], b[k]);
-                        break;
-                    case BOP_SUB:
-#pragma unroll
-                        for (int k = 0; k < K; ++k) acc[k] = __fsub_rn(a[k], b[k]);
-                        break;
-                    case BOP_MUL:
-#pragma unroll
-                        for (int k = 0; k < K; ++k) acc[k] = __fmul_rn(a[k], b[k]);
-                        break;
-                    case BOP_DIV:
-#pragma unroll
-                        for (int k = 0; k < K; ++k) acc[k] = __fdiv_rn(a[k], b[k]);
-                        break;
-                    default:
-#pragma unroll
-                        for (int k = 0; k < K; ++k) acc[k] = powf(a[k], b[k]);
-                        break;
-                }
-            }
         }
     }
 }
@@ -471,6 +507,7 @@ struct WarpSmem {
     float* fw;       /* per constant: forward log-density term   */
     float* bw;       /* per constant: backward log-density term  */
     float* stk;      /* value stack: [levels][K][32]             */
+    float* scr;      /* transcendental staging: [2K][32]         */
 };
 
 __host__ __device__ __forceinline__ size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
@@ -483,10 +520,12 @@ __host__ __device__ __forceinline__ size_t warp_smem_bytes(int PL, int max_instr
     b += align16(2 * (size_t)max_instr * 4);     /* prog */
     b += 4 * plp * 4;                            /* off, ndr, fw, bw */
     b += (size_t)levels * K * 32 * 4;            /* stack */
+    b += (size_t)2 * K * 32 * 4;                 /* scratch */
     return align16(b);
 }
 
-__device__ __forceinline__ WarpSmem carve_warp(uint8_t* base, int PL, int max_instr) {
+template <int K>
+__device__ __forceinline__ WarpSmem carve_warp(uint8_t* base, int PL, int max_instr, int levels) {
     WarpSmem w;
     size_t plp = align16((size_t)PL);
     uint8_t* p = base;
@@ -498,6 +537,7 @@ __device__ __forceinline__ WarpSmem carve_warp(uint8_t* base, int PL, int max_in
     w.fw = (float*)p; p += plp * 4;
     w.bw = (float*)p; p += plp * 4;
     w.stk = (float*)p;
+    w.scr = w.stk + (size_t)levels * K * 32;
     return w;
 }
 
@@ -508,13 +548,15 @@ struct LaneData {
     uint32_t valid;  /* bit k: point lane + 32k exists */
 };
 
-/* log-likelihood of one program: returns -inf when any point is invalid
- * (main.cu:459,462).  On FP32 overflow of the residual sum the warp recomputes
- * the sum in FP64 (the reference accumulates in double). */
+/* Log-likelihood of one program, as a double-float at the bookkeeping scale
+ * 2^-64 (the per-point weights w carry the scale).  -inf when any point is
+ * invalid (main.cu:459,462).  Each lane sums its points in FP32; the 32 lane
+ * sums are combined with error-free transforms (FP64 on GB300 runs at about
+ * 1/70 of the FP32 rate, so no FP64 instruction is issued here). */
 template <int K, bool ONEPASS>
-__device__ double eval_loglik(const uint32_t* prog, const float* Cs, float* stk,
-                              const LaneData<K>& ld, const float* sx, const float* sy,
-                              const float* sw, const KParams& p, int lane, int& pts) {
+__device__ __forceinline__ df eval_loglik(const uint32_t* prog, const float* Cs, float* stk, float* scr,
+                                          const LaneData<K>& ld, const float* sx, const float* sy,
+                                          const float* sw, const KParams& p, int lane, int& pts) {
     float s = 0.0f;
     bool bad = false;
     const int npass = ONEPASS ? 1 : (p.nd + 32 * K - 1) / (32 * K);
@@ -540,7 +582,7 @@ __device__ double eval_loglik(const uint32_t* prog, const float* Cs, float* stk,
                 valid |= (v ? 1u : 0u) << k;
             }
         }
-        run_program<K>(prog, Cs, x, acc, stk, lane);
+        run_program<K>(prog, Cs, x, acc, stk, scr, lane);
         pts += ONEPASS ? p.nd : min(32 * K, p.nd - pass * 32 * K);
 #pragma unroll
         for (int k = 0; k < K; ++k) {
@@ -551,47 +593,24 @@ __device__ double eval_loglik(const uint32_t* prog, const float* Cs, float* stk,
                 s = fmaf(q, wv[k], s);
             }
         }
-        if (__any_sync(FULLMASK, bad)) return -INFINITY;
+        if (__any_sync(FULLMASK, bad)) return df_make(-INFINITY, 0.0f);
     }
-    float S = warp_sum(s);
-    if (S <= FLT_MAX) return -(double)S - p.normsum;
-    /* rare: the FP32 sum overflowed while every term is finite */
-    double sd = 0.0;
-#pragma unroll 1
-    for (int pass = 0; pass < (p.nd + 32 * K - 1) / (32 * K); ++pass) {
-        float x[K], acc[K];
-        const int base = pass * 32 * K + lane;
-#pragma unroll
-        for (int k = 0; k < K; ++k) { int i = base + 32 * k; x[k] = i < p.nd ? sx[i] : 0.0f; }
-        run_program<K>(prog, Cs, x, acc, stk, lane);
-#pragma unroll
-        for (int k = 0; k < K; ++k) {
-            int i = base + 32 * k;
-            if (i < p.nd) {
-                float r = __fsub_rn(acc[k], sy[i]);
-                float q = __fmul_rn(r, r);
-                double sdv = (double)p.dsd[i];
-                sd += (double)q / (2.0 * sdv * sdv);
-            }
-        }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) sd += __shfl_xor_sync(FULLMASK, sd, o);
-    return -sd - p.normsum;
+    df S = warp_sum_df(df_make(s, 0.0f));
+    if (!isfinite(S.hi)) return df_make(-INFINITY, 0.0f);
+    return df_sub(df_neg(S), df_make(p.normsum_hi, p.normsum_lo));
 }
 
-/* Sum over all constants of lcauchypdf(C, 1) (main.cu:303-305, 537-540). */
-__device__ __forceinline__ float cauchy_sum(const float* Cs, const KParams& p, int lane) {
-    float s = 0.0f;
+/* Sum over all constants of lcauchypdf(C, 1) (main.cu:303-305, 537-540), each
+ * FP32 term added exactly (double-float), at the bookkeeping scale. */
+__device__ __forceinline__ df cauchy_sum(const float* Cs, const KParams& p, int lane) {
+    df s = df_make(0.0f, 0.0f);
     for (int c = lane; c < p.PL; c += 32) {
         float x = Cs[c];
         float a = __fadd_rn(1.0f, __fmul_rn(x, x));
-        s += __fsub_rn(-p.lpi_f, logf(a));
+        s = df_add(s, df_make(__fmul_rn(__fsub_rn(-p.lpi_f, logf(a)), GPR_DF_SCALE), 0.0f));
     }
-    return warp_sum(s);
+    return warp_sum_df(s);
 }
-
-__device__ __forceinline__ bool is_invalid_d(double v) { return isnan(v) || !isfinite(v); }
 
 /* lnormalpdf(x, 1.0) (main.cu:299-301) */
 __device__ __forceinline__ float lnormal1(float x, const KParams& p) {
@@ -649,7 +668,7 @@ __device__ __forceinline__ void propose_constant(Rng& r, float old, float& nc, f
  * constants whose offset changed are redone, until nothing changes. */
 template <int RNG>
 __device__ void constant_move(Rng& r, const WarpSmem& w, const float* Cold, float* Cnew,
-                              float& fw_sum, float& bw_sum, const KParams& p, int lane) {
+                              df& fw_sum, df& bw_sum, const KParams& p, int lane) {
     const int PL = p.PL;
     const int nominal = (p.const_mode == 0) ? 4 : 3;
     for (int c = lane; c < PL; c += 32) { w.off[c] = nominal * c; w.ndr[c] = -1; }
@@ -692,10 +711,13 @@ __device__ void constant_move(Rng& r, const WarpSmem& w, const float* Cold, floa
     }
     if (!converged && lane == 0) atomicOr(p.err, 2);
     __syncwarp();
-    float f = 0.0f, b = 0.0f;
-    for (int c = lane; c < PL; c += 32) { f += w.fw[c]; b += w.bw[c]; }
-    fw_sum = warp_sum(f);
-    bw_sum = warp_sum(b);
+    df f = df_make(0.0f, 0.0f), b = df_make(0.0f, 0.0f);
+    for (int c = lane; c < PL; c += 32) {
+        f = df_add(f, df_make(__fmul_rn(w.fw[c], GPR_DF_SCALE), 0.0f));
+        b = df_add(b, df_make(__fmul_rn(w.bw[c], GPR_DF_SCALE), 0.0f));
+    }
+    fw_sum = warp_sum_df(f);
+    bw_sum = warp_sum_df(b);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -732,8 +754,25 @@ static __device__ void stage_dataset(float* sx, float* sy, float* sw, uint64_t* 
     if (!done) atomicOr(p.err, 1);
 }
 
+/* The accept rule of main.cu:728-740 / 790-802, in its exact evaluation order:
+ * acceptance = proposal - current + backward - forward; the uniform draw is
+ * consumed only when the proposal is valid and acceptance <= 0; an invalid
+ * current state accepts anything. */
+template <int RNG>
+__device__ __forceinline__ bool mh_accept(df ppost, df cur_post, df backward, df forward, Rng& r,
+                                          const KParams& p) {
+    const df acc = df_sub(df_add(df_sub(ppost, cur_post), backward), forward);
+    bool accept = false;
+    if (!df_invalid(ppost)) {
+        if (df_gt0(acc)) accept = true;
+        else accept = random_float<RNG>(r, p) < expf(__fmul_rn(acc.hi, (float)GPR_DF_UNSCALE));
+    }
+    if (df_invalid(cur_post)) accept = true;
+    return accept;
+}
+
 template <int K, bool ONEPASS, int RNG>
-__global__ void __launch_bounds__(256) mh_block_kernel(const KParams p) {
+__global__ void __launch_bounds__(256) mh_block_kernel(const __grid_constant__ KParams p) {
     extern __shared__ __align__(128) uint8_t smem[];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -745,7 +784,7 @@ __global__ void __launch_bounds__(256) mh_block_kernel(const KParams p) {
     float* sw = sy + p.nd_pad;
     uint8_t* wbase = smem + 16 + align16((size_t)3 * p.nd_pad * 4);
     const size_t wbytes = warp_smem_bytes(p.PL, p.max_instr, p.levels, K);
-    WarpSmem ws = carve_warp(wbase + (size_t)warp * wbytes, p.PL, p.max_instr);
+    const WarpSmem ws = carve_warp<K>(wbase + (size_t)warp * wbytes, p.PL, p.max_instr, p.levels);
 
     stage_dataset(sx, sy, sw, bar, p);
 
@@ -771,47 +810,43 @@ __global__ void __launch_bounds__(256) mh_block_kernel(const KParams p) {
         chain = __shfl_sync(FULLMASK, chain, 0);
         if (chain >= p.N) break;
 
-        /* load the chain (reference layout) */
+        /* load the chain (reference layout) into buffer 0 */
         for (int i = lane; i < PL; i += 32) {
             int o = p.P[(size_t)i * p.N + chain];
             ws.ops[0][i] = (uint8_t)((o >= 0 && o < OP_NREF) ? o : 255);
             ws.Cs[0][i] = p.C[(size_t)i * p.N + chain];
         }
         __syncwarp();
-        int cur = 0;       /* which ops/prog buffer is current */
-        int ccur = 0;      /* which constants buffer is current */
-        CompileOut co = compile_program(ws.ops[0], PL, ws.prog[0], lane);
-        __syncwarp();
-        float cs = cauchy_sum(ws.Cs[0], p, lane);
-        double prior_len = (double)(-co.length) * p.log_nops1;
-        double cur_prior = prior_len + (double)cs;
-        int pts0 = 0;
-        double cur_lik = eval_loglik<K, ONEPASS>(ws.prog[0], ws.Cs[0], ws.stk, ld, sx, sy, sw, p, lane, pts0);
-        double cur_post = cur_prior + cur_lik;
-        int cur_count = co.count;
-        float cur_cs = cs;
-        unsigned long long st_pts = (unsigned long long)pts0;
+
+        int cur = 0;           /* ops/prog buffer of the current state */
+        int ccur = 0;          /* constants buffer of the current state */
+        float cur_len = 0.0f;
+        int cur_count = 0;
+        df cur_prior = df_make(0.f, 0.f), cur_lik = df_make(0.f, 0.f), cur_post = df_make(0.f, 0.f);
+        df cur_cs = df_make(0.f, 0.f);
+        df forward = df_make(0.f, 0.f), backward = df_make(0.f, 0.f);
 
         Rng r;
         r.key0 = p.seed; r.key1 = (uint32_t)chain; r.blk = 0xffffffffu; r.drawn = 0;
         r.w0 = r.w1 = r.w2 = r.w3 = 0u;
-        if (RNG == 0) r.s = (p.seed + (uint32_t)chain) & 0x7fffffffu;   /* rx = random_seed + idx */
-        else r.s = 0u;
+        r.s = (RNG == 0) ? ((p.seed + (uint32_t)chain) & 0x7fffffffu) : 0u;   /* rx = random_seed + idx */
 
-        double forward = 0.0, backward = 0.0;
-        unsigned long long st_nodes = 0, st_np = 0;
-        int st_evals = 1, st_sp = 0, st_sa = 0, st_cp = 0, st_ca = 0;
-        {
-            st_nodes += (unsigned long long)cur_count;
-            st_np += (unsigned long long)(cur_count + 4) * (unsigned long long)pts0;
-        }
+        unsigned long long st_nodes = 0, st_np = 0, st_pts = 0;
+        int st_evals = 0, st_sp = 0, st_sa = 0, st_cp = 0, st_ca = 0;
 
+        /* step -1 evaluates the loaded state (main.cu:683-685); steps 0..steps-1
+         * are the MH iterations (main.cu:697-808).  One call site each for
+         * compile, prior and likelihood keeps the kernel's hot code small. */
 #pragma unroll 1
-        for (int step = 0; step < p.steps; ++step) {
-            if (step % 5 == 0) {
+        for (int step = -1; step < p.steps; ++step) {
+            const bool init = step < 0;
+            const bool structural = !init && (step % 5 == 0);
+            int pbuf = cur, cbuf = ccur;
+            bool need_compile = init, need_cauchy = init;
+            if (structural) {
                 /* ---- structure move (main.cu:699-742) ---- */
-                forward = -(double)p.logcount[cur_count];
-                int n = is_invalid_d(cur_post) ? 0 : random_int<RNG>(r, PL, p.mag_pl);
+                forward = df_make(__fmul_rn(-p.logcount[cur_count], GPR_DF_SCALE), 0.0f);
+                const int n = df_invalid(cur_post) ? 0 : random_int<RNG>(r, PL, p.mag_pl);
                 const uint8_t* oc = ws.ops[cur];
                 uint8_t* opn = ws.ops[cur ^ 1];
                 for (int i = lane; i < PL; i += 32) opn[i] = oc[i];
@@ -819,65 +854,54 @@ __global__ void __launch_bounds__(256) mh_block_kernel(const KParams p) {
                 const int m = n + 1;
 #pragma unroll 1
                 for (int d = 0;; ++d) {
-                    int lo = m << d;
+                    const int lo = m << d;
                     if (lo > PL) break;
-                    int hi = min(lo + (1 << d) - 1, PL);
+                    const int hi = min(lo + (1 << d) - 1, PL);
 #pragma unroll 1
                     for (int j = lo; j <= hi; ++j) {
-                        int k = random_int<RNG>(r, p.nops, p.mag_nops);
+                        const int k = random_int<RNG>(r, p.nops, p.mag_nops);
                         if (lane == 0) opn[j - 1] = (uint8_t)p.opmap[k];
                     }
                 }
-                __syncwarp();
-                CompileOut cp = compile_program(opn, PL, ws.prog[cur ^ 1], lane);
-                __syncwarp();
-                backward = -(double)p.logcount[cp.count];
-                double pprior = (double)(-cp.length) * p.log_nops1 + (double)cur_cs;
-                int pts = 0;
-                double plik = eval_loglik<K, ONEPASS>(ws.prog[cur ^ 1], ws.Cs[ccur], ws.stk, ld, sx, sy, sw, p, lane, pts);
-                st_evals++; st_sp++; st_pts += (unsigned)pts; st_nodes += (unsigned)cp.count;
-                st_np += (unsigned long long)(cp.count + 4) * (unsigned)pts;
-                double ppost = pprior + plik;
-                double acc = ppost - cur_post + backward - forward;
-                bool accept = false;
-                if (!is_invalid_d(ppost)) {
-                    if (acc > 0.0) accept = true;
-                    else accept = random_float<RNG>(r, p) < expf((float)acc);
-                }
-                if (is_invalid_d(cur_post)) accept = true;
-                if (accept) {
-                    st_sa++;
-                    cur ^= 1;
-                    cur_post = ppost; cur_lik = plik; cur_prior = pprior;
-                    cur_count = cp.count;
-                    co = cp;
-                }
-            } else {
+                pbuf = cur ^ 1;
+                need_compile = true;
+            } else if (!init) {
                 /* ---- constant move (main.cu:743-806) ---- */
-                float fws, bws;
+                df fws, bws;
                 constant_move<RNG>(r, ws, ws.Cs[ccur], ws.Cs[ccur ^ 1], fws, bws, p, lane);
-                if (p.const_mode == 0) { forward += (double)fws; backward += (double)bws; }
+                if (p.const_mode == 0) { forward = df_add(forward, fws); backward = df_add(backward, bws); }
+                cbuf = ccur ^ 1;
+                need_cauchy = true;
+            }
+            __syncwarp();
+            float len = cur_len;
+            int count = cur_count;
+            if (need_compile) {
+                CompileOut co;
+                if (lane == 0) co = compile_program(ws.ops[pbuf], PL, ws.prog[pbuf]);
+                len = __shfl_sync(FULLMASK, co.length, 0);
+                count = __shfl_sync(FULLMASK, co.count, 0);
                 __syncwarp();
-                float ncs = cauchy_sum(ws.Cs[ccur ^ 1], p, lane);
-                double pprior = (double)(-co.length) * p.log_nops1 + (double)ncs;
-                int pts = 0;
-                double plik = eval_loglik<K, ONEPASS>(ws.prog[cur], ws.Cs[ccur ^ 1], ws.stk, ld, sx, sy, sw, p, lane, pts);
-                st_evals++; st_cp++; st_pts += (unsigned)pts; st_nodes += (unsigned)co.count;
-                st_np += (unsigned long long)(co.count + 4) * (unsigned)pts;
-                double ppost = pprior + plik;
-                double acc = ppost - cur_post + backward - forward;
-                bool accept = false;
-                if (!is_invalid_d(ppost)) {
-                    if (acc > 0.0) accept = true;
-                    else accept = random_float<RNG>(r, p) < expf((float)acc);
-                }
-                if (is_invalid_d(cur_post)) accept = true;
-                if (accept) {
-                    st_ca++;
-                    ccur ^= 1;
-                    cur_post = ppost; cur_lik = plik; cur_prior = pprior;
-                    cur_cs = ncs;
-                }
+            }
+            df cs = cur_cs;
+            if (need_cauchy) cs = cauchy_sum(ws.Cs[cbuf], p, lane);
+            if (structural) backward = df_make(__fmul_rn(-p.logcount[count], GPR_DF_SCALE), 0.0f);
+            int pts = 0;
+            const df lik = eval_loglik<K, ONEPASS>(ws.prog[pbuf], ws.Cs[cbuf], ws.stk, ws.scr, ld, sx, sy, sw,
+                                                   p, lane, pts);
+            const df prior = df_add(length_prior(len, p), cs);
+            const df post = df_add(prior, lik);
+            st_evals++; st_pts += (unsigned)pts; st_nodes += (unsigned)count;
+            st_np += (unsigned long long)(count + 4) * (unsigned)pts;
+            bool accept = true;
+            if (!init) {
+                accept = mh_accept<RNG>(post, cur_post, backward, forward, r, p);
+                if (structural) { st_sp++; st_sa += accept; } else { st_cp++; st_ca += accept; }
+            }
+            if (accept) {
+                cur = pbuf; ccur = cbuf;
+                cur_len = len; cur_count = count; cur_cs = cs;
+                cur_prior = prior; cur_lik = lik; cur_post = post;
             }
             __syncwarp();
         }
@@ -889,7 +913,8 @@ __global__ void __launch_bounds__(256) mh_block_kernel(const KParams p) {
             p.C[(size_t)i * p.N + chain] = ws.Cs[ccur][i];
         }
         if (lane == 0) {
-            p.prior[chain] = cur_prior; p.lik[chain] = cur_lik;
+            p.prior[chain] = df_to_double_unscaled(cur_prior);
+            p.lik[chain] = df_to_double_unscaled(cur_lik);
             if (p.stats) {
                 atomicAdd(&p.stats[GPR_STAT_EVALS], (unsigned long long)st_evals);
                 atomicAdd(&p.stats[GPR_STAT_EVAL_NODES], st_nodes);

@@ -3,8 +3,8 @@
 #include "gpr_mh.cuh"
 
 namespace gpr {
-template __global__ void mh_block_kernel<4, true, 0>(const KParams p);
-template __global__ void mh_block_kernel<4, true, 1>(const KParams p);
+template __global__ void mh_block_kernel<4, true, 0>(const __grid_constant__ KParams p);
+template __global__ void mh_block_kernel<4, true, 1>(const __grid_constant__ KParams p);
 const void* mh_kernel_k4(int rng) {
     return rng ? (const void*)mh_block_kernel<4, true, 1> : (const void*)mh_block_kernel<4, true, 0>;
 }

@@ -1,0 +1,349 @@
+/*
+ * gpr_oracle.c -- plain-C restatement of the reference's sampler path.
+ * TEST INFRASTRUCTURE ONLY: used by tests/ (and bench.py's CPU baseline when
+ * the reference itself cannot be built); the product never links it.
+ *
+ * It restates, in this project's own code, what main.cu computes for one
+ * chain, keeping the reference's float/double typing so results can be
+ * compared bit for bit with the reference compiled for the host
+ * (oracle/build_ref.py).  Each function names the main.cu lines it follows.
+ * It also carries the extensions the reference cannot express (Philox stream,
+ * random-walk constant moves, op subsets) and an FP64 evaluator used to state
+ * the FP32 path's error against FP64.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../gpuropolis_gb300/csrc/gpr_philox.h"
+#include "../gpuropolis_gb300/csrc/gpr_rngmath.h"
+
+/* op codes of the reference enum (main.cu:53) */
+enum { ONE, CONST, INV, A, B, PLUS, MINUS, RMINUS, CPLUS, TIMES, CTIMES, DIV, RDIV, LOG, EXP, POW,
+       CPOW, RPOW, CRPOW, SQRT, SIN, ASIN, COS, ACOS, TAN, ATAN, ABS, NREF };
+
+#define PIF 3.141592653589          /* main.cu:194 */
+#define MY_RAND_MAX 2147483647      /* main.cu:210 */
+static const float PROPOSE_INT = 0.15f;     /* main.cu:32 */
+static const float PROPOSE_GEOM_R = 0.1f;   /* main.cu:34 */
+
+typedef struct {
+    int program_length;  /* PL = NCONSTANTS */
+    int n_ops;
+    int ops[32];
+    int rng;             /* 0 LCG, 1 Philox */
+    int const_mode;      /* 0 independence (reference), 1 random walk */
+    float rw_sd;
+    int project_math;    /* logf/sinf of the random transforms from gpr_rngmath.h */
+} port_cfg;
+
+typedef struct {
+    int rng;
+    int lcg;                 /* reference: int rx (main.cu:691) */
+    gpr_philox_stream ph;
+} port_rng;
+
+/* ---- random stream (main.cu:207-254) ----------------------------------- */
+static int port_next(port_rng* r) {
+    if (r->rng == 0) {
+        /* (rx*1103515245 + 12345) & MY_RAND_MAX with 32-bit wrap-around */
+        uint32_t x = (uint32_t)r->lcg * 1103515245u + 12345u;
+        r->lcg = (int)(x & 0x7fffffffu);
+        return r->lcg;
+    }
+    return gpr_philox_stream_next(&r->ph);
+}
+static int port_random_int(int n, port_rng* r) {
+    int divisor = MY_RAND_MAX / (n + 1), v;
+    do { v = port_next(r) / divisor; } while (v >= n);
+    return v;
+}
+static float port_random_float(port_rng* r) { return (float)((double)(float)port_random_int(1000000, r) / 1000000.0); }
+static float port_logf(float x, int pm) { return pm ? gpr_rng_logf(x) : logf(x); }
+static float port_sinf(float x, int pm) { return pm ? gpr_rng_sinf(x) : sinf(x); }
+static float port_random_normal(port_rng* r, int pm) {
+    float u = port_random_float(r);
+    float v = port_random_float(r);
+    float a = sqrtf((float)(-2.0 * (double)port_logf(u, pm)));
+    return a * port_sinf((float)(2.0 * PIF * (double)v), pm);
+}
+static float port_random_geometric(float rr, port_rng* r, int pm) {
+    return ceilf(port_logf(port_random_float(r), pm) / port_logf(rr, pm));
+}
+
+/* ---- densities (main.cu:299-309, 190-192) ----------------------------- */
+static double port_lnormalpdf(float x, float s) {
+    return (double)(-(x * x)) / (2.0 * s * s) - 0.5 * ((double)logf((float)(2.0 * PIF)) + 2.0 * (double)logf(s));
+}
+static double port_lcauchypdf(float x, float s) {
+    float t = -logf((float)PIF) - logf(s);
+    return (double)(t - logf((float)(1.0 + (double)(x * x / s))));
+}
+static double port_lgeometricpdf(float n, float r) {
+    return (double)((n - 1) * logf(r)) + log(1.0 - (double)r);
+}
+static double port_logplusexp(double a, double b) {
+    double m = a > b ? a : b;
+    return (double)logf(expf((float)(a - m)) + expf((float)(b - m))) + m;
+}
+static int port_is_int(float x) { return fabsf(x - (float)lroundf(x)) < 1.0e-6; }
+
+/* ---- tree folds over the heap (main.cu:371-393) ------------------------ */
+#define OP(P, N, idx, j) ((P)[(size_t)((j) - 1) * (N) + (idx)])
+#define CV(C, N, idx, j) ((C)[(size_t)((j) - 1) * (N) + (idx)])
+
+/* dispatch_eval (main.cu:397-444), reachable nodes only (the value of the
+ * root never depends on the others). */
+static float eval_node(const int32_t* P, const float* C, int N, int PL, int idx, int j, float x) {
+    if (j > PL) return x;
+    const int o = OP(P, N, idx, j);
+    const float c = CV(C, N, idx, j);
+#define L eval_node(P, C, N, PL, idx, 2 * j, x)
+#define R eval_node(P, C, N, PL, idx, 2 * j + 1, x)
+    switch (o) {
+        case ONE: return 1.0f;
+        case CONST: return c;
+        case INV: return 1.0f / L;
+        case A: return L;
+        case B: return R;
+        case PLUS: { float a = L, b = R; return a + b; }
+        case CPLUS: return L + c;
+        case MINUS: { float a = L, b = R; return a - b; }
+        case RMINUS: { float a = L, b = R; return b - a; }
+        case TIMES: { float a = L, b = R; return a * b; }
+        case CTIMES: return c * L;
+        case DIV: { float a = L, b = R; return a / b; }
+        case RDIV: { float a = L, b = R; return b / a; }
+        case SQRT: return sqrtf(L);
+        case LOG: return logf(L);
+        case SIN: return sinf(L);
+        case ASIN: return asinf(L);
+        case COS: return cosf(L);
+        case ACOS: return acosf(L);
+        case TAN: return tanf(L);
+        case ATAN: return atanf(L);
+        case EXP: return expf(L);
+        case POW: { float a = L, b = R; return powf(a, b); }
+        case CPOW: return powf(L, c);
+        case RPOW: { float a = L, b = R; return powf(b, a); }
+        case CRPOW: return powf(c, L);
+        case ABS: return fabsf(L);
+        default: return NAN;
+    }
+#undef L
+#undef R
+}
+
+/* The same expression evaluated in FP64 throughout (for error statements). */
+static double eval_node_f64(const int32_t* P, const float* C, int N, int PL, int idx, int j, double x) {
+    if (j > PL) return x;
+    const int o = OP(P, N, idx, j);
+    const double c = CV(C, N, idx, j);
+#define L eval_node_f64(P, C, N, PL, idx, 2 * j, x)
+#define R eval_node_f64(P, C, N, PL, idx, 2 * j + 1, x)
+    switch (o) {
+        case ONE: return 1.0;
+        case CONST: return c;
+        case INV: return 1.0 / L;
+        case A: return L;
+        case B: return R;
+        case PLUS: { double a = L, b = R; return a + b; }
+        case CPLUS: return L + c;
+        case MINUS: { double a = L, b = R; return a - b; }
+        case RMINUS: { double a = L, b = R; return b - a; }
+        case TIMES: { double a = L, b = R; return a * b; }
+        case CTIMES: return c * L;
+        case DIV: { double a = L, b = R; return a / b; }
+        case RDIV: { double a = L, b = R; return b / a; }
+        case SQRT: return sqrt(L);
+        case LOG: return log(L);
+        case SIN: return sin(L);
+        case ASIN: return asin(L);
+        case COS: return cos(L);
+        case ACOS: return acos(L);
+        case TAN: return tan(L);
+        case ATAN: return atan(L);
+        case EXP: return exp(L);
+        case POW: { double a = L, b = R; return pow(a, b); }
+        case CPOW: return pow(L, c);
+        case RPOW: { double a = L, b = R; return pow(b, a); }
+        case CRPOW: return pow(c, L);
+        case ABS: return fabs(L);
+        default: return NAN;
+    }
+#undef L
+#undef R
+}
+
+/* dispatch_length (main.cu:477-526) with X_LENGTH_PRIOR = CONST_LENGTH_PRIOR = 1 */
+static float length_node(const int32_t* P, int N, int PL, int idx, int j) {
+    if (j > PL) return 1.0f;
+    int o = OP(P, N, idx, j);
+    switch (o) {
+        case ONE: case CONST: return 1.0f;
+        case A: return length_node(P, N, PL, idx, 2 * j);
+        case B: return length_node(P, N, PL, idx, 2 * j + 1);
+        case CPLUS: case CTIMES: case CPOW: case CRPOW: return 1.0f + length_node(P, N, PL, idx, 2 * j) + 1.0f;
+        case PLUS: case MINUS: case RMINUS: case TIMES: case DIV: case RDIV: case POW: case RPOW:
+            return 1.0f + length_node(P, N, PL, idx, 2 * j) + length_node(P, N, PL, idx, 2 * j + 1);
+        case INV: case LOG: case EXP: case SQRT: case SIN: case ASIN: case COS: case ACOS: case TAN:
+        case ATAN: case ABS:
+            return 1.0f + length_node(P, N, PL, idx, 2 * j);
+        default: return NAN;
+    }
+}
+/* dispatch_countnodes (main.cu:553-601): leaves x count 0 */
+static int count_node(const int32_t* P, int N, int PL, int idx, int j) {
+    if (j > PL) return 0;
+    int o = OP(P, N, idx, j);
+    switch (o) {
+        case ONE: case CONST: return 1;
+        case A: return count_node(P, N, PL, idx, 2 * j);
+        case B: return count_node(P, N, PL, idx, 2 * j + 1);
+        case PLUS: case MINUS: case RMINUS: case TIMES: case DIV: case RDIV: case POW: case RPOW:
+            return 1 + count_node(P, N, PL, idx, 2 * j) + count_node(P, N, PL, idx, 2 * j + 1);
+        default: return 1 + count_node(P, N, PL, idx, 2 * j);
+    }
+}
+
+float gpr_port_eval(const int32_t* P, const float* C, int N, int PL, int idx, float x) {
+    return eval_node(P, C, N, PL, idx, 1, x);
+}
+double gpr_port_eval_f64(const int32_t* P, const float* C, int N, int PL, int idx, double x) {
+    return eval_node_f64(P, C, N, PL, idx, 1, x);
+}
+float gpr_port_length(const int32_t* P, int N, int PL, int idx) { return length_node(P, N, PL, idx, 1); }
+int gpr_port_count(const int32_t* P, int N, int PL, int idx) { return count_node(P, N, PL, idx, 1); }
+
+/* compute_prior (main.cu:529-544) */
+double gpr_port_prior(const int32_t* P, const float* C, int N, int PL, int idx, int n_ops) {
+    float length = length_node(P, N, PL, idx, 1);
+    double prior = (double)(-1.0f * length) * log((double)n_ops + 1);
+    for (int c = 0; c < PL; c++) prior += port_lcauchypdf(C[(size_t)c * N + idx], 1.0f);
+    return prior;
+}
+
+/* compute_likelihood (main.cu:454-468); D is (x, y, sd) triples */
+double gpr_port_likelihood(const int32_t* P, const float* C, int N, int PL, int idx, const float* D, int nd) {
+    double ll = 0.0;
+    for (int d = 0; d < nd; d++) {
+        float fx = eval_node(P, C, N, PL, idx, 1, D[3 * d]);
+        if (isnan(fx) || !isfinite(fx)) return -INFINITY;
+        double l = port_lnormalpdf(fx - D[3 * d + 1], D[3 * d + 2]);
+        if (isnan(l) || !isfinite(l)) return -INFINITY;
+        ll += l;
+    }
+    return ll;
+}
+
+/* The same likelihood with the program evaluated in FP64 and summed in FP64. */
+double gpr_port_likelihood_f64(const int32_t* P, const float* C, int N, int PL, int idx, const float* D, int nd) {
+    double ll = 0.0;
+    for (int d = 0; d < nd; d++) {
+        double fx = eval_node_f64(P, C, N, PL, idx, 1, D[3 * d]);
+        if (!isfinite(fx)) return -INFINITY;
+        double r = fx - (double)D[3 * d + 1], s = D[3 * d + 2];
+        ll += -(r * r) / (2.0 * s * s) - 0.5 * (log(2.0 * PIF) + 2.0 * log(s));
+    }
+    return ll;
+}
+
+/* is_descendant (main.cu:660-677): node k (0-based) in the subtree of n */
+static int port_is_descendant(int n, int k) {
+    if (k == n) return 1;
+    n++; k++;
+    while (k > n) { k >>= 1; if (k == n) return 1; }
+    return 0;
+}
+
+static int port_valid(double v) { return !(isnan(v) || !isfinite(v)); }
+
+/* One chain for `steps` MH steps: MH_simple_kernel (main.cu:679-813). */
+static void mh_chain(const port_cfg* cfg, int N, int idx, int32_t* P, float* C, const float* D, int nd,
+                     int steps, double* prior_out, double* lik_out, int random_seed) {
+    const int PL = cfg->program_length;
+    const int pm = cfg->project_math;
+    double cur_prior = gpr_port_prior(P, C, N, PL, idx, cfg->n_ops);
+    double cur_lik = gpr_port_likelihood(P, C, N, PL, idx, D, nd);
+    double cur_post = cur_prior + cur_lik;
+    port_rng r;
+    r.rng = cfg->rng;
+    r.lcg = (int)((uint32_t)random_seed + (uint32_t)idx);
+    gpr_philox_stream_init(&r.ph, (uint32_t)random_seed, (uint32_t)idx);
+    int32_t old_program[256];
+    float old_C[256];
+    double forward = 0.0, backward = 0.0;
+    for (int step = 0; step < steps; step++) {
+        if (step % 5 == 0) {
+            forward = -(double)logf((float)count_node(P, N, PL, idx, 1));
+            int n = port_valid(cur_post) ? port_random_int(PL, &r) : 0;
+            for (int i = n; i < PL; i++) {
+                old_program[i] = P[(size_t)i * N + idx];
+                if (port_is_descendant(n, i)) P[(size_t)i * N + idx] = cfg->ops[port_random_int(cfg->n_ops, &r)];
+            }
+            backward = -(double)logf((float)count_node(P, N, PL, idx, 1));
+            double pp = gpr_port_prior(P, C, N, PL, idx, cfg->n_ops);
+            double pl = gpr_port_likelihood(P, C, N, PL, idx, D, nd);
+            double post = pp + pl;
+            double acc = post - cur_post + backward - forward;
+            if ((port_valid(post) && (acc > 0.0 || port_random_float(&r) < expf((float)acc))) || !port_valid(cur_post)) {
+                cur_post = post; cur_lik = pl; cur_prior = pp;
+            } else {
+                for (int i = n; i < PL; i++) P[(size_t)i * N + idx] = old_program[i];
+            }
+        } else {
+            for (int c = 0; c < PL; c++) {
+                size_t i = (size_t)c * N + idx;
+                old_C[c] = C[i];
+                if (port_random_float(&r) < (cfg->const_mode == 0 ? 1.0f : 0.0f)) {
+                    if (port_random_float(&r) < PROPOSE_INT) {
+                        float sgn = port_random_float(&r) < 0.5 ? -1.0f : 1.0f;
+                        C[i] = sgn * port_random_geometric(PROPOSE_GEOM_R, &r, pm) - 1;
+                        forward += port_lgeometricpdf(C[i] + 1, PROPOSE_GEOM_R) + (C[i] == 0.0 ? 0.0 : log(2.0)) +
+                                   (double)logf(PROPOSE_INT);
+                    } else {
+                        C[i] = 1.0f * port_random_normal(&r, pm);
+                        forward += port_lnormalpdf(C[i] / 1.0f, 1.0f) + log(1.0 - (double)PROPOSE_INT);
+                    }
+                    if (port_is_int(old_C[c])) {
+                        backward += port_logplusexp(
+                            port_lgeometricpdf(old_C[c] + 1, PROPOSE_GEOM_R) + (C[i] == 0.0 ? 0.0 : log(2.0)) +
+                                (double)logf(PROPOSE_INT),
+                            port_lnormalpdf(old_C[c] / 1.0f, 1.0f) + log(1.0 - (double)PROPOSE_INT));
+                    } else {
+                        backward += port_lnormalpdf(old_C[c] / 1.0f, 1.0f) + log(1.0 - (double)PROPOSE_INT);
+                    }
+                } else if (cfg->const_mode == 1) {
+                    C[i] = C[i] + cfg->rw_sd * port_random_normal(&r, pm);
+                } else {
+                    int order = port_random_int(8, &r) - 4;
+                    C[i] = C[i] + 1.0f * powf(10.0f, (float)order) * port_random_normal(&r, pm);
+                }
+            }
+            double pp = gpr_port_prior(P, C, N, PL, idx, cfg->n_ops);
+            double pl = gpr_port_likelihood(P, C, N, PL, idx, D, nd);
+            double post = pp + pl;
+            double acc = post - cur_post + backward - forward;
+            if ((port_valid(post) && (acc > 0.0 || port_random_float(&r) < expf((float)acc))) || !port_valid(cur_post)) {
+                cur_post = post; cur_lik = pl; cur_prior = pp;
+            } else {
+                for (int c = 0; c < PL; c++) C[(size_t)c * N + idx] = old_C[c];
+            }
+        }
+    }
+    prior_out[idx] = cur_prior;
+    lik_out[idx] = cur_lik;
+}
+
+/* One block over chains [c0, c1) (the kernel launch of main.cu:1160). */
+void gpr_port_run_block(const port_cfg* cfg, int N, int c0, int c1, int32_t* P, float* C, const float* D,
+                        int nd, int steps, double* prior, double* lik, int random_seed, int nthreads) {
+#if defined(_OPENMP)
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+    for (int idx = c0; idx < c1; idx++) mh_chain(cfg, N, idx, P, C, D, nd, steps, prior, lik, random_seed);
+}
+
+int gpr_port_sizeof_cfg(void) { return (int)sizeof(port_cfg); }

@@ -1,0 +1,99 @@
+"""ctypes view of the C restatement oracle (oracle/gpr_oracle.c).
+TEST INFRASTRUCTURE ONLY."""
+import ctypes
+
+import numpy as np
+
+from . import build_port
+
+
+class PortCfg(ctypes.Structure):
+    _fields_ = [("program_length", ctypes.c_int), ("n_ops", ctypes.c_int), ("ops", ctypes.c_int * 32),
+                ("rng", ctypes.c_int), ("const_mode", ctypes.c_int), ("rw_sd", ctypes.c_float),
+                ("project_math", ctypes.c_int)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        L = ctypes.CDLL(build_port.build())
+        vp, ip, fp, dp = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_double
+        L.gpr_port_eval.argtypes = [vp, vp, ip, ip, ip, fp]
+        L.gpr_port_eval.restype = fp
+        L.gpr_port_eval_f64.argtypes = [vp, vp, ip, ip, ip, dp]
+        L.gpr_port_eval_f64.restype = dp
+        L.gpr_port_length.argtypes = [vp, ip, ip, ip]
+        L.gpr_port_length.restype = fp
+        L.gpr_port_count.argtypes = [vp, ip, ip, ip]
+        L.gpr_port_prior.argtypes = [vp, vp, ip, ip, ip, ip]
+        L.gpr_port_prior.restype = dp
+        L.gpr_port_likelihood.argtypes = [vp, vp, ip, ip, ip, vp, ip]
+        L.gpr_port_likelihood.restype = dp
+        L.gpr_port_likelihood_f64.argtypes = [vp, vp, ip, ip, ip, vp, ip]
+        L.gpr_port_likelihood_f64.restype = dp
+        L.gpr_port_run_block.argtypes = [ctypes.POINTER(PortCfg), ip, ip, ip, vp, vp, vp, ip, ip, vp, vp, ip, ip]
+        assert L.gpr_port_sizeof_cfg() == ctypes.sizeof(PortCfg)
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def pack(x, y, sd):
+    d = np.empty((len(x), 3), np.float32)
+    d[:, 0], d[:, 1], d[:, 2] = x, y, sd
+    return np.ascontiguousarray(d)
+
+
+def cfg(PL=31, ops=None, rng=0, const_mode=0, rw_sd=0.1, project_math=1):
+    c = PortCfg()
+    c.program_length = PL
+    ops = list(range(27)) if ops is None else list(ops)
+    c.n_ops = len(ops)
+    for i, o in enumerate(ops):
+        c.ops[i] = o
+    c.rng, c.const_mode, c.rw_sd, c.project_math = rng, const_mode, rw_sd, project_math
+    return c
+
+
+def run_block(c, P, C, x, y, sd, steps, seed, nthreads=0, chains=None):
+    PL, N = P.shape
+    assert P.dtype == np.int32 and C.dtype == np.float32 and P.flags.c_contiguous and C.flags.c_contiguous
+    D = pack(x, y, sd)
+    prior = np.zeros(N)
+    lik = np.zeros(N)
+    c0, c1 = chains if chains else (0, N)
+    lib().gpr_port_run_block(ctypes.byref(c), N, c0, c1, _p(P), _p(C), _p(D), len(x), steps, _p(prior),
+                             _p(lik), int(seed), nthreads)
+    return prior, lik
+
+
+def call(P, C, idx, x):
+    return lib().gpr_port_eval(_p(P), _p(C), P.shape[1], P.shape[0], idx, float(x))
+
+
+def call_f64(P, C, idx, x):
+    return lib().gpr_port_eval_f64(_p(P), _p(C), P.shape[1], P.shape[0], idx, float(x))
+
+
+def length(P, idx):
+    return lib().gpr_port_length(_p(P), P.shape[1], P.shape[0], idx)
+
+
+def count(P, idx):
+    return lib().gpr_port_count(_p(P), P.shape[1], P.shape[0], idx)
+
+
+def prior(P, C, idx, n_ops):
+    return lib().gpr_port_prior(_p(P), _p(C), P.shape[1], P.shape[0], idx, n_ops)
+
+
+def likelihood(P, C, idx, x, y, sd, f64=False):
+    D = pack(x, y, sd)
+    f = lib().gpr_port_likelihood_f64 if f64 else lib().gpr_port_likelihood
+    return f(_p(P), _p(C), P.shape[1], P.shape[0], idx, _p(D), len(x))
