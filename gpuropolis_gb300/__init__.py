@@ -82,6 +82,7 @@ def library():
     lib.gpr_launch_geometry.argtypes = [vp, vp, vp, vp, vp, vp]
     lib.gpr_stream.argtypes = [vp]
     lib.gpr_stream.restype = vp
+    lib.gpr_debug_math.argtypes = [vp, ip, vp, vp, vp, ip]
     lib.gpr_get_stats.argtypes = [vp, vp, ip]
     lib.gpr_reset_stats.argtypes = [vp]
     # host side (include/gpuropolis_host.h)
@@ -191,6 +192,15 @@ class Sampler:
         self._check(self.lib.gpr_debug_eval_values(self.h, _ptr(xs), len(xs), _ptr(out),
                                                    _ptr(length), _ptr(count)))
         return out, length, count
+
+    def math(self, op, a, b=None):
+        """The evaluator's exp ('exp'), log ('log') or pow ('pow') on the GPU."""
+        code = {"exp": 0, "log": 1, "pow": 2}[op]
+        a = np.ascontiguousarray(a, np.float32)
+        b = np.ascontiguousarray(a if b is None else b, np.float32)
+        out = np.empty_like(a)
+        self._check(self.lib.gpr_debug_math(self.h, code, _ptr(a), _ptr(b), _ptr(out), len(a)))
+        return out
 
     def launch_geometry(self):
         v = [ctypes.c_int() for _ in range(4)] + [ctypes.c_int64()]

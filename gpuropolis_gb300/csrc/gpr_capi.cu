@@ -212,9 +212,13 @@ int gpr_create(const gpr_config* cfg, int n_chains, gpr_handle** out) {
     kp.next_chain = h->dcounter;
     kp.err = h->dcounter + 1;
     kp.stats = h->dstats;
+    kp.lockstep = getenv("GPR_LOCKSTEP") ? atoi(getenv("GPR_LOCKSTEP")) : 1;
     kp.max_instr = GPR_MAX_INSTR(PL);
+    /* Value-stack depth: a push happens at a binary node whose children are
+     * both subtrees, so at a node j <= PL/2; pending pushes lie on one
+     * root-to-node path, at most floor(log2(PL/2)) + 1 of them. */
     int lev = 1;
-    while ((1 << lev) <= PL) ++lev;   /* heap levels: pending pushes never exceed this */
+    while ((1 << lev) <= PL / 2) ++lev;
     kp.levels = lev;
     gpr::fill_lcg_jump_table(kp);
     *out = h;
@@ -398,6 +402,25 @@ done:
     if (e != cudaSuccess) rc = fail(h, GPR_ERR_CUDA, "gpr_debug_eval_values: %s", cudaGetErrorString(e));
     cudaFree(dxs); cudaFree(dout); cudaFree(dlen); cudaFree(dcnt);
     return rc;
+}
+
+int gpr_debug_math(gpr_handle* h, int op, const float* a, const float* b, float* out, int n) {
+    if (!h || n < 0 || op < 0 || op > 2 || (n > 0 && (!a || !out || (op == 2 && !b))))
+        return fail(h, GPR_ERR_ARG, "bad arguments");
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    float* d = nullptr;
+    const size_t bytes = (size_t)(n + 1) * sizeof(float);
+    CUDA_TRY(h, cudaMalloc(&d, 3 * bytes));
+    float *da = d, *db = d + (n + 1), *dout = d + 2 * (size_t)(n + 1);
+    cudaError_t e = cudaMemcpyAsync(da, a, (size_t)n * sizeof(float), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess && op == 2)
+        e = cudaMemcpyAsync(db, b, (size_t)n * sizeof(float), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = gpr::launch_math(op, da, db, dout, n, h->stream);
+    if (e == cudaSuccess) { h->launches++; e = cudaMemcpyAsync(out, dout, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, h->stream); }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return fail(h, GPR_ERR_CUDA, "gpr_debug_math: %s", cudaGetErrorString(e));
+    return GPR_OK;
 }
 
 int gpr_launch_geometry(gpr_handle* h, int* K, int* onepass, int* warps_per_cta, int* ctas, int64_t* smem) {

@@ -63,7 +63,6 @@ enum gpr_icode {
     I_END = 0,
     I_LDX = 1, I_LDC = 2, I_LD1 = 3, I_PUSH = 4, I_LDNAN = 5,
     U_INV = 8, U_LOG, U_EXP, U_SQRT, U_SIN, U_ASIN, U_COS, U_ACOS, U_TAN, U_ATAN, U_ABS,
-    U_CPLUS, U_CTIMES, U_CPOW, U_CRPOW,
     I_BIN0 = 32   /* 32 + bop*8 + accleft*4 + src */
 };
 enum gpr_bop { BOP_ADD = 0, BOP_SUB = 1, BOP_MUL = 2, BOP_DIV = 3, BOP_POW = 4 };

@@ -93,4 +93,21 @@ cudaError_t launch_eval_values(const KParams& p, const float* xs, int nx, float*
     return cudaGetLastError();
 }
 
+/* Diagnostics: the evaluator's exp (op 0), log (1), pow (2) elementwise. */
+__global__ void math_kernel(int op, const float* a, const float* b, float* out, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float r;
+    if (op == 0) r = gx_exp(a[i]);
+    else if (op == 1) r = gx_log(a[i]);
+    else r = gx_pow(a[i], b[i]);
+    out[i] = r;
+}
+
+cudaError_t launch_math(int op, const float* a, const float* b, float* out, int n, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    math_kernel<<<(n + 255) / 256, 256, 0, st>>>(op, a, b, out, n);
+    return cudaGetLastError();
+}
+
 }  // namespace gpr

@@ -63,6 +63,7 @@ struct KParams {
     int* next_chain;   /* dynamic chain counter (zeroed before launch)          */
     int* err;          /* device error flags                                    */
     unsigned long long* stats;  /* GPR_STAT_* counters, accumulated per launch  */
+    int lockstep;      /* 1: the warps of a CTA step their chains in lockstep     */
     int levels;        /* value-stack slots per lane                            */
     int max_instr;     /* instruction buffer length per program                 */
 
@@ -98,6 +99,8 @@ cudaError_t mh_occupancy(const KParams& p, int K, int onepass, int warps_per_cta
  * compiled length / node count (used by the parity tests). */
 cudaError_t launch_eval_values(const KParams& p, const float* xs, int nx, float* out,
                                float* length, int* count, cudaStream_t st);
+
+cudaError_t launch_math(int op, const float* a, const float* b, float* out, int n, cudaStream_t st);
 
 }  // namespace gpr
 

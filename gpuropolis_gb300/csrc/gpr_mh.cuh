@@ -31,6 +31,7 @@
 #include "gpr_rngmath.h"
 #include "gpr_philox.h"
 #include "gpr_kernels.cuh"
+#include "gpr_fastmath.cuh"
 
 namespace gpr {
 
@@ -222,8 +223,7 @@ __device__ __forceinline__ int unary_code(int o) {
         case OP_INV: return U_INV;   case OP_LOG: return U_LOG;   case OP_EXP: return U_EXP;
         case OP_SQRT: return U_SQRT; case OP_SIN: return U_SIN;   case OP_ASIN: return U_ASIN;
         case OP_COS: return U_COS;   case OP_ACOS: return U_ACOS; case OP_TAN: return U_TAN;
-        case OP_ATAN: return U_ATAN; case OP_ABS: return U_ABS;   case OP_CPLUS: return U_CPLUS;
-        case OP_CTIMES: return U_CTIMES; case OP_CPOW: return U_CPOW; default: return U_CRPOW;
+        case OP_ATAN: return U_ATAN; default: return U_ABS;
     }
 }
 /* base op and operand order of a binary heap op: value = bop(u, v) with
@@ -260,7 +260,15 @@ static __device__ __noinline__ CompileOut compile_program(const uint8_t* ops, in
         int o = ops[j - 1];
         int cls = gpr_op_class(o);
         if (cls == CLS_UNARY || cls == CLS_CUNARY) {
-            uint32_t ui = (uint32_t)unary_code(o) | ((uint32_t)(j - 1) << 8);
+            /* the C-ops are binary ops with the node's constant as one operand:
+             * CPLUS a+C, CTIMES C*a, CPOW a^C, CRPOW C^a (main.cu:405-425) */
+            uint32_t ui;
+            if (o == OP_CPLUS) ui = GPR_BIN(BOP_ADD, 1, SRC_C);
+            else if (o == OP_CTIMES) ui = GPR_BIN(BOP_MUL, 1, SRC_C);
+            else if (o == OP_CPOW) ui = GPR_BIN(BOP_POW, 1, SRC_C);
+            else if (o == OP_CRPOW) ui = GPR_BIN(BOP_POW, 0, SRC_C);
+            else ui = (uint32_t)unary_code(o);
+            ui |= ((uint32_t)(j - 1) << 8);
             if (ph == 0) {
                 out.count += 1;
                 out.length += (cls == CLS_CUNARY) ? 2.0f : 1.0f;
@@ -329,45 +337,37 @@ static __device__ __noinline__ CompileOut compile_program(const uint8_t* ops, in
 /* ------------------------------------------------------------------------ */
 /* The evaluator: acc[k] = f(x[k]) for this lane's K points.
  *
- * Cheap ops (loads, push/pop, + - * /, abs, the C-ops + and *) run unrolled
- * over the K values in registers.  Transcendental ops and pow run through one
- * non-unrolled loop over the K values staged in the warp's shared scratch, so
- * the kernel carries a single copy of each math routine: with every warp of an
- * SM executing a different program, instruction-cache footprint, not FP32
- * throughput, is what limits an unrolled interpreter. */
-enum gpr_xop { XOP_LOG, XOP_EXP, XOP_SQRT, XOP_SIN, XOP_ASIN, XOP_COS, XOP_ACOS, XOP_TAN, XOP_ATAN,
-               XOP_CPOW, XOP_CRPOW, XOP_POW };
+ * Arithmetic, exp, log, pow and sqrt run unrolled over the K values in
+ * registers, with the compact routines of gpr_fastmath.cuh.  The trigonometric
+ * ops (CUDA's math library, with large-argument reduction paths) run through
+ * one non-unrolled loop over the K values staged in the warp's shared scratch,
+ * so the kernel carries a single copy of each: with every warp of an SM
+ * executing a different program, instruction-cache footprint, not FP32
+ * throughput, limits an interpreter. */
+enum gpr_xop { XOP_SIN, XOP_ASIN, XOP_COS, XOP_ACOS, XOP_TAN, XOP_ATAN };
 
 __device__ __forceinline__ int xop_of_unary(uint32_t code) {
     switch (code) {
-        case U_LOG: return XOP_LOG;   case U_EXP: return XOP_EXP;   case U_SQRT: return XOP_SQRT;
         case U_SIN: return XOP_SIN;   case U_ASIN: return XOP_ASIN; case U_COS: return XOP_COS;
         case U_ACOS: return XOP_ACOS; case U_TAN: return XOP_TAN;   case U_ATAN: return XOP_ATAN;
-        case U_CPOW: return XOP_CPOW; case U_CRPOW: return XOP_CRPOW;
         default: return -1;
     }
 }
 
-/* scr[(k)*32 + lane] holds first operands, scr[(K+k)*32 + lane] second ones. */
+/* scr[k*32 + lane] holds the K operands of this lane; results replace them. */
 template <int K>
-__device__ __noinline__ void expensive_loop(float* __restrict__ scr, int xop, float c, int lane) {
+__device__ __noinline__ void expensive_loop(float* __restrict__ scr, int xop, int lane) {
 #pragma unroll 1
     for (int k = 0; k < K; ++k) {
         const float u = scr[k * 32 + lane];
         float r;
         switch (xop) {
-            case XOP_LOG: r = logf(u); break;
-            case XOP_EXP: r = expf(u); break;
-            case XOP_SQRT: r = __fsqrt_rn(u); break;
             case XOP_SIN: r = sinf(u); break;
             case XOP_ASIN: r = asinf(u); break;
             case XOP_COS: r = cosf(u); break;
             case XOP_ACOS: r = acosf(u); break;
             case XOP_TAN: r = tanf(u); break;
-            case XOP_ATAN: r = atanf(u); break;
-            case XOP_CPOW: r = powf(u, c); break;
-            case XOP_CRPOW: r = powf(c, u); break;
-            default: r = powf(u, scr[(K + k) * 32 + lane]); break;
+            default: r = atanf(u); break;
         }
         scr[k * 32 + lane] = r;
     }
@@ -409,31 +409,31 @@ __device__ __forceinline__ void run_program(const uint32_t* __restrict__ prog,
             if (bop == BOP_POW) {
 #pragma unroll
                 for (int k = 0; k < K; ++k) {
-                    scr[k * 32 + lane] = accleft ? acc[k] : v[k];
-                    scr[(K + k) * 32 + lane] = accleft ? v[k] : acc[k];
+                    const float u = accleft ? acc[k] : v[k];
+                    const float w = accleft ? v[k] : acc[k];
+                    acc[k] = gx_pow(u, w);
                 }
-                expensive_loop<K>(scr, XOP_POW, 0.0f, lane);
+            } else if (bop == BOP_ADD) {   /* commutative: operand order is irrelevant */
 #pragma unroll
-                for (int k = 0; k < K; ++k) acc[k] = scr[k * 32 + lane];
-            } else {
-                float a[K], b[K];
+                for (int k = 0; k < K; ++k) acc[k] = __fadd_rn(acc[k], v[k]);
+            } else if (bop == BOP_MUL) {
 #pragma unroll
-                for (int k = 0; k < K; ++k) {
-                    a[k] = accleft ? acc[k] : v[k];
-                    b[k] = accleft ? v[k] : acc[k];
-                }
-                if (bop == BOP_ADD) {
+                for (int k = 0; k < K; ++k) acc[k] = __fmul_rn(acc[k], v[k]);
+            } else if (bop == BOP_SUB) {
+                if (accleft) {
 #pragma unroll
-                    for (int k = 0; k < K; ++k) acc[k] = __fadd_rn(a[k], b[k]);
-                } else if (bop == BOP_SUB) {
-#pragma unroll
-                    for (int k = 0; k < K; ++k) acc[k] = __fsub_rn(a[k], b[k]);
-                } else if (bop == BOP_MUL) {
-#pragma unroll
-                    for (int k = 0; k < K; ++k) acc[k] = __fmul_rn(a[k], b[k]);
+                    for (int k = 0; k < K; ++k) acc[k] = __fsub_rn(acc[k], v[k]);
                 } else {
 #pragma unroll
-                    for (int k = 0; k < K; ++k) acc[k] = __fdiv_rn(a[k], b[k]);
+                    for (int k = 0; k < K; ++k) acc[k] = __fsub_rn(v[k], acc[k]);
+                }
+            } else {
+                if (accleft) {
+#pragma unroll
+                    for (int k = 0; k < K; ++k) acc[k] = __fdiv_rn(acc[k], v[k]);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < K; ++k) acc[k] = __fdiv_rn(v[k], acc[k]);
                 }
             }
             continue;
@@ -442,12 +442,24 @@ __device__ __forceinline__ void run_program(const uint32_t* __restrict__ prog,
         if (xop >= 0) {
 #pragma unroll
             for (int k = 0; k < K; ++k) scr[k * 32 + lane] = acc[k];
-            expensive_loop<K>(scr, xop, c, lane);
+            expensive_loop<K>(scr, xop, lane);
 #pragma unroll
             for (int k = 0; k < K; ++k) acc[k] = scr[k * 32 + lane];
             continue;
         }
         switch (code) {
+            case U_EXP:
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = gx_exp(acc[k]);
+                break;
+            case U_LOG:
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = gx_log(acc[k]);
+                break;
+            case U_SQRT:
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = __fsqrt_rn(acc[k]);
+                break;
             case I_LDX:
 #pragma unroll
                 for (int k = 0; k < K; ++k) acc[k] = x[k];
@@ -477,14 +489,6 @@ __device__ __forceinline__ void run_program(const uint32_t* __restrict__ prog,
 #pragma unroll
                 for (int k = 0; k < K; ++k) acc[k] = fabsf(acc[k]);
                 break;
-            case U_CPLUS:
-#pragma unroll
-                for (int k = 0; k < K; ++k) acc[k] = __fadd_rn(acc[k], c);
-                break;
-            case U_CTIMES:
-#pragma unroll
-                for (int k = 0; k < K; ++k) acc[k] = __fmul_rn(c, acc[k]);
-                break;
             default:
                 break;
         }
@@ -497,7 +501,9 @@ __device__ __forceinline__ float warp_sum(float v) {
     return v;
 }
 
-/* Shared-memory pointers of one warp. */
+/* Shared-memory pointers of one warp.  The constant-move records (off, ndr,
+ * fw, bw) are only live during a constant proposal, the value stack and the
+ * transcendental scratch only during an evaluation, so they share one region. */
 struct WarpSmem {
     uint8_t* ops[2];
     float* Cs[2];
@@ -512,15 +518,19 @@ struct WarpSmem {
 
 __host__ __device__ __forceinline__ size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
 
+__host__ __device__ __forceinline__ size_t shared_region_bytes(int PL, int levels, int K) {
+    const size_t eval = (size_t)(levels + 2) * K * 32 * 4;
+    const size_t cmove = 4 * align16((size_t)PL) * 4;
+    return align16(eval > cmove ? eval : cmove);
+}
+
 __host__ __device__ __forceinline__ size_t warp_smem_bytes(int PL, int max_instr, int levels, int K) {
     size_t plp = align16((size_t)PL);
     size_t b = 0;
     b += 2 * plp;                                /* ops */
     b += align16(2 * plp * 4);                   /* Cs */
     b += align16(2 * (size_t)max_instr * 4);     /* prog */
-    b += 4 * plp * 4;                            /* off, ndr, fw, bw */
-    b += (size_t)levels * K * 32 * 4;            /* stack */
-    b += (size_t)2 * K * 32 * 4;                 /* scratch */
+    b += shared_region_bytes(PL, levels, K);     /* stack + scratch | constant-move records */
     return align16(b);
 }
 
@@ -532,19 +542,19 @@ __device__ __forceinline__ WarpSmem carve_warp(uint8_t* base, int PL, int max_in
     w.ops[0] = p; w.ops[1] = p + plp; p += 2 * plp;
     w.Cs[0] = (float*)p; w.Cs[1] = (float*)p + plp; p += align16(2 * plp * 4);
     w.prog[0] = (uint32_t*)p; w.prog[1] = (uint32_t*)p + max_instr; p += align16(2 * (size_t)max_instr * 4);
-    w.off = (int*)p; p += plp * 4;
-    w.ndr = (int*)p; p += plp * 4;
-    w.fw = (float*)p; p += plp * 4;
-    w.bw = (float*)p; p += plp * 4;
     w.stk = (float*)p;
     w.scr = w.stk + (size_t)levels * K * 32;
+    w.off = (int*)p;
+    w.ndr = w.off + plp;
+    w.fw = (float*)(w.ndr + plp);
+    w.bw = w.fw + plp;
     return w;
 }
 
 /* Per-lane data of the single-pass layout (nd <= 32*K). */
 template <int K>
 struct LaneData {
-    float x[K], y[K], w[K];
+    float x[K];
     uint32_t valid;  /* bit k: point lane + 32k exists */
 };
 
@@ -563,22 +573,19 @@ __device__ __forceinline__ df eval_loglik(const uint32_t* prog, const float* Cs,
 #pragma unroll 1
     for (int pass = 0; pass < npass; ++pass) {
         float x[K], acc[K];
-        float yv[K], wv[K];
         uint32_t valid;
+        const int base = pass * 32 * K + lane;
         if (ONEPASS) {
 #pragma unroll
-            for (int k = 0; k < K; ++k) { x[k] = ld.x[k]; yv[k] = ld.y[k]; wv[k] = ld.w[k]; }
+            for (int k = 0; k < K; ++k) x[k] = ld.x[k];
             valid = ld.valid;
         } else {
             valid = 0u;
-            const int base = pass * 32 * K + lane;
 #pragma unroll
             for (int k = 0; k < K; ++k) {
                 int i = base + 32 * k;
                 bool v = i < p.nd;
                 x[k] = v ? sx[i] : 0.0f;
-                yv[k] = v ? sy[i] : 0.0f;
-                wv[k] = v ? sw[i] : 0.0f;
                 valid |= (v ? 1u : 0u) << k;
             }
         }
@@ -587,10 +594,11 @@ __device__ __forceinline__ df eval_loglik(const uint32_t* prog, const float* Cs,
 #pragma unroll
         for (int k = 0; k < K; ++k) {
             if (valid & (1u << k)) {
-                float r = __fsub_rn(acc[k], yv[k]);
+                const int i = base + 32 * k;
+                float r = __fsub_rn(acc[k], sy[i]);
                 float q = __fmul_rn(r, r);
                 bad |= !(q <= FLT_MAX);
-                s = fmaf(q, wv[k], s);
+                s = fmaf(q, sw[i], s);
             }
         }
         if (__any_sync(FULLMASK, bad)) return df_make(-INFINITY, 0.0f);
@@ -607,7 +615,7 @@ __device__ __forceinline__ df cauchy_sum(const float* Cs, const KParams& p, int 
     for (int c = lane; c < p.PL; c += 32) {
         float x = Cs[c];
         float a = __fadd_rn(1.0f, __fmul_rn(x, x));
-        s = df_add(s, df_make(__fmul_rn(__fsub_rn(-p.lpi_f, logf(a)), GPR_DF_SCALE), 0.0f));
+        s = df_add(s, df_make(__fmul_rn(__fsub_rn(-p.lpi_f, gx_log(a)), GPR_DF_SCALE), 0.0f));
     }
     return warp_sum_df(s);
 }
@@ -652,7 +660,7 @@ __device__ __forceinline__ void propose_constant(Rng& r, float old, float& nc, f
         if (is_int_ref(old)) {
             float bg = __fadd_rn(__fadd_rn(lgeom_plus1(old, p), (nc == 0.0f) ? 0.0f : p.log2_f), p.logpi_f);
             float m = fmaxf(bg, bn);
-            dbw = logf(expf(bg - m) + expf(bn - m)) + m;
+            dbw = gx_log(gx_exp(bg - m) + gx_exp(bn - m)) + m;
         } else {
             dbw = bn;
         }
@@ -712,6 +720,7 @@ __device__ void constant_move(Rng& r, const WarpSmem& w, const float* Cold, floa
     if (!converged && lane == 0) atomicOr(p.err, 2);
     __syncwarp();
     df f = df_make(0.0f, 0.0f), b = df_make(0.0f, 0.0f);
+    if (p.const_mode != 0) { fw_sum = f; bw_sum = b; return; }   /* random walk: symmetric, no terms */
     for (int c = lane; c < PL; c += 32) {
         f = df_add(f, df_make(__fmul_rn(w.fw[c], GPR_DF_SCALE), 0.0f));
         b = df_add(b, df_make(__fmul_rn(w.bw[c], GPR_DF_SCALE), 0.0f));
@@ -772,7 +781,7 @@ __device__ __forceinline__ bool mh_accept(df ppost, df cur_post, df backward, df
 }
 
 template <int K, bool ONEPASS, int RNG>
-__global__ void __launch_bounds__(256) mh_block_kernel(const __grid_constant__ KParams p) {
+__global__ void __launch_bounds__(256, 3) mh_block_kernel(const __grid_constant__ KParams p) {
     extern __shared__ __align__(128) uint8_t smem[];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -796,21 +805,35 @@ __global__ void __launch_bounds__(256) mh_block_kernel(const __grid_constant__ K
             int i = lane + 32 * k;
             bool v = i < p.nd;
             ld.x[k] = v ? sx[i] : 0.0f;
-            ld.y[k] = v ? sy[i] : 0.0f;
-            ld.w[k] = v ? sw[i] : 0.0f;
             ld.valid |= (v ? 1u : 0u) << k;
         }
     }
     const int PL = p.PL;
 
+    __shared__ int s_group_base;
+    const int nwarps = blockDim.x >> 5;
+
 #pragma unroll 1
     for (;;) {
         int chain = 0;
-        if (lane == 0) chain = atomicAdd(p.next_chain, 1);
-        chain = __shfl_sync(FULLMASK, chain, 0);
-        if (chain >= p.N) break;
+        if (p.lockstep) {
+            /* CTA-wide chain groups: every warp of the CTA runs the same step at
+             * the same time, so the warps share instruction-cache lines */
+            __syncthreads();
+            if (threadIdx.x == 0) s_group_base = atomicAdd(p.next_chain, nwarps);
+            __syncthreads();
+            const int base = s_group_base;
+            if (base >= p.N) break;
+            chain = base + warp;
+        } else {
+            if (lane == 0) chain = atomicAdd(p.next_chain, 1);
+            chain = __shfl_sync(FULLMASK, chain, 0);
+            if (chain >= p.N) break;
+        }
+        const bool active = chain < p.N;
 
         /* load the chain (reference layout) into buffer 0 */
+        if (active)
         for (int i = lane; i < PL; i += 32) {
             int o = p.P[(size_t)i * p.N + chain];
             ws.ops[0][i] = (uint8_t)((o >= 0 && o < OP_NREF) ? o : 255);
@@ -839,6 +862,8 @@ __global__ void __launch_bounds__(256) mh_block_kernel(const __grid_constant__ K
          * compile, prior and likelihood keeps the kernel's hot code small. */
 #pragma unroll 1
         for (int step = -1; step < p.steps; ++step) {
+          if (p.lockstep) __syncthreads();
+          if (active) {
             const bool init = step < 0;
             const bool structural = !init && (step % 5 == 0);
             int pbuf = cur, cbuf = ccur;
@@ -904,15 +929,17 @@ __global__ void __launch_bounds__(256) mh_block_kernel(const __grid_constant__ K
                 cur_prior = prior; cur_lik = lik; cur_post = post;
             }
             __syncwarp();
+          }
         }
 
         /* write back (main.cu:811-812 and the in-place P, C) */
+        if (active)
         for (int i = lane; i < PL; i += 32) {
             uint8_t o = ws.ops[cur][i];
             if (o != 255) p.P[(size_t)i * p.N + chain] = (int32_t)o;
             p.C[(size_t)i * p.N + chain] = ws.Cs[ccur][i];
         }
-        if (lane == 0) {
+        if (active && lane == 0) {
             p.prior[chain] = df_to_double_unscaled(cur_prior);
             p.lik[chain] = df_to_double_unscaled(cur_lik);
             if (p.stats) {

@@ -67,10 +67,16 @@ GPR_HD float gpr_u2f(uint32_t u) {
 #endif
 }
 
-/* float((double)k / 1e6) for 0 <= k <= 10^6: the correctly rounded float
- * quotient equals the double-rounded one for every k in range (exhaustive). */
+/* float((double)k / 1e6) for 0 <= k <= 10^6.  The correctly rounded float
+ * quotient equals the double-rounded one for every k in range, and one FMA
+ * correction of k * float(1e-6) equals the correctly rounded quotient for
+ * every k in range (both checked exhaustively), so no division is needed. */
 GPR_HD float gpr_rng_k_over_1e6(int k) {
-    return GPR_FDIV((float)k, 1000000.0f);
+    const float kf = (float)k;
+    const float r = 9.99999997475242708e-07f;      /* float(1e-6) */
+    const float q = GPR_FMUL(kf, r);
+    const float e = GPR_FMA(-q, 1000000.0f, kf);
+    return GPR_FMA(e, r, q);
 }
 
 /* float(6.283185307178 * (double)v), i.e. the argument the reference passes to

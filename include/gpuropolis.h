@@ -120,6 +120,10 @@ const char* gpr_version(void);
 int gpr_debug_eval_values(gpr_handle* h, const float* xs, int nx, float* out, float* length,
                           int* count);
 
+/* The evaluator's exp (op 0), log (op 1) and pow (op 2, second operand b)
+ * applied elementwise to n host values (for accuracy tests against FP64). */
+int gpr_debug_math(gpr_handle* h, int op, const float* a, const float* b, float* out, int n);
+
 /* Launch geometry chosen for the current dataset: points per lane K, whether
  * the data stay in registers (onepass), warps per CTA, CTAs, shared bytes. */
 int gpr_launch_geometry(gpr_handle* h, int* K, int* onepass, int* warps_per_cta, int* ctas,

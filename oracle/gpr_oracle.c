@@ -15,6 +15,9 @@
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
+#if defined(_OPENMP)
+#include <omp.h>
+#endif
 
 #include "../gpuropolis_gb300/csrc/gpr_philox.h"
 #include "../gpuropolis_gb300/csrc/gpr_rngmath.h"
@@ -260,8 +263,20 @@ static int port_is_descendant(int n, int k) {
 static int port_valid(double v) { return !(isnan(v) || !isfinite(v)); }
 
 /* One chain for `steps` MH steps: MH_simple_kernel (main.cu:679-813). */
+/* trace (optional): per step GPR_TRACE doubles -- proposal posterior, current
+ * posterior, acceptance log-ratio, the uniform draw (-1 when none was drawn),
+ * the decision (1 accept, 0 reject), and the conditioning of the proposal's
+ * and of the current state's FP32 log-likelihood: |L32 - L64| / max(|L64|, 1)
+ * with L64 the same program evaluated and summed in FP64 (inf when exactly one
+ * of them is finite). */
+#define GPR_TRACE 8
+static double port_cond(double l32, double l64) {
+    if (isfinite(l32) != isfinite(l64)) return INFINITY;
+    if (!isfinite(l32)) return 0.0;
+    return fabs(l32 - l64) / (fabs(l64) > 1.0 ? fabs(l64) : 1.0);
+}
 static void mh_chain(const port_cfg* cfg, int N, int idx, int32_t* P, float* C, const float* D, int nd,
-                     int steps, double* prior_out, double* lik_out, int random_seed) {
+                     int steps, double* prior_out, double* lik_out, int random_seed, double* trace) {
     const int PL = cfg->program_length;
     const int pm = cfg->project_math;
     double cur_prior = gpr_port_prior(P, C, N, PL, idx, cfg->n_ops);
@@ -274,6 +289,7 @@ static void mh_chain(const port_cfg* cfg, int N, int idx, int32_t* P, float* C, 
     int32_t old_program[256];
     float old_C[256];
     double forward = 0.0, backward = 0.0;
+    double cond_cur = trace ? port_cond(cur_lik, gpr_port_likelihood_f64(P, C, N, PL, idx, D, nd)) : 0.0;
     for (int step = 0; step < steps; step++) {
         if (step % 5 == 0) {
             forward = -(double)logf((float)count_node(P, N, PL, idx, 1));
@@ -287,7 +303,22 @@ static void mh_chain(const port_cfg* cfg, int N, int idx, int32_t* P, float* C, 
             double pl = gpr_port_likelihood(P, C, N, PL, idx, D, nd);
             double post = pp + pl;
             double acc = post - cur_post + backward - forward;
-            if ((port_valid(post) && (acc > 0.0 || port_random_float(&r) < expf((float)acc))) || !port_valid(cur_post)) {
+            double udraw = -1.0;
+            int accept = 0;
+            if (port_valid(post)) {
+                if (acc > 0.0) accept = 1;
+                else { float u = port_random_float(&r); udraw = u; accept = u < expf((float)acc); }
+            }
+            if (!port_valid(cur_post)) accept = 1;
+            double cond_prop = 0.0;
+            if (trace) {
+                cond_prop = port_cond(pl, gpr_port_likelihood_f64(P, C, N, PL, idx, D, nd));
+                double* t = trace + GPR_TRACE * (size_t)step;
+                t[0] = post; t[1] = cur_post; t[2] = acc; t[3] = udraw; t[4] = accept;
+                t[5] = cond_prop; t[6] = cond_cur; t[7] = 0.0;
+            }
+            if (accept) cond_cur = cond_prop;
+            if (accept) {
                 cur_post = post; cur_lik = pl; cur_prior = pp;
             } else {
                 for (int i = n; i < PL; i++) P[(size_t)i * N + idx] = old_program[i];
@@ -325,7 +356,22 @@ static void mh_chain(const port_cfg* cfg, int N, int idx, int32_t* P, float* C, 
             double pl = gpr_port_likelihood(P, C, N, PL, idx, D, nd);
             double post = pp + pl;
             double acc = post - cur_post + backward - forward;
-            if ((port_valid(post) && (acc > 0.0 || port_random_float(&r) < expf((float)acc))) || !port_valid(cur_post)) {
+            double udraw = -1.0;
+            int accept = 0;
+            if (port_valid(post)) {
+                if (acc > 0.0) accept = 1;
+                else { float u = port_random_float(&r); udraw = u; accept = u < expf((float)acc); }
+            }
+            if (!port_valid(cur_post)) accept = 1;
+            double cond_prop = 0.0;
+            if (trace) {
+                cond_prop = port_cond(pl, gpr_port_likelihood_f64(P, C, N, PL, idx, D, nd));
+                double* t = trace + GPR_TRACE * (size_t)step;
+                t[0] = post; t[1] = cur_post; t[2] = acc; t[3] = udraw; t[4] = accept;
+                t[5] = cond_prop; t[6] = cond_cur; t[7] = 0.0;
+            }
+            if (accept) cond_cur = cond_prop;
+            if (accept) {
                 cur_post = post; cur_lik = pl; cur_prior = pp;
             } else {
                 for (int c = 0; c < PL; c++) C[(size_t)c * N + idx] = old_C[c];
@@ -343,7 +389,18 @@ void gpr_port_run_block(const port_cfg* cfg, int N, int c0, int c1, int32_t* P, 
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #pragma omp parallel for schedule(dynamic, 1)
 #endif
-    for (int idx = c0; idx < c1; idx++) mh_chain(cfg, N, idx, P, C, D, nd, steps, prior, lik, random_seed);
+    for (int idx = c0; idx < c1; idx++) mh_chain(cfg, N, idx, P, C, D, nd, steps, prior, lik, random_seed, NULL);
+}
+
+/* The same with a per-chain, per-step trace: trace[(idx * steps + step) * 5 + k]. */
+void gpr_port_run_block_trace(const port_cfg* cfg, int N, int32_t* P, float* C, const float* D, int nd, int steps,
+                              double* prior, double* lik, int random_seed, double* trace, int nthreads) {
+#if defined(_OPENMP)
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+    for (int idx = 0; idx < N; idx++)
+        mh_chain(cfg, N, idx, P, C, D, nd, steps, prior, lik, random_seed, trace + (size_t)idx * steps * GPR_TRACE);
 }
 
 int gpr_port_sizeof_cfg(void) { return (int)sizeof(port_cfg); }

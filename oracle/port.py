@@ -35,6 +35,7 @@ def lib():
         L.gpr_port_likelihood_f64.argtypes = [vp, vp, ip, ip, ip, vp, ip]
         L.gpr_port_likelihood_f64.restype = dp
         L.gpr_port_run_block.argtypes = [ctypes.POINTER(PortCfg), ip, ip, ip, vp, vp, vp, ip, ip, vp, vp, ip, ip]
+        L.gpr_port_run_block_trace.argtypes = [ctypes.POINTER(PortCfg), ip, vp, vp, vp, ip, ip, vp, vp, ip, vp, ip]
         assert L.gpr_port_sizeof_cfg() == ctypes.sizeof(PortCfg)
         _lib = L
     return _lib
@@ -71,6 +72,20 @@ def run_block(c, P, C, x, y, sd, steps, seed, nthreads=0, chains=None):
     lib().gpr_port_run_block(ctypes.byref(c), N, c0, c1, _p(P), _p(C), _p(D), len(x), steps, _p(prior),
                              _p(lik), int(seed), nthreads)
     return prior, lik
+
+
+def run_block_trace(c, P, C, x, y, sd, steps, seed, nthreads=0):
+    """run_block over all chains, also returning trace[N, steps, 8] =
+    (proposal posterior, current posterior, acceptance, uniform or -1, accepted,
+    conditioning of the proposal's and of the current FP32 log-likelihood)."""
+    PL, N = P.shape
+    D = pack(x, y, sd)
+    prior = np.zeros(N)
+    lik = np.zeros(N)
+    tr = np.zeros((N, max(steps, 1), 8))
+    lib().gpr_port_run_block_trace(ctypes.byref(c), N, _p(P), _p(C), _p(D), len(x), steps, _p(prior), _p(lik),
+                                   int(seed), _p(tr), nthreads)
+    return prior, lik, tr
 
 
 def call(P, C, idx, x):

@@ -47,11 +47,21 @@ def test_eval_values_match_reference(lib, PL):
     rcnt = np.array([o.count_nodes(P, C, i) for i in range(N)], np.int32)
     np.testing.assert_array_equal(length, rlen)
     np.testing.assert_array_equal(count, rcnt)
+    from oracle import port
+    f64 = np.array([[port.call_f64(P, C, i, xv) for xv in xs] for i in range(N)])
+    with np.errstate(all="ignore"):
+        # how far the reference's own FP32 value is from FP64: the problem's conditioning
+        cond = np.where(np.isfinite(ref) & np.isfinite(f64),
+                        np.abs(ref.astype(np.float64) - f64) / np.maximum(np.abs(f64), 1e-30), np.inf)
+    edge = ~np.isfinite(f64) | (np.abs(f64) > 1e37) | (cond > 1e-6)
     cls = H.same_class(out, ref)
-    assert cls.mean() > 0.995, "finite/non-finite class differs on %.4f of points" % (1 - cls.mean())
+    assert np.all(cls | edge), np.argwhere(~(cls | edge))[:5]
     both = np.isfinite(out) & np.isfinite(ref)
-    rel = H.rel_err(out[both], ref[both], floor=1e-30)
-    assert np.mean(rel <= 1e-5) > 0.995, np.sort(rel)[-10:]
+    rel = np.zeros_like(cond)
+    rel[both] = H.rel_err(out[both], ref[both], floor=1e-30)
+    bad = both & (rel > 1e-5) & ~edge
+    assert not bad.any(), [(tuple(ix), rel[tuple(ix)], cond[tuple(ix)]) for ix in np.argwhere(bad)[:5]]
+    assert both.mean() > 0.2
     s.close()
 
 
@@ -71,11 +81,20 @@ def test_prior_likelihood_match_reference(lib, data):
     assert np.all(H.same_class(prior, rprior))
     fin = np.isfinite(rprior)
     assert H.rel_err(prior[fin], rprior[fin]).max() <= 1e-5
-    assert H.same_class(lik, rlik).mean() > 0.995
+    from oracle import port
+    f64 = np.array([port.likelihood(P, C, i, x, y, sd, f64=True) for i in range(N)])
+    with np.errstate(all="ignore"):
+        cond = np.where(np.isfinite(rlik) & np.isfinite(f64),
+                        np.abs(rlik - f64) / np.maximum(np.abs(f64), 1.0), np.inf)
+    edge = ~np.isfinite(f64) | (cond > 1e-6)
+    cls = H.same_class(lik, rlik)
+    assert np.all(cls | edge)
     fin = np.isfinite(lik) & np.isfinite(rlik)
     assert fin.sum() > N // 10
-    rel = H.rel_err(lik[fin], rlik[fin])
-    assert np.mean(rel <= 1e-5) > 0.99, np.sort(rel)[-10:]
+    rel = np.zeros(N)
+    rel[fin] = H.rel_err(lik[fin], rlik[fin])
+    bad = fin & (rel > 1e-5) & ~edge
+    assert not bad.any(), list(zip(np.where(bad)[0][:5], rel[bad][:5], cond[bad][:5]))
     s.close()
 
 
@@ -89,10 +108,32 @@ CASES = [
 ]
 
 
+def _fragile(tr):
+    """True when an accept decision of the reference (one trace record of the C
+    restatement, which is bit-identical to the reference) is not determined by
+    FP32 arithmetic: the acceptance sits within the evaluation noise of its
+    threshold (acceptance > 0, or u < exp(acceptance)).  The noise is 1e-5 of
+    the posteriors' magnitude plus, for programs whose FP32 log-likelihood is
+    itself ill-conditioned, 30x its measured distance from FP64."""
+    post, cur, acc, u, _, cond_p, cond_c, _ = tr
+    if not np.isfinite(cond_p) or not np.isfinite(cond_c):
+        return True           # validity itself depends on FP32 rounding
+    if not (np.isfinite(post) and np.isfinite(cur)):
+        return False
+    noise = 1e-5 * (abs(post) + abs(cur)) + 30 * (cond_p * max(abs(post), 1) + cond_c * max(abs(cur), 1)) + 1e-4
+    if u < 0:
+        return abs(acc) <= noise
+    return abs(np.log(max(u, 1e-30)) - acc) <= noise or abs(acc) <= noise
+
+
 @pytest.mark.parametrize("case", CASES, ids=lambda c: "pl%d-%s-%s-%s" % (
     c[0], "basic" if c[1] else "ref", "philox" if c[2] else "lcg", "rw" if c[3] else "indep"))
 def test_mh_block_matches_reference(lib, case):
+    """After a block, chains are bit-identical to the reference's; every chain
+    that is not first departs at an accept decision that lies within FP32
+    noise of its threshold (the proposals themselves are bit-exact)."""
     _need_ref()
+    from oracle import port
     PL, ops, rng, cmode, rw_sd, data = case
     N, steps, seed = 1024, 25, 987654
     x, y, sd = H.quad_data() if data == "quad" else H.expdecay_data()
@@ -107,9 +148,37 @@ def test_mh_block_matches_reference(lib, case):
     Pr, Cr = P.copy(), C.copy()
     prior_r, lik_r = o.run_kernel(Pr, Cr, x, y, sd, steps, seed)
     same = np.all(Pg == Pr, axis=0) & np.all(Cg.view(np.int32) == Cr.view(np.int32), axis=0)
-    assert same.mean() >= 0.98, "bit-identical chains: %.4f" % same.mean()
+    assert same.mean() >= 0.9, "bit-identical chains: %.4f" % same.mean()
+
+    # every divergence starts at a fragile decision of the reference
+    c = port.cfg(PL, ops=o.ops, rng=int(rng == g.RNG_PHILOX), const_mode=cmode, rw_sd=rw_sd, project_math=1)
+    _, _, trace = port.run_block_trace(c, P.copy(), C.copy(), x, y, sd, steps, seed)
+    first = np.full(N, -1)
+    pending = ~same
+    for st in range(1, steps + 1):
+        if not pending.any():
+            break
+        s.set_state(P, C)
+        s.run_block(st, seed)
+        Pd, Cd, _, _ = s.get_state()
+        Pp, Cp = P.copy(), C.copy()
+        port.run_block(c, Pp, Cp, x, y, sd, st, seed)
+        differ = ~(np.all(Pd == Pp, axis=0) & np.all(Cd.view(np.int32) == Cp.view(np.int32), axis=0))
+        newly = pending & differ
+        first[newly] = st - 1
+        pending &= ~differ
+    unexplained = [i for i in np.where(~same)[0] if first[i] < 0 or not _fragile(trace[i, first[i]])]
+    assert not unexplained, [(i, first[i], trace[i, max(first[i], 0)]) for i in unexplained[:5]]
+
+    # scores of identical chains: 1e-5 relative, unless the FP32 value itself
+    # is ill-conditioned (the reference's FP32 result sits further than 1e-6
+    # from the FP64 evaluation of the same program)
     ok = same & np.isfinite(lik_r) & np.isfinite(prior_r)
     assert H.rel_err(prior_g[ok], prior_r[ok]).max() <= 1e-5
-    rel = H.rel_err(lik_g[ok], lik_r[ok])
-    assert np.mean(rel <= 1e-5) > 0.99
+    idx = np.where(ok)[0]
+    f64 = np.array([port.likelihood(Pr, Cr, i, x, y, sd, f64=True) for i in idx])
+    cond = np.abs(lik_r[idx] - f64) / np.maximum(np.abs(f64), 1.0)
+    rel = H.rel_err(lik_g[idx], lik_r[idx])
+    bad = (rel > 1e-5) & (cond <= 1e-6)
+    assert not bad.any(), list(zip(idx[bad][:5], rel[bad][:5], cond[bad][:5]))
     s.close()
