@@ -200,10 +200,11 @@ def run_gpu(args, w):
         resample_host(P, C, prior, lik, w["map_delta"], ops, hostrng)
         s.set_state(P, C)
 
-    # warm-up blocks (untimed)
+    # warm-up blocks (untimed), then the layout autotuner on the warmed state
     for i in range(args.warmup):
         block(i)
         resample()
+    tuned = s.autotune(steps=100, seed=4242)
     torch.cuda.synchronize()
     s.reset_stats()
     launches0 = s.launch_count()
@@ -287,7 +288,7 @@ def run_gpu(args, w):
         "config": {"workload": args.workload, **{k: w[k] for k in ("N", "PL", "nd", "mh_steps", "map_delta")},
                    "ops": w["ops"], "const_proposal": "rw:%g" % w["rw_sd"], "rng": "lcg",
                    "l2": "flushed between blocks (256 MB write)", "parallelism": "replicas" if world > 1 else "1 GPU",
-                   "launch": geo},
+                   "launch": geo, "autotuned": tuned},
         "e2e": {"value": e2e_value, "unit": "chain-steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "blocks": e2e_blocks},
         "gpu_launches": launches,

@@ -83,6 +83,9 @@ def library():
     lib.gpr_stream.argtypes = [vp]
     lib.gpr_stream.restype = vp
     lib.gpr_debug_math.argtypes = [vp, ip, vp, vp, vp, ip]
+    lib.gpr_autotune.argtypes = [vp, ip, ip, vp, vp, vp, vp]
+    lib.gpr_set_layout.argtypes = [vp, ip, ip, ip]
+    lib.gpr_layout_rolled.argtypes = [vp]
     lib.gpr_get_stats.argtypes = [vp, vp, ip]
     lib.gpr_reset_stats.argtypes = [vp]
     # host side (include/gpuropolis_host.h)
@@ -202,11 +205,22 @@ class Sampler:
         self._check(self.lib.gpr_debug_math(self.h, code, _ptr(a), _ptr(b), _ptr(out), len(a)))
         return out
 
+    def autotune(self, steps=50, seed=1):
+        """Pick the fastest evaluation layout on the current state and data."""
+        k, op, ro = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        ms = ctypes.c_float()
+        self._check(self.lib.gpr_autotune(self.h, steps, seed, ctypes.byref(k), ctypes.byref(op),
+                                          ctypes.byref(ro), ctypes.byref(ms)))
+        return dict(K=k.value, onepass=op.value, rolled=ro.value, ms=ms.value)
+
+    def set_layout(self, K, onepass, rolled):
+        self._check(self.lib.gpr_set_layout(self.h, K, int(onepass), int(rolled)))
+
     def launch_geometry(self):
         v = [ctypes.c_int() for _ in range(4)] + [ctypes.c_int64()]
         self._check(self.lib.gpr_launch_geometry(self.h, *[ctypes.byref(a) for a in v]))
         return dict(K=v[0].value, onepass=v[1].value, warps_per_cta=v[2].value,
-                    ctas=v[3].value, smem_bytes=v[4].value)
+                    ctas=v[3].value, smem_bytes=v[4].value, rolled=int(self.lib.gpr_layout_rolled(self.h)))
 
     STAT_NAMES = ("evals", "eval_nodes", "eval_points", "eval_node_points", "struct_proposed",
                   "struct_accepted", "const_proposed", "const_accepted")

@@ -235,12 +235,14 @@ int gpr_destroy(gpr_handle* h) {
     return GPR_OK;
 }
 
-static int choose_launch(gpr_handle* h) {
+/* Launch geometry for a given layout: K points per lane, data in registers
+ * (onepass) or streamed from shared memory, heavy ops rolled or unrolled. */
+static int configure_launch(gpr_handle* h, int K, int onepass, int rolled) {
     gpr::KParams& kp = h->kp;
     gpr::LaunchCfg lc;
-    if (kp.nd <= 128) { lc.K = 4; lc.onepass = 1; }
-    else if (kp.nd <= 256) { lc.K = 8; lc.onepass = 1; }
-    else { lc.K = 8; lc.onepass = 0; }
+    lc.K = K;
+    lc.onepass = onepass;
+    lc.rolled = rolled;
     int wpc = 8;
     size_t smem = gpr::mh_smem_bytes(kp, lc.K, wpc);
     while (smem > 227 * 1024 && wpc > 1) {
@@ -249,17 +251,24 @@ static int choose_launch(gpr_handle* h) {
     }
     if (smem > 227 * 1024)
         return fail(h, GPR_ERR_ARG, "dataset of %d points does not fit in shared memory", kp.nd);
+    lc.warps_per_cta = wpc;
+    lc.smem_bytes = smem;
     int per_sm = 0;
-    CUDA_TRY(h, gpr::mh_occupancy(kp, lc.K, lc.onepass, wpc, smem, &per_sm));
+    CUDA_TRY(h, gpr::mh_occupancy(kp, lc, &per_sm));
     if (per_sm < 1) return fail(h, GPR_ERR_ARG, "kernel cannot be resident (smem %zu)", smem);
     long long ctas = (long long)h->num_sms * per_sm;
     long long need = (h->N + wpc - 1) / wpc;
     if (ctas > need) ctas = need;
-    lc.warps_per_cta = wpc;
     lc.ctas = (int)ctas;
-    lc.smem_bytes = smem;
     h->lc = lc;
     return GPR_OK;
+}
+
+/* Default layout before any autotuning: K = 4 points per lane, one pass
+ * when the data fit, heavy ops unrolled (the fastest layout measured on the
+ * 250-point, PROGRAM_LENGTH 63 workload; gpr_autotune re-checks per dataset). */
+static int choose_launch(gpr_handle* h) {
+    return configure_launch(h, 4, h->kp.nd <= 128 ? 1 : 0, 0);
 }
 
 int gpr_set_data(gpr_handle* h, const float* x, const float* y, const float* sd, int n) {
@@ -423,6 +432,80 @@ int gpr_debug_math(gpr_handle* h, int op, const float* a, const float* b, float*
     return GPR_OK;
 }
 
+int gpr_autotune(gpr_handle* h, int steps, int seed, int* K, int* onepass, int* rolled, float* best_ms) {
+    if (!h || steps <= 0) return fail(h, GPR_ERR_ARG, "bad arguments");
+    if (h->nd < 0) return fail(h, GPR_ERR_STATE, "gpr_set_data has not been called");
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    const size_t cnt = (size_t)h->N * h->PL;
+    int32_t* sP = nullptr; float* sC = nullptr; double* sPr = nullptr; double* sLi = nullptr;
+    unsigned long long* sSt = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int rc = GPR_OK;
+    struct Cand { int K, onepass, rolled; } cands[8];
+    int nc = 0;
+    for (int Kc : {4, 8})
+        for (int op = 1; op >= 0; --op)
+            for (int ro = 0; ro <= 1; ++ro)
+                if (!op || h->nd <= 32 * Kc) cands[nc++] = {Kc, op, ro};
+    const gpr::LaunchCfg orig = h->lc;
+    float best = 1e30f;
+    gpr::LaunchCfg bestlc = orig;
+    cudaError_t e;
+#define AT_TRY(call) do { if ((e = (call)) != cudaSuccess) { rc = fail(h, GPR_ERR_CUDA, "gpr_autotune: %s: %s", #call, cudaGetErrorString(e)); goto done; } } while (0)
+    AT_TRY(cudaMalloc(&sP, cnt * sizeof(int32_t)));
+    AT_TRY(cudaMalloc(&sC, cnt * sizeof(float)));
+    AT_TRY(cudaMalloc(&sPr, h->N * sizeof(double)));
+    AT_TRY(cudaMalloc(&sLi, h->N * sizeof(double)));
+    AT_TRY(cudaMalloc(&sSt, GPR_NSTATS * sizeof(unsigned long long)));
+    AT_TRY(cudaMemcpyAsync(sP, h->dP, cnt * sizeof(int32_t), cudaMemcpyDeviceToDevice, h->stream));
+    AT_TRY(cudaMemcpyAsync(sC, h->dC, cnt * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
+    AT_TRY(cudaMemcpyAsync(sPr, h->dprior, h->N * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+    AT_TRY(cudaMemcpyAsync(sLi, h->dlik, h->N * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+    AT_TRY(cudaMemcpyAsync(sSt, h->dstats, GPR_NSTATS * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, h->stream));
+    AT_TRY(cudaEventCreate(&e0));
+    AT_TRY(cudaEventCreate(&e1));
+    for (int i = 0; i < nc; ++i) {
+        if (configure_launch(h, cands[i].K, cands[i].onepass, cands[i].rolled) != GPR_OK) continue;
+        for (int rep = 0; rep < 2; ++rep) {   /* first run warms up, second is timed */
+            AT_TRY(cudaMemcpyAsync(h->dP, sP, cnt * sizeof(int32_t), cudaMemcpyDeviceToDevice, h->stream));
+            AT_TRY(cudaMemcpyAsync(h->dC, sC, cnt * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
+            AT_TRY(cudaEventRecord(e0, h->stream));
+            if ((rc = run(h, steps, seed)) != GPR_OK) goto done;
+            AT_TRY(cudaEventRecord(e1, h->stream));
+            AT_TRY(cudaEventSynchronize(e1));
+        }
+        float ms = 0.0f;
+        AT_TRY(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best) { best = ms; bestlc = h->lc; }
+    }
+    h->lc = bestlc;
+    AT_TRY(cudaMemcpyAsync(h->dP, sP, cnt * sizeof(int32_t), cudaMemcpyDeviceToDevice, h->stream));
+    AT_TRY(cudaMemcpyAsync(h->dC, sC, cnt * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
+    AT_TRY(cudaMemcpyAsync(h->dprior, sPr, h->N * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+    AT_TRY(cudaMemcpyAsync(h->dlik, sLi, h->N * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+    AT_TRY(cudaMemcpyAsync(h->dstats, sSt, GPR_NSTATS * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, h->stream));
+    AT_TRY(cudaStreamSynchronize(h->stream));
+    if (K) *K = h->lc.K;
+    if (onepass) *onepass = h->lc.onepass;
+    if (rolled) *rolled = h->lc.rolled;
+    if (best_ms) *best_ms = best;
+#undef AT_TRY
+done:
+    if (rc != GPR_OK) h->lc = orig;
+    cudaFree(sP); cudaFree(sC); cudaFree(sPr); cudaFree(sLi); cudaFree(sSt);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    return rc;
+}
+
+int gpr_set_layout(gpr_handle* h, int K, int onepass, int rolled) {
+    if (!h) return GPR_ERR_ARG;
+    if ((K != 4 && K != 8) || (onepass && h->kp.nd > 32 * K))
+        return fail(h, GPR_ERR_ARG, "invalid layout K=%d onepass=%d for %d points", K, onepass, h->kp.nd);
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    return configure_launch(h, K, onepass ? 1 : 0, rolled ? 1 : 0);
+}
+
 int gpr_launch_geometry(gpr_handle* h, int* K, int* onepass, int* warps_per_cta, int* ctas, int64_t* smem) {
     if (!h) return GPR_ERR_ARG;
     if (K) *K = h->lc.K;
@@ -434,6 +517,8 @@ int gpr_launch_geometry(gpr_handle* h, int* K, int* onepass, int* warps_per_cta,
 }
 
 void* gpr_stream(gpr_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+int gpr_layout_rolled(gpr_handle* h) { return h ? h->lc.rolled : 0; }
 
 int gpr_get_stats(gpr_handle* h, uint64_t* out, int n) {
     if (!h || !out || n < 0) return GPR_ERR_ARG;

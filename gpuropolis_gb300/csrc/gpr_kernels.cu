@@ -13,10 +13,9 @@ size_t mh_smem_bytes(const KParams& p, int K, int warps_per_cta) {
            (size_t)warps_per_cta * warp_smem_bytes(p.PL, p.max_instr, p.levels, K);
 }
 
-static const void* pick_kernel(int K, int onepass, int rng) {
-    if (K == 4 && onepass) return mh_kernel_k4(rng);
-    if (K == 8 && onepass) return mh_kernel_k8(rng);
-    if (K == 8 && !onepass) return mh_kernel_k8m(rng);
+static const void* pick_kernel(int K, int onepass, int rng, int rolled) {
+    if (K == 4) return onepass ? mh_kernel_k4(rng, rolled) : mh_kernel_k4m(rng, rolled);
+    if (K == 8) return onepass ? mh_kernel_k8(rng, rolled) : mh_kernel_k8m(rng, rolled);
     return nullptr;
 }
 
@@ -29,17 +28,16 @@ void fill_lcg_jump_table(KParams& p) {
     }
 }
 
-cudaError_t mh_occupancy(const KParams& p, int K, int onepass, int warps_per_cta, size_t smem,
-                         int* ctas_per_sm) {
-    const void* f = pick_kernel(K, onepass, p.rng_mode);
+cudaError_t mh_occupancy(const KParams& p, const LaunchCfg& lc, int* ctas_per_sm) {
+    const void* f = pick_kernel(lc.K, lc.onepass, p.rng_mode, lc.rolled);
     if (!f) return cudaErrorInvalidValue;
-    cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lc.smem_bytes);
     if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, f, warps_per_cta * 32, smem);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, f, lc.warps_per_cta * 32, lc.smem_bytes);
 }
 
 cudaError_t launch_mh_block(const KParams& p, const LaunchCfg& lc, cudaStream_t st) {
-    const void* f = pick_kernel(lc.K, lc.onepass, p.rng_mode);
+    const void* f = pick_kernel(lc.K, lc.onepass, p.rng_mode, lc.rolled);
     if (!f) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lc.smem_bytes);
     if (e != cudaSuccess) return e;
@@ -76,7 +74,7 @@ __global__ void __launch_bounds__(128) eval_values_kernel(const __grid_constant_
         float x[1], acc[1];
         int i = b + lane;
         x[0] = i < nx ? xs[i] : 0.0f;
-        run_program<1>(ws.prog[0], ws.Cs[0], x, acc, ws.stk, ws.scr, lane);
+        run_program<1, false>(ws.prog[0], ws.Cs[0], x, acc, ws.stk, ws.scr, lane);
         if (i < nx) out[(size_t)chain * nx + i] = acc[0];
     }
 }

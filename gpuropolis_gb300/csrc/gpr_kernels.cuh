@@ -77,14 +77,16 @@ struct KParams {
 void fill_lcg_jump_table(KParams& p);
 
 /* Kernel entry points of the translation units gpr_mh_k*.cu. */
-const void* mh_kernel_k4(int rng);
-const void* mh_kernel_k8(int rng);
-const void* mh_kernel_k8m(int rng);
+const void* mh_kernel_k4(int rng, int rolled);
+const void* mh_kernel_k4m(int rng, int rolled);
+const void* mh_kernel_k8(int rng, int rolled);
+const void* mh_kernel_k8m(int rng, int rolled);
 
 /* Launch geometry picked by the host (persistent grid). */
 struct LaunchCfg {
     int K;             /* points per lane per pass: 1, 2, 4 or 8                */
     int onepass;       /* nd <= 32*K: data kept in registers                    */
+    int rolled;        /* heavy ops through the non-unrolled loop                */
     int warps_per_cta;
     int ctas;
     size_t smem_bytes;
@@ -92,8 +94,7 @@ struct LaunchCfg {
 
 size_t mh_smem_bytes(const KParams& p, int K, int warps_per_cta);
 cudaError_t launch_mh_block(const KParams& p, const LaunchCfg& lc, cudaStream_t st);
-cudaError_t mh_occupancy(const KParams& p, int K, int onepass, int warps_per_cta, size_t smem,
-                         int* ctas_per_sm);
+cudaError_t mh_occupancy(const KParams& p, const LaunchCfg& lc, int* ctas_per_sm);
 
 /* Diagnostics: evaluate every chain's program at nx points, and report the
  * compiled length / node count (used by the parity tests). */

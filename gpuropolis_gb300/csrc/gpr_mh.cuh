@@ -344,29 +344,38 @@ static __device__ __noinline__ CompileOut compile_program(const uint8_t* ops, in
  * so the kernel carries a single copy of each: with every warp of an SM
  * executing a different program, instruction-cache footprint, not FP32
  * throughput, limits an interpreter. */
-enum gpr_xop { XOP_SIN, XOP_ASIN, XOP_COS, XOP_ACOS, XOP_TAN, XOP_ATAN };
+enum gpr_hop { H_EXP, H_LOG, H_SQRT, H_INV, H_DIV, H_POW, H_SIN, H_ASIN, H_COS, H_ACOS, H_TAN, H_ATAN };
 
-__device__ __forceinline__ int xop_of_unary(uint32_t code) {
+__device__ __forceinline__ int trig_hop(uint32_t code) {
     switch (code) {
-        case U_SIN: return XOP_SIN;   case U_ASIN: return XOP_ASIN; case U_COS: return XOP_COS;
-        case U_ACOS: return XOP_ACOS; case U_TAN: return XOP_TAN;   case U_ATAN: return XOP_ATAN;
+        case U_SIN: return H_SIN;   case U_ASIN: return H_ASIN; case U_COS: return H_COS;
+        case U_ACOS: return H_ACOS; case U_TAN: return H_TAN;   case U_ATAN: return H_ATAN;
         default: return -1;
     }
 }
 
-/* scr[k*32 + lane] holds the K operands of this lane; results replace them. */
+/* One non-unrolled pass over this lane's K staged values: scr[k*32 + lane]
+ * holds first operands u, scr[(K+k)*32 + lane] second operands w; results
+ * replace u.  The single copy of each routine keeps the code footprint small. */
 template <int K>
-__device__ __noinline__ void expensive_loop(float* __restrict__ scr, int xop, int lane) {
+__device__ __noinline__ void heavy_loop(float* __restrict__ scr, int hop, int lane) {
 #pragma unroll 1
     for (int k = 0; k < K; ++k) {
         const float u = scr[k * 32 + lane];
+        const float w = scr[(K + k) * 32 + lane];
         float r;
-        switch (xop) {
-            case XOP_SIN: r = sinf(u); break;
-            case XOP_ASIN: r = asinf(u); break;
-            case XOP_COS: r = cosf(u); break;
-            case XOP_ACOS: r = acosf(u); break;
-            case XOP_TAN: r = tanf(u); break;
+        switch (hop) {
+            case H_EXP: r = gx_exp(u); break;
+            case H_LOG: r = gx_log(u); break;
+            case H_SQRT: r = __fsqrt_rn(u); break;
+            case H_INV: r = __fdiv_rn(1.0f, u); break;
+            case H_DIV: r = __fdiv_rn(u, w); break;
+            case H_POW: r = gx_pow(u, w); break;
+            case H_SIN: r = sinf(u); break;
+            case H_ASIN: r = asinf(u); break;
+            case H_COS: r = cosf(u); break;
+            case H_ACOS: r = acosf(u); break;
+            case H_TAN: r = tanf(u); break;
             default: r = atanf(u); break;
         }
         scr[k * 32 + lane] = r;
@@ -374,6 +383,21 @@ __device__ __noinline__ void expensive_loop(float* __restrict__ scr, int xop, in
 }
 
 template <int K>
+__device__ __forceinline__ void heavy_staged(float (&acc)[K], const float (&w)[K], float* scr, int hop,
+                                             int lane) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) { scr[k * 32 + lane] = acc[k]; scr[(K + k) * 32 + lane] = w[k]; }
+    heavy_loop<K>(scr, hop, lane);
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc[k] = scr[k * 32 + lane];
+}
+
+/* acc = f(acc) / acc = op(acc, v) / acc = op(v, acc) for one instruction.
+ * ROLLED: division, pow, exp, log, sqrt and 1/x go through heavy_loop (small
+ * code, one value at a time); otherwise they are unrolled over K in registers
+ * (more code, full ILP).  Which is faster depends on how much of the kernel
+ * the instruction cache holds; gpr_autotune measures it. */
+template <int K, bool ROLLED>
 __device__ __forceinline__ void run_program(const uint32_t* __restrict__ prog,
                                             const float* __restrict__ Cs,
                                             const float (&x)[K], float (&acc)[K],
@@ -406,14 +430,7 @@ __device__ __forceinline__ void run_program(const uint32_t* __restrict__ prog,
 #pragma unroll
                 for (int k = 0; k < K; ++k) v[k] = stk[(sp * K + k) * 32 + lane];
             }
-            if (bop == BOP_POW) {
-#pragma unroll
-                for (int k = 0; k < K; ++k) {
-                    const float u = accleft ? acc[k] : v[k];
-                    const float w = accleft ? v[k] : acc[k];
-                    acc[k] = gx_pow(u, w);
-                }
-            } else if (bop == BOP_ADD) {   /* commutative: operand order is irrelevant */
+            if (bop == BOP_ADD) {            /* commutative: operand order is irrelevant */
 #pragma unroll
                 for (int k = 0; k < K; ++k) acc[k] = __fadd_rn(acc[k], v[k]);
             } else if (bop == BOP_MUL) {
@@ -428,38 +445,24 @@ __device__ __forceinline__ void run_program(const uint32_t* __restrict__ prog,
                     for (int k = 0; k < K; ++k) acc[k] = __fsub_rn(v[k], acc[k]);
                 }
             } else {
-                if (accleft) {
+                /* DIV, POW: bring the operands into (u, w) order */
+                if (!accleft) {
+#pragma unroll
+                    for (int k = 0; k < K; ++k) { const float t = acc[k]; acc[k] = v[k]; v[k] = t; }
+                }
+                if (ROLLED) {
+                    heavy_staged<K>(acc, v, scr, bop == BOP_DIV ? H_DIV : H_POW, lane);
+                } else if (bop == BOP_DIV) {
 #pragma unroll
                     for (int k = 0; k < K; ++k) acc[k] = __fdiv_rn(acc[k], v[k]);
                 } else {
 #pragma unroll
-                    for (int k = 0; k < K; ++k) acc[k] = __fdiv_rn(v[k], acc[k]);
+                    for (int k = 0; k < K; ++k) acc[k] = gx_pow(acc[k], v[k]);
                 }
             }
             continue;
         }
-        const int xop = xop_of_unary(code);
-        if (xop >= 0) {
-#pragma unroll
-            for (int k = 0; k < K; ++k) scr[k * 32 + lane] = acc[k];
-            expensive_loop<K>(scr, xop, lane);
-#pragma unroll
-            for (int k = 0; k < K; ++k) acc[k] = scr[k * 32 + lane];
-            continue;
-        }
         switch (code) {
-            case U_EXP:
-#pragma unroll
-                for (int k = 0; k < K; ++k) acc[k] = gx_exp(acc[k]);
-                break;
-            case U_LOG:
-#pragma unroll
-                for (int k = 0; k < K; ++k) acc[k] = gx_log(acc[k]);
-                break;
-            case U_SQRT:
-#pragma unroll
-                for (int k = 0; k < K; ++k) acc[k] = __fsqrt_rn(acc[k]);
-                break;
             case I_LDX:
 #pragma unroll
                 for (int k = 0; k < K; ++k) acc[k] = x[k];
@@ -481,16 +484,37 @@ __device__ __forceinline__ void run_program(const uint32_t* __restrict__ prog,
                 for (int k = 0; k < K; ++k) stk[(sp * K + k) * 32 + lane] = acc[k];
                 ++sp;
                 break;
-            case U_INV:
-#pragma unroll
-                for (int k = 0; k < K; ++k) acc[k] = __fdiv_rn(1.0f, acc[k]);
-                break;
             case U_ABS:
 #pragma unroll
                 for (int k = 0; k < K; ++k) acc[k] = fabsf(acc[k]);
                 break;
-            default:
+            case U_EXP:
+            case U_LOG:
+            case U_SQRT:
+            case U_INV:
+                if (ROLLED) {
+                    heavy_staged<K>(acc, acc, scr,
+                                    code == U_EXP ? H_EXP : code == U_LOG ? H_LOG : code == U_SQRT ? H_SQRT : H_INV,
+                                    lane);
+                } else if (code == U_EXP) {
+#pragma unroll
+                    for (int k = 0; k < K; ++k) acc[k] = gx_exp(acc[k]);
+                } else if (code == U_LOG) {
+#pragma unroll
+                    for (int k = 0; k < K; ++k) acc[k] = gx_log(acc[k]);
+                } else if (code == U_SQRT) {
+#pragma unroll
+                    for (int k = 0; k < K; ++k) acc[k] = __fsqrt_rn(acc[k]);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < K; ++k) acc[k] = __fdiv_rn(1.0f, acc[k]);
+                }
                 break;
+            default: {
+                const int hop = trig_hop(code);
+                if (hop >= 0) heavy_staged<K>(acc, acc, scr, hop, lane);
+                break;
+            }
         }
     }
 }
@@ -563,7 +587,7 @@ struct LaneData {
  * invalid (main.cu:459,462).  Each lane sums its points in FP32; the 32 lane
  * sums are combined with error-free transforms (FP64 on GB300 runs at about
  * 1/70 of the FP32 rate, so no FP64 instruction is issued here). */
-template <int K, bool ONEPASS>
+template <int K, bool ONEPASS, bool ROLLED>
 __device__ __forceinline__ df eval_loglik(const uint32_t* prog, const float* Cs, float* stk, float* scr,
                                           const LaneData<K>& ld, const float* sx, const float* sy,
                                           const float* sw, const KParams& p, int lane, int& pts) {
@@ -589,7 +613,7 @@ __device__ __forceinline__ df eval_loglik(const uint32_t* prog, const float* Cs,
                 valid |= (v ? 1u : 0u) << k;
             }
         }
-        run_program<K>(prog, Cs, x, acc, stk, scr, lane);
+        run_program<K, ROLLED>(prog, Cs, x, acc, stk, scr, lane);
         pts += ONEPASS ? p.nd : min(32 * K, p.nd - pass * 32 * K);
 #pragma unroll
         for (int k = 0; k < K; ++k) {
@@ -612,6 +636,7 @@ __device__ __forceinline__ df eval_loglik(const uint32_t* prog, const float* Cs,
  * FP32 term added exactly (double-float), at the bookkeeping scale. */
 __device__ __forceinline__ df cauchy_sum(const float* Cs, const KParams& p, int lane) {
     df s = df_make(0.0f, 0.0f);
+    #pragma unroll 1
     for (int c = lane; c < p.PL; c += 32) {
         float x = Cs[c];
         float a = __fadd_rn(1.0f, __fmul_rn(x, x));
@@ -679,12 +704,14 @@ __device__ void constant_move(Rng& r, const WarpSmem& w, const float* Cold, floa
                               df& fw_sum, df& bw_sum, const KParams& p, int lane) {
     const int PL = p.PL;
     const int nominal = (p.const_mode == 0) ? 4 : 3;
+    #pragma unroll 1
     for (int c = lane; c < PL; c += 32) { w.off[c] = nominal * c; w.ndr[c] = -1; }
     __syncwarp();
     bool converged = false;
 #pragma unroll 1
     for (int iter = 0; iter <= PL && !converged; ++iter) {
         /* (re)do the constants marked dirty (ndr < 0) at their current offset */
+        #pragma unroll 1
         for (int c = lane; c < PL; c += 32) {
             if (w.ndr[c] >= 0) continue;
             Rng rc = r;
@@ -698,6 +725,7 @@ __device__ void constant_move(Rng& r, const WarpSmem& w, const float* Cold, floa
         /* exclusive prefix sum of draw counts, 32 constants at a time */
         bool changed = false;
         int base = 0;
+        #pragma unroll 1
         for (int c0 = 0; c0 < PL; c0 += 32) {
             int c = c0 + lane;
             int v = (c < PL) ? w.ndr[c] : 0;
@@ -721,6 +749,7 @@ __device__ void constant_move(Rng& r, const WarpSmem& w, const float* Cold, floa
     __syncwarp();
     df f = df_make(0.0f, 0.0f), b = df_make(0.0f, 0.0f);
     if (p.const_mode != 0) { fw_sum = f; bw_sum = b; return; }   /* random walk: symmetric, no terms */
+    #pragma unroll 1
     for (int c = lane; c < PL; c += 32) {
         f = df_add(f, df_make(__fmul_rn(w.fw[c], GPR_DF_SCALE), 0.0f));
         b = df_add(b, df_make(__fmul_rn(w.bw[c], GPR_DF_SCALE), 0.0f));
@@ -780,7 +809,7 @@ __device__ __forceinline__ bool mh_accept(df ppost, df cur_post, df backward, df
     return accept;
 }
 
-template <int K, bool ONEPASS, int RNG>
+template <int K, bool ONEPASS, int RNG, bool ROLLED>
 __global__ void __launch_bounds__(256, 3) mh_block_kernel(const __grid_constant__ KParams p) {
     extern __shared__ __align__(128) uint8_t smem[];
     const int lane = threadIdx.x & 31;
@@ -874,6 +903,7 @@ __global__ void __launch_bounds__(256, 3) mh_block_kernel(const __grid_constant_
                 const int n = df_invalid(cur_post) ? 0 : random_int<RNG>(r, PL, p.mag_pl);
                 const uint8_t* oc = ws.ops[cur];
                 uint8_t* opn = ws.ops[cur ^ 1];
+                #pragma unroll 1
                 for (int i = lane; i < PL; i += 32) opn[i] = oc[i];
                 __syncwarp();
                 const int m = n + 1;
@@ -912,7 +942,7 @@ __global__ void __launch_bounds__(256, 3) mh_block_kernel(const __grid_constant_
             if (need_cauchy) cs = cauchy_sum(ws.Cs[cbuf], p, lane);
             if (structural) backward = df_make(__fmul_rn(-p.logcount[count], GPR_DF_SCALE), 0.0f);
             int pts = 0;
-            const df lik = eval_loglik<K, ONEPASS>(ws.prog[pbuf], ws.Cs[cbuf], ws.stk, ws.scr, ld, sx, sy, sw,
+            const df lik = eval_loglik<K, ONEPASS, ROLLED>(ws.prog[pbuf], ws.Cs[cbuf], ws.stk, ws.scr, ld, sx, sy, sw,
                                                    p, lane, pts);
             const df prior = df_add(length_prior(len, p), cs);
             const df post = df_add(prior, lik);

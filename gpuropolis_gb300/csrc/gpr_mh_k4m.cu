@@ -1,0 +1,14 @@
+/* Instantiations of the MH block kernel for K = 4 points per lane, dataset read from shared memory in passes
+ * (a translation unit of its own so the kernels compile in parallel). */
+#include "gpr_mh.cuh"
+
+namespace gpr {
+template __global__ void mh_block_kernel<4, false, 0, false>(const __grid_constant__ KParams p);
+template __global__ void mh_block_kernel<4, false, 1, false>(const __grid_constant__ KParams p);
+template __global__ void mh_block_kernel<4, false, 0, true>(const __grid_constant__ KParams p);
+template __global__ void mh_block_kernel<4, false, 1, true>(const __grid_constant__ KParams p);
+const void* mh_kernel_k4m(int rng, int rolled) {
+    if (rolled) return rng ? (const void*)mh_block_kernel<4, false, 1, true> : (const void*)mh_block_kernel<4, false, 0, true>;
+    return rng ? (const void*)mh_block_kernel<4, false, 1, false> : (const void*)mh_block_kernel<4, false, 0, false>;
+}
+}  // namespace gpr

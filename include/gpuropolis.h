@@ -124,6 +124,17 @@ int gpr_debug_eval_values(gpr_handle* h, const float* xs, int nx, float* out, fl
  * applied elementwise to n host values (for accuracy tests against FP64). */
 int gpr_debug_math(gpr_handle* h, int op, const float* a, const float* b, float* out, int n);
 
+/* Layout autotuner (no reference counterpart): times one block of `steps`
+ * MH steps under each valid evaluation layout -- K = 4 or 8 points per lane,
+ * data held in registers (one pass) or read from shared memory in passes,
+ * transcendental/division ops unrolled or through a compact loop -- on the
+ * handle's current state and data, keeps the fastest, and restores the state,
+ * scores and counters.  Call after gpr_set_data/gpr_set_state. */
+int gpr_autotune(gpr_handle* h, int steps, int seed, int* K, int* onepass, int* rolled, float* best_ms);
+
+/* Select an evaluation layout explicitly (K 4 or 8; onepass needs n <= 32K). */
+int gpr_set_layout(gpr_handle* h, int K, int onepass, int rolled);
+
 /* Launch geometry chosen for the current dataset: points per lane K, whether
  * the data stay in registers (onepass), warps per CTA, CTAs, shared bytes. */
 int gpr_launch_geometry(gpr_handle* h, int* K, int* onepass, int* warps_per_cta, int* ctas,
@@ -131,6 +142,9 @@ int gpr_launch_geometry(gpr_handle* h, int* K, int* onepass, int* warps_per_cta,
 
 /* The cudaStream_t the handle runs on. */
 void* gpr_stream(gpr_handle* h);
+
+/* 1 when the current layout runs heavy ops through the compact loop. */
+int gpr_layout_rolled(gpr_handle* h);
 
 /* Counters accumulated by the MH kernel since the last reset (no reference
  * counterpart): [0] likelihood evaluations, [1] sum of evaluated node counts,

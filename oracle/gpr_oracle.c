@@ -179,6 +179,64 @@ static double eval_node_f64(const int32_t* P, const float* C, int N, int PL, int
 #undef R
 }
 
+/* FP64 evaluation with every node's result multiplied by (1 + rel*u), u a
+ * seeded pseudo-random number in [-1, 1]: repeated with different seeds it
+ * measures how far FP32 rounding (rel ~ a few 2^-24) can move the value of
+ * this program at this point -- its sensitivity, whatever the libm. */
+static uint32_t port_hash(uint32_t a) {
+    a ^= a >> 16; a *= 0x7feb352du; a ^= a >> 15; a *= 0x846ca68bu; a ^= a >> 16;
+    return a;
+}
+static double eval_node_f64p(const int32_t* P, const float* C, int N, int PL, int idx, int j, double x,
+                             uint32_t seed, double rel) {
+    if (j > PL) return x;
+    const int o = OP(P, N, idx, j);
+    const double c = CV(C, N, idx, j);
+    double r;
+#define L eval_node_f64p(P, C, N, PL, idx, 2 * j, x, seed, rel)
+#define R eval_node_f64p(P, C, N, PL, idx, 2 * j + 1, x, seed, rel)
+    switch (o) {
+        case ONE: r = 1.0; break;
+        case CONST: r = c; break;
+        case INV: r = 1.0 / L; break;
+        case A: return L;
+        case B: return R;
+        case PLUS: { double a = L, b = R; r = a + b; break; }
+        case CPLUS: r = L + c; break;
+        case MINUS: { double a = L, b = R; r = a - b; break; }
+        case RMINUS: { double a = L, b = R; r = b - a; break; }
+        case TIMES: { double a = L, b = R; r = a * b; break; }
+        case CTIMES: r = c * L; break;
+        case DIV: { double a = L, b = R; r = a / b; break; }
+        case RDIV: { double a = L, b = R; r = b / a; break; }
+        case SQRT: r = sqrt(L); break;
+        case LOG: r = log(L); break;
+        case SIN: r = sin(L); break;
+        case ASIN: r = asin(L); break;
+        case COS: r = cos(L); break;
+        case ACOS: r = acos(L); break;
+        case TAN: r = tan(L); break;
+        case ATAN: r = atan(L); break;
+        case EXP: r = exp(L); break;
+        case POW: { double a = L, b = R; r = pow(a, b); break; }
+        case CPOW: r = pow(L, c); break;
+        case RPOW: { double a = L, b = R; r = pow(b, a); break; }
+        case CRPOW: r = pow(c, L); break;
+        case ABS: r = fabs(L); break;
+        default: return NAN;
+    }
+#undef L
+#undef R
+    if (o == ONE || o == CONST) return r;
+    double u = (double)port_hash(seed * 2654435761u + (uint32_t)j) / 4294967295.0 * 2.0 - 1.0;
+    return r * (1.0 + rel * u);
+}
+
+double gpr_port_eval_f64_perturbed(const int32_t* P, const float* C, int N, int PL, int idx, double x,
+                                   unsigned seed, double rel) {
+    return eval_node_f64p(P, C, N, PL, idx, 1, x, seed, rel);
+}
+
 /* dispatch_length (main.cu:477-526) with X_LENGTH_PRIOR = CONST_LENGTH_PRIOR = 1 */
 static float length_node(const int32_t* P, int N, int PL, int idx, int j) {
     if (j > PL) return 1.0f;

@@ -25,6 +25,8 @@ def lib():
         L.gpr_port_eval.restype = fp
         L.gpr_port_eval_f64.argtypes = [vp, vp, ip, ip, ip, dp]
         L.gpr_port_eval_f64.restype = dp
+        L.gpr_port_eval_f64_perturbed.argtypes = [vp, vp, ip, ip, ip, dp, ctypes.c_uint, dp]
+        L.gpr_port_eval_f64_perturbed.restype = dp
         L.gpr_port_length.argtypes = [vp, ip, ip, ip]
         L.gpr_port_length.restype = fp
         L.gpr_port_count.argtypes = [vp, ip, ip, ip]
@@ -94,6 +96,21 @@ def call(P, C, idx, x):
 
 def call_f64(P, C, idx, x):
     return lib().gpr_port_eval_f64(_p(P), _p(C), P.shape[1], P.shape[0], idx, float(x))
+
+
+def sensitivity(P, C, idx, x, rel=2.0 ** -22, trials=6):
+    """max |f_perturbed - f| over `trials` FP64 evaluations with every node's
+    result jittered by up to `rel` (relative): the FP32 noise floor of this
+    program at x.  inf when a perturbation changes finiteness."""
+    base = call_f64(P, C, idx, x)
+    worst = 0.0
+    for t in range(trials):
+        v = lib().gpr_port_eval_f64_perturbed(_p(P), _p(C), P.shape[1], P.shape[0], idx, float(x), 977 * t + 1, rel)
+        if np.isfinite(v) != np.isfinite(base):
+            return np.inf
+        if np.isfinite(v):
+            worst = max(worst, abs(v - base))
+    return worst
 
 
 def length(P, idx):

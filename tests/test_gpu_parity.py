@@ -48,20 +48,33 @@ def test_eval_values_match_reference(lib, PL):
     np.testing.assert_array_equal(length, rlen)
     np.testing.assert_array_equal(count, rcnt)
     from oracle import port
-    f64 = np.array([[port.call_f64(P, C, i, xv) for xv in xs] for i in range(N)])
-    with np.errstate(all="ignore"):
-        # how far the reference's own FP32 value is from FP64: the problem's conditioning
-        cond = np.where(np.isfinite(ref) & np.isfinite(f64),
-                        np.abs(ref.astype(np.float64) - f64) / np.maximum(np.abs(f64), 1e-30), np.inf)
-    edge = ~np.isfinite(f64) | (np.abs(f64) > 1e37) | (cond > 1e-6)
     cls = H.same_class(out, ref)
-    assert np.all(cls | edge), np.argwhere(~(cls | edge))[:5]
     both = np.isfinite(out) & np.isfinite(ref)
-    rel = np.zeros_like(cond)
+    rel = np.zeros(out.shape)
     rel[both] = H.rel_err(out[both], ref[both], floor=1e-30)
-    bad = both & (rel > 1e-5) & ~edge
-    assert not bad.any(), [(tuple(ix), rel[tuple(ix)], cond[tuple(ix)]) for ix in np.argwhere(bad)[:5]]
+    # candidates that are not already within 1e-5: judge them against the
+    # FP32 noise floor of the program at that point (FP64 with every node
+    # jittered by 2 ulp), which no FP32 libm can beat
+    sus = np.argwhere(~cls | (both & (rel > 1e-5)))
+    bad = []
+    for i, j in sus:
+        sens = port.sensitivity(P, C, int(i), xs[j])
+        if not np.isfinite(sens):
+            continue                      # finiteness itself depends on rounding
+        f64 = port.call_f64(P, C, int(i), xs[j])
+        if not cls[i, j]:
+            if abs(f64) > 1e37 or not np.isfinite(f64) or sens > 1e-2 * abs(f64):
+                continue                  # overflow boundary, or chaotic at FP32 precision
+            bad.append((i, j, out[i, j], ref[i, j], f64, sens))
+            continue
+        o, r = float(out[i, j]), float(ref[i, j])
+        near_ref = abs(o - r) <= 1e-5 * abs(r) + 4 * sens
+        near_f64 = abs(o - f64) <= 1e-5 * abs(f64) + 4 * sens
+        if not (near_ref or near_f64):
+            bad.append((i, j, out[i, j], ref[i, j], f64, sens))
+    assert not bad, bad[:5]
     assert both.mean() > 0.2
+    assert len(sus) < 0.01 * out.size
     s.close()
 
 
