@@ -86,6 +86,8 @@ def library():
     lib.gpr_autotune.argtypes = [vp, ip, ip, vp, vp, vp, vp]
     lib.gpr_set_layout.argtypes = [vp, ip, ip, ip]
     lib.gpr_layout_rolled.argtypes = [vp]
+    lib.gpr_layout_lockstep.argtypes = [vp]
+    lib.gpr_set_layout2.argtypes = [vp, ip, ip, ip, ip, ip]
     lib.gpr_get_stats.argtypes = [vp, vp, ip]
     lib.gpr_reset_stats.argtypes = [vp]
     # host side (include/gpuropolis_host.h)
@@ -213,14 +215,15 @@ class Sampler:
                                           ctypes.byref(ro), ctypes.byref(ms)))
         return dict(K=k.value, onepass=op.value, rolled=ro.value, ms=ms.value)
 
-    def set_layout(self, K, onepass, rolled):
-        self._check(self.lib.gpr_set_layout(self.h, K, int(onepass), int(rolled)))
+    def set_layout(self, K, onepass, rolled, lockstep=1, warps_per_cta=8):
+        self._check(self.lib.gpr_set_layout2(self.h, K, int(onepass), int(rolled), lockstep, warps_per_cta))
 
     def launch_geometry(self):
         v = [ctypes.c_int() for _ in range(4)] + [ctypes.c_int64()]
         self._check(self.lib.gpr_launch_geometry(self.h, *[ctypes.byref(a) for a in v]))
         return dict(K=v[0].value, onepass=v[1].value, warps_per_cta=v[2].value,
-                    ctas=v[3].value, smem_bytes=v[4].value, rolled=int(self.lib.gpr_layout_rolled(self.h)))
+                    ctas=v[3].value, smem_bytes=v[4].value, rolled=int(self.lib.gpr_layout_rolled(self.h)),
+                    lockstep=int(self.lib.gpr_layout_lockstep(self.h)))
 
     STAT_NAMES = ("evals", "eval_nodes", "eval_points", "eval_node_points", "struct_proposed",
                   "struct_accepted", "const_proposed", "const_accepted")

@@ -212,7 +212,7 @@ int gpr_create(const gpr_config* cfg, int n_chains, gpr_handle** out) {
     kp.next_chain = h->dcounter;
     kp.err = h->dcounter + 1;
     kp.stats = h->dstats;
-    kp.lockstep = getenv("GPR_LOCKSTEP") ? atoi(getenv("GPR_LOCKSTEP")) : 1;
+    kp.lockstep = 1;
     kp.max_instr = GPR_MAX_INSTR(PL);
     /* Value-stack depth: a push happens at a binary node whose children are
      * both subtrees, so at a node j <= PL/2; pending pushes lie on one
@@ -237,13 +237,14 @@ int gpr_destroy(gpr_handle* h) {
 
 /* Launch geometry for a given layout: K points per lane, data in registers
  * (onepass) or streamed from shared memory, heavy ops rolled or unrolled. */
-static int configure_launch(gpr_handle* h, int K, int onepass, int rolled) {
+static int configure_launch(gpr_handle* h, int K, int onepass, int rolled, int lockstep = 1, int wpc0 = 8) {
     gpr::KParams& kp = h->kp;
     gpr::LaunchCfg lc;
     lc.K = K;
     lc.onepass = onepass;
     lc.rolled = rolled;
-    int wpc = 8;
+    lc.lockstep = lockstep;
+    int wpc = wpc0;
     size_t smem = gpr::mh_smem_bytes(kp, lc.K, wpc);
     while (smem > 227 * 1024 && wpc > 1) {
         wpc /= 2;
@@ -268,7 +269,7 @@ static int configure_launch(gpr_handle* h, int K, int onepass, int rolled) {
  * when the data fit, heavy ops unrolled (the fastest layout measured on the
  * 250-point, PROGRAM_LENGTH 63 workload; gpr_autotune re-checks per dataset). */
 static int choose_launch(gpr_handle* h) {
-    return configure_launch(h, 4, h->kp.nd <= 128 ? 1 : 0, 0);
+    return configure_launch(h, 4, h->kp.nd <= 128 ? 1 : 0, 0, 1, 8);
 }
 
 int gpr_set_data(gpr_handle* h, const float* x, const float* y, const float* sd, int n) {
@@ -478,6 +479,28 @@ int gpr_autotune(gpr_handle* h, int steps, int seed, int* K, int* onepass, int* 
         AT_TRY(cudaEventElapsedTime(&ms, e0, e1));
         if (ms < best) { best = ms; bestlc = h->lc; }
     }
+    /* second stage: barrier period and CTA size for the best layout */
+    {
+        const gpr::LaunchCfg base = bestlc;
+        const int periods[3] = {1, 5, 0};
+        const int wpcs[2] = {8, 4};
+        for (int pi = 0; pi < 3; ++pi)
+            for (int wi = 0; wi < 2; ++wi) {
+                if (periods[pi] == base.lockstep && wpcs[wi] == base.warps_per_cta) continue;
+                if (configure_launch(h, base.K, base.onepass, base.rolled, periods[pi], wpcs[wi]) != GPR_OK) continue;
+                for (int rep = 0; rep < 2; ++rep) {
+                    AT_TRY(cudaMemcpyAsync(h->dP, sP, cnt * sizeof(int32_t), cudaMemcpyDeviceToDevice, h->stream));
+                    AT_TRY(cudaMemcpyAsync(h->dC, sC, cnt * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
+                    AT_TRY(cudaEventRecord(e0, h->stream));
+                    if ((rc = run(h, steps, seed)) != GPR_OK) goto done;
+                    AT_TRY(cudaEventRecord(e1, h->stream));
+                    AT_TRY(cudaEventSynchronize(e1));
+                }
+                float ms = 0.0f;
+                AT_TRY(cudaEventElapsedTime(&ms, e0, e1));
+                if (ms < best) { best = ms; bestlc = h->lc; }
+            }
+    }
     h->lc = bestlc;
     AT_TRY(cudaMemcpyAsync(h->dP, sP, cnt * sizeof(int32_t), cudaMemcpyDeviceToDevice, h->stream));
     AT_TRY(cudaMemcpyAsync(h->dC, sC, cnt * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
@@ -499,11 +522,17 @@ done:
 }
 
 int gpr_set_layout(gpr_handle* h, int K, int onepass, int rolled) {
+    return gpr_set_layout2(h, K, onepass, rolled, 1, 8);
+}
+
+int gpr_set_layout2(gpr_handle* h, int K, int onepass, int rolled, int lockstep, int warps_per_cta) {
     if (!h) return GPR_ERR_ARG;
-    if ((K != 4 && K != 8) || (onepass && h->kp.nd > 32 * K))
-        return fail(h, GPR_ERR_ARG, "invalid layout K=%d onepass=%d for %d points", K, onepass, h->kp.nd);
+    if ((K != 4 && K != 8) || (onepass && h->kp.nd > 32 * K) || lockstep < 0 ||
+        (warps_per_cta != 1 && warps_per_cta != 2 && warps_per_cta != 4 && warps_per_cta != 8))
+        return fail(h, GPR_ERR_ARG, "invalid layout K=%d onepass=%d lockstep=%d warps=%d for %d points", K,
+                    onepass, lockstep, warps_per_cta, h->kp.nd);
     CUDA_TRY(h, cudaSetDevice(h->device));
-    return configure_launch(h, K, onepass ? 1 : 0, rolled ? 1 : 0);
+    return configure_launch(h, K, onepass ? 1 : 0, rolled ? 1 : 0, lockstep, warps_per_cta);
 }
 
 int gpr_launch_geometry(gpr_handle* h, int* K, int* onepass, int* warps_per_cta, int* ctas, int64_t* smem) {
@@ -519,6 +548,7 @@ int gpr_launch_geometry(gpr_handle* h, int* K, int* onepass, int* warps_per_cta,
 void* gpr_stream(gpr_handle* h) { return h ? (void*)h->stream : nullptr; }
 
 int gpr_layout_rolled(gpr_handle* h) { return h ? h->lc.rolled : 0; }
+int gpr_layout_lockstep(gpr_handle* h) { return h ? h->lc.lockstep : 0; }
 
 int gpr_get_stats(gpr_handle* h, uint64_t* out, int n) {
     if (!h || !out || n < 0) return GPR_ERR_ARG;

@@ -42,6 +42,7 @@ cudaError_t launch_mh_block(const KParams& p, const LaunchCfg& lc, cudaStream_t 
     cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lc.smem_bytes);
     if (e != cudaSuccess) return e;
     KParams pp = p;
+    pp.lockstep = lc.lockstep;
     void* args[] = {(void*)&pp};
     return cudaLaunchKernel(f, dim3(lc.ctas), dim3(lc.warps_per_cta * 32), args, lc.smem_bytes, st);
 }

@@ -63,7 +63,7 @@ struct KParams {
     int* next_chain;   /* dynamic chain counter (zeroed before launch)          */
     int* err;          /* device error flags                                    */
     unsigned long long* stats;  /* GPR_STAT_* counters, accumulated per launch  */
-    int lockstep;      /* 1: the warps of a CTA step their chains in lockstep     */
+    int lockstep;      /* >0: the warps of a CTA realign every `lockstep` steps  */
     int levels;        /* value-stack slots per lane                            */
     int max_instr;     /* instruction buffer length per program                 */
 
@@ -87,6 +87,7 @@ struct LaunchCfg {
     int K;             /* points per lane per pass: 1, 2, 4 or 8                */
     int onepass;       /* nd <= 32*K: data kept in registers                    */
     int rolled;        /* heavy ops through the non-unrolled loop                */
+    int lockstep;      /* CTA barrier period in MH steps (0: warps run freely)   */
     int warps_per_cta;
     int ctas;
     size_t smem_bytes;

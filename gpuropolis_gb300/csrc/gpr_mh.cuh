@@ -891,7 +891,7 @@ __global__ void __launch_bounds__(256, 3) mh_block_kernel(const __grid_constant_
          * compile, prior and likelihood keeps the kernel's hot code small. */
 #pragma unroll 1
         for (int step = -1; step < p.steps; ++step) {
-          if (p.lockstep) __syncthreads();
+          if (p.lockstep > 0 && (step + 1) % p.lockstep == 0) __syncthreads();
           if (active) {
             const bool init = step < 0;
             const bool structural = !init && (step % 5 == 0);

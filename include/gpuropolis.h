@@ -127,13 +127,18 @@ int gpr_debug_math(gpr_handle* h, int op, const float* a, const float* b, float*
 /* Layout autotuner (no reference counterpart): times one block of `steps`
  * MH steps under each valid evaluation layout -- K = 4 or 8 points per lane,
  * data held in registers (one pass) or read from shared memory in passes,
- * transcendental/division ops unrolled or through a compact loop -- on the
- * handle's current state and data, keeps the fastest, and restores the state,
- * scores and counters.  Call after gpr_set_data/gpr_set_state. */
+ * transcendental/division ops unrolled or through a compact loop -- then,
+ * for the best of those, each CTA barrier period (1, 5 steps, none) and CTA
+ * size (8 or 4 chains), on the handle's current state and data; keeps the
+ * fastest and restores the state, scores and counters.  Call after
+ * gpr_set_data/gpr_set_state. */
 int gpr_autotune(gpr_handle* h, int steps, int seed, int* K, int* onepass, int* rolled, float* best_ms);
 
-/* Select an evaluation layout explicitly (K 4 or 8; onepass needs n <= 32K). */
+/* Select an evaluation layout explicitly (K 4 or 8; onepass needs n <= 32K).
+ * gpr_set_layout2 also sets the CTA barrier period in MH steps (0 = none)
+ * and the warps (chains) per CTA (1, 2, 4 or 8). */
 int gpr_set_layout(gpr_handle* h, int K, int onepass, int rolled);
+int gpr_set_layout2(gpr_handle* h, int K, int onepass, int rolled, int lockstep, int warps_per_cta);
 
 /* Launch geometry chosen for the current dataset: points per lane K, whether
  * the data stay in registers (onepass), warps per CTA, CTAs, shared bytes. */
@@ -143,8 +148,10 @@ int gpr_launch_geometry(gpr_handle* h, int* K, int* onepass, int* warps_per_cta,
 /* The cudaStream_t the handle runs on. */
 void* gpr_stream(gpr_handle* h);
 
-/* 1 when the current layout runs heavy ops through the compact loop. */
+/* 1 when the current layout runs heavy ops through the compact loop; the
+ * current CTA barrier period. */
 int gpr_layout_rolled(gpr_handle* h);
+int gpr_layout_lockstep(gpr_handle* h);
 
 /* Counters accumulated by the MH kernel since the last reset (no reference
  * counterpart): [0] likelihood evaluations, [1] sum of evaluated node counts,

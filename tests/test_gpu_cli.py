@@ -1,0 +1,89 @@
+"""The `gpuropolis` CLI as a drop-in for the reference's main() (main.cu:1011-1257):
+the same arguments give the same samples.txt header byte for byte and, for
+the chains whose trajectories agree, the same sample lines byte for byte.
+The reference side is the reference's own main() compiled for the host
+(oracle/build_ref.py), with the project's transcendental functions in its
+proposal random transforms so that proposals can agree bit for bit."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from tests import helpers as H
+
+pytestmark = pytest.mark.gpu
+g = pytest.importorskip("gpuropolis_gb300")
+oref = pytest.importorskip("oracle.ref")
+
+
+def _write_data(path, x, y, sd):
+    with open(path, "w") as f:
+        f.write("# x\ty\tsd\n")
+        for a, b, c in zip(x, y, sd):
+            f.write("%.9g\t%.9g\t%.9g\n" % (a, b, c))
+
+
+def _lines(path):
+    head, body = [], []
+    for line in open(path, encoding="latin-1").read().split("\n"):
+        (head if line.startswith("#") else body).append(line)
+    return head, [l for l in body if l]
+
+
+@pytest.mark.parametrize("extra", [[], ["--show-constants", "--thin=1"]])
+def test_cli_matches_reference(tmp_path, extra):
+    if not oref.available():
+        pytest.skip("reference oracle source not available")
+    if not os.path.exists(g.CLI_PATH):
+        pytest.skip("CLI not built")
+    x, y, sd = H.quad_data(60, seed=3)
+    data = tmp_path / "data.txt"
+    _write_data(data, x, y, sd)
+    o = oref.get(pl=31, project_math=1)
+    ref_out, our_out = tmp_path / "ref", tmp_path / "ours"
+    ref_out.mkdir(); our_out.mkdir()
+    args = ["--in=%s" % data, "--N=256", "--steps=20", "--outer=3", "--seed=12345", "--quiet"] + extra
+    r = subprocess.run([o.cli_path] + args + ["--out=%s" % ref_out], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([g.CLI_PATH] + args + ["--out=%s" % our_out], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    rh, rb = _lines(ref_out / "samples.txt")
+    oh, ob = _lines(our_out / "samples.txt")
+    # the header differs only in the output path line
+    assert [l for l in rh if "Output path" not in l] == [l for l in oh if "Output path" not in l]
+    assert len(rb) == len(ob) == 256 * 2
+
+    def same_line(a, b):
+        """Chain, block, length, degree, the three printed programs, the op
+        codes and constants exactly; posterior, prior and likelihood (printed
+        %.3f, i.e. up to 11 significant digits for large scores) within 1e-5."""
+        fa, fb = a.split("\t"), b.split("\t")
+        if len(fa) != len(fb) or fa[:2] != fb[:2] or fa[5:] != fb[5:]:
+            return False
+        for u, v in zip(fa[2:5], fb[2:5]):
+            u, v = float(u), float(v)
+            if not (u == v or abs(u - v) <= 1e-5 * max(abs(u), abs(v), 1.0)):
+                return False
+        return True
+
+    same = np.mean([same_line(a, b) for a, b in zip(rb, ob)])
+    assert same >= 0.9, same
+    # every line has the reference's layout
+    for line in ob:
+        f = line.split("\t")
+        assert len(f) == (11 + 31 + 1 if extra else 11)
+        assert f[7].startswith('"') and f[7].endswith('"') and f[10].startswith('"')
+    assert os.path.exists(our_out / "log.txt")
+
+
+def test_cli_rejects_bad_arguments(tmp_path):
+    if not os.path.exists(g.CLI_PATH):
+        pytest.skip("CLI not built")
+    r = subprocess.run([g.CLI_PATH, "--bogus"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and "Invalid command line arguments" in r.stderr
+    r = subprocess.run([g.CLI_PATH, "--in=%s" % (tmp_path / "missing.txt"), "--out=%s" % tmp_path, "--quiet"],
+                       capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1
+    r = subprocess.run([g.CLI_PATH, "--steps=0"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1
