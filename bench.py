@@ -37,6 +37,9 @@ WORKLOADS = {
                           mh_steps=1000, map_delta=20.0, blocks=20),
     "plain-mh-1k": dict(N=1024, PL=31, nd=101, data="quad", ops="basic", rw_sd=0.1,
                         mh_steps=1000, map_delta=20.0, blocks=10),
+    # the 131k workload cut to 8192 chains x 100 steps: the case ncu captures
+    "plain-mh-8k-profile": dict(N=8192, PL=63, nd=250, data="expdecay", ops="basic", rw_sd=0.1,
+                                mh_steps=100, map_delta=20.0, blocks=1),
 }
 METRIC = "MH chain-steps/s & point-evals/s (1 GB300); ESS/s gradient vs random-walk MH"
 
@@ -204,7 +207,7 @@ def run_gpu(args, w):
     for i in range(args.warmup):
         block(i)
         resample()
-    tuned = s.autotune(steps=100, seed=4242)
+    tuned = None if args.no_autotune else s.autotune(steps=100, seed=4242)
     torch.cuda.synchronize()
     s.reset_stats()
     launches0 = s.launch_count()
@@ -313,6 +316,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="plain-mh-131k", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default layout (fixed launch sequence, for profilers)")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     if args.impl == "reference":

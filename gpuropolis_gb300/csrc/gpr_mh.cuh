@@ -37,6 +37,8 @@ namespace gpr {
 
 #define FULLMASK 0xffffffffu
 
+__host__ __device__ __forceinline__ size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
+
 /* ------------------------------------------------------------------------ */
 /* Double-float ("df") numbers: value = hi + lo, |lo| <= ulp(hi)/2, built from
  * error-free transforms (Knuth's TwoSum, Dekker's Fast2Sum).  Every Bayes
@@ -172,26 +174,9 @@ __device__ __forceinline__ float random_geometric(Rng& r, const KParams& p) {
 
 /* ------------------------------------------------------------------------ */
 /* Heap-tree compiler.  Node j is 1-based, children 2j and 2j+1; a child index
- * beyond PL is the leaf x (main.cu:374-385). */
-#define LEAF_X (-1)
-#define LEAF_ONE (-2)
-#define LEAF_NAN (-3)
-#define LEAF_C0 (-16) /* LEAF_C0 - i : the constant of node i (0-based) */
+ * beyond PL is the leaf x (main.cu:374-385).  The reachable nodes become a
+ * postfix program (gpr_common.h); length and node count come with it. */
 
-__device__ __forceinline__ int resolve_leaf(const uint8_t* ops, int PL, int j) {
-    while (j <= PL) {
-        int o = ops[j - 1];
-        if (o == OP_A) j = 2 * j;
-        else if (o == OP_B) j = 2 * j + 1;
-        else break;
-    }
-    if (j > PL) return LEAF_X;
-    int o = ops[j - 1];
-    if (o == OP_ONE) return LEAF_ONE;
-    if (o == OP_CONST) return LEAF_C0 - (j - 1);
-    if (gpr_op_class(o) == CLS_INVALID) return LEAF_NAN;
-    return j;
-}
 
 struct CompileOut {
     int ninstr;
@@ -199,25 +184,6 @@ struct CompileOut {
     int count;      /* dispatch_countnodes fold, main.cu:553-601                 */
 };
 
-__device__ __forceinline__ uint32_t load_leaf_instr(int leaf) {
-    if (leaf == LEAF_X) return I_LDX;
-    if (leaf == LEAF_ONE) return I_LD1;
-    if (leaf == LEAF_NAN) return I_LDNAN;
-    return I_LDC | ((uint32_t)(LEAF_C0 - leaf) << 8);
-}
-__device__ __forceinline__ uint32_t bin_instr(int bop, int accleft, int leaf_or_pop) {
-    if (leaf_or_pop == 0) return GPR_BIN(bop, accleft, SRC_POP);
-    if (leaf_or_pop == LEAF_X) return GPR_BIN(bop, accleft, SRC_X);
-    if (leaf_or_pop == LEAF_ONE) return GPR_BIN(bop, accleft, SRC_ONE);
-    if (leaf_or_pop == LEAF_NAN) return GPR_BIN(bop, accleft, SRC_C) | (255u << 8);
-    return GPR_BIN(bop, accleft, SRC_C) | ((uint32_t)(LEAF_C0 - leaf_or_pop) << 8);
-}
-__device__ __forceinline__ void leaf_cost(int leaf, float& len, int& cnt) {
-    /* X: X_LENGTH_PRIOR, count 0; ONE/CONST: 1, count 1 (main.cu:481-482,556-557) */
-    if (leaf == LEAF_X) { len += 1.0f; }
-    else if (leaf == LEAF_NAN) { len = __int_as_float(0x7fc00000); }
-    else { len += 1.0f; cnt += 1; }
-}
 __device__ __forceinline__ int unary_code(int o) {
     switch (o) {
         case OP_INV: return U_INV;   case OP_LOG: return U_LOG;   case OP_EXP: return U_EXP;
@@ -239,98 +205,163 @@ __device__ __forceinline__ int binary_bop(int o, int& swapped) {
     }
 }
 
-/* Executed by lane 0 of the warp only (its DFS frames live in that lane's
- * registers/stack); the caller broadcasts length and count. */
-static __device__ __noinline__ CompileOut compile_program(const uint8_t* ops, int PL, uint32_t* prog) {
-    CompileOut out;
-    out.ninstr = 0; out.length = 0.0f; out.count = 0;
-    int fs_node[12], fs_phase[12], fs_aux[12];
-    int fp = 0;
-#define EMIT(w) do { prog[out.ninstr] = (w); out.ninstr++; } while (0)
-    int r0 = resolve_leaf(ops, PL, 1);
-    if (r0 < 0) {
-        EMIT(load_leaf_instr(r0));
-        leaf_cost(r0, out.length, out.count);
-    } else {
-        fs_node[0] = r0; fs_phase[0] = 0; fp = 1;
-    }
-    while (fp > 0) {
-        int j = fs_node[fp - 1];
-        int ph = fs_phase[fp - 1];
-        int o = ops[j - 1];
-        int cls = gpr_op_class(o);
-        if (cls == CLS_UNARY || cls == CLS_CUNARY) {
-            /* the C-ops are binary ops with the node's constant as one operand:
-             * CPLUS a+C, CTIMES C*a, CPOW a^C, CRPOW C^a (main.cu:405-425) */
-            uint32_t ui;
-            if (o == OP_CPLUS) ui = GPR_BIN(BOP_ADD, 1, SRC_C);
-            else if (o == OP_CTIMES) ui = GPR_BIN(BOP_MUL, 1, SRC_C);
-            else if (o == OP_CPOW) ui = GPR_BIN(BOP_POW, 1, SRC_C);
-            else if (o == OP_CRPOW) ui = GPR_BIN(BOP_POW, 0, SRC_C);
-            else ui = (uint32_t)unary_code(o);
-            ui |= ((uint32_t)(j - 1) << 8);
-            if (ph == 0) {
-                out.count += 1;
-                out.length += (cls == CLS_CUNARY) ? 2.0f : 1.0f;
-                int L = resolve_leaf(ops, PL, 2 * j);
-                if (L < 0) {
-                    leaf_cost(L, out.length, out.count);
-                    EMIT(load_leaf_instr(L));
-                    EMIT(ui);
-                    --fp;
+/* ------------------------------------------------------------------------ */
+/* Lane-parallel compiler: the program a depth-first post-order walk would
+ * emit, built level by level over the heap instead.
+ *  1. bottom-up over the heap levels: resolve A/B pass-through chains, classify
+ *     each node as leaf (x, 1, a constant) or subtree, and for subtrees compute
+ *     the number of instructions, the description length and the node count;
+ *  2. top-down: every reachable subtree root writes its own one or two
+ *     instructions at its post-order position and hands its children their
+ *     start positions.
+ * The per-node scratch (resolved node, instruction count, length, count,
+ * start) lives in the warp's shared region, free between proposal and
+ * evaluation.  Resolved codes: j > 0 a subtree rooted at node j (1-based),
+ * PL_X / PL_ONE / PL_NAN leaves, PL_C0 - i the constant of node i. */
+#define PL_X 0
+#define PL_ONE (-1)
+#define PL_NAN (-2)
+#define PL_C0 (-3)
+
+__device__ __forceinline__ uint32_t pl_load_instr(int r) {
+    if (r == PL_X) return I_LDX;
+    if (r == PL_ONE) return I_LD1;
+    if (r == PL_NAN) return I_LDNAN;
+    return I_LDC | ((uint32_t)(PL_C0 - r) << 8);
+}
+__device__ __forceinline__ uint32_t pl_bin_instr(int bop, int accleft, int r, bool pop) {
+    if (pop) return GPR_BIN(bop, accleft, SRC_POP);
+    if (r == PL_X) return GPR_BIN(bop, accleft, SRC_X);
+    if (r == PL_ONE) return GPR_BIN(bop, accleft, SRC_ONE);
+    if (r == PL_NAN) return GPR_BIN(bop, accleft, SRC_C) | (255u << 8);
+    return GPR_BIN(bop, accleft, SRC_C) | ((uint32_t)(PL_C0 - r) << 8);
+}
+
+struct CompileScratch {
+    int* res;      /* resolved code per heap node (index j, 1-based)        */
+    int* icnt;     /* instructions of the subtree rooted at j               */
+    float* len;    /* description length of that subtree                    */
+    int* cnt;      /* node count of that subtree                            */
+    int* start;    /* first instruction of that subtree, -1 if unreachable  */
+};
+
+__device__ __forceinline__ CompileScratch compile_scratch(float* region, int PL) {
+    const size_t n = align16((size_t)PL + 1);
+    CompileScratch c;
+    c.res = (int*)region;
+    c.icnt = c.res + n;
+    c.len = (float*)(c.icnt + n);
+    c.cnt = (int*)(c.len + n);
+    c.start = c.cnt + n;
+    return c;
+}
+
+__device__ __forceinline__ int child_res(const CompileScratch& cs, int PL, int j) {
+    return j > PL ? PL_X : cs.res[j];
+}
+__device__ __forceinline__ float leaf_len(int r) { return r == PL_NAN ? __int_as_float(0x7fc00000) : 1.0f; }
+__device__ __forceinline__ int leaf_cnt(int r) { return r == PL_X ? 0 : 1; }
+
+static __device__ CompileOut compile_parallel(const uint8_t* ops, int PL, uint32_t* prog, const CompileScratch& cs,
+                                       int lane) {
+    int D = 0;
+    while ((2 << D) <= PL) ++D;     /* deepest heap level */
+    /* 1. bottom-up */
+#pragma unroll 1
+    for (int d = D; d >= 0; --d) {
+        const int lo = 1 << d, hi = min((2 << d) - 1, PL);
+#pragma unroll 1
+        for (int j = lo + lane; j <= hi; j += 32) {
+            const int o = ops[j - 1];
+            const int cls = gpr_op_class(o);
+            int r = j;
+            if (cls == CLS_PASS_A) r = child_res(cs, PL, 2 * j);
+            else if (cls == CLS_PASS_B) r = child_res(cs, PL, 2 * j + 1);
+            else if (o == OP_ONE) r = PL_ONE;
+            else if (o == OP_CONST) r = PL_C0 - (j - 1);
+            else if (cls == CLS_INVALID) r = PL_NAN;
+            cs.res[j] = r;
+            cs.start[j] = -1;
+            if (r == j) {
+                int ic;
+                float ln;
+                int cn;
+                if (cls == CLS_UNARY || cls == CLS_CUNARY) {
+                    const int L = child_res(cs, PL, 2 * j);
+                    const bool lc = L > 0;
+                    ic = lc ? cs.icnt[L] + 1 : 2;
+                    ln = (cls == CLS_CUNARY ? 2.0f : 1.0f) + (lc ? cs.len[L] : leaf_len(L));
+                    cn = 1 + (lc ? cs.cnt[L] : leaf_cnt(L));
                 } else {
-                    fs_phase[fp - 1] = 1;
-                    fs_node[fp] = L; fs_phase[fp] = 0; ++fp;
+                    const int L = child_res(cs, PL, 2 * j), R = child_res(cs, PL, 2 * j + 1);
+                    const bool lc = L > 0, rc = R > 0;
+                    ic = (lc ? cs.icnt[L] : 0) + (rc ? cs.icnt[R] : 0) + ((lc && rc) ? 2 : (lc || rc) ? 1 : 2);
+                    ln = 1.0f + (lc ? cs.len[L] : leaf_len(L)) + (rc ? cs.len[R] : leaf_len(R));
+                    cn = 1 + (lc ? cs.cnt[L] : leaf_cnt(L)) + (rc ? cs.cnt[R] : leaf_cnt(R));
                 }
-            } else {
-                EMIT(ui);
-                --fp;
-            }
-        } else { /* binary */
-            int sw;
-            int bop = binary_bop(o, sw);
-            if (ph == 0) {
-                out.count += 1;
-                out.length += 1.0f;
-                int U = resolve_leaf(ops, PL, sw ? 2 * j + 1 : 2 * j);
-                int V = resolve_leaf(ops, PL, sw ? 2 * j : 2 * j + 1);
-                if (U < 0 && V < 0) {
-                    leaf_cost(U, out.length, out.count);
-                    leaf_cost(V, out.length, out.count);
-                    EMIT(load_leaf_instr(U));
-                    EMIT(bin_instr(bop, 1, V));
-                    --fp;
-                } else if (U >= 0 && V < 0) {
-                    leaf_cost(V, out.length, out.count);
-                    fs_phase[fp - 1] = 1; fs_aux[fp - 1] = V;
-                    fs_node[fp] = U; fs_phase[fp] = 0; ++fp;
-                } else if (U < 0 && V >= 0) {
-                    leaf_cost(U, out.length, out.count);
-                    fs_phase[fp - 1] = 2; fs_aux[fp - 1] = U;
-                    fs_node[fp] = V; fs_phase[fp] = 0; ++fp;
-                } else {
-                    fs_phase[fp - 1] = 3; fs_aux[fp - 1] = V;
-                    fs_node[fp] = U; fs_phase[fp] = 0; ++fp;
-                }
-            } else if (ph == 1) {
-                EMIT(bin_instr(bop, 1, fs_aux[fp - 1]));
-                --fp;
-            } else if (ph == 2) {
-                EMIT(bin_instr(bop, 0, fs_aux[fp - 1]));
-                --fp;
-            } else if (ph == 3) {
-                EMIT(I_PUSH);
-                int V = fs_aux[fp - 1];
-                fs_phase[fp - 1] = 4;
-                fs_node[fp] = V; fs_phase[fp] = 0; ++fp;
-            } else {
-                EMIT(bin_instr(bop, 0, 0));
-                --fp;
+                cs.icnt[j] = ic; cs.len[j] = ln; cs.cnt[j] = cn;
             }
         }
+        __syncwarp();
     }
-    EMIT(I_END);
-#undef EMIT
+    CompileOut out;
+    const int r0 = PL >= 1 ? cs.res[1] : PL_X;
+    if (r0 <= 0) {
+        if (lane == 0) { prog[0] = pl_load_instr(r0); prog[1] = I_END; }
+        out.ninstr = 2; out.length = leaf_len(r0); out.count = leaf_cnt(r0);
+        __syncwarp();
+        return out;
+    }
+    out.ninstr = cs.icnt[r0] + 1;
+    out.length = cs.len[r0];
+    out.count = cs.cnt[r0];
+    if (lane == 0) { cs.start[r0] = 0; prog[cs.icnt[r0]] = I_END; }
+    __syncwarp();
+    /* 2. top-down */
+#pragma unroll 1
+    for (int d = 0; d <= D; ++d) {
+        const int lo = 1 << d, hi = min((2 << d) - 1, PL);
+#pragma unroll 1
+        for (int j = lo + lane; j <= hi; j += 32) {
+            const int st = cs.start[j];
+            if (st < 0 || cs.res[j] != j) continue;
+            const int o = ops[j - 1];
+            const int cls = gpr_op_class(o);
+            if (cls == CLS_UNARY || cls == CLS_CUNARY) {
+                uint32_t ui;
+                if (o == OP_CPLUS) ui = GPR_BIN(BOP_ADD, 1, SRC_C);
+                else if (o == OP_CTIMES) ui = GPR_BIN(BOP_MUL, 1, SRC_C);
+                else if (o == OP_CPOW) ui = GPR_BIN(BOP_POW, 1, SRC_C);
+                else if (o == OP_CRPOW) ui = GPR_BIN(BOP_POW, 0, SRC_C);
+                else ui = (uint32_t)unary_code(o);
+                ui |= ((uint32_t)(j - 1) << 8);
+                const int L = child_res(cs, PL, 2 * j);
+                if (L > 0) { cs.start[L] = st; prog[st + cs.icnt[L]] = ui; }
+                else { prog[st] = pl_load_instr(L); prog[st + 1] = ui; }
+            } else {
+                int sw;
+                const int bop = binary_bop(o, sw);
+                const int U = child_res(cs, PL, sw ? 2 * j + 1 : 2 * j);
+                const int V = child_res(cs, PL, sw ? 2 * j : 2 * j + 1);
+                if (U <= 0 && V <= 0) {
+                    prog[st] = pl_load_instr(U);
+                    prog[st + 1] = pl_bin_instr(bop, 1, V, false);
+                } else if (U > 0 && V <= 0) {
+                    cs.start[U] = st;
+                    prog[st + cs.icnt[U]] = pl_bin_instr(bop, 1, V, false);
+                } else if (U <= 0 && V > 0) {
+                    cs.start[V] = st;
+                    prog[st + cs.icnt[V]] = pl_bin_instr(bop, 0, U, false);
+                } else {
+                    cs.start[U] = st;
+                    prog[st + cs.icnt[U]] = I_PUSH;
+                    cs.start[V] = st + cs.icnt[U] + 1;
+                    prog[st + cs.icnt[U] + 1 + cs.icnt[V]] = pl_bin_instr(bop, 0, 0, true);
+                }
+            }
+        }
+        __syncwarp();
+    }
     return out;
 }
 
@@ -404,11 +435,14 @@ __device__ __forceinline__ void run_program(const uint32_t* __restrict__ prog,
                                             float* __restrict__ stk, float* __restrict__ scr,
                                             int lane) {
     int sp = 0;
+    int pc = 0;
+    uint32_t ins = prog[0];
 #pragma unroll 1
-    for (int pc = 0;; ++pc) {
-        const uint32_t ins = prog[pc];
+    for (;;) {
         const uint32_t code = ins & 0xffu;
         if (code == I_END) break;
+        const uint32_t nxt = prog[pc + 1];   /* the program ends with I_END: always in bounds */
+        ++pc;
         const uint32_t node = (ins >> 8) & 0xffu;
         const float c = (node == 255u) ? __int_as_float(0x7fc00000) : Cs[node];
         if (code >= I_BIN0) {
@@ -460,7 +494,7 @@ __device__ __forceinline__ void run_program(const uint32_t* __restrict__ prog,
                     for (int k = 0; k < K; ++k) acc[k] = gx_pow(acc[k], v[k]);
                 }
             }
-            continue;
+            goto next_ins;
         }
         switch (code) {
             case I_LDX:
@@ -516,6 +550,8 @@ __device__ __forceinline__ void run_program(const uint32_t* __restrict__ prog,
                 break;
             }
         }
+    next_ins:
+        ins = nxt;
     }
 }
 
@@ -540,12 +576,14 @@ struct WarpSmem {
     float* scr;      /* transcendental staging: [2K][32]         */
 };
 
-__host__ __device__ __forceinline__ size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
 
 __host__ __device__ __forceinline__ size_t shared_region_bytes(int PL, int levels, int K) {
     const size_t eval = (size_t)(levels + 2) * K * 32 * 4;
     const size_t cmove = 4 * align16((size_t)PL) * 4;
-    return align16(eval > cmove ? eval : cmove);
+    const size_t comp = 5 * align16((size_t)PL + 1) * 4;
+    size_t m = eval > cmove ? eval : cmove;
+    m = m > comp ? m : comp;
+    return align16(m);
 }
 
 __host__ __device__ __forceinline__ size_t warp_smem_bytes(int PL, int max_instr, int levels, int K) {
@@ -699,18 +737,55 @@ __device__ __forceinline__ void propose_constant(Rng& r, float old, float& nc, f
  * in random_int), so each constant first assumes the nominal count for all
  * earlier constants; a warp prefix sum then gives the true offsets and the
  * constants whose offset changed are redone, until nothing changes. */
+/* Affine maps that move an LCG state to the nominal first draw of this
+ * lane's constants: c = lane (map) and c -> c + 32 (stride). */
+struct LaneJump {
+    uint32_t a, c;     /* state -> state after nominal*lane draws        */
+    uint32_t sa, sc;   /* state -> state after nominal*32 draws          */
+};
+
+__device__ __forceinline__ void affine_power(uint32_t k, const KParams& p, uint32_t& A, uint32_t& C) {
+    A = 1u; C = 0u;
+#pragma unroll 1
+    for (int b = 0; b < 20; ++b)
+        if ((k >> b) & 1u) { C = p.lcgA[b] * C + p.lcgC[b]; A = p.lcgA[b] * A; }
+}
+
+__device__ __forceinline__ LaneJump make_lane_jump(const KParams& p, int lane) {
+    const uint32_t nominal = (p.const_mode == 0) ? 4u : 3u;
+    LaneJump j;
+    affine_power(nominal * (uint32_t)lane, p, j.a, j.c);
+    affine_power(nominal * 32u, p, j.sa, j.sc);
+    return j;
+}
+
 template <int RNG>
 __device__ void constant_move(Rng& r, const WarpSmem& w, const float* Cold, float* Cnew,
-                              df& fw_sum, df& bw_sum, const KParams& p, int lane) {
+                              df& fw_sum, df& bw_sum, const KParams& p, const LaneJump& lj, int lane) {
     const int PL = p.PL;
     const int nominal = (p.const_mode == 0) ? 4 : 3;
-    #pragma unroll 1
-    for (int c = lane; c < PL; c += 32) { w.off[c] = nominal * c; w.ndr[c] = -1; }
+    /* first pass: every constant at its nominal offset, streams positioned by
+     * one affine map each (LCG) or a counter offset (Philox) */
+    {
+        uint32_t st = (lj.a * r.s + lj.c) & 0x7fffffffu;
+#pragma unroll 1
+        for (int c = lane; c < PL; c += 32) {
+            Rng rc = r;
+            if (RNG == 0) rc.s = st;
+            else rc.s = r.s + (uint32_t)(nominal * c);
+            rc.drawn = 0;
+            float nc, dfw, dbw;
+            propose_constant<RNG>(rc, Cold[c], nc, dfw, dbw, p);
+            Cnew[c] = nc; w.fw[c] = dfw; w.bw[c] = dbw; w.ndr[c] = (int)rc.drawn;
+            w.off[c] = nominal * c;
+            st = (lj.sa * st + lj.sc) & 0x7fffffffu;
+        }
+    }
     __syncwarp();
     bool converged = false;
 #pragma unroll 1
     for (int iter = 0; iter <= PL && !converged; ++iter) {
-        /* (re)do the constants marked dirty (ndr < 0) at their current offset */
+        /* redo the constants whose offset moved (marked ndr < 0) */
         #pragma unroll 1
         for (int c = lane; c < PL; c += 32) {
             if (w.ndr[c] >= 0) continue;
@@ -838,6 +913,7 @@ __global__ void __launch_bounds__(256, 3) mh_block_kernel(const __grid_constant_
         }
     }
     const int PL = p.PL;
+    const LaneJump ljump = make_lane_jump(p, lane);
 
     __shared__ int s_group_base;
     const int nwarps = blockDim.x >> 5;
@@ -923,7 +999,7 @@ __global__ void __launch_bounds__(256, 3) mh_block_kernel(const __grid_constant_
             } else if (!init) {
                 /* ---- constant move (main.cu:743-806) ---- */
                 df fws, bws;
-                constant_move<RNG>(r, ws, ws.Cs[ccur], ws.Cs[ccur ^ 1], fws, bws, p, lane);
+                constant_move<RNG>(r, ws, ws.Cs[ccur], ws.Cs[ccur ^ 1], fws, bws, p, ljump, lane);
                 if (p.const_mode == 0) { forward = df_add(forward, fws); backward = df_add(backward, bws); }
                 cbuf = ccur ^ 1;
                 need_cauchy = true;
@@ -932,10 +1008,10 @@ __global__ void __launch_bounds__(256, 3) mh_block_kernel(const __grid_constant_
             float len = cur_len;
             int count = cur_count;
             if (need_compile) {
-                CompileOut co;
-                if (lane == 0) co = compile_program(ws.ops[pbuf], PL, ws.prog[pbuf]);
-                len = __shfl_sync(FULLMASK, co.length, 0);
-                count = __shfl_sync(FULLMASK, co.count, 0);
+                const CompileOut co = compile_parallel(ws.ops[pbuf], PL, ws.prog[pbuf],
+                                                       compile_scratch(ws.stk, PL), lane);
+                len = co.length;
+                count = co.count;
                 __syncwarp();
             }
             df cs = cur_cs;

@@ -72,7 +72,7 @@ def test_cli_matches_reference(tmp_path, extra):
     # every line has the reference's layout
     for line in ob:
         f = line.split("\t")
-        assert len(f) == (11 + 31 + 1 if extra else 11)
+        assert len(f) == (11 + 31 + 1 if extra else 12)   # each line ends with a tab
         assert f[7].startswith('"') and f[7].endswith('"') and f[10].startswith('"')
     assert os.path.exists(our_out / "log.txt")
 
