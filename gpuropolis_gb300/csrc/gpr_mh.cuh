@@ -36,6 +36,8 @@
 namespace gpr {
 
 #define FULLMASK 0xffffffffu
+/* passes (32*K points each) a CTA-balanced evaluation can split a dataset into */
+#define GPR_MAX_PASSES 64
 
 __host__ __device__ __forceinline__ size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
 
@@ -620,6 +622,49 @@ struct LaneData {
     uint32_t valid;  /* bit k: point lane + 32k exists */
 };
 
+/* One pass (32*K points) of the likelihood of a program: this lane's FP32 sum
+ * of (f - y)^2 * w over its points, and whether any of its points is
+ * invalid.  Used by the CTA-balanced evaluation, where any warp of the CTA may
+ * evaluate any chain's pass. */
+template <int K, bool ONEPASS, bool ROLLED>
+__device__ __forceinline__ float eval_pass(const uint32_t* prog, const float* Cs, float* stk, float* scr,
+                                           const LaneData<K>& ld, const float* sx, const float* sy,
+                                           const float* sw, const KParams& p, int lane, int pass,
+                                           bool& bad, int& pts) {
+    float x[K], acc[K];
+    uint32_t valid;
+    const int base = pass * 32 * K + lane;
+    if (ONEPASS) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) x[k] = ld.x[k];
+        valid = ld.valid;
+    } else {
+        valid = 0u;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            int i = base + 32 * k;
+            bool v = i < p.nd;
+            x[k] = v ? sx[i] : 0.0f;
+            valid |= (v ? 1u : 0u) << k;
+        }
+    }
+    run_program<K, ROLLED>(prog, Cs, x, acc, stk, scr, lane);
+    pts += ONEPASS ? p.nd : min(32 * K, p.nd - pass * 32 * K);
+    float s = 0.0f;
+    bad = false;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        if (valid & (1u << k)) {
+            const int i = base + 32 * k;
+            float r = __fsub_rn(acc[k], sy[i]);
+            float q = __fmul_rn(r, r);
+            bad |= !(q <= FLT_MAX);
+            s = fmaf(q, sw[i], s);
+        }
+    }
+    return s;
+}
+
 /* Log-likelihood of one program, as a double-float at the bookkeeping scale
  * 2^-64 (the per-point weights w carry the scale).  -inf when any point is
  * invalid (main.cu:459,462).  Each lane sums its points in FP32; the 32 lane
@@ -917,6 +962,19 @@ __global__ void __launch_bounds__(256, 3) mh_block_kernel(const __grid_constant_
 
     __shared__ int s_group_base;
     const int nwarps = blockDim.x >> 5;
+    /* CTA-balanced evaluation (lockstep == 1): each warp publishes its chain's
+     * program; all warps then pull (chain, pass) tasks, longest programs
+     * first, and leave per-pass partial sums here. */
+    __shared__ const uint32_t* s_prog[8];
+    __shared__ const float* s_cs[8];
+    __shared__ int s_cost[8];
+    __shared__ int s_count[8];
+    __shared__ int s_bad[8];
+    __shared__ int s_next;
+    __shared__ float s_part_hi[8][GPR_MAX_PASSES];
+    __shared__ float s_part_lo[8][GPR_MAX_PASSES];
+    const int npass = ONEPASS ? 1 : (p.nd + 32 * K - 1) / (32 * K);
+    const bool balanced = p.lockstep == 1 && npass <= GPR_MAX_PASSES;
 
 #pragma unroll 1
     for (;;) {
@@ -965,13 +1023,17 @@ __global__ void __launch_bounds__(256, 3) mh_block_kernel(const __grid_constant_
         /* step -1 evaluates the loaded state (main.cu:683-685); steps 0..steps-1
          * are the MH iterations (main.cu:697-808).  One call site each for
          * compile, prior and likelihood keeps the kernel's hot code small. */
+        int cur_ninstr = 0;
 #pragma unroll 1
         for (int step = -1; step < p.steps; ++step) {
-          if (p.lockstep > 0 && (step + 1) % p.lockstep == 0) __syncthreads();
+          if (!balanced && p.lockstep > 0 && (step + 1) % p.lockstep == 0) __syncthreads();
+          const bool init = step < 0;
+          const bool structural = !init && (step % 5 == 0);
+          int pbuf = cur, cbuf = ccur;
+          float len = cur_len;
+          int count = cur_count, ninstr = cur_ninstr;
+          df cs = cur_cs;
           if (active) {
-            const bool init = step < 0;
-            const bool structural = !init && (step % 5 == 0);
-            int pbuf = cur, cbuf = ccur;
             bool need_compile = init, need_cauchy = init;
             if (structural) {
                 /* ---- structure move (main.cu:699-742) ---- */
@@ -1005,25 +1067,85 @@ __global__ void __launch_bounds__(256, 3) mh_block_kernel(const __grid_constant_
                 need_cauchy = true;
             }
             __syncwarp();
-            float len = cur_len;
-            int count = cur_count;
             if (need_compile) {
                 const CompileOut co = compile_parallel(ws.ops[pbuf], PL, ws.prog[pbuf],
                                                        compile_scratch(ws.stk, PL), lane);
                 len = co.length;
                 count = co.count;
+                ninstr = co.ninstr;
                 __syncwarp();
             }
-            df cs = cur_cs;
             if (need_cauchy) cs = cauchy_sum(ws.Cs[cbuf], p, lane);
             if (structural) backward = df_make(__fmul_rn(-p.logcount[count], GPR_DF_SCALE), 0.0f);
-            int pts = 0;
-            const df lik = eval_loglik<K, ONEPASS, ROLLED>(ws.prog[pbuf], ws.Cs[cbuf], ws.stk, ws.scr, ld, sx, sy, sw,
-                                                   p, lane, pts);
+          }
+          df lik = df_make(0.0f, 0.0f);
+          int pts = 0;
+          if (balanced) {
+            if (lane == 0) {
+                s_prog[warp] = ws.prog[pbuf];
+                s_cs[warp] = ws.Cs[cbuf];
+                s_cost[warp] = active ? ninstr : -1;
+                s_count[warp] = count;
+                s_bad[warp] = 0;
+            }
+            if (threadIdx.x == 0) s_next = 0;
+            __syncthreads();
+            /* rank of this lane's chain (lane < nwarps) by program length, longest first */
+            int my_rank = 64, nact = 0;
+            {
+                const int cl = lane < nwarps ? s_cost[lane] : -1;
+                int rk = 0;
+                for (int j = 0; j < nwarps; ++j) {
+                    const int cj = s_cost[j];
+                    nact += cj >= 0;
+                    rk += (cj > cl) || (cj == cl && j < lane);
+                }
+                if (cl >= 0) my_rank = rk;
+            }
+            const int ntasks = nact * npass;
+#pragma unroll 1
+            for (;;) {
+                int t = 0;
+                if (lane == 0) t = atomicAdd(&s_next, 1);
+                t = __shfl_sync(FULLMASK, t, 0);
+                if (t >= ntasks) break;
+                const int q = t / npass, pass = t - q * npass;
+                const int w = __ffs(__ballot_sync(FULLMASK, my_rank == q)) - 1;
+                if (s_bad[w]) continue;
+                bool bad;
+                const float sl = eval_pass<K, ONEPASS, ROLLED>(s_prog[w], s_cs[w], ws.stk, ws.scr, ld, sx, sy, sw,
+                                                               p, lane, pass, bad, pts);
+                const df S = warp_sum_df(df_make(sl, 0.0f));
+                const bool anybad = __any_sync(FULLMASK, bad);
+                if (lane == 0) {
+                    s_part_hi[w][pass] = S.hi;
+                    s_part_lo[w][pass] = S.lo;
+                    if (anybad) s_bad[w] = 1;
+                }
+                st_np += (unsigned long long)(s_count[w] + 4) *
+                         (unsigned)(ONEPASS ? p.nd : min(32 * K, p.nd - pass * 32 * K));
+            }
+            __syncthreads();
+            if (active) {
+                if (s_bad[warp]) {
+                    lik = df_make(-INFINITY, 0.0f);
+                } else {
+                    df S = df_make(0.0f, 0.0f);
+                    for (int q = 0; q < npass; ++q) S = df_add(S, df_make(s_part_hi[warp][q], s_part_lo[warp][q]));
+                    lik = !isfinite(S.hi) ? df_make(-INFINITY, 0.0f)
+                                          : df_sub(df_neg(S), df_make(p.normsum_hi, p.normsum_lo));
+                }
+            }
+          } else if (active) {
+            lik = eval_loglik<K, ONEPASS, ROLLED>(ws.prog[pbuf], ws.Cs[cbuf], ws.stk, ws.scr, ld, sx, sy, sw,
+                                                  p, lane, pts);
+            st_np += (unsigned long long)(count + 4) * (unsigned)pts;
+          }
+          st_pts += (unsigned)pts;
+          if (active) {
             const df prior = df_add(length_prior(len, p), cs);
             const df post = df_add(prior, lik);
-            st_evals++; st_pts += (unsigned)pts; st_nodes += (unsigned)count;
-            st_np += (unsigned long long)(count + 4) * (unsigned)pts;
+            st_evals++; st_nodes += (unsigned)count;
             bool accept = true;
             if (!init) {
                 accept = mh_accept<RNG>(post, cur_post, backward, forward, r, p);
@@ -1031,7 +1153,7 @@ __global__ void __launch_bounds__(256, 3) mh_block_kernel(const __grid_constant_
             }
             if (accept) {
                 cur = pbuf; ccur = cbuf;
-                cur_len = len; cur_count = count; cur_cs = cs;
+                cur_len = len; cur_count = count; cur_ninstr = ninstr; cur_cs = cs;
                 cur_prior = prior; cur_lik = lik; cur_post = post;
             }
             __syncwarp();
@@ -1048,11 +1170,15 @@ __global__ void __launch_bounds__(256, 3) mh_block_kernel(const __grid_constant_
         if (active && lane == 0) {
             p.prior[chain] = df_to_double_unscaled(cur_prior);
             p.lik[chain] = df_to_double_unscaled(cur_lik);
+        }
+        if (lane == 0 && p.stats) {
+            atomicAdd(&p.stats[GPR_STAT_EVAL_POINTS], st_pts);
+            atomicAdd(&p.stats[GPR_STAT_EVAL_NODE_POINTS], st_np);
+        }
+        if (active && lane == 0) {
             if (p.stats) {
                 atomicAdd(&p.stats[GPR_STAT_EVALS], (unsigned long long)st_evals);
                 atomicAdd(&p.stats[GPR_STAT_EVAL_NODES], st_nodes);
-                atomicAdd(&p.stats[GPR_STAT_EVAL_POINTS], st_pts);
-                atomicAdd(&p.stats[GPR_STAT_EVAL_NODE_POINTS], st_np);
                 atomicAdd(&p.stats[GPR_STAT_STRUCT_PROPOSED], (unsigned long long)st_sp);
                 atomicAdd(&p.stats[GPR_STAT_STRUCT_ACCEPTED], (unsigned long long)st_sa);
                 atomicAdd(&p.stats[GPR_STAT_CONST_PROPOSED], (unsigned long long)st_cp);
