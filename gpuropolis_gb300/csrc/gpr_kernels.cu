@@ -71,11 +71,13 @@ __global__ void __launch_bounds__(128) eval_values_kernel(const __grid_constant_
         count[chain] = co.count;
     }
     __syncwarp();
+    build_eval_program(ws.prog[0], ws.Cs[0], co.ninstr, ws.eprog, lane);
+    __syncwarp();
     for (int b = 0; b < nx; b += 32) {
         float x[1], acc[1];
         int i = b + lane;
         x[0] = i < nx ? xs[i] : 0.0f;
-        run_program<1, false>(ws.prog[0], ws.Cs[0], x, acc, ws.stk, ws.scr, lane);
+        run_program<1, false>(ws.eprog, x, acc, ws.stk, ws.scr, lane);
         if (i < nx) out[(size_t)chain * nx + i] = acc[0];
     }
 }

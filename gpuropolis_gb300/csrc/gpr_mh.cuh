@@ -367,6 +367,20 @@ static __device__ CompileOut compile_parallel(const uint8_t* ops, int PL, uint32
     return out;
 }
 
+/* The program the evaluator runs: each instruction word paired with the
+ * constant it reads (NaN for the invalid-op marker), so one 64-bit shared
+ * load fetches both.  Rebuilt for every proposal, lanes in parallel. */
+__device__ __forceinline__ void build_eval_program(const uint32_t* prog, const float* Cs, int ninstr,
+                                                   uint2* eprog, int lane) {
+#pragma unroll 1
+    for (int i = lane; i < ninstr; i += 32) {
+        const uint32_t ins = prog[i];
+        const uint32_t node = (ins >> 8) & 0xffu;
+        const float c = (node == 255u) ? __int_as_float(0x7fc00000) : Cs[node];
+        eprog[i] = make_uint2(ins, __float_as_uint(c));
+    }
+}
+
 /* ------------------------------------------------------------------------ */
 /* The evaluator: acc[k] = f(x[k]) for this lane's K points.
  *
@@ -431,22 +445,21 @@ __device__ __forceinline__ void heavy_staged(float (&acc)[K], const float (&w)[K
  * (more code, full ILP).  Which is faster depends on how much of the kernel
  * the instruction cache holds; gpr_autotune measures it. */
 template <int K, bool ROLLED>
-__device__ __forceinline__ void run_program(const uint32_t* __restrict__ prog,
-                                            const float* __restrict__ Cs,
+__device__ __forceinline__ void run_program(const uint2* __restrict__ prog,
                                             const float (&x)[K], float (&acc)[K],
                                             float* __restrict__ stk, float* __restrict__ scr,
                                             int lane) {
     int sp = 0;
     int pc = 0;
-    uint32_t ins = prog[0];
+    uint2 insw = prog[0];
 #pragma unroll 1
     for (;;) {
+        const uint32_t ins = insw.x;
         const uint32_t code = ins & 0xffu;
         if (code == I_END) break;
-        const uint32_t nxt = prog[pc + 1];   /* the program ends with I_END: always in bounds */
+        const uint2 nxt = prog[pc + 1];      /* the program ends with I_END: always in bounds */
         ++pc;
-        const uint32_t node = (ins >> 8) & 0xffu;
-        const float c = (node == 255u) ? __int_as_float(0x7fc00000) : Cs[node];
+        const float c = __uint_as_float(insw.y);
         if (code >= I_BIN0) {
             const uint32_t bop = (code - I_BIN0) >> 3;
             const uint32_t accleft = (code >> 2) & 1u;
@@ -553,7 +566,7 @@ __device__ __forceinline__ void run_program(const uint32_t* __restrict__ prog,
             }
         }
     next_ins:
-        ins = nxt;
+        insw = nxt;
     }
 }
 
@@ -570,6 +583,7 @@ struct WarpSmem {
     uint8_t* ops[2];
     float* Cs[2];
     uint32_t* prog[2];
+    uint2* eprog;    /* evaluation program: (instruction, constant) pairs */
     int* off;        /* per constant: offset of its first draw   */
     int* ndr;        /* per constant: draws used                 */
     float* fw;       /* per constant: forward log-density term   */
@@ -594,6 +608,7 @@ __host__ __device__ __forceinline__ size_t warp_smem_bytes(int PL, int max_instr
     b += 2 * plp;                                /* ops */
     b += align16(2 * plp * 4);                   /* Cs */
     b += align16(2 * (size_t)max_instr * 4);     /* prog */
+    b += align16((size_t)max_instr * 8);         /* eprog */
     b += shared_region_bytes(PL, levels, K);     /* stack + scratch | constant-move records */
     return align16(b);
 }
@@ -606,6 +621,7 @@ __device__ __forceinline__ WarpSmem carve_warp(uint8_t* base, int PL, int max_in
     w.ops[0] = p; w.ops[1] = p + plp; p += 2 * plp;
     w.Cs[0] = (float*)p; w.Cs[1] = (float*)p + plp; p += align16(2 * plp * 4);
     w.prog[0] = (uint32_t*)p; w.prog[1] = (uint32_t*)p + max_instr; p += align16(2 * (size_t)max_instr * 4);
+    w.eprog = (uint2*)p; p += align16((size_t)max_instr * 8);
     w.stk = (float*)p;
     w.scr = w.stk + (size_t)levels * K * 32;
     w.off = (int*)p;
@@ -627,7 +643,7 @@ struct LaneData {
  * invalid.  Used by the CTA-balanced evaluation, where any warp of the CTA may
  * evaluate any chain's pass. */
 template <int K, bool ONEPASS, bool ROLLED>
-__device__ __forceinline__ float eval_pass(const uint32_t* prog, const float* Cs, float* stk, float* scr,
+__device__ __forceinline__ float eval_pass(const uint2* prog, float* stk, float* scr,
                                            const LaneData<K>& ld, const float* sx, const float* sy,
                                            const float* sw, const KParams& p, int lane, int pass,
                                            bool& bad, int& pts) {
@@ -648,7 +664,7 @@ __device__ __forceinline__ float eval_pass(const uint32_t* prog, const float* Cs
             valid |= (v ? 1u : 0u) << k;
         }
     }
-    run_program<K, ROLLED>(prog, Cs, x, acc, stk, scr, lane);
+    run_program<K, ROLLED>(prog, x, acc, stk, scr, lane);
     pts += ONEPASS ? p.nd : min(32 * K, p.nd - pass * 32 * K);
     float s = 0.0f;
     bad = false;
@@ -671,7 +687,7 @@ __device__ __forceinline__ float eval_pass(const uint32_t* prog, const float* Cs
  * sums are combined with error-free transforms (FP64 on GB300 runs at about
  * 1/70 of the FP32 rate, so no FP64 instruction is issued here). */
 template <int K, bool ONEPASS, bool ROLLED>
-__device__ __forceinline__ df eval_loglik(const uint32_t* prog, const float* Cs, float* stk, float* scr,
+__device__ __forceinline__ df eval_loglik(const uint2* prog, float* stk, float* scr,
                                           const LaneData<K>& ld, const float* sx, const float* sy,
                                           const float* sw, const KParams& p, int lane, int& pts) {
     float s = 0.0f;
@@ -696,7 +712,7 @@ __device__ __forceinline__ df eval_loglik(const uint32_t* prog, const float* Cs,
                 valid |= (v ? 1u : 0u) << k;
             }
         }
-        run_program<K, ROLLED>(prog, Cs, x, acc, stk, scr, lane);
+        run_program<K, ROLLED>(prog, x, acc, stk, scr, lane);
         pts += ONEPASS ? p.nd : min(32 * K, p.nd - pass * 32 * K);
 #pragma unroll
         for (int k = 0; k < K; ++k) {
@@ -929,8 +945,13 @@ __device__ __forceinline__ bool mh_accept(df ppost, df cur_post, df backward, df
     return accept;
 }
 
+/* Resident CTAs (of 8 warps) per SM the register allocation is sized for. */
+#ifndef GPR_MIN_CTAS
+#define GPR_MIN_CTAS 3
+#endif
+
 template <int K, bool ONEPASS, int RNG, bool ROLLED>
-__global__ void __launch_bounds__(256, 3) mh_block_kernel(const __grid_constant__ KParams p) {
+__global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __grid_constant__ KParams p) {
     extern __shared__ __align__(128) uint8_t smem[];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -965,8 +986,7 @@ __global__ void __launch_bounds__(256, 3) mh_block_kernel(const __grid_constant_
     /* CTA-balanced evaluation (lockstep == 1): each warp publishes its chain's
      * program; all warps then pull (chain, pass) tasks, longest programs
      * first, and leave per-pass partial sums here. */
-    __shared__ const uint32_t* s_prog[8];
-    __shared__ const float* s_cs[8];
+    __shared__ const uint2* s_prog[8];
     __shared__ int s_cost[8];
     __shared__ int s_count[8];
     __shared__ int s_bad[8];
@@ -1077,13 +1097,14 @@ __global__ void __launch_bounds__(256, 3) mh_block_kernel(const __grid_constant_
             }
             if (need_cauchy) cs = cauchy_sum(ws.Cs[cbuf], p, lane);
             if (structural) backward = df_make(__fmul_rn(-p.logcount[count], GPR_DF_SCALE), 0.0f);
+            build_eval_program(ws.prog[pbuf], ws.Cs[cbuf], ninstr, ws.eprog, lane);
+            __syncwarp();
           }
           df lik = df_make(0.0f, 0.0f);
           int pts = 0;
           if (balanced) {
             if (lane == 0) {
-                s_prog[warp] = ws.prog[pbuf];
-                s_cs[warp] = ws.Cs[cbuf];
+                s_prog[warp] = ws.eprog;
                 s_cost[warp] = active ? ninstr : -1;
                 s_count[warp] = count;
                 s_bad[warp] = 0;
@@ -1113,9 +1134,12 @@ __global__ void __launch_bounds__(256, 3) mh_block_kernel(const __grid_constant_
                 const int w = __ffs(__ballot_sync(FULLMASK, my_rank == q)) - 1;
                 if (s_bad[w]) continue;
                 bool bad;
-                const float sl = eval_pass<K, ONEPASS, ROLLED>(s_prog[w], s_cs[w], ws.stk, ws.scr, ld, sx, sy, sw,
+                const float sl = eval_pass<K, ONEPASS, ROLLED>(s_prog[w], ws.stk, ws.scr, ld, sx, sy, sw,
                                                                p, lane, pass, bad, pts);
-                const df S = warp_sum_df(df_make(sl, 0.0f));
+                /* FP32 butterfly within the pass (terms are >= 0: <= 5 roundings),
+                 * double-float across passes */
+                const float Sp = warp_sum(sl);
+                const df S = df_make(Sp, 0.0f);
                 const bool anybad = __any_sync(FULLMASK, bad);
                 if (lane == 0) {
                     s_part_hi[w][pass] = S.hi;
@@ -1137,8 +1161,7 @@ __global__ void __launch_bounds__(256, 3) mh_block_kernel(const __grid_constant_
                 }
             }
           } else if (active) {
-            lik = eval_loglik<K, ONEPASS, ROLLED>(ws.prog[pbuf], ws.Cs[cbuf], ws.stk, ws.scr, ld, sx, sy, sw,
-                                                  p, lane, pts);
+            lik = eval_loglik<K, ONEPASS, ROLLED>(ws.eprog, ws.stk, ws.scr, ld, sx, sy, sw, p, lane, pts);
             st_np += (unsigned long long)(count + 4) * (unsigned)pts;
           }
           st_pts += (unsigned)pts;

@@ -145,8 +145,9 @@ def _fragile(tr):
     c[0], "basic" if c[1] else "ref", "philox" if c[2] else "lcg", "rw" if c[3] else "indep"))
 def test_mh_block_matches_reference(lib, case):
     """After a block, chains are bit-identical to the reference's; every chain
-    that is not first departs at an accept decision that lies within FP32
-    noise of its threshold (the proposals themselves are bit-exact)."""
+    that is not has, at or before its first differing step, an accept decision
+    that lies within FP32 noise of its threshold (the proposals themselves are
+    bit-exact)."""
     _need_ref()
     from oracle import port
     PL, ops, rng, cmode, rw_sd, data = case
@@ -182,7 +183,11 @@ def test_mh_block_matches_reference(lib, case):
         newly = pending & differ
         first[newly] = st - 1
         pending &= ~differ
-    unexplained = [i for i in np.where(~same)[0] if first[i] < 0 or not _fragile(trace[i, first[i]])]
+    # A fragile decision can also leave the states equal and only shift the
+    # random streams (one side accepts with acceptance > 0, the other with a
+    # uniform draw), so it may come before the first differing state.
+    unexplained = [i for i in np.where(~same)[0]
+                   if first[i] < 0 or not any(_fragile(trace[i, t]) for t in range(first[i] + 1))]
     assert not unexplained, [(i, first[i], trace[i, max(first[i], 0)]) for i in unexplained[:5]]
 
     # scores of identical chains: 1e-5 relative, unless the FP32 value itself
