@@ -14,6 +14,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -568,3 +569,209 @@ int gpr_reset_stats(gpr_handle* h) {
 }
 
 }  /* extern "C" */
+
+/* ------------------------------------------------------------------------ */
+/* gpr_run_block_noalloc: the MH block on chain state that the caller keeps in
+ * its own device memory, with everything else the kernel reads or counts in
+ * one fixed scratch array per device instead of handle allocations.
+ *
+ * Scratch layout (bytes):
+ *   [0, 8)        int[2]: [0] next chain to claim, [1] kernel error flags.
+ *                 Both must be 0 when the kernel starts; every call zeroes them
+ *                 on its stream before the launch.
+ *   [256, ...)    logf(k) for k = 0 .. program_length + 1 (Hastings terms).
+ *   [1536, ...)   x | y | w, GPR_NOALLOC_MAX_POINTS floats each, w being the
+ *                 per-point likelihood weight 2^-64 / (2 sd^2).
+ * Every call rewrites the table and the dataset before its launch, so nothing
+ * left by an earlier call is read.  Two calls in flight on one device at once
+ * share the array and race. */
+static const size_t kNoallocLogcount = 256;
+static const size_t kNoallocData = kNoallocLogcount + ((GPR_MAX_PROGRAM_LENGTH + 2) * sizeof(float) + 255) / 256 * 256;
+static const size_t kNoallocBytes = kNoallocData + 3 * (size_t)GPR_NOALLOC_MAX_POINTS * sizeof(float);
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
+
+enum { kNoallocMaxDevices = 64 };
+static std::mutex g_noalloc_mu;
+static unsigned char* g_noalloc_addr[kNoallocMaxDevices];
+static int g_noalloc_sms[kNoallocMaxDevices];
+
+/* The weights of gpr_set_data, computed in place from sd on the device (the
+ * same IEEE double operations and rounding as the host code), and zero
+ * padding up to nd_pad, which the kernel stages with the data. */
+static __global__ void noalloc_data_kernel(float* x, float* y, float* w, int n, int nd_pad) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nd_pad) return;
+    if (i < n) {
+        const double s = (double)w[i];
+        w[i] = (float)(0x1p-64 / (2.0 * s * s));
+    } else {
+        x[i] = 0.0f; y[i] = 0.0f; w[i] = 0.0f;
+    }
+}
+
+/* One-time per device (device current): the scratch's device address and the
+ * SM count. */
+static int noalloc_setup(int device, unsigned char** scratch, int* sms) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess)
+            return fail(nullptr, GPR_ERR_CUDA, "cudaGetSymbolAddress(scratch) failed: %s", cudaGetErrorString(e));
+        int n = 0;
+        e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, device);
+        if (e != cudaSuccess)
+            return fail(nullptr, GPR_ERR_CUDA, "cudaDeviceGetAttribute failed: %s", cudaGetErrorString(e));
+        g_noalloc_sms[device] = n;
+        g_noalloc_addr[device] = (unsigned char*)p;
+    }
+    *scratch = g_noalloc_addr[device];
+    *sms = g_noalloc_sms[device];
+    return GPR_OK;
+}
+
+/* The kernel parameters gpr_create derives from a configuration, with the
+ * Hastings table written to lc (program_length + 2 entries). */
+static void noalloc_params(gpr::KParams& kp, const gpr_config* cfg, int n_chains, float* lc) {
+    const int PL = cfg->program_length;
+    memset(&kp, 0, sizeof kp);
+    kp.N = n_chains; kp.PL = PL;
+    kp.rng_mode = cfg->rng;
+    kp.const_mode = cfg->const_proposal;
+    kp.rw_sd = cfg->rw_sd;
+    kp.nops = cfg->n_ops;
+    for (int i = 0; i < cfg->n_ops; ++i) kp.opmap[i] = (int8_t)cfg->ops[i];
+    kp.mag_pl = magic_for(divisor_for(PL));
+    kp.mag_nops = magic_for(divisor_for(cfg->n_ops));
+    kp.mag_1e6 = magic_for(divisor_for(1000000));
+    const double ln1 = log((double)cfg->n_ops + 1) * 0x1p-64;
+    kp.ln1_hi = (float)ln1;
+    kp.ln1_lo = (float)(ln1 - (double)kp.ln1_hi);
+    const double PIf = 3.141592653589;
+    kp.lpi_f = logf((float)PIf);
+    kp.lnorm1_f = (float)(0.5 * ((double)logf((float)(2.0 * PIf)) + 2.0 * (double)logf(1.0f)));
+    const float R = 0.1f, PI_INT = 0.15f;
+    kp.logf_r = logf(R);
+    kp.log1mr_f = (float)log(1.0 - (double)R);
+    kp.log2_f = (float)log(2.0);
+    kp.logpi_f = logf(PI_INT);
+    kp.log1mpi_f = (float)log(1.0 - (double)PI_INT);
+    kp.geom_logr = gpr_rng_logf(R);
+    kp.lockstep = 1;
+    kp.max_instr = GPR_MAX_INSTR(PL);
+    int lev = 1;
+    while ((1 << lev) <= PL / 2) ++lev;
+    kp.levels = lev;
+    gpr::fill_lcg_jump_table(kp);
+    for (int k = 0; k < PL + 2; ++k) lc[k] = logf((float)k);
+}
+
+extern "C" int gpr_run_block_noalloc(const gpr_config* cfg, int n_chains, int32_t* P, float* C,
+                                     double* prior, double* likelihood, const float* x,
+                                     const float* y, const float* sd, int ndata, int steps,
+                                     int random_seed) {
+    /* arguments first, before any CUDA call */
+    if (!cfg) return fail(nullptr, GPR_ERR_ARG, "cfg is NULL");
+    if (n_chains <= 0) return fail(nullptr, GPR_ERR_ARG, "n_chains must be > 0 (got %d)", n_chains);
+    const int PL = cfg->program_length;
+    if (PL < 1 || PL > GPR_MAX_PROGRAM_LENGTH || (PL % 2) == 0)
+        return fail(nullptr, GPR_ERR_ARG, "program_length must be odd and in [1, %d] (got %d)",
+                    GPR_MAX_PROGRAM_LENGTH, PL);
+    if (cfg->n_ops < 1 || cfg->n_ops > GPR_MAX_OPS)
+        return fail(nullptr, GPR_ERR_ARG, "n_ops must be in [1, %d] (got %d)", GPR_MAX_OPS, cfg->n_ops);
+    for (int i = 0; i < cfg->n_ops; ++i)
+        if (cfg->ops[i] < 0 || cfg->ops[i] >= OP_NREF)
+            return fail(nullptr, GPR_ERR_ARG, "ops[%d] = %d is not an op code", i, cfg->ops[i]);
+    if (cfg->rng != GPR_RNG_LCG && cfg->rng != GPR_RNG_PHILOX)
+        return fail(nullptr, GPR_ERR_ARG, "unknown rng mode %d", cfg->rng);
+    if (cfg->const_proposal != GPR_CONST_REFERENCE && cfg->const_proposal != GPR_CONST_RANDOM_WALK)
+        return fail(nullptr, GPR_ERR_ARG, "unknown constant proposal %d", cfg->const_proposal);
+    if ((long long)n_chains * PL > (1ll << 31) - 1)
+        return fail(nullptr, GPR_ERR_ARG, "n_chains * program_length exceeds 2^31-1");
+    if (!P || !C || !prior || !likelihood)
+        return fail(nullptr, GPR_ERR_ARG, "P, C, prior and likelihood must be non-NULL device pointers");
+    if (steps < 0) return fail(nullptr, GPR_ERR_ARG, "steps must be >= 0 (got %d)", steps);
+    if (ndata < 0) return fail(nullptr, GPR_ERR_ARG, "ndata must be >= 0");
+    if (ndata > GPR_NOALLOC_MAX_POINTS)
+        return fail(nullptr, GPR_ERR_ARG,
+                    "ndata = %d exceeds the %d points of the no-allocation scratch; "
+                    "use gpr_create and gpr_set_data for larger datasets", ndata, GPR_NOALLOC_MAX_POINTS);
+    if (ndata > 0 && (!x || !y || !sd)) return fail(nullptr, GPR_ERR_ARG, "x, y, sd must be non-NULL");
+    for (int i = 0; i < ndata; ++i)
+        if (!(sd[i] > 0.0f)) return fail(nullptr, GPR_ERR_ARG, "sd[%d] = %g is not > 0", i, (double)sd[i]);
+    if (cfg->device < 0 || cfg->device >= kNoallocMaxDevices)
+        return fail(nullptr, GPR_ERR_ARG, "invalid GPU device %d", cfg->device);
+
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess) return fail(nullptr, GPR_ERR_CUDA, "cudaGetDeviceCount: %s", cudaGetErrorString(e));
+    if (cfg->device >= ndev)
+        return fail(nullptr, GPR_ERR_ARG, "invalid GPU device %d (%d present)", cfg->device, ndev);
+    e = cudaSetDevice(cfg->device);
+    if (e != cudaSuccess) return fail(nullptr, GPR_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
+    unsigned char* scratch = nullptr;
+    int sms = 0;
+    int rc = noalloc_setup(cfg->device, &scratch, &sms);
+    if (rc != GPR_OK) return rc;
+
+    /* A handle on the stack that points at the caller's state and the
+     * scratch; the launch geometry, launch and error check are the handle
+     * path's own. */
+    gpr_handle h;
+    h.cfg = *cfg;
+    h.N = n_chains;
+    h.PL = PL;
+    h.device = cfg->device;
+    h.stream = (cudaStream_t)cfg->stream;
+    h.num_sms = sms;
+    h.dP = P; h.dC = C; h.dprior = prior; h.dlik = likelihood;
+    h.dcounter = (int*)scratch;
+    h.dlogcount = (float*)(scratch + kNoallocLogcount);
+    float* sx = (float*)(scratch + kNoallocData);
+    float* sy = sx + GPR_NOALLOC_MAX_POINTS;
+    float* sw = sy + GPR_NOALLOC_MAX_POINTS;
+    float lc[GPR_MAX_PROGRAM_LENGTH + 2];
+    gpr::KParams& kp = h.kp;
+    noalloc_params(kp, cfg, n_chains, lc);
+    kp.P = P; kp.C = C; kp.prior = prior; kp.lik = likelihood;
+    kp.logcount = h.dlogcount;
+    kp.next_chain = h.dcounter;
+    kp.err = h.dcounter + 1;
+    kp.stats = nullptr;
+
+    const int nd_pad = (ndata + 3) & ~3;
+    double normsum = 0.0;
+    const double PIf = 3.141592653589;
+    for (int i = 0; i < ndata; ++i)
+        normsum += 0.5 * ((double)logf((float)(2.0 * PIf)) + 2.0 * (double)logf(sd[i]));
+    h.nd = ndata;
+    h.nd_pad = nd_pad;
+    h.normsum = normsum;
+    kp.nd = ndata; kp.nd_pad = nd_pad;
+    const double ns = normsum * 0x1p-64;
+    kp.normsum_hi = (float)ns;
+    kp.normsum_lo = (float)(ns - (double)kp.normsum_hi);
+    kp.dx = sx; kp.dy = sy; kp.dw = sw;
+
+    auto report = [&](int code) { g_create_error = h.err; return code; };
+#define NA_TRY(call)                                                                            \
+    do {                                                                                        \
+        cudaError_t e_ = (call);                                                                \
+        if (e_ != cudaSuccess)                                                                  \
+            return fail(nullptr, GPR_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+    NA_TRY(cudaMemsetAsync(h.dcounter, 0, 2 * sizeof(int), h.stream));
+    NA_TRY(cudaMemcpyAsync(h.dlogcount, lc, (PL + 2) * sizeof(float), cudaMemcpyHostToDevice, h.stream));
+    if (ndata > 0) {
+        NA_TRY(cudaMemcpyAsync(sx, x, ndata * sizeof(float), cudaMemcpyHostToDevice, h.stream));
+        NA_TRY(cudaMemcpyAsync(sy, y, ndata * sizeof(float), cudaMemcpyHostToDevice, h.stream));
+        NA_TRY(cudaMemcpyAsync(sw, sd, ndata * sizeof(float), cudaMemcpyHostToDevice, h.stream));
+        noalloc_data_kernel<<<(nd_pad + 255) / 256, 256, 0, h.stream>>>(sx, sy, sw, ndata, nd_pad);
+        NA_TRY(cudaGetLastError());
+    }
+#undef NA_TRY
+    if ((rc = choose_launch(&h)) != GPR_OK) return report(rc);
+    if ((rc = run(&h, steps, random_seed)) != GPR_OK) return report(rc);
+    if ((rc = gpr_sync(&h)) != GPR_OK) return report(rc);
+    return GPR_OK;
+}

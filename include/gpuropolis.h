@@ -161,6 +161,43 @@ int gpr_layout_lockstep(gpr_handle* h);
 int gpr_get_stats(gpr_handle* h, uint64_t* out, int n);
 int gpr_reset_stats(gpr_handle* h);
 
+/* ---- running without allocating (no counterpart in the reference) ---- */
+
+/* Largest dataset gpr_run_block_noalloc takes: its fixed device scratch holds
+ * x, y and a weight for this many points (48 KB, plus 1.5 KB of tables). */
+#define GPR_NOALLOC_MAX_POINTS 4096
+
+/* Run `steps` MH steps (as gpr_run_block) on chains whose state the caller
+ * keeps in its own device memory, allocating nothing: no handle, no device
+ * memory, no host buffers.  It is for callers that must not allocate: a
+ * process whose device memory belongs to another allocator's pool (a library
+ * cudaMalloc beside that pool can fail, or fragment and shrink it), or a
+ * loop that cannot pay for cudaMalloc/cudaFree, which may synchronise the
+ * whole device.
+ *
+ * P, C (program_length * n_chains, the reference layout P[i*N + chain]; P must
+ * hold valid op codes), prior and likelihood (n_chains doubles) are DEVICE
+ * pointers, read and updated in place like the reference kernel's arguments
+ * (main.cu:1160).  x, y, sd are HOST arrays of ndata points, sd > 0.  A
+ * dataset of more than GPR_NOALLOC_MAX_POINTS points is rejected with
+ * GPR_ERR_ARG before any device work; use gpr_create + gpr_set_data for it.
+ * The results are those of gpr_create + gpr_set_data + gpr_set_state +
+ * gpr_run_block with the default layout and the same seed.
+ *
+ * The dataset, the Hastings-term table and two counters (next chain, error
+ * flags: both must be 0 when the kernel starts) live in one fixed scratch
+ * array per device.  Each call writes all of them on its stream before its
+ * launch, so the caller zeroes nothing.  Two calls that overlap on one device
+ * (from other threads, or on other streams) share that array and race:
+ * serialise them.  Runs on cfg->stream (NULL: the default stream) and returns
+ * when the block has finished, reporting kernel error flags as gpr_sync does.
+ * The first call on each device does one-time setup (looks up the scratch's
+ * address and loads the device code): make it before any stream capture.
+ * Failures are described by gpr_last_error(NULL). */
+int gpr_run_block_noalloc(const gpr_config* cfg, int n_chains, int32_t* P, float* C,
+                          double* prior, double* likelihood, const float* x, const float* y,
+                          const float* sd, int ndata, int steps, int random_seed);
+
 #ifdef __cplusplus
 }
 #endif
