@@ -113,3 +113,25 @@ def test_host_init_matches_reference(opset):
     P1, C1 = g.host_init_chains(64, 31, 12345, ops=o.ops)
     np.testing.assert_array_equal(P0, P1)
     np.testing.assert_array_equal(C0.view(np.int32), C1.view(np.int32))
+
+
+def _declared_functions(path):
+    """Names of the functions a public header declares (comments stripped)."""
+    import re
+    text = re.sub(r"/\*.*?\*/", "", open(path).read(), flags=re.S)
+    text = re.sub(r"//[^\n]*", "", text)
+    return sorted(set(re.findall(r"\b(gpr_\w+)\s*\(", text)) - {"gpr_config"})
+
+
+@pytest.mark.parametrize("header", ["gpuropolis.h", "gpuropolis_host.h"])
+def test_library_exports_every_declared_function(header):
+    """libgpuropolis.so loads without a GPU and exports every function its
+    headers declare (no compute call is made)."""
+    _lib()
+    import ctypes
+    path = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", header)
+    names = _declared_functions(path)
+    assert len(names) >= 8, names
+    lib = ctypes.CDLL(g.LIB_PATH)
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
