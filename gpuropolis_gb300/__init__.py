@@ -90,6 +90,10 @@ def library():
     lib.gpr_set_layout2.argtypes = [vp, ip, ip, ip, ip, ip]
     lib.gpr_get_stats.argtypes = [vp, vp, ip]
     lib.gpr_reset_stats.argtypes = [vp]
+    lib.gpr_set_scores.argtypes = [vp, vp, vp]
+    lib.gpr_resample.argtypes = [vp, ip, dp, ctypes.c_uint32, vp, vp]
+    lib.gpr_top_chains.argtypes = [vp, ip, dp, vp, ip, vp, vp]
+    lib.gpr_map_chain.argtypes = [vp, vp, vp]
     # host side (include/gpuropolis_host.h)
     lib.gpr_load_data_file.argtypes = [ctypes.c_char_p, fp, ip, ip, P(vp), P(vp), P(vp), P(ip)]
     lib.gpr_free.argtypes = [vp]
@@ -104,6 +108,13 @@ def library():
     lib.gpr_host_srand.argtypes = [ctypes.c_uint]
     lib.gpr_host_init_chains.argtypes = [vp, vp, ip, ip, vp, ip]
     lib.gpr_host_resample.argtypes = [vp, vp, vp, vp, ip, ip, vp, ip, ip, ctypes.c_double]
+    lib.gpr_tops_new.argtypes = [ip]
+    lib.gpr_tops_new.restype = vp
+    lib.gpr_tops_free.argtypes = [vp]
+    lib.gpr_tops_add_text.argtypes = [vp, ctypes.c_char_p, ctypes.c_int64]
+    lib.gpr_tops_add_lines.argtypes = [vp, ctypes.c_char_p, ctypes.c_int64, vp, ip]
+    lib.gpr_tops_write.argtypes = [vp, ctypes.c_char_p]
+    lib.gpr_tops_write.restype = ctypes.c_int64
     _lib = lib
     return lib
 
@@ -236,6 +247,34 @@ class Sampler:
     def reset_stats(self):
         self._check(self.lib.gpr_reset_stats(self.h))
 
+    def set_scores(self, prior, lik):
+        prior = np.ascontiguousarray(prior, np.float64)
+        lik = np.ascontiguousarray(lik, np.float64)
+        assert prior.shape == (self.N,) and lik.shape == (self.N,)
+        self._check(self.lib.gpr_set_scores(self.h, _ptr(prior), _ptr(lik)))
+
+    def resample(self, mode=0, param=0.5, seed=1):
+        """Device resampling (gpr_resample): returns (chains re-drawn, cutoff)."""
+        n, cut = ctypes.c_int(), ctypes.c_double()
+        self._check(self.lib.gpr_resample(self.h, int(mode), float(param), int(seed) & 0xffffffff,
+                                          ctypes.byref(n), ctypes.byref(cut)))
+        return n.value, cut.value
+
+    def top_chains(self, k, margin=0.0, capacity=None):
+        """Candidate chains for the k best (gpr_top_chains): (chains, count, threshold)."""
+        capacity = self.N if capacity is None else capacity
+        out = np.empty(max(capacity, 1), np.int32)
+        n, t = ctypes.c_int(), ctypes.c_double()
+        self._check(self.lib.gpr_top_chains(self.h, int(k), float(margin), _ptr(out), capacity,
+                                            ctypes.byref(n), ctypes.byref(t)))
+        return out[:min(n.value, capacity)].copy(), n.value, t.value
+
+    def map_chain(self):
+        """(MAP chain index, its posterior) (gpr_map_chain)."""
+        c, v = ctypes.c_int(), ctypes.c_double()
+        self._check(self.lib.gpr_map_chain(self.h, ctypes.byref(c), ctypes.byref(v)))
+        return c.value, v.value
+
     def launch_count(self):
         return int(self.lib.gpr_launch_count(self.h))
 
@@ -320,3 +359,41 @@ def host_resample(P, C, prior, lik, ops=None, mode=0, param=0.5):
     lik = np.ascontiguousarray(lik, np.float64)
     return lib.gpr_host_resample(_ptr(P), _ptr(C), _ptr(prior), _ptr(lik), P.shape[1], P.shape[0],
                                  _ptr(ops), len(ops), mode, param)
+
+
+class Tops:
+    """The k lines `LC_ALL=C sort -g -k3 | tail -n k` keeps (gpr_tops_*)."""
+
+    def __init__(self, k):
+        self.lib = library()
+        self.t = self.lib.gpr_tops_new(int(k))
+        if not self.t:
+            raise GprError(1, "k must be >= 1")
+
+    def add_text(self, text):
+        b = text.encode("latin-1") if isinstance(text, str) else text
+        if self.lib.gpr_tops_add_text(self.t, b, len(b)) != 0:
+            raise GprError(1, "gpr_tops_add_text failed")
+
+    def add_lines(self, text, lines):
+        b = text.encode("latin-1") if isinstance(text, str) else text
+        lines = np.ascontiguousarray(lines, np.int32)
+        if self.lib.gpr_tops_add_lines(self.t, b, len(b), _ptr(lines), len(lines)) != 0:
+            raise GprError(1, "gpr_tops_add_lines failed")
+
+    def write(self, path):
+        n = self.lib.gpr_tops_write(self.t, path.encode())
+        if n < 0:
+            raise GprError(1, "gpr_tops_write failed")
+        return n
+
+    def close(self):
+        if self.t:
+            self.lib.gpr_tops_free(self.t)
+            self.t = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

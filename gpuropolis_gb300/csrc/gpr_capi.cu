@@ -14,6 +14,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <algorithm>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -22,6 +23,7 @@
 #include "gpr_common.h"
 #include "gpr_kernels.cuh"
 #include "gpr_rngmath.h"
+#include "gpr_select.h"
 
 #define GPR_VERSION_STRING "gpuropolis-gb300 0.1 (sm_103a)"
 
@@ -42,6 +44,12 @@ struct gpr_handle {
     int* dcounter = nullptr;   /* [0] next chain, [1] error flags */
     unsigned long long* dstats = nullptr;
     float* ddata = nullptr;    /* x | y | w | sd, each nd_pad floats */
+    /* selection scratch, allocated by the first gpr_resample/gpr_top_chains/gpr_map_chain */
+    unsigned long long* dkeys = nullptr;   /* N posterior keys                   */
+    unsigned long long* dsel = nullptr;    /* [0] selected key                   */
+    int* dseli = nullptr;                  /* [0] count, [1] first index         */
+    int* dtop = nullptr;                   /* candidate chains, dtop_cap entries */
+    int dtop_cap = 0;
     int nd = -1;
     int nd_pad = 0;
     double normsum = 0.0;
@@ -108,6 +116,7 @@ int64_t gpr_launch_count(gpr_handle* h) { return h ? h->launches : 0; }
 static void free_all(gpr_handle* h) {
     cudaFree(h->dP); cudaFree(h->dC); cudaFree(h->dprior); cudaFree(h->dlik);
     cudaFree(h->dlogcount); cudaFree(h->dcounter); cudaFree(h->ddata); cudaFree(h->dstats);
+    cudaFree(h->dkeys); cudaFree(h->dsel); cudaFree(h->dseli); cudaFree(h->dtop);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
 }
 
@@ -214,6 +223,9 @@ int gpr_create(const gpr_config* cfg, int n_chains, gpr_handle** out) {
     kp.err = h->dcounter + 1;
     kp.stats = h->dstats;
     kp.lockstep = 1;
+    kp.struct_every = 5;                                           /* main.cu:699 */
+    kp.hmc_eps = 0.01f;
+    kp.hmc_L = 8;
     kp.max_instr = GPR_MAX_INSTR(PL);
     /* Value-stack depth: a push happens at a binary node whose children are
      * both subtrees, so at a node j <= PL/2; pending pushes lie on one
@@ -326,6 +338,16 @@ int gpr_set_state(gpr_handle* h, const int32_t* P, const float* C) {
     CUDA_TRY(h, cudaSetDevice(h->device));
     CUDA_TRY(h, cudaMemcpyAsync(h->dP, P, cnt * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
     CUDA_TRY(h, cudaMemcpyAsync(h->dC, C, cnt * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return GPR_OK;
+}
+
+int gpr_set_scores(gpr_handle* h, const double* prior, const double* likelihood) {
+    if (!h) return GPR_ERR_ARG;
+    if (!prior || !likelihood) return fail(h, GPR_ERR_ARG, "prior and likelihood must be non-NULL");
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    CUDA_TRY(h, cudaMemcpyAsync(h->dprior, prior, h->N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(h->dlik, likelihood, h->N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     return GPR_OK;
 }
@@ -568,6 +590,120 @@ int gpr_reset_stats(gpr_handle* h) {
     return GPR_OK;
 }
 
+/* ---- selection over posteriors (gpr_resample.cu) ---- */
+
+static int ensure_select(gpr_handle* h) {
+    if (!h->dkeys) {
+        CUDA_TRY(h, cudaMalloc(&h->dkeys, (size_t)h->N * sizeof(unsigned long long)));
+        CUDA_TRY(h, cudaMalloc(&h->dsel, 2 * sizeof(unsigned long long)));
+        CUDA_TRY(h, cudaMalloc(&h->dseli, 4 * sizeof(int)));
+    }
+    return GPR_OK;
+}
+
+/* The posterior at ascending rank `rank` (reference comparator order). */
+static int select_rank(gpr_handle* h, int rank, unsigned long long* key) {
+    int rc = ensure_select(h);
+    if (rc != GPR_OK) return rc;
+    CUDA_TRY(h, gpr::launch_select(h->kp, rank, h->dkeys, h->dsel, h->stream));
+    h->launches += 2;
+    if (key) {
+        CUDA_TRY(h, cudaMemcpyAsync(key, h->dsel, sizeof *key, cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    }
+    return GPR_OK;
+}
+
+int gpr_resample(gpr_handle* h, int mode, double param, uint32_t seed, int* n_redrawn, double* cutoff) {
+    if (!h) return GPR_ERR_ARG;
+    if (mode != 0 && mode != 1) return fail(h, GPR_ERR_ARG, "unknown resample mode %d", mode);
+    if (h->cfg.n_ops < 2)
+        return fail(h, GPR_ERR_ARG, "re-drawing ops needs at least 2 ops (random_int(n_ops - 1))");
+    int rank = h->N - 1;
+    if (mode == 0) {
+        const double r = (double)h->N * param;
+        if (!(r >= 0.0 && r < (double)h->N)) return fail(h, GPR_ERR_ARG, "quantile %g is not in [0, 1)", param);
+        rank = (int)r;
+    } else if (!(param >= 0.0)) {
+        return fail(h, GPR_ERR_ARG, "map-delta %g is not >= 0", param);
+    }
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    int rc = select_rank(h, rank, nullptr);
+    if (rc != GPR_OK) return rc;
+    CUDA_TRY(h, cudaMemsetAsync(h->dseli, 0, sizeof(int), h->stream));
+    const gpr::Magic mops1 = magic_for(divisor_for(h->cfg.n_ops - 1));
+    const gpr::Magic morder = magic_for(divisor_for(8));
+    CUDA_TRY(h, gpr::launch_redraw(h->kp, h->dsel, mode, param, seed, mops1, morder, h->dseli, h->stream));
+    h->launches++;
+    if (n_redrawn || cutoff) {
+        unsigned long long key = 0;
+        int cnt = 0;
+        CUDA_TRY(h, cudaMemcpyAsync(&key, h->dsel, sizeof key, cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(h, cudaMemcpyAsync(&cnt, h->dseli, sizeof cnt, cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        if (n_redrawn) *n_redrawn = cnt;
+        if (cutoff) *cutoff = gpr_key_value(key) - (mode == 1 ? param : 0.0);
+    }
+    return GPR_OK;
+}
+
+int gpr_top_chains(gpr_handle* h, int k, double margin, int* chains, int capacity, int* n, double* threshold) {
+    if (!h) return GPR_ERR_ARG;
+    if (k < 1 || k > h->N) return fail(h, GPR_ERR_ARG, "k = %d is not in [1, %d]", k, h->N);
+    if (!(margin >= 0.0)) return fail(h, GPR_ERR_ARG, "margin %g is not >= 0", margin);
+    if (capacity < 0 || (capacity > 0 && !chains) || !n) return fail(h, GPR_ERR_ARG, "bad output arguments");
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    unsigned long long key = 0;
+    int rc = select_rank(h, h->N - k, &key);
+    if (rc != GPR_OK) return rc;
+    const double t = gpr_key_value(key);
+    if (threshold) *threshold = t;
+    /* every non-NaN chain when fewer than k are non-NaN */
+    const unsigned long long kmin = key == 0ull ? 1ull : gpr_post_key(t - margin);
+    if (capacity > h->dtop_cap) {
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        cudaFree(h->dtop);
+        h->dtop = nullptr;
+        h->dtop_cap = 0;
+        CUDA_TRY(h, cudaMalloc(&h->dtop, (size_t)capacity * sizeof(int)));
+        h->dtop_cap = capacity;
+    }
+    CUDA_TRY(h, cudaMemsetAsync(h->dseli, 0, sizeof(int), h->stream));
+    CUDA_TRY(h, gpr::launch_collect(h->dkeys, h->N, kmin, h->dtop, capacity, h->dseli, h->stream));
+    h->launches++;
+    int cnt = 0;
+    CUDA_TRY(h, cudaMemcpyAsync(&cnt, h->dseli, sizeof cnt, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    const int m = cnt < capacity ? cnt : capacity;
+    if (m > 0) {
+        CUDA_TRY(h, cudaMemcpyAsync(chains, h->dtop, (size_t)m * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        std::sort(chains, chains + m);
+    }
+    *n = cnt;
+    return GPR_OK;
+}
+
+int gpr_map_chain(gpr_handle* h, int* chain, double* posterior) {
+    if (!h) return GPR_ERR_ARG;
+    if (!chain) return fail(h, GPR_ERR_ARG, "chain is NULL");
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    int rc = select_rank(h, h->N - 1, nullptr);
+    if (rc != GPR_OK) return rc;
+    const int big = 0x7fffffff;
+    CUDA_TRY(h, cudaMemcpyAsync(h->dseli + 1, &big, sizeof big, cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, gpr::launch_first_index(h->dkeys, h->N, h->dsel, h->dseli + 1, h->stream));
+    h->launches++;
+    unsigned long long key = 0;
+    int idx = big;
+    CUDA_TRY(h, cudaMemcpyAsync(&key, h->dsel, sizeof key, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(&idx, h->dseli + 1, sizeof idx, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    *chain = key == 0ull ? -1 : idx;
+    if (posterior) *posterior = gpr_key_value(key);
+    return GPR_OK;
+}
+
 }  /* extern "C" */
 
 /* ------------------------------------------------------------------------ */
@@ -658,6 +794,9 @@ static void noalloc_params(gpr::KParams& kp, const gpr_config* cfg, int n_chains
     kp.log1mpi_f = (float)log(1.0 - (double)PI_INT);
     kp.geom_logr = gpr_rng_logf(R);
     kp.lockstep = 1;
+    kp.struct_every = 5;
+    kp.hmc_eps = 0.01f;
+    kp.hmc_L = 8;
     kp.max_instr = GPR_MAX_INSTR(PL);
     int lev = 1;
     while ((1 << lev) <= PL / 2) ++lev;

@@ -14,7 +14,11 @@
  * Additional options (all off by default, so the defaults reproduce the
  * reference): --program-length=PL (or --max-len=PL+1), --ops=reference|basic|
  * <comma-separated op codes>, --rng=lcg|philox, --const-proposal=reference|
- * rw:SD, --resample=quantile:Q|map-delta:D, --threads=T.
+ * rw:SD, --resample=quantile:Q|map-delta:D, --threads=T, --device-resample
+ * (resample on the GPU from a Philox stream keyed by the block seed, without
+ * copying the state back and forth), --tops=K (write tops.txt: the K
+ * lines of this run's samples.txt that `sort -g -k3 | tail -n K`, run-all.sh:45,
+ * selects, found with the device's top-k instead of an external sort).
  */
 #include <getopt.h>
 #include <stdio.h>
@@ -36,9 +40,10 @@ static int PL = 31, rng_mode = GPR_RNG_LCG, const_mode = GPR_CONST_REFERENCE, th
 static float rw_sd = 0.1f;
 static int resample_mode = GPR_RESAMPLE_QUANTILE;
 static double resample_param = 0.5;
+static int device_resample = 0, tops_k = 0;
 static std::vector<int> ops;
 
-enum { OPT_PL = 1000, OPT_MAXLEN, OPT_OPS, OPT_RNG, OPT_CONST, OPT_RESAMPLE, OPT_THREADS };
+enum { OPT_PL = 1000, OPT_MAXLEN, OPT_OPS, OPT_RNG, OPT_CONST, OPT_RESAMPLE, OPT_THREADS, OPT_DEVRES, OPT_TOPS };
 
 static struct option long_options[] = {
     {"in", required_argument, NULL, 'd'},
@@ -63,6 +68,8 @@ static struct option long_options[] = {
     {"const-proposal", required_argument, NULL, OPT_CONST},
     {"resample", required_argument, NULL, OPT_RESAMPLE},
     {"threads", required_argument, NULL, OPT_THREADS},
+    {"device-resample", no_argument, NULL, OPT_DEVRES},
+    {"tops", required_argument, NULL, OPT_TOPS},
     {NULL, 0, 0, 0}};
 
 static int parse_ops(const char* s) {
@@ -119,6 +126,8 @@ static int process_arguments(int argc, char** argv) {
                 else return 1;
                 break;
             case OPT_THREADS: threads = atoi(optarg); break;
+            case OPT_DEVRES: device_resample = 1; break;
+            case OPT_TOPS: tops_k = atoi(optarg); if (tops_k < 1) return 1; break;
             default: return 1;
         }
     return 0;
@@ -189,14 +198,23 @@ int main(int argc, char** argv) {
 
     FILE* fp = fopen(SAMPLE_PATH.c_str(), "a");
     if (!fp) { fprintf(stderr, "*** ERROR: Cannot open file:\t%s\n", SAMPLE_PATH.c_str()); gpr_destroy(h); return 1; }
-    write_params(fp, ndata, wgpu);
+    char* head = nullptr;
+    size_t head_len = 0;
+    FILE* hs = open_memstream(&head, &head_len);
+    if (!hs) { fclose(fp); gpr_destroy(h); FAIL("out of memory"); }
+    write_params(hs, ndata, wgpu);
     gpr_host_srand((unsigned)seed);                     /* main.cu:1107 */
-    fprintf(fp, "# -----------------------------------------------------------------\n");
-    fprintf(fp, "# -- Data:\n");
-    fprintf(fp, "# -----------------------------------------------------------------\n");
-    for (int i = 0; i < ndata; i++) fprintf(fp, "# \t%f\t%f\t%f\n", x[i], y[i], sd[i]);
-    fprintf(fp, "#\n#\n");
+    fprintf(hs, "# -----------------------------------------------------------------\n");
+    fprintf(hs, "# -- Data:\n");
+    fprintf(hs, "# -----------------------------------------------------------------\n");
+    for (int i = 0; i < ndata; i++) fprintf(hs, "# \t%f\t%f\t%f\n", x[i], y[i], sd[i]);
+    fprintf(hs, "#\n#\n");
+    fclose(hs);
+    fwrite(head, 1, head_len, fp);
     fclose(fp);
+    gpr_tops* tops = tops_k > 0 ? gpr_tops_new(tops_k) : nullptr;
+    if (tops) gpr_tops_add_text(tops, head, (int64_t)head_len);
+    free(head);
 
     FILE* lg = fopen(LOG_PATH.c_str(), "a");
     if (lg) {
@@ -204,8 +222,8 @@ int main(int argc, char** argv) {
         fprintf(lg, "# \tRNG: %s\n# \tConstant proposal: %s", rng_mode == GPR_RNG_PHILOX ? "philox" : "lcg",
                 const_mode == GPR_CONST_RANDOM_WALK ? "rw:" : "reference");
         if (const_mode == GPR_CONST_RANDOM_WALK) fprintf(lg, "%g", rw_sd);
-        fprintf(lg, "\n# \tResample: %s:%g\n# \tOps:", resample_mode == GPR_RESAMPLE_MAP_DELTA ? "map-delta" : "quantile",
-                resample_param);
+        fprintf(lg, "\n# \tResample: %s:%g%s\n# \tOps:", resample_mode == GPR_RESAMPLE_MAP_DELTA ? "map-delta" : "quantile",
+                resample_param, device_resample ? " (device)" : "");
         for (int o : ops) fprintf(lg, " %d", o);
         fprintf(lg, "\n# \tLibrary: %s\n", gpr_version());
     }
@@ -224,31 +242,63 @@ int main(int argc, char** argv) {
     if (!QUIET) progress_bar(0.0f);
     struct timespec t0, t1;
     clock_gettime(CLOCK_MONOTONIC, &t0);
+    std::vector<int> cand(tops ? (size_t)N : 0);
     for (int o = 0; o < outer; o++) {
         int block_seed = gpr_host_rand();                /* main.cu:1160 */
+        const bool write = o > burn && o % thin == 0;    /* main.cu:1170 */
         if (gpr_run_block(h, steps, block_seed) != GPR_OK ||
-            gpr_get_state(h, P.data(), C.data(), prior.data(), lik.data()) != GPR_OK) {
+            ((write || !device_resample) &&
+             gpr_get_state(h, P.data(), C.data(), prior.data(), lik.data()) != GPR_OK)) {
             fprintf(stderr, "CUDA error: %s\n", gpr_last_error(h));
             gpr_destroy(h);
             return 1;
         }
-        if (o > burn && o % thin == 0) {                 /* main.cu:1170 */
+        if (write) {
             char* buf = nullptr;
             int64_t n = gpr_format_samples(P.data(), C.data(), prior.data(), lik.data(), N, PL, o,
                                            SHOW_CONSTANTS, threads, &buf);
             fp = fopen(SAMPLE_PATH.c_str(), "a");
             if (fp && n > 0) fwrite(buf, 1, (size_t)n, fp);
             if (fp) fclose(fp);
+            if (tops && n > 0) {
+                /* candidates: the chains within 0.002 of the K-th best posterior,
+                 * more than the %.3f rounding can move a line past it */
+                int nc = 0;
+                double thr = 0.0;
+                if (tops_k >= N || gpr_top_chains(h, tops_k, 0.002, cand.data(), N, &nc, &thr) != GPR_OK ||
+                    thr != thr) {
+                    gpr_tops_add_text(tops, buf, n);
+                } else {
+                    gpr_tops_add_lines(tops, buf, n, cand.data(), nc < N ? nc : N);
+                }
+            }
             gpr_free(buf);
         }
-        gpr_host_resample(P.data(), C.data(), prior.data(), lik.data(), N, PL, ops.data(), (int)ops.size(),
-                          resample_mode, resample_param);
-        if (gpr_set_state(h, P.data(), C.data()) != GPR_OK) {
-            fprintf(stderr, "CUDA error: %s\n", gpr_last_error(h));
-            gpr_destroy(h);
-            return 1;
+        if (device_resample) {
+            /* keyed by the block seed: the re-draw streams (seed, chain | 2^31)
+             * never meet the block's own (seed, chain), and the host rand()
+             * stream stays the one the host path draws when nothing is re-drawn */
+            if (gpr_resample(h, resample_mode, resample_param, (uint32_t)block_seed, nullptr, nullptr) != GPR_OK) {
+                fprintf(stderr, "CUDA error: %s\n", gpr_last_error(h));
+                gpr_destroy(h);
+                return 1;
+            }
+        } else {
+            gpr_host_resample(P.data(), C.data(), prior.data(), lik.data(), N, PL, ops.data(), (int)ops.size(),
+                              resample_mode, resample_param);
+            if (gpr_set_state(h, P.data(), C.data()) != GPR_OK) {
+                fprintf(stderr, "CUDA error: %s\n", gpr_last_error(h));
+                gpr_destroy(h);
+                return 1;
+            }
         }
         if (!QUIET) progress_bar(float(o) / float(outer));
+    }
+    if (tops) {
+        std::string TOPS_PATH = out_path + "/tops.txt";
+        if (gpr_tops_write(tops, TOPS_PATH.c_str()) < 0)
+            fprintf(stderr, "*** ERROR: Cannot write file:\t%s\n", TOPS_PATH.c_str());
+        gpr_tops_free(tops);
     }
     clock_gettime(CLOCK_MONOTONIC, &t1);
     if (!QUIET) progress_bar(1.1f);

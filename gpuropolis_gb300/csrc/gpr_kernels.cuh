@@ -67,6 +67,14 @@ struct KParams {
     int levels;        /* value-stack slots per lane                            */
     int max_instr;     /* instruction buffer length per program                 */
 
+    /* move schedule and Hamiltonian constant moves */
+    int struct_every;  /* a structure move every this many steps (main.cu:699: 5); 0 = never */
+    float hmc_eps;     /* leapfrog step of the gradient constant moves          */
+    int hmc_L;         /* leapfrog steps (1 = MALA)                             */
+    float* trace;      /* optional: C[0..trace_n) of each chain after each step,
+                        * trace[(chain * steps + step) * trace_n + i]             */
+    int trace_n;       /* <= 32 */
+
     /* the reference LCG (main.cu:215) advanced 2^b steps is the affine map
      * x -> lcgA[b]*x + lcgC[b] (mod 2^32, then masked to 31 bits) */
     uint32_t lcgA[20];
@@ -103,6 +111,22 @@ cudaError_t launch_eval_values(const KParams& p, const float* xs, int nx, float*
                                float* length, int* count, cudaStream_t st);
 
 cudaError_t launch_math(int op, const float* a, const float* b, float* out, int n, cudaStream_t st);
+
+/* Selection over the chains' posteriors (gpr_resample.cu).  launch_select
+ * writes one order-preserving key per chain (gpr_select.h) into keys and the
+ * key of ascending rank `rank` into *out.  launch_redraw re-draws every chain
+ * whose posterior is below the cutoff -- the value of *sel_key, minus delta
+ * when map_delta -- from the initial distribution, counting them in
+ * *n_redrawn.  launch_collect appends the chains with key >= kmin to out and
+ * counts them; launch_first_index writes the smallest chain with key == k. */
+cudaError_t launch_select(const KParams& p, int rank, unsigned long long* keys, unsigned long long* out,
+                          cudaStream_t st);
+cudaError_t launch_redraw(const KParams& p, const unsigned long long* sel_key, int map_delta, double delta,
+                          uint32_t seed, Magic mag_ops1, Magic mag_order, int* n_redrawn, cudaStream_t st);
+cudaError_t launch_collect(const unsigned long long* keys, int N, unsigned long long kmin, int* out, int cap,
+                           int* count, cudaStream_t st);
+cudaError_t launch_first_index(const unsigned long long* keys, int N, const unsigned long long* k, int* out,
+                               cudaStream_t st);
 
 }  // namespace gpr
 

@@ -945,6 +945,32 @@ __device__ __forceinline__ bool mh_accept(df ppost, df cur_post, df backward, df
     return accept;
 }
 
+/* Structure proposal (main.cu:699-742): a node n uniform in [0, PL) -- the
+ * root when the current state is invalid -- and every node of its subtree
+ * redrawn from the op set, in heap order level by level.  opn receives the
+ * proposal, a copy of oc with that subtree replaced. */
+template <int RNG>
+__device__ __forceinline__ void structure_move(Rng& r, const uint8_t* oc, uint8_t* opn, bool cur_invalid,
+                                               const KParams& p, int lane) {
+    const int PL = p.PL;
+    const int n = cur_invalid ? 0 : random_int<RNG>(r, PL, p.mag_pl);
+#pragma unroll 1
+    for (int i = lane; i < PL; i += 32) opn[i] = oc[i];
+    __syncwarp();
+    const int m = n + 1;
+#pragma unroll 1
+    for (int d = 0;; ++d) {
+        const int lo = m << d;
+        if (lo > PL) break;
+        const int hi = min(lo + (1 << d) - 1, PL);
+#pragma unroll 1
+        for (int j = lo; j <= hi; ++j) {
+            const int k = random_int<RNG>(r, p.nops, p.mag_nops);
+            if (lane == 0) opn[j - 1] = (uint8_t)p.opmap[k];
+        }
+    }
+}
+
 /* Resident CTAs (of 8 warps) per SM the register allocation is sized for. */
 #ifndef GPR_MIN_CTAS
 #define GPR_MIN_CTAS 3
@@ -1048,7 +1074,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
         for (int step = -1; step < p.steps; ++step) {
           if (!balanced && p.lockstep > 0 && (step + 1) % p.lockstep == 0) __syncthreads();
           const bool init = step < 0;
-          const bool structural = !init && (step % 5 == 0);
+          const bool structural = !init && p.struct_every > 0 && (step % p.struct_every == 0);
           int pbuf = cur, cbuf = ccur;
           float len = cur_len;
           int count = cur_count, ninstr = cur_ninstr;
@@ -1058,24 +1084,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
             if (structural) {
                 /* ---- structure move (main.cu:699-742) ---- */
                 forward = df_make(__fmul_rn(-p.logcount[cur_count], GPR_DF_SCALE), 0.0f);
-                const int n = df_invalid(cur_post) ? 0 : random_int<RNG>(r, PL, p.mag_pl);
-                const uint8_t* oc = ws.ops[cur];
-                uint8_t* opn = ws.ops[cur ^ 1];
-                #pragma unroll 1
-                for (int i = lane; i < PL; i += 32) opn[i] = oc[i];
-                __syncwarp();
-                const int m = n + 1;
-#pragma unroll 1
-                for (int d = 0;; ++d) {
-                    const int lo = m << d;
-                    if (lo > PL) break;
-                    const int hi = min(lo + (1 << d) - 1, PL);
-#pragma unroll 1
-                    for (int j = lo; j <= hi; ++j) {
-                        const int k = random_int<RNG>(r, p.nops, p.mag_nops);
-                        if (lane == 0) opn[j - 1] = (uint8_t)p.opmap[k];
-                    }
-                }
+                structure_move<RNG>(r, ws.ops[cur], ws.ops[cur ^ 1], df_invalid(cur_post), p, lane);
                 pbuf = cur ^ 1;
                 need_compile = true;
             } else if (!init) {
@@ -1180,6 +1189,8 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                 cur_prior = prior; cur_lik = lik; cur_post = post;
             }
             __syncwarp();
+            if (p.trace && !init && lane < p.trace_n)
+                p.trace[((size_t)chain * p.steps + step) * p.trace_n + lane] = ws.Cs[ccur][lane];
           }
         }
 

@@ -81,6 +81,12 @@ int gpr_set_data(gpr_handle* h, const float* x, const float* y, const float* sd,
  * P holds program_length*N ints, C program_length*N floats (host memory). */
 int gpr_set_state(gpr_handle* h, const int32_t* P, const float* C);
 
+/* Upload prior and likelihood per chain (host arrays of N doubles; the
+ * reference copies them to the device too, main.cu:1146-1147).  The MH kernel
+ * recomputes both, so this matters only to the selection calls below on a
+ * state the device has not scored. */
+int gpr_set_scores(gpr_handle* h, const double* prior, const double* likelihood);
+
 /* Download chain state (main.cu:1163-1166).  Any pointer may be NULL. */
 int gpr_get_state(gpr_handle* h, int32_t* P, float* C, double* prior, double* likelihood);
 
@@ -160,6 +166,37 @@ int gpr_layout_lockstep(gpr_handle* h);
  * [6]/[7] constant moves proposed/accepted.  Copies min(n, 8) values. */
 int gpr_get_stats(gpr_handle* h, uint64_t* out, int n);
 int gpr_reset_stats(gpr_handle* h);
+
+/* ---- selection over the chains' posteriors, on the device ---- */
+
+/* Resampling of the reference's outer loop (main.cu:1215-1231) without the
+ * two full-state copies around it.  The cutoff is the posterior (prior +
+ * likelihood of the last block) at ascending rank (int)(N * param) in the
+ * order of the reference's comparator, NaN lowest (main.cu:987-995, 1219;
+ * mode GPR_RESAMPLE_QUANTILE = 0, param 0.5 in the reference), or the largest
+ * posterior minus param (mode GPR_RESAMPLE_MAP_DELTA = 1).  Every chain
+ * strictly below it is re-drawn from the initial distribution, all ops then
+ * all constants as main.cu:1224-1228 does: op = ops[random_int(n_ops - 1)],
+ * constant = 10^(random_int(8) - 4) * random_normal().  The draws come from
+ * the Philox stream keyed by (seed, chain | 2^31), not from the host's rand(),
+ * so this is the device counterpart of gpr_host_resample, not a bit-exact
+ * replacement.  Queued on the handle's stream; when n_redrawn or cutoff is
+ * non-NULL the call waits and reports them.  Needs n_ops >= 2. */
+int gpr_resample(gpr_handle* h, int mode, double param, uint32_t seed, int* n_redrawn, double* cutoff);
+
+/* Candidates for the k best chains: every chain whose posterior is >= the
+ * k-th largest posterior minus margin (NaN never; all non-NaN chains when
+ * fewer than k are non-NaN).  Up to `capacity` chain indices are written to
+ * chains in ascending order, *n receives how many qualify (possibly more than
+ * k, or than capacity) and *threshold the k-th largest posterior.  With a
+ * margin above the rounding of the printed score this yields every line that
+ * `sort -g -k3 samples.txt | tail -n k` (run-all.sh:45, tops.txt) can select
+ * from one block. */
+int gpr_top_chains(gpr_handle* h, int k, double margin, int* chains, int capacity, int* n, double* threshold);
+
+/* The MAP chain: the smallest chain index with the largest posterior, and
+ * that posterior (chain -1 when every posterior is NaN). */
+int gpr_map_chain(gpr_handle* h, int* chain, double* posterior);
 
 /* ---- running without allocating (no counterpart in the reference) ---- */
 

@@ -62,6 +62,19 @@ void gpr_host_init_chains(int32_t* P, float* C, int N, int PL, const int* ops, i
 int gpr_host_resample(int32_t* P, float* C, const double* prior, const double* lik, int N, int PL,
                       const int* ops, int n_ops, int mode, double param);
 
+/* tops.txt without the external sort (run-all.sh:45 writes it with
+ * `sort -g -k3 samples.txt | tail -n K`): a set that keeps, of all lines
+ * offered to it, the K lines that command prints in the C locale, and writes
+ * them in its order.  Lines are offered as text ('\n'-separated): all of a
+ * buffer, or the lines at given 0-based indices (ascending). */
+typedef struct gpr_tops gpr_tops;
+gpr_tops* gpr_tops_new(int k);
+int gpr_tops_add_text(gpr_tops* t, const char* text, int64_t len);
+int gpr_tops_add_lines(gpr_tops* t, const char* text, int64_t len, const int* lines, int n);
+/* Write the kept lines, ascending; returns the number written or -1. */
+int64_t gpr_tops_write(gpr_tops* t, const char* path);
+void gpr_tops_free(gpr_tops* t);
+
 #ifdef __cplusplus
 }
 #endif

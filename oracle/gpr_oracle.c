@@ -462,3 +462,45 @@ void gpr_port_run_block_trace(const port_cfg* cfg, int N, int32_t* P, float* C, 
 }
 
 int gpr_port_sizeof_cfg(void) { return (int)sizeof(port_cfg); }
+
+/* ---- resampling (main.cu:1215-1231) with the device's random stream ------ */
+
+/* cmp (main.cu:987-995): NaN sorts below every value. */
+static int port_cmp_bayes(const void* a, const void* b) {
+    double ap = *(const double*)a, bp = *(const double*)b;
+    if (ap > bp || (bp != bp)) return 1;
+    if (ap < bp || (ap != ap)) return -1;
+    return 0;
+}
+
+/* The cutoff of main.cu:1216-1219 (mode 0: sorted[(int)(N*param)]) or the
+ * largest posterior minus param (mode 1); then every chain strictly below it
+ * is re-drawn as main.cu:1224-1228 does -- all PL ops as ops[random_int(n_ops-1)],
+ * then all PL constants as powf(10, random_int(8) - 4) * random_normal() --
+ * from the Philox stream keyed by (seed, chain | 2^31).  Returns the number of
+ * chains re-drawn; *cutoff_out receives the cutoff. */
+int gpr_port_resample(const port_cfg* cfg, int N, int32_t* P, float* C, const double* prior, const double* lik,
+                      int mode, double param, uint32_t seed, double* cutoff_out) {
+    double* post = (double*)malloc((size_t)N * sizeof(double));
+    for (int h = 0; h < N; ++h) post[h] = prior[h] + lik[h];
+    qsort(post, (size_t)N, sizeof(double), port_cmp_bayes);
+    const double cutoff = mode == 1 ? post[N - 1] - param : post[(int)(N * param)];
+    free(post);
+    int redrawn = 0;
+    const int PL = cfg->program_length;
+    for (int h = 0; h < N; ++h) {
+        if (!(prior[h] + lik[h] < cutoff)) continue;
+        port_rng r;
+        r.rng = 1;
+        r.lcg = 0;
+        gpr_philox_stream_init(&r.ph, seed, (uint32_t)h | 0x80000000u);
+        for (int i = 0; i < PL; ++i) P[(size_t)i * N + h] = cfg->ops[port_random_int(cfg->n_ops - 1, &r)];
+        for (int i = 0; i < PL; ++i) {
+            int order = port_random_int(4 - (-4), &r) + (-4);           /* C_MAX_ORDER - C_MIN_ORDER */
+            C[(size_t)i * N + h] = 1.0f * powf(10.0f, (float)order) * port_random_normal(&r, 1);
+        }
+        ++redrawn;
+    }
+    if (cutoff_out) *cutoff_out = cutoff;
+    return redrawn;
+}

@@ -38,6 +38,7 @@ def lib():
         L.gpr_port_likelihood_f64.restype = dp
         L.gpr_port_run_block.argtypes = [ctypes.POINTER(PortCfg), ip, ip, ip, vp, vp, vp, ip, ip, vp, vp, ip, ip]
         L.gpr_port_run_block_trace.argtypes = [ctypes.POINTER(PortCfg), ip, vp, vp, vp, ip, ip, vp, vp, ip, vp, ip]
+        L.gpr_port_resample.argtypes = [ctypes.POINTER(PortCfg), ip, vp, vp, vp, vp, ip, dp, ctypes.c_uint, vp]
         assert L.gpr_port_sizeof_cfg() == ctypes.sizeof(PortCfg)
         _lib = L
     return _lib
@@ -129,3 +130,16 @@ def likelihood(P, C, idx, x, y, sd, f64=False):
     D = pack(x, y, sd)
     f = lib().gpr_port_likelihood_f64 if f64 else lib().gpr_port_likelihood
     return f(_p(P), _p(C), P.shape[1], P.shape[0], idx, _p(D), len(x))
+
+
+def resample(c, P, C, prior, lik, mode, param, seed):
+    """In-place re-draw of the chains below the cutoff with the device's
+    random stream; returns (number re-drawn, cutoff)."""
+    PL, N = P.shape
+    assert P.dtype == np.int32 and C.dtype == np.float32 and P.flags.c_contiguous and C.flags.c_contiguous
+    prior = np.ascontiguousarray(prior, np.float64)
+    lik = np.ascontiguousarray(lik, np.float64)
+    cut = ctypes.c_double()
+    n = lib().gpr_port_resample(ctypes.byref(c), N, _p(P), _p(C), _p(prior), _p(lik), mode, param, seed,
+                                ctypes.byref(cut))
+    return n, cut.value

@@ -70,6 +70,8 @@ class RefOracle:
         lib.gpr_ref_load_data.argtypes = [ctypes.c_char_p, fp, ip, ip, vp, ip]
         lib.gpr_ref_host_random_int.restype = ip
         lib.gpr_ref_host_init.argtypes = [vp, vp, ip, ctypes.c_uint]
+        lib.gpr_ref_resample_cutoff.argtypes = [ip, vp, vp, vp]
+        lib.gpr_ref_resample_cutoff.restype = ctypes.c_double
         self.ops = [lib.gpr_ref_opmap(k) for k in range(self.nops)]
 
     @staticmethod
@@ -126,6 +128,14 @@ class RefOracle:
         n = self.lib.gpr_ref_load_data(path.encode(), sdscale, int(first_half), int(even_half), _p(out),
                                        out.shape[0])
         return out[:n, 0].copy(), out[:n, 1].copy(), out[:n, 2].copy()
+
+    def resample_cutoff(self, prior, lik):
+        """(cutoff, re-drawn flags) of main.cu:1215-1223 on these scores."""
+        prior = np.ascontiguousarray(prior, np.float64)
+        lik = np.ascontiguousarray(lik, np.float64)
+        flags = np.zeros(len(prior), np.int32)
+        cut = self.lib.gpr_ref_resample_cutoff(len(prior), _p(prior), _p(lik), _p(flags))
+        return cut, flags.astype(bool)
 
     def host_init(self, N, seed):
         """srand(seed) then main.cu:1133-1137, with the reference's host RNG."""

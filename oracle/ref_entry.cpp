@@ -117,6 +117,23 @@ void gpr_ref_host_init(int* P, float* C, int N, unsigned seed) {
     }
 }
 
+/* The cutoff statements of main() (main.cu:1215-1219) on caller arrays, with
+ * the reference's own comparator cmp (main.cu:987-995); flags[h] = 1 for the
+ * chains the test of main.cu:1223 re-draws. */
+double gpr_ref_resample_cutoff(int N, const double* prior, const double* lik, int* flags) {
+    bayes_t* host_posterior = (bayes_t*)malloc((size_t)N * sizeof(bayes_t));
+    for (int h = 0; h < N; h++) host_posterior[h] = prior[h] + lik[h];
+    qsort((void*)host_posterior, N, sizeof(bayes_t), cmp);
+#if GPR_REF_MAPD
+    bayes_t cutoff = host_posterior[N - 1] - (GPR_REF_MAP_DELTA);
+#else
+    bayes_t cutoff = host_posterior[int(N * RESAMPLE_QUANTILE)];
+#endif
+    free(host_posterior);
+    for (int h = 0; h < N; h++) flags[h] = (prior[h] + lik[h] < cutoff) ? 1 : 0;
+    return cutoff;
+}
+
 /* The reference's main() (main.cu:1011), renamed. */
 int gpr_ref_cli(int argc, char** argv) { optind = 1; return gpr_ref_main(argc, argv); }
 

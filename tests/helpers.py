@@ -64,3 +64,18 @@ def same_class(a, b):
     both_nan = np.isnan(a) & np.isnan(b)
     same_inf = (~fa) & (~fb) & (a == b)
     return (fa & fb) | both_nan | same_inf
+
+
+def mixed_scores(N, seed, nan=0.05, ninf=0.05, ties=True):
+    """(prior, likelihood) per chain whose sums cover the cases the
+    resampling comparator orders specially: NaN, -inf, ties, signed zeros."""
+    r = np.random.default_rng(seed)
+    post = -np.abs(r.normal(0, 1e3, N)) * 10.0 ** r.integers(-3, 4, N)
+    if ties:
+        post[r.integers(0, N, N // 10)] = -12.5
+        post[r.integers(0, N, 3)] = 0.0
+        post[r.integers(0, N, 3)] = -0.0
+    post[r.random(N) < ninf] = -np.inf
+    prior = np.zeros(N)
+    prior[r.random(N) < nan] = np.nan
+    return prior, post.copy()

@@ -87,3 +87,52 @@ def test_cli_rejects_bad_arguments(tmp_path):
     assert r.returncode == 1
     r = subprocess.run([g.CLI_PATH, "--steps=0"], capture_output=True, text=True, timeout=60)
     assert r.returncode == 1
+
+
+def _run_cli(tmp_path, name, args):
+    out = tmp_path / name
+    out.mkdir()
+    r = subprocess.run([g.CLI_PATH] + args + ["--out=%s" % out], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    return out
+
+
+@pytest.mark.parametrize("k", [50, 700, 5000])
+def test_cli_tops_matches_sort_tail(tmp_path, k):
+    """--tops=K writes what `sort -g -k3 samples.txt | tail -n K` (run-all.sh:45)
+    prints in the C locale, with candidates from the device top-k."""
+    import shutil
+    if not os.path.exists(g.CLI_PATH):
+        pytest.skip("CLI not built")
+    if not shutil.which("sort"):
+        pytest.skip("coreutils sort not available")
+    x, y, sd = H.quad_data(60, seed=3)
+    data = tmp_path / "data.txt"
+    _write_data(data, x, y, sd)
+    out = _run_cli(tmp_path, "run", ["--in=%s" % data, "--N=512", "--steps=30", "--outer=4", "--seed=7",
+                                     "--quiet", "--tops=%d" % k])
+    want = subprocess.run("sort -g -k3 %s | tail -n %d" % (out / "samples.txt", k), shell=True,
+                          capture_output=True, env={"LC_ALL": "C", "PATH": os.environ.get("PATH", "")},
+                          check=True).stdout
+    assert (out / "tops.txt").read_bytes() == want
+
+
+def test_cli_device_resample(tmp_path):
+    """--device-resample: with a cutoff that re-draws nothing (quantile 0) the
+    run is the host path's byte for byte; with map-delta it re-draws chains on
+    the device and completes."""
+    if not os.path.exists(g.CLI_PATH):
+        pytest.skip("CLI not built")
+    x, y, sd = H.quad_data(60, seed=3)
+    data = tmp_path / "data.txt"
+    _write_data(data, x, y, sd)
+    base = ["--in=%s" % data, "--N=512", "--steps=20", "--outer=4", "--seed=11", "--quiet"]
+    a = _run_cli(tmp_path, "host", base + ["--resample=quantile:0"])
+    b = _run_cli(tmp_path, "dev", base + ["--resample=quantile:0", "--device-resample"])
+    ha, la = _lines(a / "samples.txt")
+    hb, lb = _lines(b / "samples.txt")
+    assert len(la) == 512 * 3 and la == lb
+    assert "(device)" in (b / "log.txt").read_text()
+    c = _run_cli(tmp_path, "dev_md", base + ["--resample=map-delta:20", "--device-resample"])
+    _, lc = _lines(c / "samples.txt")
+    assert len(lc) == 512 * 3 and lc[:512] != la[:512]

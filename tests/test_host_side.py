@@ -135,3 +135,56 @@ def test_library_exports_every_declared_function(header):
     lib = ctypes.CDLL(g.LIB_PATH)
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing
+
+
+def _samples_text(N, PL, blocks, seed):
+    """A samples.txt as the CLI writes it: the parameter and data header, then
+    the lines of `blocks` blocks (ties, -inf and nan posteriors included)."""
+    r = np.random.default_rng(seed)
+    head = ["# -----------------------------------------------------------------",
+            "# -- Parameters:", "# \tInput data path: data.txt", "# \tOutput path: out/",
+            "# \tMCMC Iterations (per block): 1000", "# \tBlocks: %d" % blocks, "# \tN chains: %d" % N,
+            "# \tSeed: 5", "# \tMax program length: %d" % PL, "# \tGPU: 0", "#", "#", "# -- Data:"]
+    head += ["# \t%f\t%f\t%f" % (a, b, c) for a, b, c in r.normal(0, 30, (20, 3))]
+    text = "\n".join(head + ["#", "#"]) + "\n"
+    out = [text]
+    for b in range(1, blocks + 1):
+        P, C = H.random_programs(N, PL, seed=seed + b)
+        lik = -np.abs(r.normal(0, 50, N)).round(2)
+        lik[r.integers(0, N, N // 20)] = -np.inf
+        lik[r.integers(0, N, 3)] = np.nan
+        lik[r.integers(0, N, N // 8)] = -7.25
+        prior = np.where(r.random(N) < 0.1, -0.0, -np.abs(r.normal(0, 5, N)).round(3))
+        out.append(g.format_samples(P, C, prior, lik, b))
+    return "".join(out)
+
+
+@pytest.mark.parametrize("k", [1, 7, 100, 250, 5000])
+def test_tops_matches_sort_tail(tmp_path, k):
+    """gpr_tops keeps exactly what `LC_ALL=C sort -g -k3 samples.txt | tail -n k`
+    (run-all.sh:45) prints, header lines with numeric third fields included."""
+    import shutil
+    import subprocess
+    _lib()
+    if not shutil.which("sort") or not shutil.which("tail"):
+        pytest.skip("coreutils sort/tail not available")
+    text = _samples_text(300, 15, 3, seed=k)
+    path = tmp_path / "samples.txt"
+    path.write_bytes(text.encode("latin-1"))
+    want = subprocess.run("sort -g -k3 %s | tail -n %d" % (path, k), shell=True, capture_output=True,
+                          env={"LC_ALL": "C", "PATH": os.environ.get("PATH", "")}, check=True).stdout
+    t = g.Tops(k)
+    t.add_text(text)
+    t.write(str(tmp_path / "tops_all.txt"))
+    assert (tmp_path / "tops_all.txt").read_bytes() == want
+    # the same, offering the header whole and each block's lines by index,
+    # in several pieces
+    head_end = text.index("\n#\n#\n") + 5
+    t2 = g.Tops(k)
+    t2.add_text(text[:head_end])
+    body = text[head_end:]
+    nlines = body.count("\n")
+    t2.add_lines(body, np.arange(0, nlines, 2))
+    t2.add_lines(body, np.arange(1, nlines, 2))
+    t2.write(str(tmp_path / "tops_lines.txt"))
+    assert (tmp_path / "tops_lines.txt").read_bytes() == want

@@ -70,3 +70,24 @@ def test_port_mh_block_matches_reference(case):
     np.testing.assert_array_equal(Cp.view(np.int32), Cr.view(np.int32))
     np.testing.assert_array_equal(pr_p, pr_r)
     np.testing.assert_array_equal(lk_p, lk_r)
+
+
+@pytest.mark.parametrize("N", [1, 7, 1000, 4097])
+@pytest.mark.parametrize("map_delta", [0.0, 20.0])
+def test_port_resample_cutoff_matches_reference(N, map_delta):
+    """The restated resampling picks the reference's cutoff and chains
+    (main.cu:1215-1223, the reference's own cmp), NaN and ties included; its
+    re-draws follow the Philox stream instead of rand()."""
+    _need_ref()
+    o = oref.get(pl=31, project_math=1, map_delta=map_delta)
+    prior, lik = H.mixed_scores(N, seed=N)
+    cut_ref, flags = o.resample_cutoff(prior, lik)
+    P0, C0 = H.random_programs(N, 31, seed=N + 3)
+    P, C = P0.copy(), C0.copy()
+    mode, param = (1, map_delta) if map_delta > 0 else (0, 0.5)
+    n, cut = port.resample(port.cfg(PL=31), P, C, prior, lik, mode, param, 77)
+    assert (np.isnan(cut) and np.isnan(cut_ref)) or cut == cut_ref
+    changed = np.any(P != P0, axis=0) | np.any(C.view(np.uint32) != C0.view(np.uint32), axis=0)
+    assert n == int(flags.sum()) and np.array_equal(changed, flags)
+    # re-drawn ops come from the op set minus its last op (random_int(n_ops - 1))
+    assert np.all(P[:, flags] < 26)
