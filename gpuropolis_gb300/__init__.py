@@ -27,7 +27,7 @@ OPSET_REFERENCE = list(range(27))
 OPSET_BASIC = [CONST, A, B, PLUS, MINUS, TIMES, DIV, LOG, EXP, POW]
 
 RNG_LCG, RNG_PHILOX = 0, 1
-CONST_REFERENCE, CONST_RANDOM_WALK = 0, 1
+CONST_REFERENCE, CONST_RANDOM_WALK, CONST_HMC = 0, 1, 2
 
 GPR_OK = 0
 ERRORS = {1: "GPR_ERR_ARG", 2: "GPR_ERR_CUDA", 3: "GPR_ERR_STATE", 4: "GPR_ERR_DEVICE",
@@ -91,6 +91,11 @@ def library():
     lib.gpr_get_stats.argtypes = [vp, vp, ip]
     lib.gpr_reset_stats.argtypes = [vp]
     lib.gpr_set_scores.argtypes = [vp, vp, vp]
+    lib.gpr_set_moves.argtypes = [vp, ip, fp, ip]
+    lib.gpr_adapt_scales.argtypes = [vp, fp]
+    lib.gpr_chain_scales.argtypes = [vp, vp]
+    lib.gpr_loglik_grad.argtypes = [vp, vp, vp]
+    lib.gpr_run_block_traced.argtypes = [vp, ip, ip, ip, vp]
     lib.gpr_resample.argtypes = [vp, ip, dp, ctypes.c_uint32, vp, vp]
     lib.gpr_top_chains.argtypes = [vp, ip, dp, vp, ip, vp, vp]
     lib.gpr_map_chain.argtypes = [vp, vp, vp]
@@ -246,6 +251,31 @@ class Sampler:
 
     def reset_stats(self):
         self._check(self.lib.gpr_reset_stats(self.h))
+
+    def set_moves(self, struct_every=5, hmc_eps=0.01, hmc_steps=8):
+        self._check(self.lib.gpr_set_moves(self.h, int(struct_every), float(hmc_eps), int(hmc_steps)))
+
+    def adapt_scales(self, target_accept):
+        self._check(self.lib.gpr_adapt_scales(self.h, float(target_accept)))
+
+    def chain_scales(self):
+        out = np.empty(self.N, np.float32)
+        self._check(self.lib.gpr_chain_scales(self.h, _ptr(out)))
+        return out
+
+    def loglik_grad(self):
+        """(grad (PL, N) float64, likelihood (N,) float64) of the current state."""
+        grad = np.empty((self.PL, self.N), np.float64)
+        lik = np.empty(self.N, np.float64)
+        self._check(self.lib.gpr_loglik_grad(self.h, _ptr(grad), _ptr(lik)))
+        return grad, lik
+
+    def run_block_traced(self, steps, seed, trace_n):
+        """run_block, returning the first trace_n constants after every step:
+        an array (N, steps, trace_n)."""
+        tr = np.empty((self.N, steps, trace_n), np.float32)
+        self._check(self.lib.gpr_run_block_traced(self.h, int(steps), int(seed), int(trace_n), _ptr(tr)))
+        return tr
 
     def set_scores(self, prior, lik):
         prior = np.ascontiguousarray(prior, np.float64)

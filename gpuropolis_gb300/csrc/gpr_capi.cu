@@ -45,6 +45,7 @@ struct gpr_handle {
     unsigned long long* dstats = nullptr;
     float* ddata = nullptr;    /* x | y | w | sd, each nd_pad floats */
     /* selection scratch, allocated by the first gpr_resample/gpr_top_chains/gpr_map_chain */
+    float* dscale = nullptr;               /* per-chain proposal scales          */
     unsigned long long* dkeys = nullptr;   /* N posterior keys                   */
     unsigned long long* dsel = nullptr;    /* [0] selected key                   */
     int* dseli = nullptr;                  /* [0] count, [1] first index         */
@@ -116,7 +117,7 @@ int64_t gpr_launch_count(gpr_handle* h) { return h ? h->launches : 0; }
 static void free_all(gpr_handle* h) {
     cudaFree(h->dP); cudaFree(h->dC); cudaFree(h->dprior); cudaFree(h->dlik);
     cudaFree(h->dlogcount); cudaFree(h->dcounter); cudaFree(h->ddata); cudaFree(h->dstats);
-    cudaFree(h->dkeys); cudaFree(h->dsel); cudaFree(h->dseli); cudaFree(h->dtop);
+    cudaFree(h->dkeys); cudaFree(h->dsel); cudaFree(h->dseli); cudaFree(h->dtop); cudaFree(h->dscale);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
 }
 
@@ -136,7 +137,8 @@ int gpr_create(const gpr_config* cfg, int n_chains, gpr_handle** out) {
             return fail(nullptr, GPR_ERR_ARG, "ops[%d] = %d is not an op code", i, cfg->ops[i]);
     if (cfg->rng != GPR_RNG_LCG && cfg->rng != GPR_RNG_PHILOX)
         return fail(nullptr, GPR_ERR_ARG, "unknown rng mode %d", cfg->rng);
-    if (cfg->const_proposal != GPR_CONST_REFERENCE && cfg->const_proposal != GPR_CONST_RANDOM_WALK)
+    if (cfg->const_proposal != GPR_CONST_REFERENCE && cfg->const_proposal != GPR_CONST_RANDOM_WALK &&
+        cfg->const_proposal != GPR_CONST_HMC)
         return fail(nullptr, GPR_ERR_ARG, "unknown constant proposal %d", cfg->const_proposal);
     if ((long long)n_chains * PL > (1ll << 31) - 1)
         return fail(nullptr, GPR_ERR_ARG, "n_chains * program_length exceeds 2^31-1");
@@ -250,8 +252,33 @@ int gpr_destroy(gpr_handle* h) {
 
 /* Launch geometry for a given layout: K points per lane, data in registers
  * (onepass) or streamed from shared memory, heavy ops rolled or unrolled. */
+/* The MH kernel with Hamiltonian constant moves: one chain per warp, 4 warps
+ * per CTA, one point per lane per pass, a persistent grid. */
+static int configure_hmc(gpr_handle* h) {
+    gpr::KParams& kp = h->kp;
+    gpr::LaunchCfg lc;
+    lc.K = 1; lc.onepass = 0; lc.rolled = 0; lc.lockstep = 0;
+    int wpc = 4;
+    size_t smem = gpr::grad_smem_bytes(kp, wpc);
+    while (smem > 227 * 1024 && wpc > 1) smem = gpr::grad_smem_bytes(kp, wpc /= 2);
+    if (smem > 227 * 1024)
+        return fail(h, GPR_ERR_ARG, "dataset of %d points does not fit in shared memory", kp.nd);
+    int per_sm = 0;
+    CUDA_TRY(h, gpr::hmc_occupancy(kp, wpc, smem, &per_sm));
+    if (per_sm < 1) return fail(h, GPR_ERR_ARG, "kernel cannot be resident (smem %zu)", smem);
+    long long ctas = (long long)h->num_sms * per_sm;
+    const long long need = (h->N + wpc - 1) / wpc;
+    if (ctas > need) ctas = need;
+    lc.warps_per_cta = wpc;
+    lc.smem_bytes = smem;
+    lc.ctas = (int)ctas;
+    h->lc = lc;
+    return GPR_OK;
+}
+
 static int configure_launch(gpr_handle* h, int K, int onepass, int rolled, int lockstep = 1, int wpc0 = 8) {
     gpr::KParams& kp = h->kp;
+    if (kp.const_mode == GPR_CONST_HMC) return configure_hmc(h);
     gpr::LaunchCfg lc;
     lc.K = K;
     lc.onepass = onepass;
@@ -370,7 +397,8 @@ static int run(gpr_handle* h, int steps, int seed) {
     h->kp.steps = steps;
     h->kp.seed = (uint32_t)seed;
     CUDA_TRY(h, cudaMemsetAsync(h->dcounter, 0, sizeof(int), h->stream));
-    CUDA_TRY(h, gpr::launch_mh_block(h->kp, h->lc, h->stream));
+    if (h->kp.const_mode == GPR_CONST_HMC) CUDA_TRY(h, gpr::launch_hmc_block(h->kp, h->lc, h->stream));
+    else CUDA_TRY(h, gpr::launch_mh_block(h->kp, h->lc, h->stream));
     h->launches++;
     return GPR_OK;
 }
@@ -459,6 +487,13 @@ int gpr_debug_math(gpr_handle* h, int op, const float* a, const float* b, float*
 int gpr_autotune(gpr_handle* h, int steps, int seed, int* K, int* onepass, int* rolled, float* best_ms) {
     if (!h || steps <= 0) return fail(h, GPR_ERR_ARG, "bad arguments");
     if (h->nd < 0) return fail(h, GPR_ERR_STATE, "gpr_set_data has not been called");
+    if (h->kp.const_mode == GPR_CONST_HMC) {   /* one layout only */
+        if (K) *K = h->lc.K;
+        if (onepass) *onepass = h->lc.onepass;
+        if (rolled) *rolled = h->lc.rolled;
+        if (best_ms) *best_ms = 0.0f;
+        return GPR_OK;
+    }
     CUDA_TRY(h, cudaSetDevice(h->device));
     const size_t cnt = (size_t)h->N * h->PL;
     int32_t* sP = nullptr; float* sC = nullptr; double* sPr = nullptr; double* sLi = nullptr;
@@ -475,6 +510,9 @@ int gpr_autotune(gpr_handle* h, int steps, int seed, int* K, int* onepass, int* 
     float best = 1e30f;
     gpr::LaunchCfg bestlc = orig;
     cudaError_t e;
+    /* trial blocks leave the per-chain scales alone */
+    const float saved_target = h->kp.adapt_target;
+    h->kp.adapt_target = 0.0f;
 #define AT_TRY(call) do { if ((e = (call)) != cudaSuccess) { rc = fail(h, GPR_ERR_CUDA, "gpr_autotune: %s: %s", #call, cudaGetErrorString(e)); goto done; } } while (0)
     AT_TRY(cudaMalloc(&sP, cnt * sizeof(int32_t)));
     AT_TRY(cudaMalloc(&sC, cnt * sizeof(float)));
@@ -537,6 +575,7 @@ int gpr_autotune(gpr_handle* h, int steps, int seed, int* K, int* onepass, int* 
     if (best_ms) *best_ms = best;
 #undef AT_TRY
 done:
+    h->kp.adapt_target = saved_target;
     if (rc != GPR_OK) h->lc = orig;
     cudaFree(sP); cudaFree(sC); cudaFree(sPr); cudaFree(sLi); cudaFree(sSt);
     if (e0) cudaEventDestroy(e0);
@@ -550,6 +589,7 @@ int gpr_set_layout(gpr_handle* h, int K, int onepass, int rolled) {
 
 int gpr_set_layout2(gpr_handle* h, int K, int onepass, int rolled, int lockstep, int warps_per_cta) {
     if (!h) return GPR_ERR_ARG;
+    if (h->kp.const_mode == GPR_CONST_HMC) return fail(h, GPR_ERR_ARG, "the HMC kernel has a single layout");
     if ((K != 4 && K != 8) || (onepass && h->kp.nd > 32 * K) || lockstep < 0 ||
         (warps_per_cta != 1 && warps_per_cta != 2 && warps_per_cta != 4 && warps_per_cta != 8))
         return fail(h, GPR_ERR_ARG, "invalid layout K=%d onepass=%d lockstep=%d warps=%d for %d points", K,
@@ -588,6 +628,97 @@ int gpr_reset_stats(gpr_handle* h) {
     CUDA_TRY(h, cudaSetDevice(h->device));
     CUDA_TRY(h, cudaMemsetAsync(h->dstats, 0, GPR_NSTATS * sizeof(unsigned long long), h->stream));
     return GPR_OK;
+}
+
+/* ---- move schedule, Hamiltonian moves, gradients, adaptation ---- */
+
+int gpr_set_moves(gpr_handle* h, int struct_every, float hmc_eps, int hmc_steps) {
+    if (!h) return GPR_ERR_ARG;
+    if (struct_every < 0) return fail(h, GPR_ERR_ARG, "struct_every must be >= 0 (got %d)", struct_every);
+    if (!(hmc_eps > 0.0f) || !(hmc_eps < 1e30f)) return fail(h, GPR_ERR_ARG, "hmc_eps must be > 0");
+    if (hmc_steps < 1 || hmc_steps > 1024) return fail(h, GPR_ERR_ARG, "hmc_steps must be in [1, 1024]");
+    h->kp.struct_every = struct_every;
+    h->kp.hmc_eps = hmc_eps;
+    h->kp.hmc_L = hmc_steps;
+    return GPR_OK;
+}
+
+int gpr_adapt_scales(gpr_handle* h, float target_accept) {
+    if (!h) return GPR_ERR_ARG;
+    if (!(target_accept >= 0.0f && target_accept < 1.0f))
+        return fail(h, GPR_ERR_ARG, "target acceptance %g is not in [0, 1)", (double)target_accept);
+    if (h->kp.const_mode == GPR_CONST_REFERENCE)
+        return fail(h, GPR_ERR_ARG, "the reference's constant proposals have no scale to adapt");
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    if (!h->dscale) {
+        CUDA_TRY(h, cudaMalloc(&h->dscale, (size_t)h->N * sizeof(float)));
+        const float s0 = h->kp.const_mode == GPR_CONST_HMC ? h->kp.hmc_eps : h->kp.rw_sd;
+        std::vector<float> init((size_t)h->N, s0);
+        CUDA_TRY(h, cudaMemcpyAsync(h->dscale, init.data(), init.size() * sizeof(float), cudaMemcpyHostToDevice,
+                                    h->stream));
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        h->kp.chain_scale = h->dscale;
+    }
+    h->kp.adapt_target = target_accept;
+    return GPR_OK;
+}
+
+int gpr_chain_scales(gpr_handle* h, float* out) {
+    if (!h || !out) return GPR_ERR_ARG;
+    if (!h->dscale) return fail(h, GPR_ERR_STATE, "no per-chain scales (gpr_adapt_scales has not been called)");
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    CUDA_TRY(h, cudaMemcpyAsync(out, h->dscale, (size_t)h->N * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return GPR_OK;
+}
+
+int gpr_loglik_grad(gpr_handle* h, double* grad, double* likelihood) {
+    if (!h) return GPR_ERR_ARG;
+    if (!grad) return fail(h, GPR_ERR_ARG, "grad is NULL");
+    if (h->nd < 0) return fail(h, GPR_ERR_STATE, "gpr_set_data has not been called");
+    if (gpr::grad_smem_bytes(h->kp, 4) > 227 * 1024)
+        return fail(h, GPR_ERR_ARG, "dataset of %d points does not fit in shared memory", h->nd);
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    const size_t cnt = (size_t)h->N * h->PL;
+    double* dg = nullptr;
+    double* dl = nullptr;
+    cudaError_t e = cudaMalloc(&dg, cnt * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&dl, (size_t)h->N * sizeof(double));
+    if (e == cudaSuccess) e = gpr::launch_loglik_grad(h->kp, dg, dl, h->stream);
+    if (e == cudaSuccess) {
+        h->launches++;
+        e = cudaMemcpyAsync(grad, dg, cnt * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+    }
+    if (e == cudaSuccess && likelihood)
+        e = cudaMemcpyAsync(likelihood, dl, (size_t)h->N * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(dg);
+    cudaFree(dl);
+    if (e != cudaSuccess) return fail(h, GPR_ERR_CUDA, "gpr_loglik_grad: %s", cudaGetErrorString(e));
+    return gpr_sync(h);
+}
+
+int gpr_run_block_traced(gpr_handle* h, int steps, int random_seed, int trace_n, float* trace) {
+    if (!h) return GPR_ERR_ARG;
+    if (steps < 1) return fail(h, GPR_ERR_ARG, "steps must be >= 1 (got %d)", steps);
+    if (trace_n < 1 || trace_n > 32 || trace_n > h->PL || !trace)
+        return fail(h, GPR_ERR_ARG, "trace_n must be in [1, min(32, program_length)] with a buffer");
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    const size_t cnt = (size_t)h->N * (size_t)steps * (size_t)trace_n;
+    float* dt = nullptr;
+    CUDA_TRY(h, cudaMalloc(&dt, cnt * sizeof(float)));
+    h->kp.trace = dt;
+    h->kp.trace_n = trace_n;
+    int rc = run(h, steps, random_seed);
+    h->kp.trace = nullptr;
+    h->kp.trace_n = 0;
+    cudaError_t e = cudaSuccess;
+    if (rc == GPR_OK) e = cudaMemcpyAsync(trace, dt, cnt * sizeof(float), cudaMemcpyDeviceToHost, h->stream);
+    if (rc == GPR_OK && e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(dt);
+    if (rc != GPR_OK) return rc;
+    if (e != cudaSuccess) return fail(h, GPR_ERR_CUDA, "gpr_run_block_traced: %s", cudaGetErrorString(e));
+    return gpr_sync(h);
 }
 
 /* ---- selection over posteriors (gpr_resample.cu) ---- */

@@ -74,6 +74,10 @@ struct KParams {
     float* trace;      /* optional: C[0..trace_n) of each chain after each step,
                         * trace[(chain * steps + step) * trace_n + i]             */
     int trace_n;       /* <= 32 */
+    float* chain_scale;   /* optional: per-chain random-walk sd (const_mode 1) or
+                           * leapfrog step (Hamiltonian moves), else rw_sd / hmc_eps */
+    float adapt_target;   /* > 0: adapt chain_scale toward this acceptance rate
+                           * during the block and write it back at its end */
 
     /* the reference LCG (main.cu:215) advanced 2^b steps is the affine map
      * x -> lcgA[b]*x + lcgC[b] (mod 2^32, then masked to 31 bits) */
@@ -111,6 +115,14 @@ cudaError_t launch_eval_values(const KParams& p, const float* xs, int nx, float*
                                float* length, int* count, cudaStream_t st);
 
 cudaError_t launch_math(int op, const float* a, const float* b, float* out, int n, cudaStream_t st);
+
+/* Gradient of the log-likelihood and the MH kernel with Hamiltonian constant
+ * moves (gpr_hmc.cu).  grad_smem_bytes: dynamic shared memory of either for
+ * a CTA of warps_per_cta chains. */
+size_t grad_smem_bytes(const KParams& p, int warps_per_cta);
+cudaError_t launch_loglik_grad(const KParams& p, double* grad, double* lik, cudaStream_t st);
+cudaError_t hmc_occupancy(const KParams& p, int warps_per_cta, size_t smem, int* ctas_per_sm);
+cudaError_t launch_hmc_block(const KParams& p, const LaunchCfg& lc, cudaStream_t st);
 
 /* Selection over the chains' posteriors (gpr_resample.cu).  launch_select
  * writes one order-preserving key per chain (gpr_select.h) into keys and the

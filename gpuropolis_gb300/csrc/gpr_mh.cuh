@@ -764,7 +764,7 @@ __device__ __forceinline__ bool is_int_ref(float x) {
  * held in r.  Writes the new value and the forward/backward terms. */
 template <int RNG>
 __device__ __forceinline__ void propose_constant(Rng& r, float old, float& nc, float& dfw,
-                                                 float& dbw, const KParams& p) {
+                                                 float& dbw, const KParams& p, float rw_sd) {
     dfw = 0.0f; dbw = 0.0f;
     float u0 = random_float<RNG>(r, p);
     const float p_geom = (p.const_mode == 0) ? 1.0f : 0.0f;   /* P_PROPOSE_C_GEOMETRIC */
@@ -790,7 +790,7 @@ __device__ __forceinline__ void propose_constant(Rng& r, float old, float& nc, f
         }
     } else {
         float z = random_normal<RNG>(r, p);
-        nc = __fadd_rn(old, __fmul_rn(p.rw_sd, z));
+        nc = __fadd_rn(old, __fmul_rn(rw_sd, z));
     }
 }
 
@@ -822,7 +822,8 @@ __device__ __forceinline__ LaneJump make_lane_jump(const KParams& p, int lane) {
 
 template <int RNG>
 __device__ void constant_move(Rng& r, const WarpSmem& w, const float* Cold, float* Cnew,
-                              df& fw_sum, df& bw_sum, const KParams& p, const LaneJump& lj, int lane) {
+                              df& fw_sum, df& bw_sum, const KParams& p, const LaneJump& lj, int lane,
+                              float rw_sd) {
     const int PL = p.PL;
     const int nominal = (p.const_mode == 0) ? 4 : 3;
     /* first pass: every constant at its nominal offset, streams positioned by
@@ -836,7 +837,7 @@ __device__ void constant_move(Rng& r, const WarpSmem& w, const float* Cold, floa
             else rc.s = r.s + (uint32_t)(nominal * c);
             rc.drawn = 0;
             float nc, dfw, dbw;
-            propose_constant<RNG>(rc, Cold[c], nc, dfw, dbw, p);
+            propose_constant<RNG>(rc, Cold[c], nc, dfw, dbw, p, rw_sd);
             Cnew[c] = nc; w.fw[c] = dfw; w.bw[c] = dbw; w.ndr[c] = (int)rc.drawn;
             w.off[c] = nominal * c;
             st = (lj.sa * st + lj.sc) & 0x7fffffffu;
@@ -854,7 +855,7 @@ __device__ void constant_move(Rng& r, const WarpSmem& w, const float* Cold, floa
             rng_jump<RNG>(rc, (uint32_t)w.off[c], p);
             rc.drawn = 0;
             float nc, dfw, dbw;
-            propose_constant<RNG>(rc, Cold[c], nc, dfw, dbw, p);
+            propose_constant<RNG>(rc, Cold[c], nc, dfw, dbw, p, rw_sd);
             Cnew[c] = nc; w.fw[c] = dfw; w.bw[c] = dbw; w.ndr[c] = (int)rc.drawn;
         }
         __syncwarp();
@@ -943,6 +944,25 @@ __device__ __forceinline__ bool mh_accept(df ppost, df cur_post, df backward, df
     }
     if (df_invalid(cur_post)) accept = true;
     return accept;
+}
+
+/* min(1, exp(acceptance)) of the rule above: the probability the move is
+ * taken (1 from an invalid current state, 0 for an invalid proposal).  For
+ * step-size adaptation only; the decision itself is mh_accept's. */
+__device__ __forceinline__ float accept_prob(df ppost, df cur_post, df backward, df forward) {
+    if (df_invalid(cur_post)) return 1.0f;
+    if (df_invalid(ppost)) return 0.0f;
+    const df acc = df_sub(df_add(df_sub(ppost, cur_post), backward), forward);
+    if (df_gt0(acc)) return 1.0f;
+    return expf(__fmul_rn(acc.hi, (float)GPR_DF_UNSCALE));
+}
+
+/* Robbins-Monro step on the log of a random-walk proposal scale toward a
+ * target acceptance rate: log s += (alpha - target) / (m + 10)^0.6 after the
+ * m-th move. */
+__device__ __forceinline__ float rm_update(float log_s, float alpha, float target, int m) {
+    const float gain = __powf((float)(m + 10), -0.6f);
+    return fminf(fmaxf(__fadd_rn(log_s, __fmul_rn(gain, __fsub_rn(alpha, target))), -30.0f), 10.0f);
 }
 
 /* Structure proposal (main.cu:699-742): a node n uniform in [0, PL) -- the
@@ -1062,6 +1082,10 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
         r.key0 = p.seed; r.key1 = (uint32_t)chain; r.blk = 0xffffffffu; r.drawn = 0;
         r.w0 = r.w1 = r.w2 = r.w3 = 0u;
         r.s = (RNG == 0) ? ((p.seed + (uint32_t)chain) & 0x7fffffffu) : 0u;   /* rx = random_seed + idx */
+        /* random-walk scale: the configured one, or this chain's own (adapted) */
+        float rw_sd = (p.chain_scale && active) ? p.chain_scale[chain] : p.rw_sd;
+        float log_sd = logf(rw_sd);
+        int n_cmoves = 0;
 
         unsigned long long st_nodes = 0, st_np = 0, st_pts = 0;
         int st_evals = 0, st_sp = 0, st_sa = 0, st_cp = 0, st_ca = 0;
@@ -1090,7 +1114,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
             } else if (!init) {
                 /* ---- constant move (main.cu:743-806) ---- */
                 df fws, bws;
-                constant_move<RNG>(r, ws, ws.Cs[ccur], ws.Cs[ccur ^ 1], fws, bws, p, ljump, lane);
+                constant_move<RNG>(r, ws, ws.Cs[ccur], ws.Cs[ccur ^ 1], fws, bws, p, ljump, lane, rw_sd);
                 if (p.const_mode == 0) { forward = df_add(forward, fws); backward = df_add(backward, bws); }
                 cbuf = ccur ^ 1;
                 need_cauchy = true;
@@ -1180,6 +1204,11 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
             st_evals++; st_nodes += (unsigned)count;
             bool accept = true;
             if (!init) {
+                if (!structural && p.adapt_target > 0.0f && p.const_mode == 1) {
+                    log_sd = rm_update(log_sd, accept_prob(post, cur_post, backward, forward), p.adapt_target,
+                                       n_cmoves++);
+                    rw_sd = expf(log_sd);
+                }
                 accept = mh_accept<RNG>(post, cur_post, backward, forward, r, p);
                 if (structural) { st_sp++; st_sa += accept; } else { st_cp++; st_ca += accept; }
             }
@@ -1204,6 +1233,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
         if (active && lane == 0) {
             p.prior[chain] = df_to_double_unscaled(cur_prior);
             p.lik[chain] = df_to_double_unscaled(cur_lik);
+            if (p.chain_scale && p.adapt_target > 0.0f && p.const_mode == 1) p.chain_scale[chain] = rw_sd;
         }
         if (lane == 0 && p.stats) {
             atomicAdd(&p.stats[GPR_STAT_EVAL_POINTS], st_pts);

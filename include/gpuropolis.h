@@ -43,7 +43,7 @@ enum {
 };
 
 enum { GPR_RNG_LCG = 0, GPR_RNG_PHILOX = 1 };
-enum { GPR_CONST_REFERENCE = 0, GPR_CONST_RANDOM_WALK = 1 };
+enum { GPR_CONST_REFERENCE = 0, GPR_CONST_RANDOM_WALK = 1, GPR_CONST_HMC = 2 };
 
 #define GPR_MAX_PROGRAM_LENGTH 255
 #define GPR_MAX_OPS 32
@@ -53,7 +53,7 @@ typedef struct gpr_config {
     int n_ops;               /* size of the op set drawn by proposals                         */
     int ops[GPR_MAX_OPS];    /* op codes of the set, in draw order (reference: 0..NOPS-1)     */
     int rng;                 /* GPR_RNG_LCG (main.cu:213-216) or GPR_RNG_PHILOX               */
-    int const_proposal;      /* GPR_CONST_REFERENCE (main.cu:746-785) or GPR_CONST_RANDOM_WALK */
+    int const_proposal;      /* GPR_CONST_REFERENCE (main.cu:746-785), GPR_CONST_RANDOM_WALK or GPR_CONST_HMC */
     float rw_sd;             /* random-walk sd for GPR_CONST_RANDOM_WALK                      */
     int device;              /* CUDA device ordinal (--gpu, main.cu:104)                      */
     void* stream;            /* cudaStream_t to run on, or NULL to let the handle create one  */
@@ -166,6 +166,38 @@ int gpr_layout_lockstep(gpr_handle* h);
  * [6]/[7] constant moves proposed/accepted.  Copies min(n, 8) values. */
 int gpr_get_stats(gpr_handle* h, uint64_t* out, int n);
 int gpr_reset_stats(gpr_handle* h);
+
+/* ---- gradients and Hamiltonian constant moves (no reference counterpart) ---- */
+
+/* Move schedule: a structure move every struct_every steps (the reference:
+ * 5, main.cu:699; 0: never, i.e. constants only) and, for GPR_CONST_HMC
+ * handles, the leapfrog step hmc_eps and step count hmc_steps (1 = MALA) of
+ * the Hamiltonian constant moves that take the place of the reference's
+ * constant proposals.  Defaults: 5, 0.01, 8. */
+int gpr_set_moves(gpr_handle* h, int struct_every, float hmc_eps, int hmc_steps);
+
+/* Per-chain proposal scales: with target_accept in (0, 1), the following
+ * blocks adapt each chain's own random-walk sd (GPR_CONST_RANDOM_WALK:
+ * Robbins-Monro on log sd) or leapfrog step (GPR_CONST_HMC: dual averaging,
+ * Hoffman and Gelman 2014) toward that acceptance rate of its constant moves;
+ * 0 stops adapting and keeps the scales reached.  The first call gives every
+ * chain the configured scale.  gpr_chain_scales copies the N scales out. */
+int gpr_adapt_scales(gpr_handle* h, float target_accept);
+int gpr_chain_scales(gpr_handle* h, float* out);
+
+/* d log-likelihood / d C for every chain's current state (the likelihood of
+ * main.cu:454-468 differentiated in each constant), by a reverse-mode
+ * adjoint of the device evaluator (FP32 sums at the likelihood's 2^-64 scale,
+ * so gradients beyond the FP32 range survive): grad[i*N + chain] (host,
+ * program_length*N doubles; 0 for constants the program does not read) and,
+ * when non-NULL, likelihood[chain].  Where an intermediate of the FP32 sweep
+ * leaves the FP32 range, that chain's gradient comes out non-finite. */
+int gpr_loglik_grad(gpr_handle* h, double* grad, double* likelihood);
+
+/* gpr_run_block that also records, after every step, the first trace_n
+ * constants of every chain: trace[(chain*steps + step)*trace_n + i] (host,
+ * N*steps*trace_n floats).  For mixing measurements. */
+int gpr_run_block_traced(gpr_handle* h, int steps, int random_seed, int trace_n, float* trace);
 
 /* ---- selection over the chains' posteriors, on the device ---- */
 

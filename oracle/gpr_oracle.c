@@ -504,3 +504,151 @@ int gpr_port_resample(const port_cfg* cfg, int N, int32_t* P, float* C, const do
     if (cutoff_out) *cutoff_out = cutoff;
     return redrawn;
 }
+
+/* ---- FP64 log-likelihood gradient in the constants (extension) ----------
+ * The program of chain idx evaluated in FP64 with its constants taken from
+ * Cd[0..PL) (double, so finite differences can move them by less than a
+ * float ulp), and the derivative of the log-likelihood of main.cu:454-468
+ * in each constant by reverse mode on the heap tree. */
+
+/* Optional jitter of every operation's result, as in eval_node_f64p, so the
+ * gradient's own FP32 noise floor can be measured (0: none). */
+static double g_evd_rel = 0.0;
+static uint32_t g_evd_seed = 0u;
+
+static double evd(const int32_t* P, int N, int PL, int idx, const double* Cd, int j, double x) {
+    if (j > PL) return x;
+    const int o = OP(P, N, idx, j);
+    const double c = Cd[j - 1];
+    double r;
+#define L evd(P, N, PL, idx, Cd, 2 * j, x)
+#define R evd(P, N, PL, idx, Cd, 2 * j + 1, x)
+    switch (o) {
+        case ONE: return 1.0;
+        case CONST: return c;
+        case INV: r = 1.0 / L; break;
+        case A: return L;
+        case B: return R;
+        case PLUS: { double a = L, b = R; r = a + b; break; }
+        case CPLUS: r = L + c; break;
+        case MINUS: { double a = L, b = R; r = a - b; break; }
+        case RMINUS: { double a = L, b = R; r = b - a; break; }
+        case TIMES: { double a = L, b = R; r = a * b; break; }
+        case CTIMES: r = c * L; break;
+        case DIV: { double a = L, b = R; r = a / b; break; }
+        case RDIV: { double a = L, b = R; r = b / a; break; }
+        case SQRT: r = sqrt(L); break;
+        case LOG: r = log(L); break;
+        case SIN: r = sin(L); break;
+        case ASIN: r = asin(L); break;
+        case COS: r = cos(L); break;
+        case ACOS: r = acos(L); break;
+        case TAN: r = tan(L); break;
+        case ATAN: r = atan(L); break;
+        case EXP: r = exp(L); break;
+        case POW: { double a = L, b = R; r = pow(a, b); break; }
+        case CPOW: r = pow(L, c); break;
+        case RPOW: { double a = L, b = R; r = pow(b, a); break; }
+        case CRPOW: r = pow(c, L); break;
+        case ABS: r = fabs(L); break;
+        default: return NAN;
+    }
+#undef L
+#undef R
+    if (g_evd_rel == 0.0) return r;
+    double u = (double)port_hash(g_evd_seed * 2654435761u + (uint32_t)j) / 4294967295.0 * 2.0 - 1.0;
+    return r * (1.0 + g_evd_rel * u);
+}
+
+/* d(a^b)/da and d(a^b)/db */
+static double dpow_da(double a, double b) { return b * pow(a, b - 1.0); }
+static double dpow_db(double a, double b) { double r = pow(a, b); return r == 0.0 ? 0.0 : r * log(a); }
+
+/* adds adj * d f_j / d Cd[k] to g[k] for every constant of the subtree at j */
+static void gradd(const int32_t* P, int N, int PL, int idx, const double* Cd, int j, double x, double adj, double* g) {
+    if (j > PL) return;
+    const int o = OP(P, N, idx, j);
+    const double c = Cd[j - 1];
+#define L evd(P, N, PL, idx, Cd, 2 * j, x)
+#define R evd(P, N, PL, idx, Cd, 2 * j + 1, x)
+#define GL(d) gradd(P, N, PL, idx, Cd, 2 * j, x, adj * (d), g)
+#define GR(d) gradd(P, N, PL, idx, Cd, 2 * j + 1, x, adj * (d), g)
+    switch (o) {
+        case ONE: return;
+        case CONST: g[j - 1] += adj; return;
+        case A: GL(1.0); return;
+        case B: GR(1.0); return;
+        case INV: { double a = L; GL(-1.0 / (a * a)); return; }
+        case LOG: { double a = L; GL(1.0 / a); return; }
+        case EXP: { double a = L; GL(exp(a)); return; }
+        case SQRT: { double a = L; GL(0.5 / sqrt(a)); return; }
+        case SIN: { double a = L; GL(cos(a)); return; }
+        case ASIN: { double a = L; GL(1.0 / sqrt(1.0 - a * a)); return; }
+        case COS: { double a = L; GL(-sin(a)); return; }
+        case ACOS: { double a = L; GL(-1.0 / sqrt(1.0 - a * a)); return; }
+        case TAN: { double t = tan(L); GL(1.0 + t * t); return; }
+        case ATAN: { double a = L; GL(1.0 / (1.0 + a * a)); return; }
+        case ABS: { double a = L; GL(a > 0 ? 1.0 : (a < 0 ? -1.0 : 0.0)); return; }
+        case CPLUS: GL(1.0); g[j - 1] += adj; return;
+        case CTIMES: { double a = L; GL(c); g[j - 1] += adj * a; return; }
+        case CPOW: { double a = L; GL(dpow_da(a, c)); g[j - 1] += adj * dpow_db(a, c); return; }
+        case CRPOW: { double a = L; GL(dpow_db(c, a)); g[j - 1] += adj * dpow_da(c, a); return; }
+        case PLUS: GL(1.0); GR(1.0); return;
+        case MINUS: GL(1.0); GR(-1.0); return;
+        case RMINUS: GL(-1.0); GR(1.0); return;
+        case TIMES: { double a = L, b = R; GL(b); GR(a); return; }
+        case DIV: { double a = L, b = R; GL(1.0 / b); GR(-a / (b * b)); return; }
+        case RDIV: { double a = L, b = R; GL(-b / (a * a)); GR(1.0 / a); return; }
+        case POW: { double a = L, b = R; GL(dpow_da(a, b)); GR(dpow_db(a, b)); return; }
+        case RPOW: { double a = L, b = R; GL(dpow_db(b, a)); GR(dpow_da(b, a)); return; }
+        default: return;
+    }
+#undef L
+#undef R
+#undef GL
+#undef GR
+}
+
+double gpr_port_loglik_f64d(const int32_t* P, int N, int PL, int idx, const double* Cd, const float* D, int nd) {
+    double ll = 0.0;
+    for (int d = 0; d < nd; d++) {
+        double fx = evd(P, N, PL, idx, Cd, 1, D[3 * d]);
+        if (!isfinite(fx)) return -INFINITY;
+        double r = fx - (double)D[3 * d + 1], s = D[3 * d + 2];
+        ll += -(r * r) / (2.0 * s * s) - 0.5 * (log(2.0 * PIF) + 2.0 * log(s));
+    }
+    return ll;
+}
+
+/* Returns the FP64 log-likelihood and writes d loglik / d Cd[k] to g[k];
+ * when gabs is non-NULL, also the sum over points of the absolute per-point
+ * terms of each g[k] (the scale against which cancellation in the sum is
+ * judged). */
+double gpr_port_loglik_grad_f64(const int32_t* P, int N, int PL, int idx, const double* Cd, const float* D, int nd,
+                                double* g, double* gabs) {
+    double* gd = (double*)calloc((size_t)PL, sizeof(double));
+    for (int k = 0; k < PL; ++k) { g[k] = 0.0; if (gabs) gabs[k] = 0.0; }
+    double ll = 0.0;
+    for (int d = 0; d < nd; d++) {
+        double fx = evd(P, N, PL, idx, Cd, 1, D[3 * d]);
+        if (!isfinite(fx)) { ll = -INFINITY; break; }
+        double r = fx - (double)D[3 * d + 1], s = D[3 * d + 2];
+        ll += -(r * r) / (2.0 * s * s) - 0.5 * (log(2.0 * PIF) + 2.0 * log(s));
+        for (int k = 0; k < PL; ++k) gd[k] = 0.0;
+        gradd(P, N, PL, idx, Cd, 1, D[3 * d], -r / (s * s), gd);
+        for (int k = 0; k < PL; ++k) { g[k] += gd[k]; if (gabs) gabs[k] += fabs(gd[k]); }
+    }
+    free(gd);
+    return ll;
+}
+
+/* The same gradient with every operation's result jittered by up to rel
+ * (seeded): repeated over seeds it measures the gradient's FP32 noise floor. */
+double gpr_port_loglik_grad_f64p(const int32_t* P, int N, int PL, int idx, const double* Cd, const float* D, int nd,
+                                 double* g, unsigned seed, double rel) {
+    g_evd_rel = rel;
+    g_evd_seed = seed;
+    double ll = gpr_port_loglik_grad_f64(P, N, PL, idx, Cd, D, nd, g, NULL);
+    g_evd_rel = 0.0;
+    return ll;
+}

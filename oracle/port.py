@@ -38,6 +38,12 @@ def lib():
         L.gpr_port_likelihood_f64.restype = dp
         L.gpr_port_run_block.argtypes = [ctypes.POINTER(PortCfg), ip, ip, ip, vp, vp, vp, ip, ip, vp, vp, ip, ip]
         L.gpr_port_run_block_trace.argtypes = [ctypes.POINTER(PortCfg), ip, vp, vp, vp, ip, ip, vp, vp, ip, vp, ip]
+        L.gpr_port_loglik_f64d.argtypes = [vp, ip, ip, ip, vp, vp, ip]
+        L.gpr_port_loglik_f64d.restype = dp
+        L.gpr_port_loglik_grad_f64.argtypes = [vp, ip, ip, ip, vp, vp, ip, vp, vp]
+        L.gpr_port_loglik_grad_f64.restype = dp
+        L.gpr_port_loglik_grad_f64p.argtypes = [vp, ip, ip, ip, vp, vp, ip, vp, ctypes.c_uint, dp]
+        L.gpr_port_loglik_grad_f64p.restype = dp
         L.gpr_port_resample.argtypes = [ctypes.POINTER(PortCfg), ip, vp, vp, vp, vp, ip, dp, ctypes.c_uint, vp]
         assert L.gpr_port_sizeof_cfg() == ctypes.sizeof(PortCfg)
         _lib = L
@@ -143,3 +149,39 @@ def resample(c, P, C, prior, lik, mode, param, seed):
     n = lib().gpr_port_resample(ctypes.byref(c), N, _p(P), _p(C), _p(prior), _p(lik), mode, param, seed,
                                 ctypes.byref(cut))
     return n, cut.value
+
+
+def loglik_f64(P, idx, Cd, x, y, sd):
+    """FP64 log-likelihood of chain idx with constants Cd (PL doubles)."""
+    PL, N = P.shape
+    D = pack(x, y, sd)
+    Cd = np.ascontiguousarray(Cd, np.float64)
+    return lib().gpr_port_loglik_f64d(_p(P), N, PL, idx, _p(Cd), _p(D), len(x))
+
+
+def loglik_grad_f64(P, idx, Cd, x, y, sd):
+    """(FP64 log-likelihood, d loglik / d Cd, sum of |per-point terms|) of chain idx."""
+    PL, N = P.shape
+    D = pack(x, y, sd)
+    Cd = np.ascontiguousarray(Cd, np.float64)
+    g = np.zeros(PL)
+    ga = np.zeros(PL)
+    ll = lib().gpr_port_loglik_grad_f64(_p(P), N, PL, idx, _p(Cd), _p(D), len(x), _p(g), _p(ga))
+    return ll, g, ga
+
+
+def grad_sensitivity(P, idx, Cd, x, y, sd, rel=2.0 ** -22, trials=4):
+    """max over trials of |g_perturbed - g| per constant: the FP32 noise floor
+    of the log-likelihood gradient (inf where a jitter changes finiteness)."""
+    PL, N = P.shape
+    D = pack(x, y, sd)
+    Cd = np.ascontiguousarray(Cd, np.float64)
+    _, g0, _ = loglik_grad_f64(P, idx, Cd, x, y, sd)
+    worst = np.zeros(PL)
+    for t in range(trials):
+        g = np.zeros(PL)
+        lib().gpr_port_loglik_grad_f64p(_p(P), N, PL, idx, _p(Cd), _p(D), len(x), _p(g), 977 * t + 1, rel)
+        with np.errstate(invalid="ignore"):
+            d = np.where(np.isfinite(g) == np.isfinite(g0), np.abs(g - g0), np.inf)
+        worst = np.maximum(worst, np.nan_to_num(d, nan=np.inf))
+    return worst

@@ -79,3 +79,63 @@ def mixed_scores(N, seed, nan=0.05, ninf=0.05, ties=True):
     prior = np.zeros(N)
     prior[r.random(N) < nan] = np.nan
     return prior, post.copy()
+
+
+def rational_coefficients(seed=0):
+    """b_i ~ N(0, 1), redrawn until 1 + b4 x + b5 x^2 stays above 0.2 on [-3, 3]."""
+    r = np.random.default_rng(seed)
+    grid = np.linspace(-3, 3, 601)
+    while True:
+        b = r.normal(0, 1, 5)
+        if np.min(1 + b[3] * grid + b[4] * grid ** 2) > 0.2:
+            return b, r
+
+
+def rational_data(n=1024, seed=0):
+    """x ~ U[-3, 3], y = (b1 + b2 x + b3 x^2) / (1 + b4 x + b5 x^2) + N(0, 0.02)
+    with b from rational_coefficients(seed); sd = 0.02."""
+    b, r = rational_coefficients(seed)
+    x = r.uniform(-3, 3, n)
+    y = (b[0] + b[1] * x + b[2] * x ** 2) / (1 + b[3] * x + b[4] * x ** 2) + r.normal(0, 0.02, n)
+    return x.astype(np.float32), y.astype(np.float32), np.full(n, 0.02, np.float32)
+
+
+# heap nodes (1-based) of the constants of rational_program, in b order
+RATIONAL_NODES = (2, 9, 18, 15, 30)
+
+
+def rational_program(N, b, PL=31):
+    """N copies of (b1 + x (b2 + b3 x)) / (1 + x (b4 + b5 x)) as heap programs:
+    node 1 DIV(2, 3); 2 CPLUS b1 over 4 TIMES(8, 9), 8 A -> 16 A -> x,
+    9 CPLUS b2 over 18 CTIMES b3 over x; 3 PLUS(6, 7), 6 ONE, 7 TIMES(14, 15),
+    14 A -> 28 A -> x, 15 CPLUS b4 over 30 CTIMES b5 over x.  Unreachable nodes
+    are ONE with constant 0."""
+    assert PL == 31
+    P = np.zeros((PL, N), np.int32)
+    C = np.zeros((PL, N), np.float32)
+    ops = {1: 11, 2: 8, 4: 9, 8: 3, 16: 3, 9: 8, 18: 10, 3: 5, 6: 0, 7: 9, 14: 3, 28: 3, 15: 8, 30: 10}
+    for j, o in ops.items():
+        P[j - 1] = o
+    for j, v in zip(RATIONAL_NODES, b):
+        C[j - 1] = v
+    return P, C
+
+
+def used_constants(P):
+    """Mask (PL, N): the constants each program reads -- CONST leaves and the
+    constant ops (+C, *C, ^C, C^), reachable from the root through the A/B
+    pass-throughs."""
+    PL, N = P.shape
+    used = np.zeros((PL, N), bool)
+    reach = np.zeros((PL + 1, N), bool)
+    reach[1] = True
+    for j in range(1, PL + 1):
+        o = P[j - 1]
+        r = reach[j]
+        used[j - 1] = r & np.isin(o, (1, 8, 10, 16, 18))
+        unary = np.isin(o, (2, 8, 10, 13, 14, 16, 18, 19, 20, 21, 22, 23, 24, 25, 26))
+        binary = np.isin(o, (5, 6, 7, 9, 11, 12, 15, 17))
+        for child, m in ((2 * j, np.isin(o, (3,)) | unary | binary), (2 * j + 1, np.isin(o, (4,)) | binary)):
+            if child <= PL:
+                reach[child] |= r & m
+    return used

@@ -188,3 +188,21 @@ def test_tops_matches_sort_tail(tmp_path, k):
     t2.add_lines(body, np.arange(1, nlines, 2))
     t2.write(str(tmp_path / "tops_lines.txt"))
     assert (tmp_path / "tops_lines.txt").read_bytes() == want
+
+
+def test_ess_geyer_on_ar1():
+    """ESS of AR(1) series with coefficient a is close to T (1 - a) / (1 + a);
+    an independent series gives about T; a constant series gives 0."""
+    from gpuropolis_gb300.diagnostics import ess_geyer
+    r = np.random.default_rng(0)
+    T, n = 4000, 400
+    for a in (0.0, 0.5, 0.9):
+        e = r.normal(size=(n, T))
+        x = np.empty_like(e)
+        x[:, 0] = e[:, 0] / np.sqrt(1 - a * a)
+        for t in range(1, T):
+            x[:, t] = a * x[:, t - 1] + e[:, t]
+        ess = ess_geyer(x)
+        want = T * (1 - a) / (1 + a)
+        assert abs(np.median(ess) / want - 1) < 0.1, (a, np.median(ess), want)
+    assert ess_geyer(np.ones((2, 100)))[0] == 0

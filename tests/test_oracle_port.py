@@ -91,3 +91,49 @@ def test_port_resample_cutoff_matches_reference(N, map_delta):
     assert n == int(flags.sum()) and np.array_equal(changed, flags)
     # re-drawn ops come from the op set minus its last op (random_int(n_ops - 1))
     assert np.all(P[:, flags] < 26)
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_port_gradient_matches_finite_differences(seed):
+    """The oracle's FP64 reverse-mode gradient of the log-likelihood in the
+    constants agrees with central FP64 finite differences (h = 1e-6) to 1e-4
+    relative, wherever the difference quotient itself is stable."""
+    x, y, sd = H.rational_data(200, seed=seed)
+    P, C = H.random_programs(300, 15, seed=seed)
+    used = H.used_constants(P)
+    h = 1e-6
+    checked = absorbed = 0
+    for idx in range(P.shape[1]):
+        Cd = C[:, idx].astype(np.float64)
+        ll, g, _ = port.loglik_grad_f64(P, idx, Cd, x, y, sd)
+        if not np.isfinite(ll):
+            continue
+        for k in np.where(used[:, idx])[0]:
+            def fd(step):
+                a, b = Cd.copy(), Cd.copy()
+                a[k] += step
+                b[k] -= step
+                return (port.loglik_f64(P, idx, a, x, y, sd) - port.loglik_f64(P, idx, b, x, y, sd)) / (2 * step)
+            f1, f2 = fd(h), fd(h / 2)
+            if not (np.isfinite(f1) and np.isfinite(f2)):
+                continue
+            if abs(f1 - f2) > 1e-5 * max(abs(f1), 1e-6 * (abs(ll) + 1)):
+                continue                      # the difference quotient is not stable here
+            if np.isnan(g[k]):
+                # a finite value computed through a NaN subexpression (pow(NaN, 0) = 1)
+                # has no derivative through it; the chain rule yields NaN there
+                absorbed += 1
+                continue
+            assert abs(g[k] - f1) <= 1e-4 * max(abs(f1), 1e-6 * (abs(ll) + 1)), (idx, k, g[k], f1)
+            checked += 1
+    assert checked >= 50 and absorbed <= 0.05 * checked, (checked, absorbed)
+
+
+def test_rational_program_reads_its_five_constants():
+    b, _ = H.rational_coefficients(0)
+    x, y, sd = H.rational_data(200, seed=0)
+    P, C = H.rational_program(1, b)
+    assert sorted(np.where(H.used_constants(P)[:, 0])[0] + 1) == sorted(H.RATIONAL_NODES)
+    f = np.array([port.call_f64(P, C, 0, v) for v in x])
+    want = (b[0] + b[1] * x + b[2] * x ** 2) / (1 + b[3] * x + b[4] * x ** 2)
+    assert np.allclose(f, want, rtol=1e-5, atol=1e-6)
