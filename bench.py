@@ -17,6 +17,11 @@ e2e       : the same through the C ABI with host buffers: each block uploads
 cpu_baseline / --impl reference : the reference's own per-chain code
             (main.cu:679-813) compiled for the host cores, OpenMP over chains,
             on a bounded sample of the same chains.
+ess       : ESS/s of constants, gradient moves (HMC, MALA) against
+            random-walk MH, on 65536 chains of the rational function
+            y = (b1 + b2 x + b3 x^2)/(1 + b4 x + b5 x^2) fitted to 1024 points
+            (x ~ U[-3, 3], noise N(0, 0.02)), constants-only moves
+            (see ess_comparison).
 """
 import argparse
 import json
@@ -118,6 +123,107 @@ def measured_peaks():
         return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except (OSError, ValueError):
         return {}
+
+
+# constants-mixing comparison: 65536 chains of the rational function's own
+# structure (five constants), 1024 points, constants-only moves
+ESS_WORKLOAD = dict(N=65536, PL=31, nd=1024, traced=4096, rw_steps=3000)
+
+
+def ess_comparison(g, stream, dev):
+    """ESS/s of the constants under Gaussian random-walk MH (the configured sd
+    0.1, and a per-chain adapted sd) and under gradient moves (HMC with 8
+    leapfrog steps, MALA), each from the same burned-in state, with per-chain
+    step sizes adapted beforehand; gradient arms run for the random walk's
+    wall time.  ESS per chain = min over its five constants of Geyer's
+    initial-monotone-sequence ESS, from a traced subsample of chains (the
+    same trajectories, recorded); ESS/s = mean ESS per chain x N / seconds of
+    the untraced block."""
+    import torch
+    from gpuropolis_gb300.diagnostics import chain_ess
+    w = ESS_WORKLOAD
+    N, PL, NT = w["N"], w["PL"], w["traced"]
+    b, _ = H.rational_coefficients(0)
+    x, y, sd = H.rational_data(w["nd"], seed=0)
+    P, C = H.rational_program(N, b)
+    used = H.used_constants(P)
+
+    def sampler(mode, **kw):
+        if mode == "rw":
+            s = g.Sampler(N, program_length=PL, ops=H.OPSET_BASIC, const_proposal=g.CONST_RANDOM_WALK,
+                          rw_sd=kw["sd"], stream=stream.cuda_stream)
+            s.set_moves(0)
+        else:
+            s = g.Sampler(N, program_length=PL, ops=H.OPSET_BASIC, const_proposal=g.CONST_HMC,
+                          stream=stream.cuda_stream)
+            s.set_moves(0, kw["eps"], kw["L"])
+        s.set_data(x, y, sd)
+        return s
+
+    def timed(s, steps, seed, state):
+        s.set_state(*state)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.reset_stats()
+        e0.record(stream)
+        s.run_block(steps, seed)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3, s.stats()
+
+    def arm(s, steps, seed, state, extra):
+        dt, st = timed(s, steps, seed, state)
+        s.set_state(*state)
+        tr = s.run_block_traced(steps, seed, PL)[:NT]
+        e = chain_ess(tr, used[:, :NT])
+        out = {"steps": steps, "seconds": dt, "chain_steps_per_s": N * steps / dt,
+               "acceptance": st["const_accepted"] / max(1, st["const_proposed"]),
+               "ess_per_chain": float(e.mean()), "ess_per_s": float(e.mean() * N / dt)}
+        out.update(extra)
+        return out
+
+    # burn-in from the generating constants with an adapted random walk
+    s = sampler("rw", sd=0.001)
+    s.set_state(P, C)
+    s.adapt_scales(0.234)
+    for i in range(4):
+        s.run_block(1000, 10 + i)
+    state = s.get_state()[:2]
+    s.adapt_scales(0.0)
+    res = {}
+    s.close()
+    s = sampler("rw", sd=0.1)
+    res["rw_sd_0.1"] = arm(s, w["rw_steps"], 1, state, {"sd": 0.1})
+    s.close()
+    s = sampler("rw", sd=0.001)
+    s.set_state(*state)
+    s.adapt_scales(0.234)
+    for i in range(2):
+        s.run_block(1000, 20 + i)
+    s.adapt_scales(0.0)
+    sc = s.chain_scales()
+    res["rw_adapted"] = arm(s, w["rw_steps"], 2, state, {"sd_median": float(np.median(sc)), "target": 0.234})
+    t_rw = res["rw_adapted"]["seconds"]
+    s.close()
+    for name, L, tgt, adapt_steps in (("hmc_L8", 8, 0.8, 150), ("mala", 1, 0.574, 600)):
+        s = sampler("hmc", eps=0.0005, L=L)
+        s.set_state(*state)
+        s.adapt_scales(tgt)
+        for i in range(2):
+            s.run_block(adapt_steps, 30 + i)
+        s.adapt_scales(0.0)
+        sc = s.chain_scales()
+        dt, _ = timed(s, 20, 5, state)
+        steps = max(50, int(t_rw / (dt / 20)))
+        res[name] = arm(s, steps, 3, state, {"leapfrog_steps": L, "eps_median": float(np.median(sc)),
+                                             "target": tgt})
+        s.close()
+    best = max(res["hmc_L8"]["ess_per_s"], res["mala"]["ess_per_s"])
+    return {"workload": "rational-65k", "N": N, "PL": PL, "nd": w["nd"], "constants": 5,
+            "moves": "constants only (no structure moves)", "traced_chains": NT, **res,
+            "ratio_gradient_vs_rw_sd_0.1": best / max(res["rw_sd_0.1"]["ess_per_s"], 1e-300),
+            "ratio_gradient_vs_rw_adapted": best / res["rw_adapted"]["ess_per_s"],
+            "method": "Geyer initial monotone sequence ESS, min over the five constants per chain"}
 
 
 def cpu_reference_rate(w, P, C, x, y, sd, target_s=12.0, threads=0, chains=None):
@@ -275,6 +381,7 @@ def run_gpu(args, w):
     achieved_tops = alg_ops / (kernel_ms / 1e3) / 1e12
     geo = s.launch_geometry()
 
+    ess = None if args.no_ess else ess_comparison(g, stream, dev)
     cpu = None
     if not args.no_cpu_baseline:
         Pw, Cw, _, _ = s.get_state()
@@ -304,6 +411,7 @@ def run_gpu(args, w):
                        "constant": st["const_accepted"] / max(1, st["const_proposed"])},
         "clocks": clocks,
         "cpu_baseline": cpu,
+        "ess": ess,
     }
     print(json.dumps(line))
 
@@ -316,6 +424,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="plain-mh-131k", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-ess", action="store_true", help="skip the constants-mixing (ESS/s) comparison")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default layout (fixed launch sequence, for profilers)")
     args = ap.parse_args()
