@@ -253,11 +253,13 @@ int gpr_destroy(gpr_handle* h) {
 /* Launch geometry for a given layout: K points per lane, data in registers
  * (onepass) or streamed from shared memory, heavy ops rolled or unrolled. */
 /* The MH kernel with Hamiltonian constant moves: one chain per warp, 4 warps
- * per CTA, one point per lane per pass, a persistent grid. */
+ * per CTA, four points per lane per pass, a persistent grid. */
 static int configure_hmc(gpr_handle* h) {
     gpr::KParams& kp = h->kp;
+    if (!gpr::grad_supported(kp))
+        return fail(h, GPR_ERR_ARG, "gradient moves support program_length <= 127 (got %d)", kp.PL);
     gpr::LaunchCfg lc;
-    lc.K = 1; lc.onepass = 0; lc.rolled = 0; lc.lockstep = 0;
+    lc.K = 4; lc.onepass = 0; lc.rolled = 0; lc.lockstep = 0;
     int wpc = 4;
     size_t smem = gpr::grad_smem_bytes(kp, wpc);
     while (smem > 227 * 1024 && wpc > 1) smem = gpr::grad_smem_bytes(kp, wpc /= 2);
@@ -676,6 +678,8 @@ int gpr_loglik_grad(gpr_handle* h, double* grad, double* likelihood) {
     if (!h) return GPR_ERR_ARG;
     if (!grad) return fail(h, GPR_ERR_ARG, "grad is NULL");
     if (h->nd < 0) return fail(h, GPR_ERR_STATE, "gpr_set_data has not been called");
+    if (!gpr::grad_supported(h->kp))
+        return fail(h, GPR_ERR_ARG, "gradients support program_length <= 127 (got %d)", h->PL);
     if (gpr::grad_smem_bytes(h->kp, 4) > 227 * 1024)
         return fail(h, GPR_ERR_ARG, "dataset of %d points does not fit in shared memory", h->nd);
     CUDA_TRY(h, cudaSetDevice(h->device));

@@ -4,8 +4,10 @@
  * step) instead of the reference's independence / random-walk proposals.
  *
  * Adjoint.  The compiled postfix program (gpr_common.h) is run forward once
- * per batch of data points with every instruction's result kept on a tape in
- * shared memory; the backward sweep then walks the instructions in reverse,
+ * per batch of K data points per lane with every instruction's result kept on
+ * a tape in the thread's local memory (one 16-byte row per instruction for
+ * K = 4; L1-resident for programs of realistic length, and leaving shared
+ * memory to occupancy); the backward sweep then walks the instructions in reverse,
  * carrying d loglik / d acc, splitting it at each binary instruction into the
  * accumulator's and the operand's share, and adding the operand's share to
  * the constant it read (an instruction with a constant operand, or a constant
@@ -32,6 +34,13 @@
 namespace gpr {
 
 #define GPR_GACC_STRIDE 33   /* per-constant gradient rows, padded against bank conflicts */
+#define GPR_ASTK_MAX 8       /* adjoint-stack rows: value-stack depth for PROGRAM_LENGTH <= 255 */
+
+/* One tape row: an instruction's result at this lane's K points. */
+template <int K>
+struct alignas(K == 4 ? 16 : (K == 2 ? 8 : 4)) Row {
+    float v[K];
+};
 
 /* Per-warp shared memory of the gradient evaluator and the HMC kernel. */
 struct GradSmem {
@@ -40,15 +49,20 @@ struct GradSmem {
     uint32_t* prog[2];
     uint2* eprog;
     int16_t* match;     /* POP instruction -> index of its PUSH                 */
-    float* tape;        /* [max_instr][K][32]; also the compiler's scratch      */
-    float* astk;        /* adjoint stack [levels][K][32]                        */
-    float* gacc;        /* [PL][GPR_GACC_STRIDE]: per-lane gradient sums        */
+    float* gacc;        /* [PL][GPR_GACC_STRIDE]: per-lane gradient sums; also
+                         * the compiler's scratch                               */
     float* gcur;        /* gradient of the log-posterior at the current state   */
     float* gnew;        /* ... at the trajectory's position                     */
     float* mom;         /* momentum                                             */
 };
 
-__host__ __device__ __forceinline__ size_t grad_warp_bytes(int PL, int max_instr, int levels, int K) {
+__host__ __device__ __forceinline__ size_t grad_rows_bytes(int PL) {
+    const size_t gacc = (size_t)PL * GPR_GACC_STRIDE * 4;
+    const size_t comp = 5 * align16((size_t)PL + 1) * 4;
+    return align16(gacc > comp ? gacc : comp);
+}
+
+__host__ __device__ __forceinline__ size_t grad_warp_bytes(int PL, int max_instr) {
     const size_t plp = align16((size_t)PL);
     size_t b = 0;
     b += 2 * plp;                                              /* ops */
@@ -56,17 +70,12 @@ __host__ __device__ __forceinline__ size_t grad_warp_bytes(int PL, int max_instr
     b += align16(2 * (size_t)max_instr * 4);                   /* prog */
     b += align16((size_t)max_instr * 8);                       /* eprog */
     b += align16((size_t)max_instr * 2);                       /* match */
-    const size_t tape = (size_t)max_instr * K * 32 * 4;
-    const size_t comp = 5 * align16((size_t)PL + 1) * 4;
-    b += align16(tape > comp ? tape : comp);                   /* tape | compiler scratch */
-    b += align16((size_t)levels * K * 32 * 4);                 /* adjoint stack */
-    b += align16((size_t)PL * GPR_GACC_STRIDE * 4);            /* gradient rows */
+    b += grad_rows_bytes(PL);                                  /* gradient rows | compiler scratch */
     b += 3 * align16(plp * 4);                                 /* gcur, gnew, mom */
     return align16(b);
 }
 
-template <int K>
-__device__ __forceinline__ GradSmem carve_grad(uint8_t* base, int PL, int max_instr, int levels) {
+__device__ __forceinline__ GradSmem carve_grad(uint8_t* base, int PL, int max_instr) {
     GradSmem w;
     const size_t plp = align16((size_t)PL);
     uint8_t* p = base;
@@ -75,11 +84,7 @@ __device__ __forceinline__ GradSmem carve_grad(uint8_t* base, int PL, int max_in
     w.prog[0] = (uint32_t*)p; w.prog[1] = (uint32_t*)p + max_instr; p += align16(2 * (size_t)max_instr * 4);
     w.eprog = (uint2*)p; p += align16((size_t)max_instr * 8);
     w.match = (int16_t*)p; p += align16((size_t)max_instr * 2);
-    const size_t tape = (size_t)max_instr * K * 32 * 4;
-    const size_t comp = 5 * align16((size_t)PL + 1) * 4;
-    w.tape = (float*)p; p += align16(tape > comp ? tape : comp);
-    w.astk = (float*)p; p += align16((size_t)levels * K * 32 * 4);
-    w.gacc = (float*)p; p += align16((size_t)PL * GPR_GACC_STRIDE * 4);
+    w.gacc = (float*)p; p += grad_rows_bytes(PL);
     w.gcur = (float*)p; p += align16(plp * 4);
     w.gnew = (float*)p; p += align16(plp * 4);
     w.mom = (float*)p;
@@ -111,7 +116,7 @@ __device__ __forceinline__ void pop_match(const uint32_t* prog, int ninstr, int1
  * value (the tape entry of the matching PUSH). */
 template <int K>
 __device__ __forceinline__ void operand(uint32_t src, float c, int i, const int16_t* match, const float (&x)[K],
-                                        const float* tape, int lane, float (&v)[K]) {
+                                        const Row<K>* tape, float (&v)[K]) {
     if (src == SRC_X) {
 #pragma unroll
         for (int k = 0; k < K; ++k) v[k] = x[k];
@@ -122,9 +127,9 @@ __device__ __forceinline__ void operand(uint32_t src, float c, int i, const int1
 #pragma unroll
         for (int k = 0; k < K; ++k) v[k] = 1.0f;
     } else {
-        const int j = match[i];
+        const Row<K> t = tape[match[i]];
 #pragma unroll
-        for (int k = 0; k < K; ++k) v[k] = tape[(j * K + k) * 32 + lane];
+        for (int k = 0; k < K; ++k) v[k] = t.v[k];
     }
 }
 
@@ -132,7 +137,7 @@ __device__ __forceinline__ void operand(uint32_t src, float c, int i, const int1
  * The arithmetic is the evaluator's (run_program), operation for operation. */
 template <int K>
 __device__ __forceinline__ void forward_tape(const uint2* __restrict__ prog, int ninstr, const int16_t* match,
-                                             const float (&x)[K], float* __restrict__ tape, int lane) {
+                                             const float (&x)[K], Row<K>* __restrict__ tape) {
     float acc[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) acc[k] = 0.0f;
@@ -145,7 +150,7 @@ __device__ __forceinline__ void forward_tape(const uint2* __restrict__ prog, int
             const uint32_t bop = (code - I_BIN0) >> 3;
             const uint32_t accleft = (code >> 2) & 1u;
             float v[K];
-            operand<K>(code & 3u, c, i, match, x, tape, lane, v);
+            operand<K>(code & 3u, c, i, match, x, tape, v);
 #pragma unroll
             for (int k = 0; k < K; ++k) {
                 const float u = accleft ? acc[k] : v[k];
@@ -200,8 +205,10 @@ __device__ __forceinline__ void forward_tape(const uint2* __restrict__ prog, int
                     break;
             }
         }
+        Row<K> row;
 #pragma unroll
-        for (int k = 0; k < K; ++k) tape[(i * K + k) * 32 + lane] = acc[k];
+        for (int k = 0; k < K; ++k) row.v[k] = acc[k];
+        tape[i] = row;
     }
 }
 
@@ -213,8 +220,8 @@ __device__ __forceinline__ float adj_mul(float adj, float d) { return adj == 0.0
  * per-constant shares are added to this lane's gradient rows. */
 template <int K>
 __device__ __forceinline__ void backward_tape(const uint2* __restrict__ prog, int ninstr, const int16_t* match,
-                                              const float (&x)[K], const float* __restrict__ tape,
-                                              float (&adj)[K], float* __restrict__ astk, float* __restrict__ gacc,
+                                              const float (&x)[K], const Row<K>* __restrict__ tape,
+                                              float (&adj)[K], Row<K>* __restrict__ astk, float* __restrict__ gacc,
                                               int PL, int lane) {
     int sp = 0;
 #pragma unroll 1
@@ -228,12 +235,17 @@ __device__ __forceinline__ void backward_tape(const uint2* __restrict__ prog, in
             const uint32_t accleft = (code >> 2) & 1u;
             const uint32_t src = code & 3u;
             float v[K];
-            operand<K>(src, c, i, match, x, tape, lane, v);
+            operand<K>(src, c, i, match, x, tape, v);
             float share = 0.0f;
+            /* the accumulator's input; the result only where a partial needs it */
+            const Row<K> ain = tape[i - 1];
+            Row<K> rres;
+            if (bop == BOP_DIV || bop == BOP_POW) rres = tape[i];
+            Row<K> spill;
 #pragma unroll
             for (int k = 0; k < K; ++k) {
-                const float a = tape[((i - 1) * K + k) * 32 + lane];
-                const float res = tape[(i * K + k) * 32 + lane];
+                const float a = ain.v[k];
+                const float res = (bop == BOP_DIV || bop == BOP_POW) ? rres.v[k] : 0.0f;
                 const float u = accleft ? a : v[k];
                 const float w = accleft ? v[k] : a;
                 float du, dw;
@@ -248,10 +260,10 @@ __device__ __forceinline__ void backward_tape(const uint2* __restrict__ prog, in
                 const float au = adj_mul(adj[k], du), aw = adj_mul(adj[k], dw);
                 const float av = accleft ? aw : au;
                 adj[k] = accleft ? au : aw;
-                if (src == SRC_POP) astk[(sp * K + k) * 32 + lane] = av;
+                spill.v[k] = av;
                 share = __fadd_rn(share, av);
             }
-            if (src == SRC_POP) ++sp;
+            if (src == SRC_POP) astk[sp++] = spill;
             else if (src == SRC_C && (int)node < PL) gacc[node * GPR_GACC_STRIDE + lane] += share;
         } else if (code == I_LDC) {
             float share = 0.0f;
@@ -262,14 +274,15 @@ __device__ __forceinline__ void backward_tape(const uint2* __restrict__ prog, in
 #pragma unroll
             for (int k = 0; k < K; ++k) adj[k] = 0.0f;
         } else if (code == I_PUSH) {
-            --sp;
+            const Row<K> t = astk[--sp];
 #pragma unroll
-            for (int k = 0; k < K; ++k) adj[k] = astk[(sp * K + k) * 32 + lane];
+            for (int k = 0; k < K; ++k) adj[k] = t.v[k];
         } else {
+            const Row<K> ain = tape[i - 1], rres = tape[i];
 #pragma unroll 1
             for (int k = 0; k < K; ++k) {
-                const float a = tape[((i - 1) * K + k) * 32 + lane];
-                const float res = tape[(i * K + k) * 32 + lane];
+                const float a = ain.v[k];
+                const float res = rres.v[k];
                 float d;
                 switch (code) {
                     case U_INV: d = -__fmul_rn(res, res); break;
@@ -295,11 +308,13 @@ __device__ __forceinline__ void backward_tape(const uint2* __restrict__ prog, in
  * g[i] = 2^-64 d loglik / d C[i] in FP32, at the bookkeeping scale like the
  * likelihood (0 for constants the program does not read).  The gradient is
  * meaningful only when the likelihood is finite. */
-template <int K>
+template <int K, int MAXI>
 __device__ df eval_loglik_grad(const uint2* prog, int ninstr, const GradSmem& ws, const float* sx,
                                const float* sy, const float* sw, const KParams& p, int lane, int& pts,
                                float* g) {
     const int PL = p.PL;
+    Row<K> tape[MAXI];             /* thread-local: results of every instruction */
+    Row<K> astk[GPR_ASTK_MAX];     /* adjoints of pushed values                  */
 #pragma unroll 1
     for (int j = lane; j < PL * GPR_GACC_STRIDE; j += 32) ws.gacc[j] = 0.0f;
     __syncwarp();
@@ -318,14 +333,16 @@ __device__ df eval_loglik_grad(const uint2* prog, int ninstr, const GradSmem& ws
             x[k] = v ? sx[i] : 0.0f;
             valid |= (v ? 1u : 0u) << k;
         }
-        forward_tape<K>(prog, ninstr, ws.match, x, ws.tape, lane);
+        forward_tape<K>(prog, ninstr, ws.match, x, tape);
         pts += min(32 * K, p.nd - pass * 32 * K);
+#pragma unroll
+        const Row<K> fres = tape[ninstr - 2];
 #pragma unroll
         for (int k = 0; k < K; ++k) {
             adj[k] = 0.0f;
             if (valid & (1u << k)) {
                 const int i = base + 32 * k;
-                const float f = ws.tape[((ninstr - 2) * K + k) * 32 + lane];
+                const float f = fres.v[k];
                 const float r = __fsub_rn(f, sy[i]);
                 const float q = __fmul_rn(r, r);
                 bad |= !(q <= FLT_MAX);
@@ -334,7 +351,7 @@ __device__ df eval_loglik_grad(const uint2* prog, int ninstr, const GradSmem& ws
             }
         }
         bad = __any_sync(FULLMASK, bad);
-        if (!bad) backward_tape<K>(prog, ninstr, ws.match, x, ws.tape, adj, ws.astk, ws.gacc, PL, lane);
+        if (!bad) backward_tape<K>(prog, ninstr, ws.match, x, tape, adj, astk, ws.gacc, PL, lane);
     }
     __syncwarp();
 #pragma unroll 1
@@ -373,7 +390,7 @@ __device__ __forceinline__ float hmc_momentum(uint32_t seed, uint32_t chain, uin
 /* ------------------------------------------------------------------------ */
 /* d loglik / d C for every chain's current state (gpr_loglik_grad): one warp
  * per chain, grad[i*N + chain] (double, unscaled) and lik[chain]. */
-template <int K>
+template <int K, int MAXI>
 __global__ void __launch_bounds__(128) loglik_grad_kernel(const __grid_constant__ KParams p, double* grad,
                                                           double* lik_out) {
     extern __shared__ __align__(128) uint8_t smem[];
@@ -384,8 +401,7 @@ __global__ void __launch_bounds__(128) loglik_grad_kernel(const __grid_constant_
     float* sy = sx + p.nd_pad;
     float* sw = sy + p.nd_pad;
     uint8_t* wbase = smem + 16 + align16((size_t)3 * p.nd_pad * 4);
-    const GradSmem ws = carve_grad<K>(wbase + (size_t)warp * grad_warp_bytes(p.PL, p.max_instr, p.levels, K),
-                                      p.PL, p.max_instr, p.levels);
+    const GradSmem ws = carve_grad(wbase + (size_t)warp * grad_warp_bytes(p.PL, p.max_instr), p.PL, p.max_instr);
     stage_dataset(sx, sy, sw, bar, p);
     const int chain = blockIdx.x * (blockDim.x >> 5) + warp;
     if (chain >= p.N) return;
@@ -396,12 +412,12 @@ __global__ void __launch_bounds__(128) loglik_grad_kernel(const __grid_constant_
         ws.Cs[0][i] = p.C[(size_t)i * p.N + chain];
     }
     __syncwarp();
-    const CompileOut co = compile_parallel(ws.ops[0], PL, ws.prog[0], compile_scratch(ws.tape, PL), lane);
+    const CompileOut co = compile_parallel(ws.ops[0], PL, ws.prog[0], compile_scratch(ws.gacc, PL), lane);
     __syncwarp();
     build_eval_program(ws.prog[0], ws.Cs[0], co.ninstr, ws.eprog, lane);
     pop_match(ws.prog[0], co.ninstr, ws.match, lane);
     int pts = 0;
-    const df lik = eval_loglik_grad<K>(ws.eprog, co.ninstr, ws, sx, sy, sw, p, lane, pts, ws.gnew);
+    const df lik = eval_loglik_grad<K, MAXI>(ws.eprog, co.ninstr, ws, sx, sy, sw, p, lane, pts, ws.gnew);
     for (int i = lane; i < PL; i += 32) grad[(size_t)i * p.N + chain] = (double)ws.gnew[i] * GPR_DF_UNSCALE;
     if (lane == 0) lik_out[chain] = df_to_double_unscaled(lik);
 }
@@ -410,7 +426,7 @@ __global__ void __launch_bounds__(128) loglik_grad_kernel(const __grid_constant_
 /* The MH block with Hamiltonian constant moves.  One warp per chain, chains
  * claimed from the global counter; evaluation with the adjoint on K points
  * per lane. */
-template <int K, int RNG>
+template <int K, int MAXI, int RNG>
 __global__ void __launch_bounds__(128) mh_hmc_kernel(const __grid_constant__ KParams p) {
     extern __shared__ __align__(128) uint8_t smem[];
     const int lane = threadIdx.x & 31;
@@ -420,8 +436,7 @@ __global__ void __launch_bounds__(128) mh_hmc_kernel(const __grid_constant__ KPa
     float* sy = sx + p.nd_pad;
     float* sw = sy + p.nd_pad;
     uint8_t* wbase = smem + 16 + align16((size_t)3 * p.nd_pad * 4);
-    const GradSmem ws = carve_grad<K>(wbase + (size_t)warp * grad_warp_bytes(p.PL, p.max_instr, p.levels, K),
-                                      p.PL, p.max_instr, p.levels);
+    const GradSmem ws = carve_grad(wbase + (size_t)warp * grad_warp_bytes(p.PL, p.max_instr), p.PL, p.max_instr);
     stage_dataset(sx, sy, sw, bar, p);
     const int PL = p.PL;
     const bool adapt = p.chain_scale && p.adapt_target > 0.0f;
@@ -477,14 +492,14 @@ __global__ void __launch_bounds__(128) mh_hmc_kernel(const __grid_constant__ KPa
                 }
                 __syncwarp();
                 const CompileOut co = compile_parallel(ws.ops[pbuf], PL, ws.prog[pbuf],
-                                                       compile_scratch(ws.tape, PL), lane);
+                                                       compile_scratch(ws.gacc, PL), lane);
                 __syncwarp();
                 const df backward = df_make(__fmul_rn(-p.logcount[co.count], GPR_DF_SCALE), 0.0f);
                 const df cs = init ? cauchy_sum(ws.Cs[ccur], p, lane) : cur_cs;
                 build_eval_program(ws.prog[pbuf], ws.Cs[ccur], co.ninstr, ws.eprog, lane);
                 pop_match(ws.prog[pbuf], co.ninstr, ws.match, lane);
                 int pe = 0;
-                const df lik = eval_loglik_grad<K>(ws.eprog, co.ninstr, ws, sx, sy, sw, p, lane, pe, ws.gnew);
+                const df lik = eval_loglik_grad<K, MAXI>(ws.eprog, co.ninstr, ws, sx, sy, sw, p, lane, pe, ws.gnew);
                 st_pts += (unsigned)pe;
                 const df prior = df_add(length_prior(co.length, p), cs);
                 const df post = df_add(prior, lik);
@@ -534,7 +549,7 @@ __global__ void __launch_bounds__(128) mh_hmc_kernel(const __grid_constant__ KPa
                         build_eval_program(ws.prog[cur], q, cur_ninstr, ws.eprog, lane);
                         __syncwarp();
                         int pe = 0;
-                        lik = eval_loglik_grad<K>(ws.eprog, cur_ninstr, ws, sx, sy, sw, p, lane, pe, ws.gnew);
+                        lik = eval_loglik_grad<K, MAXI>(ws.eprog, cur_ninstr, ws, sx, sy, sw, p, lane, pe, ws.gnew);
                         st_pts += (unsigned)pe;
                         st_evals++; st_nodes += (unsigned)cur_count;
                         st_np += (unsigned long long)(cur_count + 4) * (unsigned)pe;

@@ -120,6 +120,7 @@ cudaError_t launch_math(int op, const float* a, const float* b, float* out, int 
  * moves (gpr_hmc.cu).  grad_smem_bytes: dynamic shared memory of either for
  * a CTA of warps_per_cta chains. */
 size_t grad_smem_bytes(const KParams& p, int warps_per_cta);
+bool grad_supported(const KParams& p);   /* PROGRAM_LENGTH <= 127 */
 cudaError_t launch_loglik_grad(const KParams& p, double* grad, double* lik, cudaStream_t st);
 cudaError_t hmc_occupancy(const KParams& p, int warps_per_cta, size_t smem, int* ctas_per_sm);
 cudaError_t launch_hmc_block(const KParams& p, const LaunchCfg& lc, cudaStream_t st);
