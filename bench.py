@@ -42,6 +42,9 @@ WORKLOADS = {
                           mh_steps=1000, map_delta=20.0, blocks=20),
     "plain-mh-1k": dict(N=1024, PL=31, nd=101, data="quad", ops="basic", rw_sd=0.1,
                         mh_steps=1000, map_delta=20.0, blocks=10),
+    # Hamiltonian moves on 8192 chains of the rational model: the case ncu captures
+    "hmc-rational-8k-profile": dict(N=8192, PL=31, nd=1024, data="rational", ops="basic", rw_sd=0.0,
+                                    mh_steps=20, map_delta=0.0, blocks=1),
     # the 131k workload cut to 8192 chains x 100 steps: the case ncu captures
     "plain-mh-8k-profile": dict(N=8192, PL=63, nd=250, data="expdecay", ops="basic", rw_sd=0.1,
                                 mh_steps=100, map_delta=20.0, blocks=1),
@@ -224,6 +227,40 @@ def ess_comparison(g, stream, dev):
             "ratio_gradient_vs_rw_sd_0.1": best / max(res["rw_sd_0.1"]["ess_per_s"], 1e-300),
             "ratio_gradient_vs_rw_adapted": best / res["rw_adapted"]["ess_per_s"],
             "method": "Geyer initial monotone sequence ESS, min over the five constants per chain"}
+
+
+def run_hmc_profile(args):
+    """Throughput of the Hamiltonian-move kernel alone: 8192 chains of the
+    rational model, HMC with 8 leapfrog steps (step 0.001), constants only,
+    blocks of 20 MH steps; the case ncu captures."""
+    import torch
+    import gpuropolis_gb300 as g
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    N, steps = 8192, 20
+    b, _ = H.rational_coefficients(0)
+    x, y, sd = H.rational_data(1024, seed=0)
+    P, C = H.rational_program(N, b)
+    s = g.Sampler(N, program_length=31, ops=H.OPSET_BASIC, const_proposal=g.CONST_HMC, stream=stream.cuda_stream)
+    s.set_data(x, y, sd)
+    s.set_moves(0, 0.001, 8)
+    s.set_state(P, C)
+    for i in range(args.warmup):
+        s.run_block(steps, 1 + i)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(args.steps):
+        s.run_block(steps, 100 + i)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) / 1e3
+    print(json.dumps({"metric": "HMC chain-steps/s (8 leapfrog steps, 1024 points)", "unit": "chain-steps/s",
+                      "value": N * steps * args.steps / sec,
+                      "gradient_evals_per_s": N * steps * args.steps * 8 / sec,
+                      "config": {"workload": args.workload, "N": N, "PL": 31, "nd": 1024, "mh_steps": steps},
+                      "launch": s.launch_geometry()}))
 
 
 def cpu_reference_rate(w, P, C, x, y, sd, target_s=12.0, threads=0, chains=None):
@@ -429,6 +466,9 @@ def main():
                     help="keep the default layout (fixed launch sequence, for profilers)")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
+    if args.workload == "hmc-rational-8k-profile":
+        run_hmc_profile(args)
+        return
     if args.impl == "reference":
         if int(os.environ.get("RANK", "0")) != 0:
             return
