@@ -263,12 +263,38 @@ def run_hmc_profile(args):
                       "launch": s.launch_geometry()}))
 
 
-def cpu_reference_rate(w, P, C, x, y, sd, target_s=12.0, threads=0, chains=None):
-    """chain-steps/s of the reference's own code on the host cores, measured on
-    chains [0, S) of the given state, S sized to about target_s seconds."""
+class _PortRunner:
+    """The C restatement of the reference (oracle/gpr_oracle.c) with the
+    reference oracle's run_kernel interface: the CPU baseline where the
+    reference's own source could not be built."""
+
+    def __init__(self, w):
+        from oracle import port
+        self.port = port
+        ops = H.OPSET_BASIC if w["ops"] == "basic" else None
+        self.cfg = port.cfg(PL=w["PL"], ops=ops, rng=0, const_mode=1 if w["rw_sd"] > 0 else 0,
+                            rw_sd=w["rw_sd"], project_math=0)
+
+    def run_kernel(self, P, C, x, y, sd, steps, seed, nthreads=0):
+        return self.port.run_block(self.cfg, P, C, x, y, sd, steps, seed, nthreads=nthreads)
+
+
+def cpu_runner(w):
+    """(runner, kind): the reference's own code compiled for the host, or the
+    restatement when the reference source is absent."""
     from oracle import ref as oref
-    o = oref.get(pl=w["PL"], opset=1 if w["ops"] == "basic" else 0, project_math=0,
-                 rw_sd=w["rw_sd"])
+    try:
+        return oref.get(pl=w["PL"], opset=1 if w["ops"] == "basic" else 0, project_math=0,
+                        rw_sd=w["rw_sd"]), "reference"
+    except RuntimeError:
+        return _PortRunner(w), "port"
+
+
+def cpu_reference_rate(w, P, C, x, y, sd, target_s=12.0, threads=0, chains=None):
+    """chain-steps/s of the reference's own code (or its restatement) on the
+    host cores, measured on chains [0, S) of the given state, S sized to
+    about target_s seconds."""
+    o, kind = cpu_runner(w)
     ncores = threads or os.cpu_count()
     steps = w["mh_steps"]
     if chains is None:
@@ -282,7 +308,7 @@ def cpu_reference_rate(w, P, C, x, y, sd, target_s=12.0, threads=0, chains=None)
     t0 = time.perf_counter()
     o.run_kernel(Ps, Cs, x, y, sd, steps, 12345, nthreads=ncores)
     dt = time.perf_counter() - t0
-    return chains * steps / dt, ncores, chains, dt
+    return chains * steps / dt, ncores, chains, dt, kind
 
 
 def run_reference(args, w):
@@ -293,7 +319,7 @@ def run_reference(args, w):
     rates = []
     chains = None
     for i in range(args.warmup + args.steps):
-        rate, cores, chains, dt = cpu_reference_rate(w, P, C, x, y, sd, chains=chains)
+        rate, cores, chains, dt, kind = cpu_reference_rate(w, P, C, x, y, sd, chains=chains)
         if i >= args.warmup:
             rates.append(rate)
     value = float(np.mean(rates))
@@ -305,7 +331,7 @@ def run_reference(args, w):
         "data": "synthetic (seeded)",
         "point_evals_per_s": value * w["nd"],
         "config": {"workload": args.workload, **{k: w[k] for k in ("N", "PL", "nd", "mh_steps")}},
-        "cpu_baseline": {"value": value, "unit": "chain-steps/s", "cores": ncores, "kind": "reference",
+        "cpu_baseline": {"value": value, "unit": "chain-steps/s", "cores": ncores, "kind": kind,
                          "sample": "%d chains x %d MH steps per step, from the seeded initial state"
                                    % (chains, w["mh_steps"])},
         "e2e": {"value": value, "unit": "chain-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -422,8 +448,8 @@ def run_gpu(args, w):
     cpu = None
     if not args.no_cpu_baseline:
         Pw, Cw, _, _ = s.get_state()
-        rate, cores, chains, dt = cpu_reference_rate(w, Pw, Cw, x, y, sd)
-        cpu = {"value": rate, "unit": "chain-steps/s", "cores": cores, "kind": "reference",
+        rate, cores, chains, dt, kind = cpu_reference_rate(w, Pw, Cw, x, y, sd)
+        cpu = {"value": rate, "unit": "chain-steps/s", "cores": cores, "kind": kind,
                "sample": "%d chains x %d MH steps of the warmed-up state (%.1f s)"
                          % (chains, w["mh_steps"], dt)}
     line = {

@@ -14,7 +14,9 @@
  * Additional options (all off by default, so the defaults reproduce the
  * reference): --program-length=PL (or --max-len=PL+1), --ops=reference|basic|
  * <comma-separated op codes>, --rng=lcg|philox, --const-proposal=reference|
- * rw:SD, --resample=quantile:Q|map-delta:D, --threads=T, --device-resample
+ * rw:SD|hmc:EPS:L|mala:EPS (gradient moves on the constants), --struct-every=K
+ * (a structure move every K steps; 0: constants only), --resample=quantile:Q|
+ * map-delta:D, --threads=T, --device-resample
  * (resample on the GPU from a Philox stream keyed by the block seed, without
  * copying the state back and forth), --tops=K (write tops.txt: the K
  * lines of this run's samples.txt that `sort -g -k3 | tail -n K`, run-all.sh:45,
@@ -37,13 +39,14 @@ static int N = 1024, steps = 1000, outer = 100, thin = 1, seed = -1, burn = 0, Q
 static int WHICH_GPU = 0, FIRST_HALF_DATA = 0, EVEN_HALF_DATA = 0, SHOW_CONSTANTS = 0;
 static std::string in_file_path = "data.txt", out_path = "out/";
 static int PL = 31, rng_mode = GPR_RNG_LCG, const_mode = GPR_CONST_REFERENCE, threads = 0;
-static float rw_sd = 0.1f;
+static float rw_sd = 0.1f, hmc_eps = 0.01f;
+static int hmc_steps = 8, struct_every = 5;
 static int resample_mode = GPR_RESAMPLE_QUANTILE;
 static double resample_param = 0.5;
 static int device_resample = 0, tops_k = 0;
 static std::vector<int> ops;
 
-enum { OPT_PL = 1000, OPT_MAXLEN, OPT_OPS, OPT_RNG, OPT_CONST, OPT_RESAMPLE, OPT_THREADS, OPT_DEVRES, OPT_TOPS };
+enum { OPT_PL = 1000, OPT_MAXLEN, OPT_OPS, OPT_RNG, OPT_CONST, OPT_RESAMPLE, OPT_THREADS, OPT_DEVRES, OPT_TOPS, OPT_STRUCT };
 
 static struct option long_options[] = {
     {"in", required_argument, NULL, 'd'},
@@ -70,6 +73,7 @@ static struct option long_options[] = {
     {"threads", required_argument, NULL, OPT_THREADS},
     {"device-resample", no_argument, NULL, OPT_DEVRES},
     {"tops", required_argument, NULL, OPT_TOPS},
+    {"struct-every", required_argument, NULL, OPT_STRUCT},
     {NULL, 0, 0, 0}};
 
 static int parse_ops(const char* s) {
@@ -118,6 +122,15 @@ static int process_arguments(int argc, char** argv) {
             case OPT_CONST:
                 if (!strcmp(optarg, "reference")) const_mode = GPR_CONST_REFERENCE;
                 else if (!strncmp(optarg, "rw:", 3)) { const_mode = GPR_CONST_RANDOM_WALK; rw_sd = (float)atof(optarg + 3); }
+                else if (!strncmp(optarg, "hmc:", 4)) {
+                    const_mode = GPR_CONST_HMC;
+                    if (sscanf(optarg + 4, "%f:%d", &hmc_eps, &hmc_steps) != 2) return 1;
+                }
+                else if (!strncmp(optarg, "mala:", 5)) {
+                    const_mode = GPR_CONST_HMC;
+                    hmc_steps = 1;
+                    if (sscanf(optarg + 5, "%f", &hmc_eps) != 1) return 1;
+                }
                 else return 1;
                 break;
             case OPT_RESAMPLE:
@@ -128,6 +141,7 @@ static int process_arguments(int argc, char** argv) {
             case OPT_THREADS: threads = atoi(optarg); break;
             case OPT_DEVRES: device_resample = 1; break;
             case OPT_TOPS: tops_k = atoi(optarg); if (tops_k < 1) return 1; break;
+            case OPT_STRUCT: struct_every = atoi(optarg); if (struct_every < 0) return 1; break;
             default: return 1;
         }
     return 0;
@@ -186,6 +200,11 @@ int main(int argc, char** argv) {
             fprintf(stderr, "Invalid GPU device %d\n", WHICH_GPU);   /* main.cu:1045 */
         return 1;
     }
+    if (gpr_set_moves(h, struct_every, hmc_eps, hmc_steps) != GPR_OK) {
+        fprintf(stderr, "%s\n", gpr_last_error(h));
+        gpr_destroy(h);
+        return 1;
+    }
     const int wgpu = WHICH_GPU;
     std::string SAMPLE_PATH = out_path + "/samples.txt";
     std::string LOG_PATH = out_path + "/log.txt";
@@ -220,8 +239,10 @@ int main(int argc, char** argv) {
     if (lg) {
         write_params(lg, ndata, wgpu);
         fprintf(lg, "# \tRNG: %s\n# \tConstant proposal: %s", rng_mode == GPR_RNG_PHILOX ? "philox" : "lcg",
-                const_mode == GPR_CONST_RANDOM_WALK ? "rw:" : "reference");
+                const_mode == GPR_CONST_RANDOM_WALK ? "rw:" : const_mode == GPR_CONST_HMC ? "hmc:" : "reference");
         if (const_mode == GPR_CONST_RANDOM_WALK) fprintf(lg, "%g", rw_sd);
+        if (const_mode == GPR_CONST_HMC) fprintf(lg, "%g:%d", hmc_eps, hmc_steps);
+        fprintf(lg, "\n# \tStructure move every: %d steps", struct_every);
         fprintf(lg, "\n# \tResample: %s:%g%s\n# \tOps:", resample_mode == GPR_RESAMPLE_MAP_DELTA ? "map-delta" : "quantile",
                 resample_param, device_resample ? " (device)" : "");
         for (int o : ops) fprintf(lg, " %d", o);

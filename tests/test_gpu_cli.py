@@ -136,3 +136,32 @@ def test_cli_device_resample(tmp_path):
     c = _run_cli(tmp_path, "dev_md", base + ["--resample=map-delta:20", "--device-resample"])
     _, lc = _lines(c / "samples.txt")
     assert len(lc) == 512 * 3 and lc[:512] != la[:512]
+
+
+def test_cli_gradient_moves_constants_only(tmp_path):
+    """--const-proposal=hmc:EPS:L with --struct-every=0: each chain keeps its
+    program from block to block (no structure moves, no re-draws at quantile
+    0) while its constants move; log.txt records the mode."""
+    if not os.path.exists(g.CLI_PATH):
+        pytest.skip("CLI not built")
+    x, y, sd = H.quad_data(60, seed=3)
+    data = tmp_path / "data.txt"
+    _write_data(data, x, y, sd)
+    out = _run_cli(tmp_path, "hmc", ["--in=%s" % data, "--N=256", "--steps=10", "--outer=3", "--seed=5", "--quiet",
+                                     "--const-proposal=hmc:0.001:4", "--struct-every=0", "--resample=quantile:0",
+                                     "--show-constants", "--ops=basic"])
+    _, lines = _lines(out / "samples.txt")
+    by_chain = {}
+    for l in lines:
+        f = l.split("\t")
+        by_chain.setdefault(f[0], []).append(f)
+    assert len(by_chain) == 256
+    moved = 0
+    for rows in by_chain.values():
+        assert len({r[10] for r in rows}) == 1          # the op-code string
+        moved += len({tuple(r[11:]) for r in rows}) > 1
+    assert moved > 0
+    log = (out / "log.txt").read_text()
+    assert "hmc:0.001:4" in log and "Structure move every: 0" in log
+    r = subprocess.run([g.CLI_PATH, "--const-proposal=hmc:x"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1
