@@ -211,6 +211,7 @@ def ess_comparison(g, stream, dev):
     for name, L, tgt, adapt_steps in (("hmc_L8", 8, 0.8, 150), ("mala", 1, 0.574, 600)):
         s = sampler("hmc", eps=0.0005, L=L)
         s.set_state(*state)
+        s.autotune(steps=20, seed=77)          # CTA shape against L1 for the gradient tapes
         s.adapt_scales(tgt)
         for i in range(2):
             s.run_block(adapt_steps, 30 + i)

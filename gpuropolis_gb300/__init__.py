@@ -92,6 +92,7 @@ def library():
     lib.gpr_reset_stats.argtypes = [vp]
     lib.gpr_set_scores.argtypes = [vp, vp, vp]
     lib.gpr_set_moves.argtypes = [vp, ip, fp, ip]
+    lib.gpr_set_hmc_layout.argtypes = [vp, ip, ip]
     lib.gpr_adapt_scales.argtypes = [vp, fp]
     lib.gpr_chain_scales.argtypes = [vp, vp]
     lib.gpr_loglik_grad.argtypes = [vp, vp, vp]
@@ -254,6 +255,9 @@ class Sampler:
 
     def set_moves(self, struct_every=5, hmc_eps=0.01, hmc_steps=8):
         self._check(self.lib.gpr_set_moves(self.h, int(struct_every), float(hmc_eps), int(hmc_steps)))
+
+    def set_hmc_layout(self, warps_per_cta=4, ctas_per_sm=0):
+        self._check(self.lib.gpr_set_hmc_layout(self.h, int(warps_per_cta), int(ctas_per_sm)))
 
     def adapt_scales(self, target_accept):
         self._check(self.lib.gpr_adapt_scales(self.h, float(target_accept)))

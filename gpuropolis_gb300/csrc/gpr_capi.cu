@@ -10,6 +10,7 @@
  */
 #include <cuda_runtime.h>
 #include <math.h>
+#include <cmath>
 #include <stdarg.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -252,22 +253,32 @@ int gpr_destroy(gpr_handle* h) {
 
 /* Launch geometry for a given layout: K points per lane, data in registers
  * (onepass) or streamed from shared memory, heavy ops rolled or unrolled. */
-/* The MH kernel with Hamiltonian constant moves: one chain per warp, 4 warps
- * per CTA, four points per lane per pass, a persistent grid. */
-static int configure_hmc(gpr_handle* h) {
+/* The MH kernel with Hamiltonian constant moves: one chain per warp,
+ * wpc0 warps per CTA, four points per lane per pass, a persistent grid of at
+ * most ctas_per_sm CTAs per SM (0: as many as fit).  Capping the CTAs also
+ * caps the shared-memory carveout, which leaves the rest of the SM's L1 to
+ * the thread-local gradient tapes. */
+static int configure_hmc(gpr_handle* h, int wpc0 = 4, int ctas_per_sm = 0) {
     gpr::KParams& kp = h->kp;
     if (!gpr::grad_supported(kp))
         return fail(h, GPR_ERR_ARG, "gradient moves support program_length <= 127 (got %d)", kp.PL);
     gpr::LaunchCfg lc;
-    lc.K = 4; lc.onepass = 0; lc.rolled = 0; lc.lockstep = 0;
-    int wpc = 4;
+    lc.K = 4; lc.onepass = 0; lc.rolled = 0; lc.lockstep = 0; lc.carveout = 0;
+    int wpc = wpc0;
     size_t smem = gpr::grad_smem_bytes(kp, wpc);
     while (smem > 227 * 1024 && wpc > 1) smem = gpr::grad_smem_bytes(kp, wpc /= 2);
     if (smem > 227 * 1024)
         return fail(h, GPR_ERR_ARG, "dataset of %d points does not fit in shared memory", kp.nd);
+    if (ctas_per_sm > 0) {
+        int sm_smem = 0;
+        CUDA_TRY(h, cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, h->device));
+        const double need = (double)ctas_per_sm * (double)(smem + 1024);   /* + the per-CTA reserve */
+        lc.carveout = (int)std::min(100.0, std::ceil(100.0 * need / (double)sm_smem));
+    }
     int per_sm = 0;
-    CUDA_TRY(h, gpr::hmc_occupancy(kp, wpc, smem, &per_sm));
+    CUDA_TRY(h, gpr::hmc_occupancy(kp, wpc, smem, lc.carveout, &per_sm));
     if (per_sm < 1) return fail(h, GPR_ERR_ARG, "kernel cannot be resident (smem %zu)", smem);
+    if (ctas_per_sm > 0 && per_sm > ctas_per_sm) per_sm = ctas_per_sm;
     long long ctas = (long long)h->num_sms * per_sm;
     const long long need = (h->N + wpc - 1) / wpc;
     if (ctas > need) ctas = need;
@@ -282,6 +293,7 @@ static int configure_launch(gpr_handle* h, int K, int onepass, int rolled, int l
     gpr::KParams& kp = h->kp;
     if (kp.const_mode == GPR_CONST_HMC) return configure_hmc(h);
     gpr::LaunchCfg lc;
+    lc.carveout = 0;
     lc.K = K;
     lc.onepass = onepass;
     lc.rolled = rolled;
@@ -489,14 +501,8 @@ int gpr_debug_math(gpr_handle* h, int op, const float* a, const float* b, float*
 int gpr_autotune(gpr_handle* h, int steps, int seed, int* K, int* onepass, int* rolled, float* best_ms) {
     if (!h || steps <= 0) return fail(h, GPR_ERR_ARG, "bad arguments");
     if (h->nd < 0) return fail(h, GPR_ERR_STATE, "gpr_set_data has not been called");
-    if (h->kp.const_mode == GPR_CONST_HMC) {   /* one layout only */
-        if (K) *K = h->lc.K;
-        if (onepass) *onepass = h->lc.onepass;
-        if (rolled) *rolled = h->lc.rolled;
-        if (best_ms) *best_ms = 0.0f;
-        return GPR_OK;
-    }
     CUDA_TRY(h, cudaSetDevice(h->device));
+    const bool hmc = h->kp.const_mode == GPR_CONST_HMC;
     const size_t cnt = (size_t)h->N * h->PL;
     int32_t* sP = nullptr; float* sC = nullptr; double* sPr = nullptr; double* sLi = nullptr;
     unsigned long long* sSt = nullptr;
@@ -528,6 +534,26 @@ int gpr_autotune(gpr_handle* h, int steps, int seed, int* K, int* onepass, int* 
     AT_TRY(cudaMemcpyAsync(sSt, h->dstats, GPR_NSTATS * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, h->stream));
     AT_TRY(cudaEventCreate(&e0));
     AT_TRY(cudaEventCreate(&e1));
+    /* the Hamiltonian kernel: CTA size and resident CTAs per SM, i.e. occupancy
+     * against L1 left for the gradient tapes */
+    if (hmc) {
+        const int shapes[9][2] = {{4, 0}, {4, 5}, {4, 4}, {4, 3}, {4, 2}, {8, 2}, {8, 1}, {2, 8}, {2, 6}};
+        for (int i = 0; i < 9; ++i) {
+            if (configure_hmc(h, shapes[i][0], shapes[i][1]) != GPR_OK) continue;
+            for (int rep = 0; rep < 2; ++rep) {
+                AT_TRY(cudaMemcpyAsync(h->dP, sP, cnt * sizeof(int32_t), cudaMemcpyDeviceToDevice, h->stream));
+                AT_TRY(cudaMemcpyAsync(h->dC, sC, cnt * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
+                AT_TRY(cudaEventRecord(e0, h->stream));
+                if ((rc = run(h, steps, seed)) != GPR_OK) goto done;
+                AT_TRY(cudaEventRecord(e1, h->stream));
+                AT_TRY(cudaEventSynchronize(e1));
+            }
+            float ms = 0.0f;
+            AT_TRY(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best) { best = ms; bestlc = h->lc; }
+        }
+        nc = 0;
+    }
     for (int i = 0; i < nc; ++i) {
         if (configure_launch(h, cands[i].K, cands[i].onepass, cands[i].rolled) != GPR_OK) continue;
         for (int rep = 0; rep < 2; ++rep) {   /* first run warms up, second is timed */
@@ -543,7 +569,7 @@ int gpr_autotune(gpr_handle* h, int steps, int seed, int* K, int* onepass, int* 
         if (ms < best) { best = ms; bestlc = h->lc; }
     }
     /* second stage: barrier period and CTA size for the best layout */
-    {
+    if (!hmc) {
         const gpr::LaunchCfg base = bestlc;
         const int periods[3] = {1, 5, 0};
         const int wpcs[2] = {8, 4};
@@ -583,6 +609,15 @@ done:
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     return rc;
+}
+
+int gpr_set_hmc_layout(gpr_handle* h, int warps_per_cta, int ctas_per_sm) {
+    if (!h) return GPR_ERR_ARG;
+    if (h->kp.const_mode != GPR_CONST_HMC) return fail(h, GPR_ERR_ARG, "not a GPR_CONST_HMC handle");
+    if ((warps_per_cta != 1 && warps_per_cta != 2 && warps_per_cta != 4 && warps_per_cta != 8) || ctas_per_sm < 0)
+        return fail(h, GPR_ERR_ARG, "invalid layout: %d warps per CTA, %d CTAs per SM", warps_per_cta, ctas_per_sm);
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    return configure_hmc(h, warps_per_cta, ctas_per_sm);
 }
 
 int gpr_set_layout(gpr_handle* h, int K, int onepass, int rolled) {

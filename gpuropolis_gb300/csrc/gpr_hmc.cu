@@ -35,10 +35,18 @@ static const void* hmc_kernel(const KParams& p) {
     return p.rng_mode ? (const void*)mh_hmc_kernel<GPR_HMC_K, 258, 1> : (const void*)mh_hmc_kernel<GPR_HMC_K, 258, 0>;
 }
 
-cudaError_t hmc_occupancy(const KParams& p, int warps_per_cta, size_t smem, int* ctas_per_sm) {
+/* The shared-memory share of the L1/shared array: the rest is L1, where the
+ * thread-local tapes live.  carveout 0 leaves the driver's default. */
+static cudaError_t set_carveout(const void* f, int carveout) {
+    return cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                carveout > 0 ? carveout : -1);
+}
+
+cudaError_t hmc_occupancy(const KParams& p, int warps_per_cta, size_t smem, int carveout, int* ctas_per_sm) {
     if (!grad_supported(p)) return cudaErrorInvalidValue;
     const void* f = hmc_kernel(p);
     cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = set_carveout(f, carveout);
     if (e != cudaSuccess) return e;
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, f, warps_per_cta * 32, smem);
 }
@@ -47,6 +55,7 @@ cudaError_t launch_hmc_block(const KParams& p, const LaunchCfg& lc, cudaStream_t
     if (!grad_supported(p)) return cudaErrorInvalidValue;
     const void* f = hmc_kernel(p);
     cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lc.smem_bytes);
+    if (e == cudaSuccess) e = set_carveout(f, lc.carveout);
     if (e != cudaSuccess) return e;
     KParams pp = p;
     void* args[] = {(void*)&pp};

@@ -103,6 +103,7 @@ struct LaunchCfg {
     int warps_per_cta;
     int ctas;
     size_t smem_bytes;
+    int carveout;      /* shared-memory share of L1 in percent, 0 = the driver's choice */
 };
 
 size_t mh_smem_bytes(const KParams& p, int K, int warps_per_cta);
@@ -122,7 +123,7 @@ cudaError_t launch_math(int op, const float* a, const float* b, float* out, int 
 size_t grad_smem_bytes(const KParams& p, int warps_per_cta);
 bool grad_supported(const KParams& p);   /* PROGRAM_LENGTH <= 127 */
 cudaError_t launch_loglik_grad(const KParams& p, double* grad, double* lik, cudaStream_t st);
-cudaError_t hmc_occupancy(const KParams& p, int warps_per_cta, size_t smem, int* ctas_per_sm);
+cudaError_t hmc_occupancy(const KParams& p, int warps_per_cta, size_t smem, int carveout, int* ctas_per_sm);
 cudaError_t launch_hmc_block(const KParams& p, const LaunchCfg& lc, cudaStream_t st);
 
 /* Selection over the chains' posteriors (gpr_resample.cu).  launch_select
