@@ -259,6 +259,7 @@ int gpr_destroy(gpr_handle* h) {
  * caps the shared-memory carveout, which leaves the rest of the SM's L1 to
  * the thread-local gradient tapes. */
 static int configure_hmc(gpr_handle* h, int wpc0 = 4, int ctas_per_sm = 0) {
+    if (wpc0 < 1 || wpc0 > 4) wpc0 = 4;   /* the kernel is built for CTAs of at most 128 threads */
     gpr::KParams& kp = h->kp;
     if (!gpr::grad_supported(kp))
         return fail(h, GPR_ERR_ARG, "gradient moves support program_length <= 127 (got %d)", kp.PL);
@@ -537,8 +538,8 @@ int gpr_autotune(gpr_handle* h, int steps, int seed, int* K, int* onepass, int* 
     /* the Hamiltonian kernel: CTA size and resident CTAs per SM, i.e. occupancy
      * against L1 left for the gradient tapes */
     if (hmc) {
-        const int shapes[9][2] = {{4, 0}, {4, 5}, {4, 4}, {4, 3}, {4, 2}, {8, 2}, {8, 1}, {2, 8}, {2, 6}};
-        for (int i = 0; i < 9; ++i) {
+        const int shapes[5][2] = {{4, 0}, {4, 5}, {4, 4}, {2, 0}, {1, 0}};
+        for (int i = 0; i < 5; ++i) {
             if (configure_hmc(h, shapes[i][0], shapes[i][1]) != GPR_OK) continue;
             for (int rep = 0; rep < 2; ++rep) {
                 AT_TRY(cudaMemcpyAsync(h->dP, sP, cnt * sizeof(int32_t), cudaMemcpyDeviceToDevice, h->stream));
@@ -614,7 +615,7 @@ done:
 int gpr_set_hmc_layout(gpr_handle* h, int warps_per_cta, int ctas_per_sm) {
     if (!h) return GPR_ERR_ARG;
     if (h->kp.const_mode != GPR_CONST_HMC) return fail(h, GPR_ERR_ARG, "not a GPR_CONST_HMC handle");
-    if ((warps_per_cta != 1 && warps_per_cta != 2 && warps_per_cta != 4 && warps_per_cta != 8) || ctas_per_sm < 0)
+    if ((warps_per_cta != 1 && warps_per_cta != 2 && warps_per_cta != 4) || ctas_per_sm < 0)
         return fail(h, GPR_ERR_ARG, "invalid layout: %d warps per CTA, %d CTAs per SM", warps_per_cta, ctas_per_sm);
     CUDA_TRY(h, cudaSetDevice(h->device));
     return configure_hmc(h, warps_per_cta, ctas_per_sm);
