@@ -93,6 +93,8 @@ def library():
     lib.gpr_set_scores.argtypes = [vp, vp, vp]
     lib.gpr_set_moves.argtypes = [vp, ip, fp, ip]
     lib.gpr_set_hmc_layout.argtypes = [vp, ip, ip]
+    lib.gpr_set_streaming.argtypes = [vp, ip]
+    lib.gpr_layout_streamed.argtypes = [vp]
     lib.gpr_adapt_scales.argtypes = [vp, fp]
     lib.gpr_chain_scales.argtypes = [vp, vp]
     lib.gpr_loglik_grad.argtypes = [vp, vp, vp]
@@ -240,7 +242,8 @@ class Sampler:
         self._check(self.lib.gpr_launch_geometry(self.h, *[ctypes.byref(a) for a in v]))
         return dict(K=v[0].value, onepass=v[1].value, warps_per_cta=v[2].value,
                     ctas=v[3].value, smem_bytes=v[4].value, rolled=int(self.lib.gpr_layout_rolled(self.h)),
-                    lockstep=int(self.lib.gpr_layout_lockstep(self.h)))
+                    lockstep=int(self.lib.gpr_layout_lockstep(self.h)),
+                    stream=int(self.lib.gpr_layout_streamed(self.h)))
 
     STAT_NAMES = ("evals", "eval_nodes", "eval_points", "eval_node_points", "struct_proposed",
                   "struct_accepted", "const_proposed", "const_accepted")
@@ -255,6 +258,9 @@ class Sampler:
 
     def set_moves(self, struct_every=5, hmc_eps=0.01, hmc_steps=8):
         self._check(self.lib.gpr_set_moves(self.h, int(struct_every), float(hmc_eps), int(hmc_steps)))
+
+    def set_streaming(self, always=True):
+        self._check(self.lib.gpr_set_streaming(self.h, int(bool(always))))
 
     def set_hmc_layout(self, warps_per_cta=4, ctas_per_sm=0):
         self._check(self.lib.gpr_set_hmc_layout(self.h, int(warps_per_cta), int(ctas_per_sm)))

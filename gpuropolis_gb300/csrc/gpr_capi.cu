@@ -47,6 +47,7 @@ struct gpr_handle {
     float* ddata = nullptr;    /* x | y | w | sd, each nd_pad floats */
     /* selection scratch, allocated by the first gpr_resample/gpr_top_chains/gpr_map_chain */
     float* dscale = nullptr;               /* per-chain proposal scales          */
+    int stream_data = 0;                   /* 1: always stream the dataset       */
     unsigned long long* dkeys = nullptr;   /* N posterior keys                   */
     unsigned long long* dsel = nullptr;    /* [0] selected key                   */
     int* dseli = nullptr;                  /* [0] count, [1] first index         */
@@ -265,11 +266,12 @@ static int configure_hmc(gpr_handle* h, int wpc0 = 4, int ctas_per_sm = 0) {
         return fail(h, GPR_ERR_ARG, "gradient moves support program_length <= 127 (got %d)", kp.PL);
     gpr::LaunchCfg lc;
     lc.K = 4; lc.onepass = 0; lc.rolled = 0; lc.lockstep = 0; lc.carveout = 0;
+    lc.stream = h->stream_data || gpr::grad_smem_bytes(kp, wpc0) > 227 * 1024;
     int wpc = wpc0;
-    size_t smem = gpr::grad_smem_bytes(kp, wpc);
-    while (smem > 227 * 1024 && wpc > 1) smem = gpr::grad_smem_bytes(kp, wpc /= 2);
+    size_t smem = gpr::grad_smem_bytes(kp, wpc, lc.stream);
+    while (smem > 227 * 1024 && wpc > 1) smem = gpr::grad_smem_bytes(kp, wpc /= 2, lc.stream);
     if (smem > 227 * 1024)
-        return fail(h, GPR_ERR_ARG, "dataset of %d points does not fit in shared memory", kp.nd);
+        return fail(h, GPR_ERR_ARG, "programs of length %d do not fit in shared memory", kp.PL);
     if (ctas_per_sm > 0) {
         int sm_smem = 0;
         CUDA_TRY(h, cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, h->device));
@@ -277,7 +279,7 @@ static int configure_hmc(gpr_handle* h, int wpc0 = 4, int ctas_per_sm = 0) {
         lc.carveout = (int)std::min(100.0, std::ceil(100.0 * need / (double)sm_smem));
     }
     int per_sm = 0;
-    CUDA_TRY(h, gpr::hmc_occupancy(kp, wpc, smem, lc.carveout, &per_sm));
+    CUDA_TRY(h, gpr::hmc_occupancy(kp, wpc, smem, lc.carveout, lc.stream, &per_sm));
     if (per_sm < 1) return fail(h, GPR_ERR_ARG, "kernel cannot be resident (smem %zu)", smem);
     if (ctas_per_sm > 0 && per_sm > ctas_per_sm) per_sm = ctas_per_sm;
     long long ctas = (long long)h->num_sms * per_sm;
@@ -290,23 +292,28 @@ static int configure_hmc(gpr_handle* h, int wpc0 = 4, int ctas_per_sm = 0) {
     return GPR_OK;
 }
 
+/* A dataset is streamed from device memory when the caller asks for it, or
+ * when staging it beside a full CTA of warps would not fit in shared memory;
+ * streaming uses K = 4 points per lane in passes. */
 static int configure_launch(gpr_handle* h, int K, int onepass, int rolled, int lockstep = 1, int wpc0 = 8) {
     gpr::KParams& kp = h->kp;
     if (kp.const_mode == GPR_CONST_HMC) return configure_hmc(h);
     gpr::LaunchCfg lc;
     lc.carveout = 0;
+    lc.stream = h->stream_data || gpr::mh_smem_bytes(kp, K, wpc0) > 227 * 1024;
+    if (lc.stream) { K = 4; onepass = 0; }
     lc.K = K;
     lc.onepass = onepass;
     lc.rolled = rolled;
     lc.lockstep = lockstep;
     int wpc = wpc0;
-    size_t smem = gpr::mh_smem_bytes(kp, lc.K, wpc);
+    size_t smem = gpr::mh_smem_bytes(kp, lc.K, wpc, lc.stream);
     while (smem > 227 * 1024 && wpc > 1) {
         wpc /= 2;
-        smem = gpr::mh_smem_bytes(kp, lc.K, wpc);
+        smem = gpr::mh_smem_bytes(kp, lc.K, wpc, lc.stream);
     }
     if (smem > 227 * 1024)
-        return fail(h, GPR_ERR_ARG, "dataset of %d points does not fit in shared memory", kp.nd);
+        return fail(h, GPR_ERR_ARG, "programs of length %d do not fit in shared memory", kp.PL);
     lc.warps_per_cta = wpc;
     lc.smem_bytes = smem;
     int per_sm = 0;
@@ -621,6 +628,16 @@ int gpr_set_hmc_layout(gpr_handle* h, int warps_per_cta, int ctas_per_sm) {
     return configure_hmc(h, warps_per_cta, ctas_per_sm);
 }
 
+int gpr_set_streaming(gpr_handle* h, int always) {
+    if (!h) return GPR_ERR_ARG;
+    h->stream_data = always ? 1 : 0;
+    if (h->nd < 0) return GPR_OK;
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    return choose_launch(h);
+}
+
+int gpr_layout_streamed(gpr_handle* h) { return h ? h->lc.stream : 0; }
+
 int gpr_set_layout(gpr_handle* h, int K, int onepass, int rolled) {
     return gpr_set_layout2(h, K, onepass, rolled, 1, 8);
 }
@@ -716,15 +733,16 @@ int gpr_loglik_grad(gpr_handle* h, double* grad, double* likelihood) {
     if (h->nd < 0) return fail(h, GPR_ERR_STATE, "gpr_set_data has not been called");
     if (!gpr::grad_supported(h->kp))
         return fail(h, GPR_ERR_ARG, "gradients support program_length <= 127 (got %d)", h->PL);
-    if (gpr::grad_smem_bytes(h->kp, 4) > 227 * 1024)
-        return fail(h, GPR_ERR_ARG, "dataset of %d points does not fit in shared memory", h->nd);
+
     CUDA_TRY(h, cudaSetDevice(h->device));
     const size_t cnt = (size_t)h->N * h->PL;
     double* dg = nullptr;
     double* dl = nullptr;
     cudaError_t e = cudaMalloc(&dg, cnt * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&dl, (size_t)h->N * sizeof(double));
-    if (e == cudaSuccess) e = gpr::launch_loglik_grad(h->kp, dg, dl, h->stream);
+    if (e == cudaSuccess)
+        e = gpr::launch_loglik_grad(h->kp, dg, dl, h->stream_data || gpr::grad_smem_bytes(h->kp, 4) > 227 * 1024,
+                                    h->stream);
     if (e == cudaSuccess) {
         h->launches++;
         e = cudaMemcpyAsync(grad, dg, cnt * sizeof(double), cudaMemcpyDeviceToHost, h->stream);

@@ -2,7 +2,8 @@
  * gpr_hmc.cu -- instantiations and launchers of the adjoint kernel
  * (gpr_loglik_grad) and of the MH kernel with Hamiltonian constant moves
  * (gpr_hmc.cuh).  Four points per lane; the thread-local tape holds up to
- * 130 instructions (PROGRAM_LENGTH <= 63) or 258 (PROGRAM_LENGTH <= 127).
+ * 130 instructions (PROGRAM_LENGTH <= 63) or 258 (PROGRAM_LENGTH <= 127); the
+ * dataset is staged per CTA or, when too large, read from device memory.
  */
 #include "gpr_hmc.cuh"
 
@@ -10,18 +11,24 @@ namespace gpr {
 
 #define GPR_HMC_K 4
 
-size_t grad_smem_bytes(const KParams& p, int warps_per_cta) {
-    return 16 + align16((size_t)3 * p.nd_pad * 4) + (size_t)warps_per_cta * grad_warp_bytes(p.PL, p.max_instr);
+size_t grad_smem_bytes(const KParams& p, int warps_per_cta, int stream) {
+    return 16 + (stream ? 0 : align16((size_t)3 * p.nd_pad * 4)) +
+           (size_t)warps_per_cta * grad_warp_bytes(p.PL, p.max_instr);
 }
 
 bool grad_supported(const KParams& p) { return p.max_instr <= 258 && p.levels <= GPR_ASTK_MAX; }
 
-cudaError_t launch_loglik_grad(const KParams& p, double* grad, double* lik, cudaStream_t st) {
+template <int MAXI>
+static const void* grad_kernel_t(int stream) {
+    return stream ? (const void*)loglik_grad_kernel<GPR_HMC_K, MAXI, true>
+                  : (const void*)loglik_grad_kernel<GPR_HMC_K, MAXI, false>;
+}
+
+cudaError_t launch_loglik_grad(const KParams& p, double* grad, double* lik, int stream, cudaStream_t st) {
     if (!grad_supported(p)) return cudaErrorInvalidValue;
     const int wpc = 4;
-    const size_t smem = grad_smem_bytes(p, wpc);
-    const void* f = p.max_instr <= 130 ? (const void*)loglik_grad_kernel<GPR_HMC_K, 130>
-                                       : (const void*)loglik_grad_kernel<GPR_HMC_K, 258>;
+    const size_t smem = grad_smem_bytes(p, wpc, stream);
+    const void* f = p.max_instr <= 130 ? grad_kernel_t<130>(stream) : grad_kernel_t<258>(stream);
     cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     KParams pp = p;
@@ -29,10 +36,15 @@ cudaError_t launch_loglik_grad(const KParams& p, double* grad, double* lik, cuda
     return cudaLaunchKernel(f, dim3((p.N + wpc - 1) / wpc), dim3(wpc * 32), args, smem, st);
 }
 
-static const void* hmc_kernel(const KParams& p) {
-    if (p.max_instr <= 130)
-        return p.rng_mode ? (const void*)mh_hmc_kernel<GPR_HMC_K, 130, 1> : (const void*)mh_hmc_kernel<GPR_HMC_K, 130, 0>;
-    return p.rng_mode ? (const void*)mh_hmc_kernel<GPR_HMC_K, 258, 1> : (const void*)mh_hmc_kernel<GPR_HMC_K, 258, 0>;
+template <int MAXI, int RNG>
+static const void* hmc_kernel_t(int stream) {
+    return stream ? (const void*)mh_hmc_kernel<GPR_HMC_K, MAXI, RNG, true>
+                  : (const void*)mh_hmc_kernel<GPR_HMC_K, MAXI, RNG, false>;
+}
+
+static const void* hmc_kernel(const KParams& p, int stream) {
+    if (p.max_instr <= 130) return p.rng_mode ? hmc_kernel_t<130, 1>(stream) : hmc_kernel_t<130, 0>(stream);
+    return p.rng_mode ? hmc_kernel_t<258, 1>(stream) : hmc_kernel_t<258, 0>(stream);
 }
 
 /* The shared-memory share of the L1/shared array: the rest is L1, where the
@@ -42,9 +54,10 @@ static cudaError_t set_carveout(const void* f, int carveout) {
                                 carveout > 0 ? carveout : -1);
 }
 
-cudaError_t hmc_occupancy(const KParams& p, int warps_per_cta, size_t smem, int carveout, int* ctas_per_sm) {
+cudaError_t hmc_occupancy(const KParams& p, int warps_per_cta, size_t smem, int carveout, int stream,
+                          int* ctas_per_sm) {
     if (!grad_supported(p)) return cudaErrorInvalidValue;
-    const void* f = hmc_kernel(p);
+    const void* f = hmc_kernel(p, stream);
     cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess) e = set_carveout(f, carveout);
     if (e != cudaSuccess) return e;
@@ -53,7 +66,7 @@ cudaError_t hmc_occupancy(const KParams& p, int warps_per_cta, size_t smem, int 
 
 cudaError_t launch_hmc_block(const KParams& p, const LaunchCfg& lc, cudaStream_t st) {
     if (!grad_supported(p)) return cudaErrorInvalidValue;
-    const void* f = hmc_kernel(p);
+    const void* f = hmc_kernel(p, lc.stream);
     cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lc.smem_bytes);
     if (e == cudaSuccess) e = set_carveout(f, lc.carveout);
     if (e != cudaSuccess) return e;

@@ -390,19 +390,30 @@ __device__ __forceinline__ float hmc_momentum(uint32_t seed, uint32_t chain, uin
 /* ------------------------------------------------------------------------ */
 /* d loglik / d C for every chain's current state (gpr_loglik_grad): one warp
  * per chain, grad[i*N + chain] (double, unscaled) and lik[chain]. */
-template <int K, int MAXI>
+/* The dataset: staged into this CTA's shared memory, or (STREAM) read from
+ * device memory.  Returns where the per-warp regions start. */
+template <bool STREAM>
+__device__ __forceinline__ uint8_t* grad_dataset(uint8_t* smem, const KParams& p, const float*& sx,
+                                                 const float*& sy, const float*& sw) {
+    if (STREAM) {
+        sx = p.dx; sy = p.dy; sw = p.dw;
+        return smem + 16;
+    }
+    float* fx = (float*)(smem + 16);
+    sx = fx; sy = fx + p.nd_pad; sw = fx + 2 * (size_t)p.nd_pad;
+    stage_dataset(fx, fx + p.nd_pad, fx + 2 * (size_t)p.nd_pad, (uint64_t*)smem, p);
+    return smem + 16 + align16((size_t)3 * p.nd_pad * 4);
+}
+
+template <int K, int MAXI, bool STREAM>
 __global__ void __launch_bounds__(128) loglik_grad_kernel(const __grid_constant__ KParams p, double* grad,
                                                           double* lik_out) {
     extern __shared__ __align__(128) uint8_t smem[];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    uint64_t* bar = (uint64_t*)smem;
-    float* sx = (float*)(smem + 16);
-    float* sy = sx + p.nd_pad;
-    float* sw = sy + p.nd_pad;
-    uint8_t* wbase = smem + 16 + align16((size_t)3 * p.nd_pad * 4);
+    const float *sx, *sy, *sw;
+    uint8_t* wbase = grad_dataset<STREAM>(smem, p, sx, sy, sw);
     const GradSmem ws = carve_grad(wbase + (size_t)warp * grad_warp_bytes(p.PL, p.max_instr), p.PL, p.max_instr);
-    stage_dataset(sx, sy, sw, bar, p);
     const int chain = blockIdx.x * (blockDim.x >> 5) + warp;
     if (chain >= p.N) return;
     const int PL = p.PL;
@@ -426,18 +437,14 @@ __global__ void __launch_bounds__(128) loglik_grad_kernel(const __grid_constant_
 /* The MH block with Hamiltonian constant moves.  One warp per chain, chains
  * claimed from the global counter; evaluation with the adjoint on K points
  * per lane. */
-template <int K, int MAXI, int RNG>
+template <int K, int MAXI, int RNG, bool STREAM>
 __global__ void __launch_bounds__(128) mh_hmc_kernel(const __grid_constant__ KParams p) {
     extern __shared__ __align__(128) uint8_t smem[];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    uint64_t* bar = (uint64_t*)smem;
-    float* sx = (float*)(smem + 16);
-    float* sy = sx + p.nd_pad;
-    float* sw = sy + p.nd_pad;
-    uint8_t* wbase = smem + 16 + align16((size_t)3 * p.nd_pad * 4);
+    const float *sx, *sy, *sw;
+    uint8_t* wbase = grad_dataset<STREAM>(smem, p, sx, sy, sw);
     const GradSmem ws = carve_grad(wbase + (size_t)warp * grad_warp_bytes(p.PL, p.max_instr), p.PL, p.max_instr);
-    stage_dataset(sx, sy, sw, bar, p);
     const int PL = p.PL;
     const bool adapt = p.chain_scale && p.adapt_target > 0.0f;
     const float unscale = (float)GPR_DF_UNSCALE;

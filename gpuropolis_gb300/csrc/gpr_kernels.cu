@@ -8,12 +8,13 @@
 namespace gpr {
 
 /* ------------------------------------------------------------------------ */
-size_t mh_smem_bytes(const KParams& p, int K, int warps_per_cta) {
-    return 16 + align16((size_t)3 * p.nd_pad * 4) +
+size_t mh_smem_bytes(const KParams& p, int K, int warps_per_cta, int stream) {
+    return 16 + (stream ? 0 : align16((size_t)3 * p.nd_pad * 4)) +
            (size_t)warps_per_cta * warp_smem_bytes(p.PL, p.max_instr, p.levels, K);
 }
 
-static const void* pick_kernel(int K, int onepass, int rng, int rolled) {
+static const void* pick_kernel(int K, int onepass, int rng, int rolled, int stream) {
+    if (stream) return (K == 4 && !onepass) ? mh_kernel_k4s(rng, rolled) : nullptr;
     if (K == 4) return onepass ? mh_kernel_k4(rng, rolled) : mh_kernel_k4m(rng, rolled);
     if (K == 8) return onepass ? mh_kernel_k8(rng, rolled) : mh_kernel_k8m(rng, rolled);
     return nullptr;
@@ -29,7 +30,7 @@ void fill_lcg_jump_table(KParams& p) {
 }
 
 cudaError_t mh_occupancy(const KParams& p, const LaunchCfg& lc, int* ctas_per_sm) {
-    const void* f = pick_kernel(lc.K, lc.onepass, p.rng_mode, lc.rolled);
+    const void* f = pick_kernel(lc.K, lc.onepass, p.rng_mode, lc.rolled, lc.stream);
     if (!f) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lc.smem_bytes);
     if (e != cudaSuccess) return e;
@@ -37,7 +38,7 @@ cudaError_t mh_occupancy(const KParams& p, const LaunchCfg& lc, int* ctas_per_sm
 }
 
 cudaError_t launch_mh_block(const KParams& p, const LaunchCfg& lc, cudaStream_t st) {
-    const void* f = pick_kernel(lc.K, lc.onepass, p.rng_mode, lc.rolled);
+    const void* f = pick_kernel(lc.K, lc.onepass, p.rng_mode, lc.rolled, lc.stream);
     if (!f) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lc.smem_bytes);
     if (e != cudaSuccess) return e;

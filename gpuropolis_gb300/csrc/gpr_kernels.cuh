@@ -93,6 +93,7 @@ const void* mh_kernel_k4(int rng, int rolled);
 const void* mh_kernel_k4m(int rng, int rolled);
 const void* mh_kernel_k8(int rng, int rolled);
 const void* mh_kernel_k8m(int rng, int rolled);
+const void* mh_kernel_k4s(int rng, int rolled);   /* dataset streamed from device memory */
 
 /* Launch geometry picked by the host (persistent grid). */
 struct LaunchCfg {
@@ -104,9 +105,10 @@ struct LaunchCfg {
     int ctas;
     size_t smem_bytes;
     int carveout;      /* shared-memory share of L1 in percent, 0 = the driver's choice */
+    int stream;        /* dataset read from device memory, not staged per CTA   */
 };
 
-size_t mh_smem_bytes(const KParams& p, int K, int warps_per_cta);
+size_t mh_smem_bytes(const KParams& p, int K, int warps_per_cta, int stream = 0);
 cudaError_t launch_mh_block(const KParams& p, const LaunchCfg& lc, cudaStream_t st);
 cudaError_t mh_occupancy(const KParams& p, const LaunchCfg& lc, int* ctas_per_sm);
 
@@ -120,10 +122,11 @@ cudaError_t launch_math(int op, const float* a, const float* b, float* out, int 
 /* Gradient of the log-likelihood and the MH kernel with Hamiltonian constant
  * moves (gpr_hmc.cu).  grad_smem_bytes: dynamic shared memory of either for
  * a CTA of warps_per_cta chains. */
-size_t grad_smem_bytes(const KParams& p, int warps_per_cta);
+size_t grad_smem_bytes(const KParams& p, int warps_per_cta, int stream = 0);
 bool grad_supported(const KParams& p);   /* PROGRAM_LENGTH <= 127 */
-cudaError_t launch_loglik_grad(const KParams& p, double* grad, double* lik, cudaStream_t st);
-cudaError_t hmc_occupancy(const KParams& p, int warps_per_cta, size_t smem, int carveout, int* ctas_per_sm);
+cudaError_t launch_loglik_grad(const KParams& p, double* grad, double* lik, int stream, cudaStream_t st);
+cudaError_t hmc_occupancy(const KParams& p, int warps_per_cta, size_t smem, int carveout, int stream,
+                          int* ctas_per_sm);
 cudaError_t launch_hmc_block(const KParams& p, const LaunchCfg& lc, cudaStream_t st);
 
 /* Selection over the chains' posteriors (gpr_resample.cu).  launch_select

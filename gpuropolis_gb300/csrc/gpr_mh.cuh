@@ -996,22 +996,32 @@ __device__ __forceinline__ void structure_move(Rng& r, const uint8_t* oc, uint8_
 #define GPR_MIN_CTAS 3
 #endif
 
-template <int K, bool ONEPASS, int RNG, bool ROLLED>
+/* STREAM: the dataset is read from device memory (L2-resident for a few MB)
+ * instead of being staged into each CTA's shared memory -- the layout for
+ * datasets too large to stage. */
+template <int K, bool ONEPASS, int RNG, bool ROLLED, bool STREAM>
 __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __grid_constant__ KParams p) {
     extern __shared__ __align__(128) uint8_t smem[];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
 
-    /* CTA-shared dataset */
+    /* CTA-shared dataset (or the device copy when streamed) */
     uint64_t* bar = (uint64_t*)smem;
-    float* sx = (float*)(smem + 16);
-    float* sy = sx + p.nd_pad;
-    float* sw = sy + p.nd_pad;
-    uint8_t* wbase = smem + 16 + align16((size_t)3 * p.nd_pad * 4);
+    const float* sx;
+    const float* sy;
+    const float* sw;
+    uint8_t* wbase;
+    if (STREAM) {
+        sx = p.dx; sy = p.dy; sw = p.dw;
+        wbase = smem + 16;
+    } else {
+        float* fx = (float*)(smem + 16);
+        sx = fx; sy = fx + p.nd_pad; sw = fx + 2 * (size_t)p.nd_pad;
+        wbase = smem + 16 + align16((size_t)3 * p.nd_pad * 4);
+        stage_dataset(fx, fx + p.nd_pad, fx + 2 * (size_t)p.nd_pad, bar, p);
+    }
     const size_t wbytes = warp_smem_bytes(p.PL, p.max_instr, p.levels, K);
     const WarpSmem ws = carve_warp<K>(wbase + (size_t)warp * wbytes, p.PL, p.max_instr, p.levels);
-
-    stage_dataset(sx, sy, sw, bar, p);
 
     LaneData<K> ld;
     if (ONEPASS) {

@@ -1,0 +1,16 @@
+/* Instantiations of the MH block kernel that read the dataset from device
+ * memory instead of staging it (K = 4 points per lane, in passes): the layout
+ * for datasets too large for shared memory (a translation unit of its own so
+ * the kernels compile in parallel). */
+#include "gpr_mh.cuh"
+
+namespace gpr {
+template __global__ void mh_block_kernel<4, false, 0, false, true>(const __grid_constant__ KParams p);
+template __global__ void mh_block_kernel<4, false, 1, false, true>(const __grid_constant__ KParams p);
+template __global__ void mh_block_kernel<4, false, 0, true, true>(const __grid_constant__ KParams p);
+template __global__ void mh_block_kernel<4, false, 1, true, true>(const __grid_constant__ KParams p);
+const void* mh_kernel_k4s(int rng, int rolled) {
+    if (rolled) return rng ? (const void*)mh_block_kernel<4, false, 1, true, true> : (const void*)mh_block_kernel<4, false, 0, true, true>;
+    return rng ? (const void*)mh_block_kernel<4, false, 1, false, true> : (const void*)mh_block_kernel<4, false, 0, false, true>;
+}
+}  // namespace gpr

@@ -3,12 +3,12 @@
 #include "gpr_mh.cuh"
 
 namespace gpr {
-template __global__ void mh_block_kernel<8, true, 0, false>(const __grid_constant__ KParams p);
-template __global__ void mh_block_kernel<8, true, 1, false>(const __grid_constant__ KParams p);
-template __global__ void mh_block_kernel<8, true, 0, true>(const __grid_constant__ KParams p);
-template __global__ void mh_block_kernel<8, true, 1, true>(const __grid_constant__ KParams p);
+template __global__ void mh_block_kernel<8, true, 0, false, false>(const __grid_constant__ KParams p);
+template __global__ void mh_block_kernel<8, true, 1, false, false>(const __grid_constant__ KParams p);
+template __global__ void mh_block_kernel<8, true, 0, true, false>(const __grid_constant__ KParams p);
+template __global__ void mh_block_kernel<8, true, 1, true, false>(const __grid_constant__ KParams p);
 const void* mh_kernel_k8(int rng, int rolled) {
-    if (rolled) return rng ? (const void*)mh_block_kernel<8, true, 1, true> : (const void*)mh_block_kernel<8, true, 0, true>;
-    return rng ? (const void*)mh_block_kernel<8, true, 1, false> : (const void*)mh_block_kernel<8, true, 0, false>;
+    if (rolled) return rng ? (const void*)mh_block_kernel<8, true, 1, true, false> : (const void*)mh_block_kernel<8, true, 0, true, false>;
+    return rng ? (const void*)mh_block_kernel<8, true, 1, false, false> : (const void*)mh_block_kernel<8, true, 0, false, false>;
 }
 }  // namespace gpr

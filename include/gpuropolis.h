@@ -146,6 +146,14 @@ int gpr_autotune(gpr_handle* h, int steps, int seed, int* K, int* onepass, int* 
 int gpr_set_layout(gpr_handle* h, int K, int onepass, int rolled);
 int gpr_set_layout2(gpr_handle* h, int K, int onepass, int rolled, int lockstep, int warps_per_cta);
 
+/* Read the dataset from device memory in every pass (always = 1) instead of
+ * staging it into each CTA's shared memory; 0 (default) streams only when
+ * staging does not fit, as for datasets of tens of thousands of points.
+ * Results are identical either way.  gpr_layout_streamed reports the mode
+ * of the current layout. */
+int gpr_set_streaming(gpr_handle* h, int always);
+int gpr_layout_streamed(gpr_handle* h);
+
 /* Layout of a GPR_CONST_HMC handle's kernel: warps (chains) per CTA (1, 2 or
  * 4) and at most ctas_per_sm resident CTAs per SM (0: as many as fit).
  * Fewer CTAs leave more of each SM's L1 to the gradient tapes; gpr_autotune
