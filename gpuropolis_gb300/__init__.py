@@ -19,8 +19,9 @@ CLI_PATH = os.path.join(_HERE, "_lib", "gpuropolis")
 # op codes, reference numbering (main.cu:53)
 (ONE, CONST, INV, A, B, PLUS, MINUS, RMINUS, CPLUS, TIMES, CTIMES, DIV, RDIV, LOG, EXP, POW,
  CPOW, RPOW, CRPOW, SQRT, SIN, ASIN, COS, ACOS, TAN, ATAN, ABS) = range(27)
+X1, X2, X3 = 27, 28, 29          # input variables of multivariate data (no reference counterpart)
 NOPS_REFERENCE = 27
-PROGRAM_CODE = "1CIab+-_#*@/|LE^pVPRSsCcTtA"   # main.cu:55
+PROGRAM_CODE = "1CIab+-_#*@/|LE^pVPRSsCcTtAXYZ"   # main.cu:55, then the variable leaves
 
 OPSET_REFERENCE = list(range(27))
 # {+, -, *, /, exp, log, pow, x, const}: x reached through the A/B pass-throughs
@@ -45,7 +46,7 @@ class Config(ctypes.Structure):
                 ("ops", ctypes.c_int * 32), ("rng", ctypes.c_int),
                 ("const_proposal", ctypes.c_int), ("rw_sd", ctypes.c_float),
                 ("device", ctypes.c_int), ("stream", ctypes.c_void_p),
-                ("reserved", ctypes.c_int * 8)]
+                ("n_vars", ctypes.c_int), ("reserved", ctypes.c_int * 7)]
 
 
 _lib = None
@@ -67,6 +68,7 @@ def library():
     lib.gpr_create.argtypes = [P(Config), ip, P(vp)]
     lib.gpr_destroy.argtypes = [vp]
     lib.gpr_set_data.argtypes = [vp, vp, vp, vp, ip]
+    lib.gpr_set_data3.argtypes = [vp, vp, vp, vp, vp, vp, ip]
     lib.gpr_set_state.argtypes = [vp, vp, vp]
     lib.gpr_get_state.argtypes = [vp, vp, vp, vp, vp]
     lib.gpr_run_block.argtypes = [vp, ip, ip]
@@ -132,7 +134,7 @@ def _ptr(a):
 
 
 def make_config(program_length=31, ops=None, rng=RNG_LCG, const_proposal=CONST_REFERENCE,
-                rw_sd=0.1, device=0, stream=None):
+                rw_sd=0.1, device=0, stream=None, n_vars=1):
     lib = library()
     cfg = Config()
     lib.gpr_default_config(ctypes.byref(cfg))
@@ -146,6 +148,7 @@ def make_config(program_length=31, ops=None, rng=RNG_LCG, const_proposal=CONST_R
     cfg.rw_sd = rw_sd
     cfg.device = device
     cfg.stream = stream
+    cfg.n_vars = n_vars
     return cfg
 
 
@@ -184,6 +187,10 @@ class Sampler:
         sd = np.ascontiguousarray(sd, np.float32)
         self._check(self.lib.gpr_set_data(self.h, _ptr(x), _ptr(y), _ptr(sd), len(x)))
 
+    def set_data3(self, x1, x2, x3, y, sd):
+        a = [np.ascontiguousarray(v, np.float32) for v in (x1, x2, x3, y, sd)]
+        self._check(self.lib.gpr_set_data3(self.h, *[_ptr(v) for v in a], len(a[0])))
+
     def set_state(self, P, C):
         P = np.ascontiguousarray(P, np.int32).reshape(self.PL, self.N)
         C = np.ascontiguousarray(C, np.float32).reshape(self.PL, self.N)
@@ -209,11 +216,13 @@ class Sampler:
         self._check(self.lib.gpr_sync(self.h))
 
     def eval_values(self, xs):
+        """Program values at points xs: shape (nx,), or (3, nx) for three variables."""
         xs = np.ascontiguousarray(xs, np.float32)
-        out = np.empty((self.N, len(xs)), np.float32)
+        nx = xs.shape[-1]
+        out = np.empty((self.N, nx), np.float32)
         length = np.empty(self.N, np.float32)
         count = np.empty(self.N, np.int32)
-        self._check(self.lib.gpr_debug_eval_values(self.h, _ptr(xs), len(xs), _ptr(out),
+        self._check(self.lib.gpr_debug_eval_values(self.h, _ptr(xs), nx, _ptr(out),
                                                    _ptr(length), _ptr(count)))
         return out, length, count
 

@@ -106,6 +106,7 @@ void gpr_default_config(gpr_config* cfg) {
     cfg->rng = GPR_RNG_LCG;
     cfg->const_proposal = GPR_CONST_REFERENCE;
     cfg->rw_sd = 0.1f;
+    cfg->n_vars = 1;
     cfg->device = 0;
     cfg->stream = nullptr;
 }
@@ -134,9 +135,15 @@ int gpr_create(const gpr_config* cfg, int n_chains, gpr_handle** out) {
                     GPR_MAX_PROGRAM_LENGTH, PL);
     if (cfg->n_ops < 1 || cfg->n_ops > GPR_MAX_OPS)
         return fail(nullptr, GPR_ERR_ARG, "n_ops must be in [1, %d] (got %d)", GPR_MAX_OPS, cfg->n_ops);
-    for (int i = 0; i < cfg->n_ops; ++i)
-        if (cfg->ops[i] < 0 || cfg->ops[i] >= OP_NREF)
-            return fail(nullptr, GPR_ERR_ARG, "ops[%d] = %d is not an op code", i, cfg->ops[i]);
+    const int nv = cfg->n_vars == 0 ? 1 : cfg->n_vars;
+    if (nv != 1 && nv != 3) return fail(nullptr, GPR_ERR_ARG, "n_vars must be 1 or 3 (got %d)", cfg->n_vars);
+    for (int i = 0; i < cfg->n_ops; ++i) {
+        const int o = cfg->ops[i];
+        if (o < 0 || o >= OP_NALL)
+            return fail(nullptr, GPR_ERR_ARG, "ops[%d] = %d is not an op code", i, o);
+        if ((o == OP_X2 || o == OP_X3) && nv != 3)
+            return fail(nullptr, GPR_ERR_ARG, "ops[%d] = %d reads x2/x3, which needs n_vars = 3", i, o);
+    }
     if (cfg->rng != GPR_RNG_LCG && cfg->rng != GPR_RNG_PHILOX)
         return fail(nullptr, GPR_ERR_ARG, "unknown rng mode %d", cfg->rng);
     if (cfg->const_proposal != GPR_CONST_REFERENCE && cfg->const_proposal != GPR_CONST_RANDOM_WALK &&
@@ -199,6 +206,7 @@ int gpr_create(const gpr_config* cfg, int n_chains, gpr_handle** out) {
     memset(&kp, 0, sizeof kp);
     kp.P = h->dP; kp.C = h->dC; kp.prior = h->dprior; kp.lik = h->dlik;
     kp.N = n_chains; kp.PL = PL;
+    kp.nv = nv;
     kp.rng_mode = cfg->rng;
     kp.const_mode = cfg->const_proposal;
     kp.rw_sd = cfg->rw_sd;
@@ -334,15 +342,24 @@ static int choose_launch(gpr_handle* h) {
     return configure_launch(h, 4, h->kp.nd <= 128 ? 1 : 0, 0, 1, 8);
 }
 
-int gpr_set_data(gpr_handle* h, const float* x, const float* y, const float* sd, int n) {
-    if (!h) return GPR_ERR_ARG;
+/* Device layout of a dataset: x1 | y | w | sd | x2 | x3, nd_pad floats each
+ * (x2, x3 only for three input variables). */
+static int set_data_impl(gpr_handle* h, const float* x, const float* x2, const float* x3, const float* y,
+                         const float* sd, int n) {
     if (n < 0) return fail(h, GPR_ERR_ARG, "n must be >= 0");
     if (n > 0 && (!x || !y || !sd)) return fail(h, GPR_ERR_ARG, "x, y, sd must be non-NULL");
+    const bool three = h->kp.nv == 3;
+    if (n > 0 && three && (!x2 || !x3)) return fail(h, GPR_ERR_ARG, "x2, x3 must be non-NULL");
     for (int i = 0; i < n; ++i)
         if (!(sd[i] > 0.0f)) return fail(h, GPR_ERR_ARG, "sd[%d] = %g is not > 0", i, (double)sd[i]);
     CUDA_TRY(h, cudaSetDevice(h->device));
     const int nd_pad = (n + 3) & ~3;
-    std::vector<float> host((size_t)4 * nd_pad, 0.0f);
+    std::vector<float> host((size_t)(three ? 6 : 4) * nd_pad, 0.0f);
+    if (three)
+        for (int i = 0; i < n; ++i) {
+            host[4 * (size_t)nd_pad + i] = x2[i];
+            host[5 * (size_t)nd_pad + i] = x3[i];
+        }
     double normsum = 0.0;
     const double PIf = 3.141592653589;
     for (int i = 0; i < n; ++i) {
@@ -374,16 +391,34 @@ int gpr_set_data(gpr_handle* h, const float* x, const float* y, const float* sd,
     kp.dx = h->ddata;
     kp.dy = h->ddata ? h->ddata + nd_pad : nullptr;
     kp.dw = h->ddata ? h->ddata + 2 * (size_t)nd_pad : nullptr;
+    kp.dx2 = (h->ddata && three) ? h->ddata + 4 * (size_t)nd_pad : nullptr;
+    kp.dx3 = (h->ddata && three) ? h->ddata + 5 * (size_t)nd_pad : nullptr;
     return choose_launch(h);
+}
+
+int gpr_set_data(gpr_handle* h, const float* x, const float* y, const float* sd, int n) {
+    if (!h) return GPR_ERR_ARG;
+    if (h->kp.nv == 3) return fail(h, GPR_ERR_ARG, "a handle with three input variables takes gpr_set_data3");
+    return set_data_impl(h, x, nullptr, nullptr, y, sd, n);
+}
+
+int gpr_set_data3(gpr_handle* h, const float* x1, const float* x2, const float* x3, const float* y,
+                  const float* sd, int n) {
+    if (!h) return GPR_ERR_ARG;
+    if (h->kp.nv != 3) return fail(h, GPR_ERR_ARG, "gpr_set_data3 needs a handle created with n_vars = 3");
+    return set_data_impl(h, x1, x2, x3, y, sd, n);
 }
 
 int gpr_set_state(gpr_handle* h, const int32_t* P, const float* C) {
     if (!h) return GPR_ERR_ARG;
     if (!P || !C) return fail(h, GPR_ERR_ARG, "P and C must be non-NULL");
     const size_t cnt = (size_t)h->N * h->PL;
-    for (size_t i = 0; i < cnt; ++i)
-        if (P[i] < 0 || P[i] >= OP_NREF)
+    for (size_t i = 0; i < cnt; ++i) {
+        if (P[i] < 0 || P[i] >= OP_NALL)
             return fail(h, GPR_ERR_ARG, "P[%zu] = %d is not an op code", i, P[i]);
+        if ((P[i] == OP_X2 || P[i] == OP_X3) && h->kp.nv != 3)
+            return fail(h, GPR_ERR_ARG, "P[%zu] = %d reads x2/x3, which needs n_vars = 3", i, P[i]);
+    }
     CUDA_TRY(h, cudaSetDevice(h->device));
     CUDA_TRY(h, cudaMemcpyAsync(h->dP, P, cnt * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
     CUDA_TRY(h, cudaMemcpyAsync(h->dC, C, cnt * sizeof(float), cudaMemcpyHostToDevice, h->stream));
@@ -468,13 +503,14 @@ int gpr_debug_eval_values(gpr_handle* h, const float* xs, int nx, float* out, fl
     float *dxs = nullptr, *dout = nullptr, *dlen = nullptr;
     int* dcnt = nullptr;
     const size_t no = (size_t)h->N * (size_t)nx;
+    const size_t nvx = h->kp.nv == 3 ? 3 : 1;   /* xs holds x1 | x2 | x3 for three variables */
     int rc = GPR_OK;
     cudaError_t e = cudaSuccess;
-    if ((e = cudaMalloc(&dxs, (nx + 1) * sizeof(float))) != cudaSuccess) goto done;
+    if ((e = cudaMalloc(&dxs, (nvx * (size_t)nx + 1) * sizeof(float))) != cudaSuccess) goto done;
     if ((e = cudaMalloc(&dout, (no + 1) * sizeof(float))) != cudaSuccess) goto done;
     if ((e = cudaMalloc(&dlen, h->N * sizeof(float))) != cudaSuccess) goto done;
     if ((e = cudaMalloc(&dcnt, h->N * sizeof(int))) != cudaSuccess) goto done;
-    if (nx > 0 && (e = cudaMemcpyAsync(dxs, xs, nx * sizeof(float), cudaMemcpyHostToDevice, h->stream)) != cudaSuccess) goto done;
+    if (nx > 0 && (e = cudaMemcpyAsync(dxs, xs, nvx * (size_t)nx * sizeof(float), cudaMemcpyHostToDevice, h->stream)) != cudaSuccess) goto done;
     if ((e = gpr::launch_eval_values(h->kp, dxs, nx, dout, dlen, dcnt, h->stream)) != cudaSuccess) goto done;
     h->launches++;
     if (nx > 0 && (e = cudaMemcpyAsync(out, dout, no * sizeof(float), cudaMemcpyDeviceToHost, h->stream)) != cudaSuccess) goto done;

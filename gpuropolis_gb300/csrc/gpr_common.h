@@ -17,11 +17,17 @@ enum gpr_op {
     OP_ONE = 0, OP_CONST, OP_INV, OP_A, OP_B, OP_PLUS, OP_MINUS, OP_RMINUS, OP_CPLUS,
     OP_TIMES, OP_CTIMES, OP_DIV, OP_RDIV, OP_LOG, OP_EXP, OP_POW, OP_CPOW, OP_RPOW,
     OP_CRPOW, OP_SQRT, OP_SIN, OP_ASIN, OP_COS, OP_ACOS, OP_TAN, OP_ATAN, OP_ABS,
-    OP_NREF /* 27 = NOPS of the reference's default op set */
+    OP_NREF, /* 27 = NOPS of the reference's default op set */
+    /* leaves of multivariate data (no reference counterpart): the input
+     * variables x1, x2, x3.  A child beyond the heap is x1, as the
+     * reference's x (main.cu:374-385). */
+    OP_X1 = OP_NREF, OP_X2, OP_X3,
+    OP_NALL
 };
 
-/* PROGRAM_CODE, main.cu:55: one character per op, used in samples.txt. */
-#define GPR_PROGRAM_CODE "1CIab+-_#*@/|LE^pVPRSsCcTtA"
+/* PROGRAM_CODE, main.cu:55: one character per op, used in samples.txt; the
+ * variable leaves x1, x2, x3 print as X, Y, Z. */
+#define GPR_PROGRAM_CODE "1CIab+-_#*@/|LE^pVPRSsCcTtAXYZ"
 
 enum gpr_opclass {
     CLS_LEAF0 = 0,   /* ONE, CONST: no children                                  */
@@ -41,7 +47,7 @@ enum gpr_opclass {
 
 GPR_HDI int gpr_op_class(int o) {
     switch (o) {
-        case OP_ONE: case OP_CONST: return CLS_LEAF0;
+        case OP_ONE: case OP_CONST: case OP_X1: case OP_X2: case OP_X3: return CLS_LEAF0;
         case OP_A: return CLS_PASS_A;
         case OP_B: return CLS_PASS_B;
         case OP_INV: case OP_LOG: case OP_EXP: case OP_SQRT: case OP_SIN: case OP_ASIN:
@@ -56,19 +62,23 @@ GPR_HDI int gpr_op_class(int o) {
 /* ---- compiled program: a reachable-only postfix form of the heap tree ----
  * One 32-bit word per instruction: bits 0-7 code, bits 8-15 heap node (the
  * constant C[node] an instruction reads).  The evaluator keeps the running
- * value in an accumulator; leaf operands (x, 1, a constant) are folded into
+ * value in an accumulator; leaf operands (x1..x3, 1, a constant) are folded into
  * the instruction that consumes them, so the value stack is touched only
  * where both children of a binary node are subtrees. */
 enum gpr_icode {
     I_END = 0,
-    I_LDX = 1, I_LDC = 2, I_LD1 = 3, I_PUSH = 4, I_LDNAN = 5,
+    I_LDX = 1, I_LDC = 2, I_LD1 = 3, I_PUSH = 4, I_LDNAN = 5, I_LDX2 = 6, I_LDX3 = 7,
     U_INV = 8, U_LOG, U_EXP, U_SQRT, U_SIN, U_ASIN, U_COS, U_ACOS, U_TAN, U_ATAN, U_ABS,
-    I_BIN0 = 32   /* 32 + bop*8 + accleft*4 + src */
+    I_BIN0 = 32   /* 32 + bop*16 + accleft*8 + src (3 bits) */
 };
 enum gpr_bop { BOP_ADD = 0, BOP_SUB = 1, BOP_MUL = 2, BOP_DIV = 3, BOP_POW = 4 };
-enum gpr_src { SRC_X = 0, SRC_C = 1, SRC_ONE = 2, SRC_POP = 3 };
+enum gpr_src { SRC_X = 0, SRC_C = 1, SRC_ONE = 2, SRC_POP = 3, SRC_X2 = 4, SRC_X3 = 5 };
 
-#define GPR_BIN(bop, accleft, src) (I_BIN0 + (bop) * 8 + (accleft) * 4 + (src))
+#define GPR_BIN(bop, accleft, src) (I_BIN0 + (bop) * 16 + (accleft) * 8 + (src))
+/* fields of a binary instruction code */
+#define GPR_BIN_BOP(code) (((code) - I_BIN0) >> 4)
+#define GPR_BIN_ACCLEFT(code) (((code) >> 3) & 1u)
+#define GPR_BIN_SRC(code) ((code) & 7u)
 
 /* Counters the MH kernel accumulates (gpr_get_stats). */
 enum gpr_stat {

@@ -33,6 +33,7 @@
 
 namespace gpr {
 
+#define GPR_HMC_K 4          /* points per lane of the adjoint and Hamiltonian kernels */
 #define GPR_GACC_STRIDE 33   /* per-constant gradient rows, padded against bank conflicts */
 #define GPR_ASTK_MAX 8       /* adjoint-stack rows: value-stack depth for PROGRAM_LENGTH <= 255 */
 
@@ -103,7 +104,7 @@ __device__ __forceinline__ void pop_match(const uint32_t* prog, int ninstr, int1
             if (code == I_PUSH) {
                 if (sp < 32) st[sp] = (int16_t)i;
                 ++sp;
-            } else if (code >= I_BIN0 && (code & 3u) == SRC_POP) {
+            } else if (code >= I_BIN0 && GPR_BIN_SRC(code) == SRC_POP) {
                 --sp;
                 match[i] = (sp >= 0 && sp < 32) ? st[sp] : (int16_t)0;
             }
@@ -114,12 +115,16 @@ __device__ __forceinline__ void pop_match(const uint32_t* prog, int ninstr, int1
 
 /* Value of an operand for instruction i: x, the constant, 1 or the popped
  * value (the tape entry of the matching PUSH). */
-template <int K>
-__device__ __forceinline__ void operand(uint32_t src, float c, int i, const int16_t* match, const float (&x)[K],
-                                        const Row<K>* tape, float (&v)[K]) {
+template <int K, int NV>
+__device__ __forceinline__ void operand(uint32_t src, float c, int i, const int16_t* match,
+                                        const float (&x)[NV][K], const Row<K>* tape, float (&v)[K]) {
     if (src == SRC_X) {
 #pragma unroll
-        for (int k = 0; k < K; ++k) v[k] = x[k];
+        for (int k = 0; k < K; ++k) v[k] = x[0][k];
+    } else if (NV > 1 && (src == SRC_X2 || src == SRC_X3)) {
+        const int vi = NV > 1 ? (int)(src - SRC_X2) + 1 : 0;
+#pragma unroll
+        for (int k = 0; k < K; ++k) v[k] = x[vi][k];
     } else if (src == SRC_C) {
 #pragma unroll
         for (int k = 0; k < K; ++k) v[k] = c;
@@ -135,9 +140,9 @@ __device__ __forceinline__ void operand(uint32_t src, float c, int i, const int1
 
 /* f(x) for this lane's K points, every instruction's result kept on the tape.
  * The arithmetic is the evaluator's (run_program), operation for operation. */
-template <int K>
+template <int K, int NV>
 __device__ __forceinline__ void forward_tape(const uint2* __restrict__ prog, int ninstr, const int16_t* match,
-                                             const float (&x)[K], Row<K>* __restrict__ tape) {
+                                             const float (&x)[NV][K], Row<K>* __restrict__ tape) {
     float acc[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) acc[k] = 0.0f;
@@ -147,10 +152,10 @@ __device__ __forceinline__ void forward_tape(const uint2* __restrict__ prog, int
         const uint32_t code = insw.x & 0xffu;
         const float c = __uint_as_float(insw.y);
         if (code >= I_BIN0) {
-            const uint32_t bop = (code - I_BIN0) >> 3;
-            const uint32_t accleft = (code >> 2) & 1u;
+            const uint32_t bop = GPR_BIN_BOP(code);
+            const uint32_t accleft = GPR_BIN_ACCLEFT(code);
             float v[K];
-            operand<K>(code & 3u, c, i, match, x, tape, v);
+            operand<K, NV>(GPR_BIN_SRC(code), c, i, match, x, tape, v);
 #pragma unroll
             for (int k = 0; k < K; ++k) {
                 const float u = accleft ? acc[k] : v[k];
@@ -167,8 +172,15 @@ __device__ __forceinline__ void forward_tape(const uint2* __restrict__ prog, int
             switch (code) {
                 case I_LDX:
 #pragma unroll
-                    for (int k = 0; k < K; ++k) acc[k] = x[k];
+                    for (int k = 0; k < K; ++k) acc[k] = x[0][k];
                     break;
+                case I_LDX2:
+                case I_LDX3: {
+                    const int vi = NV > 1 ? (code == I_LDX2 ? 1 : 2) : 0;
+#pragma unroll
+                    for (int k = 0; k < K; ++k) acc[k] = NV > 1 ? x[vi][k] : 0.0f;
+                    break;
+                }
                 case I_LDC:
 #pragma unroll
                     for (int k = 0; k < K; ++k) acc[k] = c;
@@ -218,9 +230,9 @@ __device__ __forceinline__ float adj_mul(float adj, float d) { return adj == 0.0
 
 /* The backward sweep: adj holds d loglik / d f per point on entry; the
  * per-constant shares are added to this lane's gradient rows. */
-template <int K>
+template <int K, int NV>
 __device__ __forceinline__ void backward_tape(const uint2* __restrict__ prog, int ninstr, const int16_t* match,
-                                              const float (&x)[K], const Row<K>* __restrict__ tape,
+                                              const float (&x)[NV][K], const Row<K>* __restrict__ tape,
                                               float (&adj)[K], Row<K>* __restrict__ astk, float* __restrict__ gacc,
                                               int PL, int lane) {
     int sp = 0;
@@ -231,11 +243,11 @@ __device__ __forceinline__ void backward_tape(const uint2* __restrict__ prog, in
         const uint32_t node = (insw.x >> 8) & 0xffu;
         const float c = __uint_as_float(insw.y);
         if (code >= I_BIN0) {
-            const uint32_t bop = (code - I_BIN0) >> 3;
-            const uint32_t accleft = (code >> 2) & 1u;
-            const uint32_t src = code & 3u;
+            const uint32_t bop = GPR_BIN_BOP(code);
+            const uint32_t accleft = GPR_BIN_ACCLEFT(code);
+            const uint32_t src = GPR_BIN_SRC(code);
             float v[K];
-            operand<K>(src, c, i, match, x, tape, v);
+            operand<K, NV>(src, c, i, match, x, tape, v);
             float share = 0.0f;
             /* the accumulator's input; the result only where a partial needs it */
             const Row<K> ain = tape[i - 1];
@@ -270,7 +282,7 @@ __device__ __forceinline__ void backward_tape(const uint2* __restrict__ prog, in
 #pragma unroll
             for (int k = 0; k < K; ++k) { share = __fadd_rn(share, adj[k]); adj[k] = 0.0f; }
             if ((int)node < PL) gacc[node * GPR_GACC_STRIDE + lane] += share;
-        } else if (code == I_LDX || code == I_LD1 || code == I_LDNAN) {
+        } else if (code == I_LDX || code == I_LD1 || code == I_LDNAN || code == I_LDX2 || code == I_LDX3) {
 #pragma unroll
             for (int k = 0; k < K; ++k) adj[k] = 0.0f;
         } else if (code == I_PUSH) {
@@ -308,10 +320,11 @@ __device__ __forceinline__ void backward_tape(const uint2* __restrict__ prog, in
  * g[i] = 2^-64 d loglik / d C[i] in FP32, at the bookkeeping scale like the
  * likelihood (0 for constants the program does not read).  The gradient is
  * meaningful only when the likelihood is finite. */
-template <int K, int MAXI>
-__device__ df eval_loglik_grad(const uint2* prog, int ninstr, const GradSmem& ws, const float* sx,
-                               const float* sy, const float* sw, const KParams& p, int lane, int& pts,
-                               float* g) {
+template <int K, int MAXI, int NV>
+__device__ df eval_loglik_grad(const uint2* prog, int ninstr, const GradSmem& ws, const DataView& dv,
+                               const KParams& p, int lane, int& pts, float* g) {
+    const float* sy = dv.y;
+    const float* sw = dv.w;
     const int PL = p.PL;
     Row<K> tape[MAXI];             /* thread-local: results of every instruction */
     Row<K> astk[GPR_ASTK_MAX];     /* adjoints of pushed values                  */
@@ -323,19 +336,11 @@ __device__ df eval_loglik_grad(const uint2* prog, int ninstr, const GradSmem& ws
     const int npass = (p.nd + 32 * K - 1) / (32 * K);
 #pragma unroll 1
     for (int pass = 0; pass < npass && !bad; ++pass) {
-        float x[K], adj[K];
-        uint32_t valid = 0u;
+        float x[NV][K], adj[K];
         const int base = pass * 32 * K + lane;
-#pragma unroll
-        for (int k = 0; k < K; ++k) {
-            const int i = base + 32 * k;
-            const bool v = i < p.nd;
-            x[k] = v ? sx[i] : 0.0f;
-            valid |= (v ? 1u : 0u) << k;
-        }
-        forward_tape<K>(prog, ninstr, ws.match, x, tape);
+        const uint32_t valid = load_points<K, NV>(dv, p, base, x);
+        forward_tape<K, NV>(prog, ninstr, ws.match, x, tape);
         pts += min(32 * K, p.nd - pass * 32 * K);
-#pragma unroll
         const Row<K> fres = tape[ninstr - 2];
 #pragma unroll
         for (int k = 0; k < K; ++k) {
@@ -351,7 +356,7 @@ __device__ df eval_loglik_grad(const uint2* prog, int ninstr, const GradSmem& ws
             }
         }
         bad = __any_sync(FULLMASK, bad);
-        if (!bad) backward_tape<K>(prog, ninstr, ws.match, x, tape, adj, astk, ws.gacc, PL, lane);
+        if (!bad) backward_tape<K, NV>(prog, ninstr, ws.match, x, tape, adj, astk, ws.gacc, PL, lane);
     }
     __syncwarp();
 #pragma unroll 1
@@ -393,33 +398,29 @@ __device__ __forceinline__ float hmc_momentum(uint32_t seed, uint32_t chain, uin
 /* The dataset: staged into this CTA's shared memory, or (STREAM) read from
  * device memory.  Returns where the per-warp regions start. */
 template <bool STREAM>
-__device__ __forceinline__ uint8_t* grad_dataset(uint8_t* smem, const KParams& p, const float*& sx,
-                                                 const float*& sy, const float*& sw) {
-    if (STREAM) {
-        sx = p.dx; sy = p.dy; sw = p.dw;
-        return smem + 16;
-    }
+__device__ __forceinline__ uint8_t* grad_dataset(uint8_t* smem, const KParams& p, DataView& dv) {
     float* fx = (float*)(smem + 16);
-    sx = fx; sy = fx + p.nd_pad; sw = fx + 2 * (size_t)p.nd_pad;
-    stage_dataset(fx, fx + p.nd_pad, fx + 2 * (size_t)p.nd_pad, (uint64_t*)smem, p);
-    return smem + 16 + align16((size_t)3 * p.nd_pad * 4);
+    dv = data_view(p, fx, STREAM);
+    if (STREAM) return smem + 16;
+    stage_dataset(fx, (uint64_t*)smem, p);
+    return smem + 16 + align16((size_t)data_arrays(p) * p.nd_pad * 4);
 }
 
-template <int K, int MAXI, bool STREAM>
+template <int K, int MAXI, bool STREAM, int NV>
 __global__ void __launch_bounds__(128) loglik_grad_kernel(const __grid_constant__ KParams p, double* grad,
                                                           double* lik_out) {
     extern __shared__ __align__(128) uint8_t smem[];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    const float *sx, *sy, *sw;
-    uint8_t* wbase = grad_dataset<STREAM>(smem, p, sx, sy, sw);
+    DataView dv;
+    uint8_t* wbase = grad_dataset<STREAM>(smem, p, dv);
     const GradSmem ws = carve_grad(wbase + (size_t)warp * grad_warp_bytes(p.PL, p.max_instr), p.PL, p.max_instr);
     const int chain = blockIdx.x * (blockDim.x >> 5) + warp;
     if (chain >= p.N) return;
     const int PL = p.PL;
     for (int i = lane; i < PL; i += 32) {
         const int o = p.P[(size_t)i * p.N + chain];
-        ws.ops[0][i] = (uint8_t)((o >= 0 && o < OP_NREF) ? o : 255);
+        ws.ops[0][i] = (uint8_t)((o >= 0 && o < OP_NALL) ? o : 255);
         ws.Cs[0][i] = p.C[(size_t)i * p.N + chain];
     }
     __syncwarp();
@@ -428,7 +429,7 @@ __global__ void __launch_bounds__(128) loglik_grad_kernel(const __grid_constant_
     build_eval_program(ws.prog[0], ws.Cs[0], co.ninstr, ws.eprog, lane);
     pop_match(ws.prog[0], co.ninstr, ws.match, lane);
     int pts = 0;
-    const df lik = eval_loglik_grad<K, MAXI>(ws.eprog, co.ninstr, ws, sx, sy, sw, p, lane, pts, ws.gnew);
+    const df lik = eval_loglik_grad<K, MAXI, NV>(ws.eprog, co.ninstr, ws, dv, p, lane, pts, ws.gnew);
     for (int i = lane; i < PL; i += 32) grad[(size_t)i * p.N + chain] = (double)ws.gnew[i] * GPR_DF_UNSCALE;
     if (lane == 0) lik_out[chain] = df_to_double_unscaled(lik);
 }
@@ -437,13 +438,13 @@ __global__ void __launch_bounds__(128) loglik_grad_kernel(const __grid_constant_
 /* The MH block with Hamiltonian constant moves.  One warp per chain, chains
  * claimed from the global counter; evaluation with the adjoint on K points
  * per lane. */
-template <int K, int MAXI, int RNG, bool STREAM>
+template <int K, int MAXI, int RNG, bool STREAM, int NV>
 __global__ void __launch_bounds__(128) mh_hmc_kernel(const __grid_constant__ KParams p) {
     extern __shared__ __align__(128) uint8_t smem[];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    const float *sx, *sy, *sw;
-    uint8_t* wbase = grad_dataset<STREAM>(smem, p, sx, sy, sw);
+    DataView dv;
+    uint8_t* wbase = grad_dataset<STREAM>(smem, p, dv);
     const GradSmem ws = carve_grad(wbase + (size_t)warp * grad_warp_bytes(p.PL, p.max_instr), p.PL, p.max_instr);
     const int PL = p.PL;
     const bool adapt = p.chain_scale && p.adapt_target > 0.0f;
@@ -458,7 +459,7 @@ __global__ void __launch_bounds__(128) mh_hmc_kernel(const __grid_constant__ KPa
 
         for (int i = lane; i < PL; i += 32) {
             const int o = p.P[(size_t)i * p.N + chain];
-            ws.ops[0][i] = (uint8_t)((o >= 0 && o < OP_NREF) ? o : 255);
+            ws.ops[0][i] = (uint8_t)((o >= 0 && o < OP_NALL) ? o : 255);
             ws.Cs[0][i] = p.C[(size_t)i * p.N + chain];
         }
         __syncwarp();
@@ -506,7 +507,7 @@ __global__ void __launch_bounds__(128) mh_hmc_kernel(const __grid_constant__ KPa
                 build_eval_program(ws.prog[pbuf], ws.Cs[ccur], co.ninstr, ws.eprog, lane);
                 pop_match(ws.prog[pbuf], co.ninstr, ws.match, lane);
                 int pe = 0;
-                const df lik = eval_loglik_grad<K, MAXI>(ws.eprog, co.ninstr, ws, sx, sy, sw, p, lane, pe, ws.gnew);
+                const df lik = eval_loglik_grad<K, MAXI, NV>(ws.eprog, co.ninstr, ws, dv, p, lane, pe, ws.gnew);
                 st_pts += (unsigned)pe;
                 const df prior = df_add(length_prior(co.length, p), cs);
                 const df post = df_add(prior, lik);
@@ -556,7 +557,7 @@ __global__ void __launch_bounds__(128) mh_hmc_kernel(const __grid_constant__ KPa
                         build_eval_program(ws.prog[cur], q, cur_ninstr, ws.eprog, lane);
                         __syncwarp();
                         int pe = 0;
-                        lik = eval_loglik_grad<K, MAXI>(ws.eprog, cur_ninstr, ws, sx, sy, sw, p, lane, pe, ws.gnew);
+                        lik = eval_loglik_grad<K, MAXI, NV>(ws.eprog, cur_ninstr, ws, dv, p, lane, pe, ws.gnew);
                         st_pts += (unsigned)pe;
                         st_evals++; st_nodes += (unsigned)cur_count;
                         st_np += (unsigned long long)(cur_count + 4) * (unsigned)pe;
@@ -629,6 +630,10 @@ __global__ void __launch_bounds__(128) mh_hmc_kernel(const __grid_constant__ KPa
         __syncwarp();
     }
 }
+
+/* The kernels for three input variables (gpr_hmc_v.cu). */
+const void* grad_kernel_v3(int maxi, int stream);
+const void* hmc_kernel_v3(const KParams& p, int stream);
 
 }  // namespace gpr
 

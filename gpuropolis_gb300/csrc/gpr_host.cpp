@@ -132,6 +132,9 @@ void display(const Tree& t, int j, const char* cfmt, bool latex, std::string& ou
             case OP_RPOW: S("("); B(); S("^"); A(); S(")"); break;
             case OP_CRPOW: S("("); Cc(); S("^"); A(); S(")"); break;
             case OP_ABS: S("abs("); A(); S(")"); break;
+            case OP_X1: S("x1"); break;
+            case OP_X2: S("x2"); break;
+            case OP_X3: S("x3"); break;
             default: S("NAN"); break;
         }
     } else {
@@ -163,6 +166,9 @@ void display(const Tree& t, int j, const char* cfmt, bool latex, std::string& ou
             case OP_RPOW: B(); S("^{"); A(); S("}"); break;
             case OP_CRPOW: Cc(); S("^{"); A(); S("}"); break;
             case OP_ABS: S("\\mid "); A(); S("\\mid "); break;
+            case OP_X1: S("x_1"); break;
+            case OP_X2: S("x_2"); break;
+            case OP_X3: S("x_3"); break;
             default: S("NAN"); break;
         }
     }
@@ -191,6 +197,7 @@ float degree_of(const Tree& t, int j) {
     auto mx = [](float a, float b) { return a > b ? a : b; };   /* the max macro, main.cu:186 */
     switch (o) {
         case OP_ONE: case OP_CONST: return 0.0f;
+        case OP_X1: case OP_X2: case OP_X3: return 1.0f;   /* total degree over the variables */
         case OP_A: return degree_of(t, 2 * j);
         case OP_B: return degree_of(t, 2 * j + 1);
         case OP_PLUS: case OP_MINUS: case OP_RMINUS:
@@ -233,7 +240,7 @@ void format_line(std::string& out, const int32_t* P, const float* C, const doubl
     static const char* code = GPR_PROGRAM_CODE;
     for (int i = 0; i < PL; ++i) {
         int o = P[(size_t)i * N + h];
-        out += (o >= 0 && o < OP_NREF) ? code[o] : '?';
+        out += (o >= 0 && o < OP_NALL) ? code[o] : '?';
     }
     out += "\"\t";
     if (show_constants) {

@@ -9,11 +9,12 @@ namespace gpr {
 
 /* ------------------------------------------------------------------------ */
 size_t mh_smem_bytes(const KParams& p, int K, int warps_per_cta, int stream) {
-    return 16 + (stream ? 0 : align16((size_t)3 * p.nd_pad * 4)) +
+    return 16 + (stream ? 0 : align16((size_t)data_arrays(p) * p.nd_pad * 4)) +
            (size_t)warps_per_cta * warp_smem_bytes(p.PL, p.max_instr, p.levels, K);
 }
 
-static const void* pick_kernel(int K, int onepass, int rng, int rolled, int stream) {
+static const void* pick_kernel(int K, int onepass, int rng, int rolled, int stream, int nv) {
+    if (nv == 3) return (K == 4 && !onepass) ? mh_kernel_k4v(rng, rolled, stream) : nullptr;
     if (stream) return (K == 4 && !onepass) ? mh_kernel_k4s(rng, rolled) : nullptr;
     if (K == 4) return onepass ? mh_kernel_k4(rng, rolled) : mh_kernel_k4m(rng, rolled);
     if (K == 8) return onepass ? mh_kernel_k8(rng, rolled) : mh_kernel_k8m(rng, rolled);
@@ -30,7 +31,7 @@ void fill_lcg_jump_table(KParams& p) {
 }
 
 cudaError_t mh_occupancy(const KParams& p, const LaunchCfg& lc, int* ctas_per_sm) {
-    const void* f = pick_kernel(lc.K, lc.onepass, p.rng_mode, lc.rolled, lc.stream);
+    const void* f = pick_kernel(lc.K, lc.onepass, p.rng_mode, lc.rolled, lc.stream, p.nv);
     if (!f) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lc.smem_bytes);
     if (e != cudaSuccess) return e;
@@ -38,7 +39,7 @@ cudaError_t mh_occupancy(const KParams& p, const LaunchCfg& lc, int* ctas_per_sm
 }
 
 cudaError_t launch_mh_block(const KParams& p, const LaunchCfg& lc, cudaStream_t st) {
-    const void* f = pick_kernel(lc.K, lc.onepass, p.rng_mode, lc.rolled, lc.stream);
+    const void* f = pick_kernel(lc.K, lc.onepass, p.rng_mode, lc.rolled, lc.stream, p.nv);
     if (!f) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lc.smem_bytes);
     if (e != cudaSuccess) return e;
@@ -62,7 +63,7 @@ __global__ void __launch_bounds__(128) eval_values_kernel(const __grid_constant_
     if (chain >= p.N) return;
     for (int i = lane; i < p.PL; i += 32) {
         int o = p.P[(size_t)i * p.N + chain];
-        ws.ops[0][i] = (uint8_t)((o >= 0 && o < OP_NREF) ? o : 255);
+        ws.ops[0][i] = (uint8_t)((o >= 0 && o < OP_NALL) ? o : 255);
         ws.Cs[0][i] = p.C[(size_t)i * p.N + chain];
     }
     __syncwarp();
@@ -75,10 +76,13 @@ __global__ void __launch_bounds__(128) eval_values_kernel(const __grid_constant_
     build_eval_program(ws.prog[0], ws.Cs[0], co.ninstr, ws.eprog, lane);
     __syncwarp();
     for (int b = 0; b < nx; b += 32) {
-        float x[1], acc[1];
+        float x[3][1], acc[1];
         int i = b + lane;
-        x[0] = i < nx ? xs[i] : 0.0f;
-        run_program<1, false>(ws.eprog, x, acc, ws.stk, ws.scr, lane);
+        const bool in = i < nx;
+        x[0][0] = in ? xs[i] : 0.0f;
+        x[1][0] = (in && p.nv == 3) ? xs[nx + i] : 0.0f;    /* multivariate: xs holds x1 | x2 | x3 */
+        x[2][0] = (in && p.nv == 3) ? xs[2 * nx + i] : 0.0f;
+        run_program<1, false, 3>(ws.eprog, x, acc, ws.stk, ws.scr, lane);
         if (i < nx) out[(size_t)chain * nx + i] = acc[0];
     }
 }

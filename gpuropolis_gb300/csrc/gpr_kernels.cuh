@@ -34,6 +34,9 @@ struct KParams {
     const float* dx;
     const float* dy;
     const float* dw;   /* 2^-64 / (2 sd^2) as float: weights at the bookkeeping scale */
+    const float* dx2;  /* multivariate data: the second and third input variables */
+    const float* dx3;
+    int nv;            /* input variables: 1, or 3 for x1, x2, x3 (0 reads as 1) */
     int nd;
     int nd_pad;        /* multiple of 4                                       */
     float normsum_hi, normsum_lo;  /* 2^-64 * sum_d 0.5*(logf(2 PIf) + 2 logf(sd_d)), double-float */
@@ -94,6 +97,7 @@ const void* mh_kernel_k4m(int rng, int rolled);
 const void* mh_kernel_k8(int rng, int rolled);
 const void* mh_kernel_k8m(int rng, int rolled);
 const void* mh_kernel_k4s(int rng, int rolled);   /* dataset streamed from device memory */
+const void* mh_kernel_k4v(int rng, int rolled, int stream);   /* three input variables */
 
 /* Launch geometry picked by the host (persistent grid). */
 struct LaunchCfg {

@@ -219,22 +219,30 @@ __device__ __forceinline__ int binary_bop(int o, int& swapped) {
  * The per-node scratch (resolved node, instruction count, length, count,
  * start) lives in the warp's shared region, free between proposal and
  * evaluation.  Resolved codes: j > 0 a subtree rooted at node j (1-based),
- * PL_X / PL_ONE / PL_NAN leaves, PL_C0 - i the constant of node i. */
+ * PL_X (x1 beyond the heap) / PL_ONE / PL_NAN / PL_X1N (an x1 node) / PL_X2 /
+ * PL_X3 leaves, PL_C0 - i the constant of node i. */
 #define PL_X 0
 #define PL_ONE (-1)
 #define PL_NAN (-2)
-#define PL_C0 (-3)
+#define PL_X1N (-3)
+#define PL_X2 (-4)
+#define PL_X3 (-5)
+#define PL_C0 (-6)
 
 __device__ __forceinline__ uint32_t pl_load_instr(int r) {
-    if (r == PL_X) return I_LDX;
+    if (r == PL_X || r == PL_X1N) return I_LDX;
     if (r == PL_ONE) return I_LD1;
     if (r == PL_NAN) return I_LDNAN;
+    if (r == PL_X2) return I_LDX2;
+    if (r == PL_X3) return I_LDX3;
     return I_LDC | ((uint32_t)(PL_C0 - r) << 8);
 }
 __device__ __forceinline__ uint32_t pl_bin_instr(int bop, int accleft, int r, bool pop) {
     if (pop) return GPR_BIN(bop, accleft, SRC_POP);
-    if (r == PL_X) return GPR_BIN(bop, accleft, SRC_X);
+    if (r == PL_X || r == PL_X1N) return GPR_BIN(bop, accleft, SRC_X);
     if (r == PL_ONE) return GPR_BIN(bop, accleft, SRC_ONE);
+    if (r == PL_X2) return GPR_BIN(bop, accleft, SRC_X2);
+    if (r == PL_X3) return GPR_BIN(bop, accleft, SRC_X3);
     if (r == PL_NAN) return GPR_BIN(bop, accleft, SRC_C) | (255u << 8);
     return GPR_BIN(bop, accleft, SRC_C) | ((uint32_t)(PL_C0 - r) << 8);
 }
@@ -281,6 +289,9 @@ static __device__ CompileOut compile_parallel(const uint8_t* ops, int PL, uint32
             else if (cls == CLS_PASS_B) r = child_res(cs, PL, 2 * j + 1);
             else if (o == OP_ONE) r = PL_ONE;
             else if (o == OP_CONST) r = PL_C0 - (j - 1);
+            else if (o == OP_X1) r = PL_X1N;
+            else if (o == OP_X2) r = PL_X2;
+            else if (o == OP_X3) r = PL_X3;
             else if (cls == CLS_INVALID) r = PL_NAN;
             cs.res[j] = r;
             cs.start[j] = -1;
@@ -444,9 +455,9 @@ __device__ __forceinline__ void heavy_staged(float (&acc)[K], const float (&w)[K
  * code, one value at a time); otherwise they are unrolled over K in registers
  * (more code, full ILP).  Which is faster depends on how much of the kernel
  * the instruction cache holds; gpr_autotune measures it. */
-template <int K, bool ROLLED>
+template <int K, bool ROLLED, int NV>
 __device__ __forceinline__ void run_program(const uint2* __restrict__ prog,
-                                            const float (&x)[K], float (&acc)[K],
+                                            const float (&x)[NV][K], float (&acc)[K],
                                             float* __restrict__ stk, float* __restrict__ scr,
                                             int lane) {
     int sp = 0;
@@ -461,19 +472,23 @@ __device__ __forceinline__ void run_program(const uint2* __restrict__ prog,
         ++pc;
         const float c = __uint_as_float(insw.y);
         if (code >= I_BIN0) {
-            const uint32_t bop = (code - I_BIN0) >> 3;
-            const uint32_t accleft = (code >> 2) & 1u;
-            const uint32_t src = code & 3u;
+            const uint32_t bop = GPR_BIN_BOP(code);
+            const uint32_t accleft = GPR_BIN_ACCLEFT(code);
+            const uint32_t src = GPR_BIN_SRC(code);
             float v[K];
             if (src == SRC_X) {
 #pragma unroll
-                for (int k = 0; k < K; ++k) v[k] = x[k];
+                for (int k = 0; k < K; ++k) v[k] = x[0][k];
             } else if (src == SRC_C) {
 #pragma unroll
                 for (int k = 0; k < K; ++k) v[k] = c;
             } else if (src == SRC_ONE) {
 #pragma unroll
                 for (int k = 0; k < K; ++k) v[k] = 1.0f;
+            } else if (NV > 1 && src != SRC_POP) {
+                const int vi = NV > 1 ? (int)(src - SRC_X2) + 1 : 0;
+#pragma unroll
+                for (int k = 0; k < K; ++k) v[k] = x[vi][k];
             } else {
                 --sp;
 #pragma unroll
@@ -514,8 +529,15 @@ __device__ __forceinline__ void run_program(const uint2* __restrict__ prog,
         switch (code) {
             case I_LDX:
 #pragma unroll
-                for (int k = 0; k < K; ++k) acc[k] = x[k];
+                for (int k = 0; k < K; ++k) acc[k] = x[0][k];
                 break;
+            case I_LDX2:
+            case I_LDX3: {
+                const int vi = NV > 1 ? (code == I_LDX2 ? 1 : 2) : 0;
+#pragma unroll
+                for (int k = 0; k < K; ++k) acc[k] = NV > 1 ? x[vi][k] : 0.0f;
+                break;
+            }
             case I_LDC:
 #pragma unroll
                 for (int k = 0; k < K; ++k) acc[k] = c;
@@ -631,6 +653,31 @@ __device__ __forceinline__ WarpSmem carve_warp(uint8_t* base, int PL, int max_in
     return w;
 }
 
+/* The dataset as the evaluators read it: the CTA's shared-memory copy, or the
+ * device arrays when streamed.  x[1], x[2] only for multivariate data. */
+struct DataView {
+    const float* x[3];
+    const float* y;
+    const float* w;
+};
+
+/* This lane's K points of one pass: the NV input variables, and which points
+ * exist (bit k). */
+template <int K, int NV>
+__device__ __forceinline__ uint32_t load_points(const DataView& dv, const KParams& p, int base,
+                                                float (&x)[NV][K]) {
+    uint32_t valid = 0u;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const int i = base + 32 * k;
+        const bool v = i < p.nd;
+#pragma unroll
+        for (int j = 0; j < NV; ++j) x[j][k] = v ? dv.x[j][i] : 0.0f;
+        valid |= (v ? 1u : 0u) << k;
+    }
+    return valid;
+}
+
 /* Per-lane data of the single-pass layout (nd <= 32*K). */
 template <int K>
 struct LaneData {
@@ -642,29 +689,23 @@ struct LaneData {
  * of (f - y)^2 * w over its points, and whether any of its points is
  * invalid.  Used by the CTA-balanced evaluation, where any warp of the CTA may
  * evaluate any chain's pass. */
-template <int K, bool ONEPASS, bool ROLLED>
+template <int K, bool ONEPASS, bool ROLLED, int NV>
 __device__ __forceinline__ float eval_pass(const uint2* prog, float* stk, float* scr,
-                                           const LaneData<K>& ld, const float* sx, const float* sy,
-                                           const float* sw, const KParams& p, int lane, int pass,
-                                           bool& bad, int& pts) {
-    float x[K], acc[K];
+                                           const LaneData<K>& ld, const DataView& dv, const KParams& p,
+                                           int lane, int pass, bool& bad, int& pts) {
+    float x[NV][K], acc[K];
     uint32_t valid;
     const int base = pass * 32 * K + lane;
+    const float* sy = dv.y;
+    const float* sw = dv.w;
     if (ONEPASS) {
 #pragma unroll
-        for (int k = 0; k < K; ++k) x[k] = ld.x[k];
+        for (int k = 0; k < K; ++k) x[0][k] = ld.x[k];
         valid = ld.valid;
     } else {
-        valid = 0u;
-#pragma unroll
-        for (int k = 0; k < K; ++k) {
-            int i = base + 32 * k;
-            bool v = i < p.nd;
-            x[k] = v ? sx[i] : 0.0f;
-            valid |= (v ? 1u : 0u) << k;
-        }
+        valid = load_points<K, NV>(dv, p, base, x);
     }
-    run_program<K, ROLLED>(prog, x, acc, stk, scr, lane);
+    run_program<K, ROLLED, NV>(prog, x, acc, stk, scr, lane);
     pts += ONEPASS ? p.nd : min(32 * K, p.nd - pass * 32 * K);
     float s = 0.0f;
     bad = false;
@@ -686,33 +727,28 @@ __device__ __forceinline__ float eval_pass(const uint2* prog, float* stk, float*
  * invalid (main.cu:459,462).  Each lane sums its points in FP32; the 32 lane
  * sums are combined with error-free transforms (FP64 on GB300 runs at about
  * 1/70 of the FP32 rate, so no FP64 instruction is issued here). */
-template <int K, bool ONEPASS, bool ROLLED>
+template <int K, bool ONEPASS, bool ROLLED, int NV>
 __device__ __forceinline__ df eval_loglik(const uint2* prog, float* stk, float* scr,
-                                          const LaneData<K>& ld, const float* sx, const float* sy,
-                                          const float* sw, const KParams& p, int lane, int& pts) {
+                                          const LaneData<K>& ld, const DataView& dv, const KParams& p,
+                                          int lane, int& pts) {
     float s = 0.0f;
     bool bad = false;
+    const float* sy = dv.y;
+    const float* sw = dv.w;
     const int npass = ONEPASS ? 1 : (p.nd + 32 * K - 1) / (32 * K);
 #pragma unroll 1
     for (int pass = 0; pass < npass; ++pass) {
-        float x[K], acc[K];
+        float x[NV][K], acc[K];
         uint32_t valid;
         const int base = pass * 32 * K + lane;
         if (ONEPASS) {
 #pragma unroll
-            for (int k = 0; k < K; ++k) x[k] = ld.x[k];
+            for (int k = 0; k < K; ++k) x[0][k] = ld.x[k];
             valid = ld.valid;
         } else {
-            valid = 0u;
-#pragma unroll
-            for (int k = 0; k < K; ++k) {
-                int i = base + 32 * k;
-                bool v = i < p.nd;
-                x[k] = v ? sx[i] : 0.0f;
-                valid |= (v ? 1u : 0u) << k;
-            }
+            valid = load_points<K, NV>(dv, p, base, x);
         }
-        run_program<K, ROLLED>(prog, x, acc, stk, scr, lane);
+        run_program<K, ROLLED, NV>(prog, x, acc, stk, scr, lane);
         pts += ONEPASS ? p.nd : min(32 * K, p.nd - pass * 32 * K);
 #pragma unroll
         for (int k = 0; k < K; ++k) {
@@ -901,21 +937,44 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) {
 }
 
 /* Stage the dataset with one bulk TMA copy per array; bounded wait. */
-static __device__ void stage_dataset(float* sx, float* sy, float* sw, uint64_t* bar, const KParams& p) {
+/* Number of float arrays of the staged dataset: x1, y, w, then x2, x3 for
+ * multivariate data. */
+__host__ __device__ __forceinline__ int data_arrays(const KParams& p) { return p.nv == 3 ? 5 : 3; }
+
+/* The dataset arrays in the order they are staged. */
+__device__ __forceinline__ const float* data_src(const KParams& p, int a) {
+    return a == 0 ? p.dx : a == 1 ? p.dy : a == 2 ? p.dw : a == 3 ? p.dx2 : p.dx3;
+}
+
+/* The view of a dataset staged at dst (arrays of nd_pad floats, staging order)
+ * or, streamed, of the device arrays. */
+__device__ __forceinline__ DataView data_view(const KParams& p, const float* dst, bool streamed) {
+    DataView dv;
+    if (streamed) {
+        dv.x[0] = p.dx; dv.y = p.dy; dv.w = p.dw; dv.x[1] = p.dx2; dv.x[2] = p.dx3;
+    } else {
+        const size_t n = (size_t)p.nd_pad;
+        dv.x[0] = dst; dv.y = dst + n; dv.w = dst + 2 * n; dv.x[1] = dst + 3 * n; dv.x[2] = dst + 4 * n;
+    }
+    return dv;
+}
+
+/* Stage the dataset into dst with one bulk TMA copy per array; bounded wait. */
+static __device__ void stage_dataset(float* dst, uint64_t* bar, const KParams& p) {
     const uint32_t bytes = (uint32_t)p.nd_pad * 4u;
     if (bytes == 0) return;
+    const int na = data_arrays(p);
     if (threadIdx.x == 0) {
         uint32_t b = smem_u32(bar);
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(3u * bytes) : "memory");
-        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                     ::"r"(smem_u32(sx)), "l"(p.dx), "r"(bytes), "r"(b) : "memory");
-        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                     ::"r"(smem_u32(sy)), "l"(p.dy), "r"(bytes), "r"(b) : "memory");
-        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                     ::"r"(smem_u32(sw)), "l"(p.dw), "r"(bytes), "r"(b) : "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"((uint32_t)na * bytes)
+                     : "memory");
+        for (int a = 0; a < na; ++a)
+            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                         ::"r"(smem_u32(dst + (size_t)a * p.nd_pad)), "l"(data_src(p, a)), "r"(bytes), "r"(b)
+                         : "memory");
     }
     __syncthreads();
     uint32_t b = smem_u32(bar);
@@ -999,26 +1058,20 @@ __device__ __forceinline__ void structure_move(Rng& r, const uint8_t* oc, uint8_
 /* STREAM: the dataset is read from device memory (L2-resident for a few MB)
  * instead of being staged into each CTA's shared memory -- the layout for
  * datasets too large to stage. */
-template <int K, bool ONEPASS, int RNG, bool ROLLED, bool STREAM>
+template <int K, bool ONEPASS, int RNG, bool ROLLED, bool STREAM, int NV>
 __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __grid_constant__ KParams p) {
     extern __shared__ __align__(128) uint8_t smem[];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
 
-    /* CTA-shared dataset (or the device copy when streamed) */
+    /* CTA-shared dataset (or the device arrays when streamed) */
     uint64_t* bar = (uint64_t*)smem;
-    const float* sx;
-    const float* sy;
-    const float* sw;
-    uint8_t* wbase;
-    if (STREAM) {
-        sx = p.dx; sy = p.dy; sw = p.dw;
-        wbase = smem + 16;
-    } else {
-        float* fx = (float*)(smem + 16);
-        sx = fx; sy = fx + p.nd_pad; sw = fx + 2 * (size_t)p.nd_pad;
-        wbase = smem + 16 + align16((size_t)3 * p.nd_pad * 4);
-        stage_dataset(fx, fx + p.nd_pad, fx + 2 * (size_t)p.nd_pad, bar, p);
+    float* fx = (float*)(smem + 16);
+    const DataView dv = data_view(p, fx, STREAM);
+    uint8_t* wbase = smem + 16;
+    if (!STREAM) {
+        wbase += align16((size_t)data_arrays(p) * p.nd_pad * 4);
+        stage_dataset(fx, bar, p);
     }
     const size_t wbytes = warp_smem_bytes(p.PL, p.max_instr, p.levels, K);
     const WarpSmem ws = carve_warp<K>(wbase + (size_t)warp * wbytes, p.PL, p.max_instr, p.levels);
@@ -1030,7 +1083,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
         for (int k = 0; k < K; ++k) {
             int i = lane + 32 * k;
             bool v = i < p.nd;
-            ld.x[k] = v ? sx[i] : 0.0f;
+            ld.x[k] = v ? dv.x[0][i] : 0.0f;
             ld.valid |= (v ? 1u : 0u) << k;
         }
     }
@@ -1075,7 +1128,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
         if (active)
         for (int i = lane; i < PL; i += 32) {
             int o = p.P[(size_t)i * p.N + chain];
-            ws.ops[0][i] = (uint8_t)((o >= 0 && o < OP_NREF) ? o : 255);
+            ws.ops[0][i] = (uint8_t)((o >= 0 && o < OP_NALL) ? o : 255);
             ws.Cs[0][i] = p.C[(size_t)i * p.N + chain];
         }
         __syncwarp();
@@ -1177,7 +1230,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                 const int w = __ffs(__ballot_sync(FULLMASK, my_rank == q)) - 1;
                 if (s_bad[w]) continue;
                 bool bad;
-                const float sl = eval_pass<K, ONEPASS, ROLLED>(s_prog[w], ws.stk, ws.scr, ld, sx, sy, sw,
+                const float sl = eval_pass<K, ONEPASS, ROLLED, NV>(s_prog[w], ws.stk, ws.scr, ld, dv,
                                                                p, lane, pass, bad, pts);
                 /* FP32 butterfly within the pass (terms are >= 0: <= 5 roundings),
                  * double-float across passes */
@@ -1204,7 +1257,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                 }
             }
           } else if (active) {
-            lik = eval_loglik<K, ONEPASS, ROLLED>(ws.eprog, ws.stk, ws.scr, ld, sx, sy, sw, p, lane, pts);
+            lik = eval_loglik<K, ONEPASS, ROLLED, NV>(ws.eprog, ws.stk, ws.scr, ld, dv, p, lane, pts);
             st_np += (unsigned long long)(count + 4) * (unsigned)pts;
           }
           st_pts += (unsigned)pts;

@@ -44,6 +44,9 @@ enum {
 
 enum { GPR_RNG_LCG = 0, GPR_RNG_PHILOX = 1 };
 enum { GPR_CONST_REFERENCE = 0, GPR_CONST_RANDOM_WALK = 1, GPR_CONST_HMC = 2 };
+/* Op codes beyond the reference's 27: the input variables of multivariate
+ * data, printed X, Y, Z in op-code strings. */
+enum { GPR_OP_X1 = 27, GPR_OP_X2 = 28, GPR_OP_X3 = 29 };
 
 #define GPR_MAX_PROGRAM_LENGTH 255
 #define GPR_MAX_OPS 32
@@ -57,7 +60,8 @@ typedef struct gpr_config {
     float rw_sd;             /* random-walk sd for GPR_CONST_RANDOM_WALK                      */
     int device;              /* CUDA device ordinal (--gpu, main.cu:104)                      */
     void* stream;            /* cudaStream_t to run on, or NULL to let the handle create one  */
-    int reserved[8];
+    int n_vars;              /* input variables: 1 (the reference) or 3 (x1, x2, x3; 0 reads as 1) */
+    int reserved[7];
 } gpr_config;
 
 typedef struct gpr_handle gpr_handle;
@@ -76,6 +80,12 @@ int gpr_destroy(gpr_handle* h);
 /* Upload the dataset: n points of (x, y, sd), host arrays (the datum array D,
  * main.cu:48,1143).  sd must be > 0 (main.cu:332). */
 int gpr_set_data(gpr_handle* h, const float* x, const float* y, const float* sd, int n);
+
+/* Multivariate data (no reference counterpart): n points of (x1, x2, x3, y,
+ * sd) for a handle created with n_vars = 3, whose op set may hold the leaf
+ * ops GPR_OP_X1..GPR_OP_X3; a child beyond the heap reads x1. */
+int gpr_set_data3(gpr_handle* h, const float* x1, const float* x2, const float* x3, const float* y,
+                  const float* sd, int n);
 
 /* Upload chain state in the reference layout (main.cu:1144-1145, 1233-1234).
  * P holds program_length*N ints, C program_length*N floats (host memory). */

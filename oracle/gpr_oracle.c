@@ -24,7 +24,8 @@
 
 /* op codes of the reference enum (main.cu:53) */
 enum { ONE, CONST, INV, A, B, PLUS, MINUS, RMINUS, CPLUS, TIMES, CTIMES, DIV, RDIV, LOG, EXP, POW,
-       CPOW, RPOW, CRPOW, SQRT, SIN, ASIN, COS, ACOS, TAN, ATAN, ABS, NREF };
+       CPOW, RPOW, CRPOW, SQRT, SIN, ASIN, COS, ACOS, TAN, ATAN, ABS, NREF,
+       X1 = NREF, X2, X3 /* input variables of multivariate data (extension) */ };
 
 #define PIF 3.141592653589          /* main.cu:194 */
 #define MY_RAND_MAX 2147483647      /* main.cu:210 */
@@ -94,6 +95,10 @@ static int port_is_int(float x) { return fabsf(x - (float)lroundf(x)) < 1.0e-6; 
 
 /* ---- tree folds over the heap (main.cu:371-393) ------------------------ */
 #define OP(P, N, idx, j) ((P)[(size_t)((j) - 1) * (N) + (idx)])
+
+/* x2, x3 of the point being evaluated, for multivariate data (x1 is the
+ * evaluators' x argument); set by the *_nv entry points below. */
+static _Thread_local double g_x2 = 0.0, g_x3 = 0.0;
 #define CV(C, N, idx, j) ((C)[(size_t)((j) - 1) * (N) + (idx)])
 
 /* dispatch_eval (main.cu:397-444), reachable nodes only (the value of the
@@ -132,6 +137,9 @@ static float eval_node(const int32_t* P, const float* C, int N, int PL, int idx,
         case RPOW: { float a = L, b = R; return powf(b, a); }
         case CRPOW: return powf(c, L);
         case ABS: return fabsf(L);
+        case X1: return x;
+        case X2: return (float)g_x2;
+        case X3: return (float)g_x3;
         default: return NAN;
     }
 #undef L
@@ -173,6 +181,9 @@ static double eval_node_f64(const int32_t* P, const float* C, int N, int PL, int
         case RPOW: { double a = L, b = R; return pow(b, a); }
         case CRPOW: return pow(c, L);
         case ABS: return fabs(L);
+        case X1: return x;
+        case X2: return g_x2;
+        case X3: return g_x3;
         default: return NAN;
     }
 #undef L
@@ -223,6 +234,9 @@ static double eval_node_f64p(const int32_t* P, const float* C, int N, int PL, in
         case RPOW: { double a = L, b = R; r = pow(b, a); break; }
         case CRPOW: r = pow(c, L); break;
         case ABS: r = fabs(L); break;
+        case X1: return x;
+        case X2: return g_x2;
+        case X3: return g_x3;
         default: return NAN;
     }
 #undef L
@@ -242,7 +256,7 @@ static float length_node(const int32_t* P, int N, int PL, int idx, int j) {
     if (j > PL) return 1.0f;
     int o = OP(P, N, idx, j);
     switch (o) {
-        case ONE: case CONST: return 1.0f;
+        case ONE: case CONST: case X1: case X2: case X3: return 1.0f;
         case A: return length_node(P, N, PL, idx, 2 * j);
         case B: return length_node(P, N, PL, idx, 2 * j + 1);
         case CPLUS: case CTIMES: case CPOW: case CRPOW: return 1.0f + length_node(P, N, PL, idx, 2 * j) + 1.0f;
@@ -259,7 +273,7 @@ static int count_node(const int32_t* P, int N, int PL, int idx, int j) {
     if (j > PL) return 0;
     int o = OP(P, N, idx, j);
     switch (o) {
-        case ONE: case CONST: return 1;
+        case ONE: case CONST: case X1: case X2: case X3: return 1;
         case A: return count_node(P, N, PL, idx, 2 * j);
         case B: return count_node(P, N, PL, idx, 2 * j + 1);
         case PLUS: case MINUS: case RMINUS: case TIMES: case DIV: case RDIV: case POW: case RPOW:
@@ -551,6 +565,9 @@ static double evd(const int32_t* P, int N, int PL, int idx, const double* Cd, in
         case RPOW: { double a = L, b = R; r = pow(b, a); break; }
         case CRPOW: r = pow(c, L); break;
         case ABS: r = fabs(L); break;
+        case X1: return x;
+        case X2: return g_x2;
+        case X3: return g_x3;
         default: return NAN;
     }
 #undef L
@@ -650,5 +667,59 @@ double gpr_port_loglik_grad_f64p(const int32_t* P, int N, int PL, int idx, const
     g_evd_seed = seed;
     double ll = gpr_port_loglik_grad_f64(P, N, PL, idx, Cd, D, nd, g, NULL);
     g_evd_rel = 0.0;
+    return ll;
+}
+
+/* ---- multivariate data (extension): D5 holds (x1, x2, x3, y, sd) per point */
+
+static void set_point(const float* D5, int d) { g_x2 = D5[5 * d + 1]; g_x3 = D5[5 * d + 2]; }
+
+float gpr_port_call_nv(const int32_t* P, const float* C, int N, int PL, int idx, float x1, float x2, float x3) {
+    g_x2 = x2; g_x3 = x3;
+    return eval_node(P, C, N, PL, idx, 1, x1);
+}
+
+/* compute_likelihood (main.cu:454-468) over multivariate points, FP32
+ * evaluation (f64 = 0) or FP64 evaluation and sum (f64 = 1). */
+double gpr_port_likelihood_nv(const int32_t* P, const float* C, int N, int PL, int idx, const float* D5, int nd,
+                              int f64) {
+    double ll = 0.0;
+    for (int d = 0; d < nd; d++) {
+        set_point(D5, d);
+        const float x1 = D5[5 * d], y = D5[5 * d + 3], sd = D5[5 * d + 4];
+        if (f64) {
+            double fx = eval_node_f64(P, C, N, PL, idx, 1, x1);
+            if (!isfinite(fx)) return -INFINITY;
+            double r = fx - (double)y, s = sd;
+            ll += -(r * r) / (2.0 * s * s) - 0.5 * (log(2.0 * PIF) + 2.0 * log(s));
+        } else {
+            float fx = eval_node(P, C, N, PL, idx, 1, x1);
+            if (isnan(fx) || !isfinite(fx)) return -INFINITY;
+            double l = port_lnormalpdf(fx - y, sd);
+            if (isnan(l) || !isfinite(l)) return -INFINITY;
+            ll += l;
+        }
+    }
+    return ll;
+}
+
+/* d loglik / d Cd over multivariate points (as gpr_port_loglik_grad_f64). */
+double gpr_port_loglik_grad_f64_nv(const int32_t* P, int N, int PL, int idx, const double* Cd, const float* D5,
+                                   int nd, double* g, double* gabs) {
+    double* gd = (double*)calloc((size_t)PL, sizeof(double));
+    for (int k = 0; k < PL; ++k) { g[k] = 0.0; if (gabs) gabs[k] = 0.0; }
+    double ll = 0.0;
+    for (int d = 0; d < nd; d++) {
+        set_point(D5, d);
+        const double x1 = D5[5 * d];
+        double fx = evd(P, N, PL, idx, Cd, 1, x1);
+        if (!isfinite(fx)) { ll = -INFINITY; break; }
+        double r = fx - (double)D5[5 * d + 3], s = D5[5 * d + 4];
+        ll += -(r * r) / (2.0 * s * s) - 0.5 * (log(2.0 * PIF) + 2.0 * log(s));
+        for (int k = 0; k < PL; ++k) gd[k] = 0.0;
+        gradd(P, N, PL, idx, Cd, 1, x1, -r / (s * s), gd);
+        for (int k = 0; k < PL; ++k) { g[k] += gd[k]; if (gabs) gabs[k] += fabs(gd[k]); }
+    }
+    free(gd);
     return ll;
 }

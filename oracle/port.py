@@ -44,6 +44,12 @@ def lib():
         L.gpr_port_loglik_grad_f64.restype = dp
         L.gpr_port_loglik_grad_f64p.argtypes = [vp, ip, ip, ip, vp, vp, ip, vp, ctypes.c_uint, dp]
         L.gpr_port_loglik_grad_f64p.restype = dp
+        L.gpr_port_call_nv.argtypes = [vp, vp, ip, ip, ip, fp, fp, fp]
+        L.gpr_port_call_nv.restype = fp
+        L.gpr_port_likelihood_nv.argtypes = [vp, vp, ip, ip, ip, vp, ip, ip]
+        L.gpr_port_likelihood_nv.restype = dp
+        L.gpr_port_loglik_grad_f64_nv.argtypes = [vp, ip, ip, ip, vp, vp, ip, vp, vp]
+        L.gpr_port_loglik_grad_f64_nv.restype = dp
         L.gpr_port_resample.argtypes = [ctypes.POINTER(PortCfg), ip, vp, vp, vp, vp, ip, dp, ctypes.c_uint, vp]
         assert L.gpr_port_sizeof_cfg() == ctypes.sizeof(PortCfg)
         _lib = L
@@ -185,3 +191,30 @@ def grad_sensitivity(P, idx, Cd, x, y, sd, rel=2.0 ** -22, trials=4):
             d = np.where(np.isfinite(g) == np.isfinite(g0), np.abs(g - g0), np.inf)
         worst = np.maximum(worst, np.nan_to_num(d, nan=np.inf))
     return worst
+
+
+def pack5(x1, x2, x3, y, sd):
+    d = np.empty((len(x1), 5), np.float32)
+    d[:, 0], d[:, 1], d[:, 2], d[:, 3], d[:, 4] = x1, x2, x3, y, sd
+    return np.ascontiguousarray(d)
+
+
+def call_nv(P, C, idx, x1, x2, x3):
+    """FP32 value of chain idx at one multivariate point."""
+    return lib().gpr_port_call_nv(_p(P), _p(C), P.shape[1], P.shape[0], idx, x1, x2, x3)
+
+
+def likelihood_nv(P, C, idx, x1, x2, x3, y, sd, f64=False):
+    D = pack5(x1, x2, x3, y, sd)
+    return lib().gpr_port_likelihood_nv(_p(P), _p(C), P.shape[1], P.shape[0], idx, _p(D), len(x1), int(f64))
+
+
+def loglik_grad_f64_nv(P, idx, Cd, x1, x2, x3, y, sd):
+    """(FP64 log-likelihood, d loglik / d Cd, sum of |per-point terms|), multivariate."""
+    PL, N = P.shape
+    D = pack5(x1, x2, x3, y, sd)
+    Cd = np.ascontiguousarray(Cd, np.float64)
+    g = np.zeros(PL)
+    ga = np.zeros(PL)
+    ll = lib().gpr_port_loglik_grad_f64_nv(_p(P), N, PL, idx, _p(Cd), _p(D), len(x1), _p(g), _p(ga))
+    return ll, g, ga

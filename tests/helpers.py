@@ -139,3 +139,16 @@ def used_constants(P):
             if child <= PL:
                 reach[child] |= r & m
     return used
+
+
+# {+, -, *, /, sin, cos, exp, const, x1, x2, x3} and the A/B pass-throughs
+OPSET_MULTI = [1, 3, 4, 5, 6, 9, 11, 20, 22, 27, 28, 29, 14]
+
+
+def multivar_data(n=65536, seed=0):
+    """x1, x2, x3 ~ N(0, 1); y = sin(x1) x2 + exp(-x3^2) + N(0, 0.05); sd 0.05."""
+    r = np.random.default_rng(seed)
+    x1, x2, x3 = r.normal(0, 1, (3, n))
+    y = np.sin(x1) * x2 + np.exp(-x3 ** 2) + r.normal(0, 0.05, n)
+    f = lambda a: a.astype(np.float32)  # noqa: E731
+    return f(x1), f(x2), f(x3), f(y), np.full(n, 0.05, np.float32)

@@ -206,3 +206,19 @@ def test_ess_geyer_on_ar1():
         want = T * (1 - a) / (1 + a)
         assert abs(np.median(ess) / want - 1) < 0.1, (a, np.median(ess), want)
     assert ess_geyer(np.ones((2, 100)))[0] == 0
+
+
+def test_variable_leaves_need_three_variables():
+    """x2/x3 leaf ops are refused for a univariate handle, before any device
+    work; the op-code string prints the variable leaves as X, Y, Z."""
+    _lib()
+    with pytest.raises(g.GprError, match="n_vars = 3"):
+        g.Sampler(4, program_length=7, ops=[g.CONST, g.X2])
+    with pytest.raises(g.GprError, match="n_vars"):
+        g.Sampler(4, program_length=7, n_vars=2)
+    P = np.zeros((7, 1), np.int32)
+    P[0, 0], P[1, 0], P[2, 0] = g.PLUS, g.X2, g.X3
+    C = np.zeros((7, 1), np.float32)
+    assert g.format_expression(P, C, 0) == "(x2+x3)"
+    line = g.format_samples(P, C, np.zeros(1), np.zeros(1), 1)
+    assert '"+YZ1111"' in line
