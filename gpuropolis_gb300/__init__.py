@@ -101,6 +101,9 @@ def library():
     lib.gpr_chain_scales.argtypes = [vp, vp]
     lib.gpr_loglik_grad.argtypes = [vp, vp, vp]
     lib.gpr_run_block_traced.argtypes = [vp, ip, ip, ip, vp]
+    lib.gpr_set_batched_data.argtypes = [vp, ip, vp, vp, vp, vp, vp, vp]
+    lib.gpr_capture_blocks.argtypes = [vp, ip, ip]
+    lib.gpr_run_captured.argtypes = [vp, vp]
     lib.gpr_resample.argtypes = [vp, ip, dp, ctypes.c_uint32, vp, vp]
     lib.gpr_top_chains.argtypes = [vp, ip, dp, vp, ip, vp, vp]
     lib.gpr_map_chain.argtypes = [vp, vp, vp]
@@ -190,6 +193,27 @@ class Sampler:
     def set_data3(self, x1, x2, x3, y, sd):
         a = [np.ascontiguousarray(v, np.float32) for v in (x1, x2, x3, y, sd)]
         self._check(self.lib.gpr_set_data3(self.h, *[_ptr(v) for v in a], len(a[0])))
+
+    def set_batched_data(self, datasets):
+        """datasets: a list of (x, y, sd) or, for three variables, of
+        (x1, x2, x3, y, sd); chain c fits dataset c // (N // len(datasets))."""
+        sizes = np.array([len(d[0]) for d in datasets], np.int32)
+        ncol = 5 if self.cfg.n_vars == 3 else 3
+        cat = [np.ascontiguousarray(np.concatenate([np.asarray(d[i], np.float32) for d in datasets])
+                                    if datasets else np.zeros(0), np.float32) for i in range(ncol)]
+        x1, x2, x3, y, sd = cat if ncol == 5 else (cat[0], None, None, cat[1], cat[2])
+        self._check(self.lib.gpr_set_batched_data(self.h, len(datasets), _ptr(sizes), _ptr(x1), _ptr(x2),
+                                                  _ptr(x3), _ptr(y), _ptr(sd)))
+
+    def capture_blocks(self, n_blocks, steps):
+        self._check(self.lib.gpr_capture_blocks(self.h, int(n_blocks), int(steps)))
+        self._captured = int(n_blocks)
+
+    def run_captured(self, seeds):
+        seeds = np.ascontiguousarray(seeds, np.int32)
+        if len(seeds) != getattr(self, "_captured", len(seeds)):
+            raise GprError(1, f"{len(seeds)} seeds for {self._captured} captured blocks")
+        self._check(self.lib.gpr_run_captured(self.h, _ptr(seeds)))
 
     def set_state(self, P, C):
         P = np.ascontiguousarray(P, np.int32).reshape(self.PL, self.N)

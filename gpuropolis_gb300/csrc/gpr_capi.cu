@@ -48,6 +48,13 @@ struct gpr_handle {
     /* selection scratch, allocated by the first gpr_resample/gpr_top_chains/gpr_map_chain */
     float* dscale = nullptr;               /* per-chain proposal scales          */
     int stream_data = 0;                   /* 1: always stream the dataset       */
+    int* dds = nullptr;                    /* batched data: off | n | order      */
+    float* dds_ns = nullptr;               /* batched data: normalising sums     */
+    /* a captured block sequence (gpr_capture_blocks) */
+    cudaGraphExec_t graph = nullptr;
+    uint32_t* dseeds = nullptr;
+    uint32_t* hseeds = nullptr;            /* pinned                             */
+    int graph_blocks = 0;
     unsigned long long* dkeys = nullptr;   /* N posterior keys                   */
     unsigned long long* dsel = nullptr;    /* [0] selected key                   */
     int* dseli = nullptr;                  /* [0] count, [1] first index         */
@@ -121,6 +128,9 @@ static void free_all(gpr_handle* h) {
     cudaFree(h->dP); cudaFree(h->dC); cudaFree(h->dprior); cudaFree(h->dlik);
     cudaFree(h->dlogcount); cudaFree(h->dcounter); cudaFree(h->ddata); cudaFree(h->dstats);
     cudaFree(h->dkeys); cudaFree(h->dsel); cudaFree(h->dseli); cudaFree(h->dtop); cudaFree(h->dscale);
+    cudaFree(h->dds); cudaFree(h->dds_ns);
+    if (h->graph) cudaGraphExecDestroy(h->graph);
+    cudaFree(h->dseeds); cudaFreeHost(h->hseeds);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
 }
 
@@ -260,8 +270,21 @@ int gpr_destroy(gpr_handle* h) {
     return GPR_OK;
 }
 
-/* Launch geometry for a given layout: K points per lane, data in registers
- * (onepass) or streamed from shared memory, heavy ops rolled or unrolled. */
+/* A captured block sequence bakes the launch parameters in: any change of
+ * data, layout or moves drops it. */
+static void drop_graph(gpr_handle* h) {
+    if (h->graph) { cudaStreamSynchronize(h->stream); cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+    h->graph_blocks = 0;
+}
+
+/* Largest CTA size (warps) that divides the chains of one dataset, so that
+ * a CTA's chain group never straddles two datasets. */
+static int batched_wpc(const gpr::KParams& kp, int wpc) {
+    if (kp.nds <= 0) return wpc;
+    while (wpc > 1 && kp.chains_per_ds % wpc) wpc /= 2;
+    return wpc;
+}
+
 /* The MH kernel with Hamiltonian constant moves: one chain per warp,
  * wpc0 warps per CTA, four points per lane per pass, a persistent grid of at
  * most ctas_per_sm CTAs per SM (0: as many as fit).  Capping the CTAs also
@@ -269,12 +292,14 @@ int gpr_destroy(gpr_handle* h) {
  * the thread-local gradient tapes. */
 static int configure_hmc(gpr_handle* h, int wpc0 = 4, int ctas_per_sm = 0) {
     if (wpc0 < 1 || wpc0 > 4) wpc0 = 4;   /* the kernel is built for CTAs of at most 128 threads */
+    drop_graph(h);
     gpr::KParams& kp = h->kp;
     if (!gpr::grad_supported(kp))
         return fail(h, GPR_ERR_ARG, "gradient moves support program_length <= 127 (got %d)", kp.PL);
     gpr::LaunchCfg lc;
     lc.K = 4; lc.onepass = 0; lc.rolled = 0; lc.lockstep = 0; lc.carveout = 0;
-    lc.stream = h->stream_data || gpr::grad_smem_bytes(kp, wpc0) > 227 * 1024;
+    /* batched data: each warp reads its own chain's dataset from device memory */
+    lc.stream = h->stream_data || kp.nds > 0 || gpr::grad_smem_bytes(kp, wpc0) > 227 * 1024;
     int wpc = wpc0;
     size_t smem = gpr::grad_smem_bytes(kp, wpc, lc.stream);
     while (smem > 227 * 1024 && wpc > 1) smem = gpr::grad_smem_bytes(kp, wpc /= 2, lc.stream);
@@ -306,8 +331,14 @@ static int configure_hmc(gpr_handle* h, int wpc0 = 4, int ctas_per_sm = 0) {
 static int configure_launch(gpr_handle* h, int K, int onepass, int rolled, int lockstep = 1, int wpc0 = 8) {
     gpr::KParams& kp = h->kp;
     if (kp.const_mode == GPR_CONST_HMC) return configure_hmc(h);
+    drop_graph(h);
     gpr::LaunchCfg lc;
     lc.carveout = 0;
+    if (kp.nds > 0) {   /* batched: CTA groups within one dataset, staged per group */
+        onepass = 0;
+        if (lockstep < 1) lockstep = 1;
+        wpc0 = batched_wpc(kp, wpc0);
+    }
     lc.stream = h->stream_data || gpr::mh_smem_bytes(kp, K, wpc0) > 227 * 1024;
     if (lc.stream) { K = 4; onepass = 0; }
     lc.K = K;
@@ -320,6 +351,7 @@ static int configure_launch(gpr_handle* h, int K, int onepass, int rolled, int l
         wpc /= 2;
         smem = gpr::mh_smem_bytes(kp, lc.K, wpc, lc.stream);
     }
+    if (kp.nds > 0) wpc = batched_wpc(kp, wpc);
     if (smem > 227 * 1024)
         return fail(h, GPR_ERR_ARG, "programs of length %d do not fit in shared memory", kp.PL);
     lc.warps_per_cta = wpc;
@@ -339,7 +371,8 @@ static int configure_launch(gpr_handle* h, int K, int onepass, int rolled, int l
  * when the data fit, heavy ops unrolled (the fastest layout measured on the
  * 250-point, PROGRAM_LENGTH 63 workload; gpr_autotune re-checks per dataset). */
 static int choose_launch(gpr_handle* h) {
-    return configure_launch(h, 4, h->kp.nd <= 128 ? 1 : 0, 0, 1, 8);
+    /* three input variables: built for K = 4 in passes only */
+    return configure_launch(h, 4, (h->kp.nd <= 128 && h->kp.nv != 3) ? 1 : 0, 0, 1, 8);
 }
 
 /* Device layout of a dataset: x1 | y | w | sd | x2 | x3, nd_pad floats each
@@ -371,6 +404,8 @@ static int set_data_impl(gpr_handle* h, const float* x, const float* x2, const f
         /* the constant part of lnormalpdf (main.cu:300), per point */
         normsum += 0.5 * ((double)logf((float)(2.0 * PIf)) + 2.0 * (double)logf(sd[i]));
     }
+    drop_graph(h);
+    h->kp.nds = 0;
     if (h->ddata) { CUDA_TRY(h, cudaStreamSynchronize(h->stream)); cudaFree(h->ddata); h->ddata = nullptr; }
     if (nd_pad > 0) {
         CUDA_TRY(h, cudaMalloc(&h->ddata, host.size() * sizeof(float)));
@@ -400,6 +435,135 @@ int gpr_set_data(gpr_handle* h, const float* x, const float* y, const float* sd,
     if (!h) return GPR_ERR_ARG;
     if (h->kp.nv == 3) return fail(h, GPR_ERR_ARG, "a handle with three input variables takes gpr_set_data3");
     return set_data_impl(h, x, nullptr, nullptr, y, sd, n);
+}
+
+int gpr_set_batched_data(gpr_handle* h, int n_datasets, const int* sizes, const float* x1, const float* x2,
+                         const float* x3, const float* y, const float* sd) {
+    if (!h) return GPR_ERR_ARG;
+    if (n_datasets < 1 || !sizes) return fail(h, GPR_ERR_ARG, "n_datasets must be >= 1 with sizes");
+    if (h->N % n_datasets) return fail(h, GPR_ERR_ARG, "%d chains do not split evenly into %d datasets",
+                                       h->N, n_datasets);
+    const int cpd = h->N / n_datasets;
+    const bool three = h->kp.nv == 3;
+    long long total = 0, maxn = 0, npad = 0;
+    for (int d = 0; d < n_datasets; ++d) {
+        if (sizes[d] < 0) return fail(h, GPR_ERR_ARG, "sizes[%d] = %d is negative", d, sizes[d]);
+        total += sizes[d];
+        npad += (sizes[d] + 3) & ~3;
+        if (sizes[d] > maxn) maxn = sizes[d];
+    }
+    if (npad > (1ll << 30)) return fail(h, GPR_ERR_ARG, "batched data too large");
+    if (total > 0 && (!x1 || !y || !sd || (three && (!x2 || !x3))))
+        return fail(h, GPR_ERR_ARG, "point arrays must be non-NULL (x2, x3 for three variables)");
+    for (long long i = 0; i < total; ++i)
+        if (!(sd[i] > 0.0f)) return fail(h, GPR_ERR_ARG, "sd[%lld] = %g is not > 0", i, (double)sd[i]);
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    drop_graph(h);
+    const size_t T = (size_t)npad;
+    std::vector<float> host((three ? 6 : 4) * T + 4, 0.0f);
+    std::vector<int> meta(3 * (size_t)n_datasets);
+    std::vector<float> ns(2 * (size_t)n_datasets);
+    const double PIf = 3.141592653589;
+    size_t off = 0, src = 0;
+    for (int d = 0; d < n_datasets; ++d) {
+        meta[d] = (int)off;
+        meta[n_datasets + d] = sizes[d];
+        double normsum = 0.0;
+        for (int i = 0; i < sizes[d]; ++i, ++src) {
+            host[off + i] = x1[src];
+            host[T + off + i] = y[src];
+            const double sdd = (double)sd[src];
+            host[2 * T + off + i] = (float)(0x1p-64 / (2.0 * sdd * sdd));
+            host[3 * T + off + i] = sd[src];
+            if (three) { host[4 * T + off + i] = x2[src]; host[5 * T + off + i] = x3[src]; }
+            normsum += 0.5 * ((double)logf((float)(2.0 * PIf)) + 2.0 * (double)logf(sd[src]));   /* main.cu:300 */
+        }
+        const double nsd = normsum * 0x1p-64;
+        ns[2 * d] = (float)nsd;
+        ns[2 * d + 1] = (float)(nsd - (double)ns[2 * d]);
+        off += (sizes[d] + 3) & ~3;
+    }
+    /* datasets claimed largest first, so that uneven sizes balance across the grid */
+    std::vector<int> order(n_datasets);
+    for (int d = 0; d < n_datasets; ++d) order[d] = d;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return sizes[a] > sizes[b]; });
+    for (int d = 0; d < n_datasets; ++d) meta[2 * n_datasets + d] = order[d];
+    if (h->ddata) { CUDA_TRY(h, cudaStreamSynchronize(h->stream)); cudaFree(h->ddata); h->ddata = nullptr; }
+    cudaFree(h->dds); cudaFree(h->dds_ns);
+    h->dds = nullptr; h->dds_ns = nullptr;
+    CUDA_TRY(h, cudaMalloc(&h->ddata, host.size() * sizeof(float)));
+    CUDA_TRY(h, cudaMalloc(&h->dds, meta.size() * sizeof(int)));
+    CUDA_TRY(h, cudaMalloc(&h->dds_ns, ns.size() * sizeof(float)));
+    CUDA_TRY(h, cudaMemcpyAsync(h->ddata, host.data(), host.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(h->dds, meta.data(), meta.size() * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(h->dds_ns, ns.data(), ns.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    gpr::KParams& kp = h->kp;
+    h->nd = (int)maxn;
+    h->nd_pad = (int)((maxn + 3) & ~3);
+    kp.nd = h->nd; kp.nd_pad = h->nd_pad;
+    kp.normsum_hi = kp.normsum_lo = 0.0f;
+    kp.dx = h->ddata; kp.dy = h->ddata + T; kp.dw = h->ddata + 2 * T;
+    kp.dx2 = three ? h->ddata + 4 * T : nullptr;
+    kp.dx3 = three ? h->ddata + 5 * T : nullptr;
+    kp.nds = n_datasets;
+    kp.chains_per_ds = cpd;
+    kp.ds_off = h->dds;
+    kp.ds_n = h->dds + n_datasets;
+    kp.ds_order = h->dds + 2 * n_datasets;
+    kp.ds_ns = h->dds_ns;
+    return choose_launch(h);
+}
+
+static int run(gpr_handle* h, int steps, int seed);
+
+int gpr_capture_blocks(gpr_handle* h, int n_blocks, int steps) {
+    if (!h) return GPR_ERR_ARG;
+    if (n_blocks < 1 || steps < 0) return fail(h, GPR_ERR_ARG, "n_blocks must be >= 1 and steps >= 0");
+    if (h->nd < 0) return fail(h, GPR_ERR_STATE, "gpr_set_data has not been called");
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    drop_graph(h);
+    cudaFree(h->dseeds); cudaFreeHost(h->hseeds);
+    h->dseeds = nullptr; h->hseeds = nullptr;
+    CUDA_TRY(h, cudaMalloc(&h->dseeds, (size_t)n_blocks * sizeof(uint32_t)));
+    CUDA_TRY(h, cudaMallocHost(&h->hseeds, (size_t)n_blocks * sizeof(uint32_t)));
+    memset(h->hseeds, 0, (size_t)n_blocks * sizeof(uint32_t));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    cudaGraph_t g = nullptr;
+    CUDA_TRY(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaMemcpyAsync(h->dseeds, h->hseeds, (size_t)n_blocks * sizeof(uint32_t),
+                                    cudaMemcpyHostToDevice, h->stream);
+    int rc = GPR_OK;
+    for (int b = 0; b < n_blocks && e == cudaSuccess && rc == GPR_OK; ++b) {
+        h->kp.seed_src = h->dseeds;
+        h->kp.seed_index = b;
+        rc = run(h, steps, 0);
+    }
+    h->kp.seed_src = nullptr;
+    h->kp.seed_index = 0;
+    const cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess && rc == GPR_OK) e = cudaGraphInstantiate(&h->graph, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (rc != GPR_OK) return rc;
+    if (e != cudaSuccess) {
+        h->graph = nullptr;
+        return fail(h, GPR_ERR_CUDA, "gpr_capture_blocks: %s", cudaGetErrorString(e));
+    }
+    h->graph_blocks = n_blocks;
+    return GPR_OK;
+}
+
+int gpr_run_captured(gpr_handle* h, const int* seeds) {
+    if (!h || !seeds) return GPR_ERR_ARG;
+    if (!h->graph) return fail(h, GPR_ERR_STATE, "no captured block sequence (gpr_capture_blocks)");
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    /* the previous replay may still be reading the pinned seeds */
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    for (int b = 0; b < h->graph_blocks; ++b) h->hseeds[b] = (uint32_t)seeds[b];
+    CUDA_TRY(h, cudaGraphLaunch(h->graph, h->stream));
+    h->launches += h->graph_blocks;
+    return GPR_OK;
 }
 
 int gpr_set_data3(gpr_handle* h, const float* x1, const float* x2, const float* x3, const float* y,
@@ -685,6 +849,8 @@ int gpr_set_layout2(gpr_handle* h, int K, int onepass, int rolled, int lockstep,
         (warps_per_cta != 1 && warps_per_cta != 2 && warps_per_cta != 4 && warps_per_cta != 8))
         return fail(h, GPR_ERR_ARG, "invalid layout K=%d onepass=%d lockstep=%d warps=%d for %d points", K,
                     onepass, lockstep, warps_per_cta, h->kp.nd);
+    if (h->kp.nv == 3 && (K != 4 || onepass))
+        return fail(h, GPR_ERR_ARG, "three input variables take K=4 in passes (got K=%d onepass=%d)", K, onepass);
     CUDA_TRY(h, cudaSetDevice(h->device));
     return configure_launch(h, K, onepass ? 1 : 0, rolled ? 1 : 0, lockstep, warps_per_cta);
 }
@@ -728,6 +894,7 @@ int gpr_set_moves(gpr_handle* h, int struct_every, float hmc_eps, int hmc_steps)
     if (struct_every < 0) return fail(h, GPR_ERR_ARG, "struct_every must be >= 0 (got %d)", struct_every);
     if (!(hmc_eps > 0.0f) || !(hmc_eps < 1e30f)) return fail(h, GPR_ERR_ARG, "hmc_eps must be > 0");
     if (hmc_steps < 1 || hmc_steps > 1024) return fail(h, GPR_ERR_ARG, "hmc_steps must be in [1, 1024]");
+    drop_graph(h);
     h->kp.struct_every = struct_every;
     h->kp.hmc_eps = hmc_eps;
     h->kp.hmc_L = hmc_steps;
@@ -750,6 +917,7 @@ int gpr_adapt_scales(gpr_handle* h, float target_accept) {
         CUDA_TRY(h, cudaStreamSynchronize(h->stream));
         h->kp.chain_scale = h->dscale;
     }
+    drop_graph(h);
     h->kp.adapt_target = target_accept;
     return GPR_OK;
 }

@@ -333,14 +333,14 @@ __device__ df eval_loglik_grad(const uint2* prog, int ninstr, const GradSmem& ws
     __syncwarp();
     float s = 0.0f;
     bool bad = false;
-    const int npass = (p.nd + 32 * K - 1) / (32 * K);
+    const int npass = (dv.nd + 32 * K - 1) / (32 * K);
 #pragma unroll 1
     for (int pass = 0; pass < npass && !bad; ++pass) {
         float x[NV][K], adj[K];
         const int base = pass * 32 * K + lane;
         const uint32_t valid = load_points<K, NV>(dv, p, base, x);
         forward_tape<K, NV>(prog, ninstr, ws.match, x, tape);
-        pts += min(32 * K, p.nd - pass * 32 * K);
+        pts += min(32 * K, dv.nd - pass * 32 * K);
         const Row<K> fres = tape[ninstr - 2];
 #pragma unroll
         for (int k = 0; k < K; ++k) {
@@ -371,7 +371,7 @@ __device__ df eval_loglik_grad(const uint2* prog, int ninstr, const GradSmem& ws
     if (bad) return df_make(-INFINITY, 0.0f);
     df S = warp_sum_df(df_make(s, 0.0f));
     if (!isfinite(S.hi)) return df_make(-INFINITY, 0.0f);
-    return df_sub(df_neg(S), df_make(p.normsum_hi, p.normsum_lo));
+    return df_sub(df_neg(S), df_make(dv.ns_hi, dv.ns_lo));
 }
 
 /* d/dc of lcauchypdf(c, 1) (main.cu:303-305). */
@@ -402,7 +402,7 @@ __device__ __forceinline__ uint8_t* grad_dataset(uint8_t* smem, const KParams& p
     float* fx = (float*)(smem + 16);
     dv = data_view(p, fx, STREAM);
     if (STREAM) return smem + 16;
-    stage_dataset(fx, (uint64_t*)smem, p);
+    stage_dataset(fx, (uint64_t*)smem, p, dv);
     return smem + 16 + align16((size_t)data_arrays(p) * p.nd_pad * 4);
 }
 
@@ -417,6 +417,7 @@ __global__ void __launch_bounds__(128) loglik_grad_kernel(const __grid_constant_
     const GradSmem ws = carve_grad(wbase + (size_t)warp * grad_warp_bytes(p.PL, p.max_instr), p.PL, p.max_instr);
     const int chain = blockIdx.x * (blockDim.x >> 5) + warp;
     if (chain >= p.N) return;
+    if (p.nds > 0) dv = data_view(p, nullptr, true, chain_dataset(p, chain));   /* batched: streamed */
     const int PL = p.PL;
     for (int i = lane; i < PL; i += 32) {
         const int o = p.P[(size_t)i * p.N + chain];
@@ -448,6 +449,7 @@ __global__ void __launch_bounds__(128) mh_hmc_kernel(const __grid_constant__ KPa
     const GradSmem ws = carve_grad(wbase + (size_t)warp * grad_warp_bytes(p.PL, p.max_instr), p.PL, p.max_instr);
     const int PL = p.PL;
     const bool adapt = p.chain_scale && p.adapt_target > 0.0f;
+    const uint32_t seed = p.seed_src ? p.seed_src[p.seed_index] : p.seed;
     const float unscale = (float)GPR_DF_UNSCALE;
 
 #pragma unroll 1
@@ -456,6 +458,7 @@ __global__ void __launch_bounds__(128) mh_hmc_kernel(const __grid_constant__ KPa
         if (lane == 0) chain = atomicAdd(p.next_chain, 1);
         chain = __shfl_sync(FULLMASK, chain, 0);
         if (chain >= p.N) break;
+        if (p.nds > 0) dv = data_view(p, nullptr, true, chain_dataset(p, chain));   /* batched: streamed */
 
         for (int i = lane; i < PL; i += 32) {
             const int o = p.P[(size_t)i * p.N + chain];
@@ -465,9 +468,9 @@ __global__ void __launch_bounds__(128) mh_hmc_kernel(const __grid_constant__ KPa
         __syncwarp();
 
         Rng r;
-        r.key0 = p.seed; r.key1 = (uint32_t)chain; r.blk = 0xffffffffu; r.drawn = 0;
+        r.key0 = seed; r.key1 = (uint32_t)chain; r.blk = 0xffffffffu; r.drawn = 0;
         r.w0 = r.w1 = r.w2 = r.w3 = 0u;
-        r.s = (RNG == 0) ? ((p.seed + (uint32_t)chain) & 0x7fffffffu) : 0u;
+        r.s = (RNG == 0) ? ((seed + (uint32_t)chain) & 0x7fffffffu) : 0u;
 
         /* leapfrog step: the configured one or this chain's own; with
          * adaptation, dual averaging of log(step) toward the target acceptance
@@ -536,7 +539,7 @@ __global__ void __launch_bounds__(128) mh_hmc_kernel(const __grid_constant__ KPa
                     float* q = ws.Cs[ccur ^ 1];
                     float k0 = 0.0f;
                     for (int i = lane; i < PL; i += 32) {
-                        const float m = hmc_momentum(p.seed, (uint32_t)chain, (uint32_t)step, (uint32_t)i);
+                        const float m = hmc_momentum(seed, (uint32_t)chain, (uint32_t)step, (uint32_t)i);
                         k0 = fmaf(m, m, k0);
                         ws.mom[i] = __fadd_rn(m, __fmul_rn(heps, ws.gcur[i]));
                         q[i] = q0[i];

@@ -37,6 +37,21 @@ struct KParams {
     const float* dx2;  /* multivariate data: the second and third input variables */
     const float* dx3;
     int nv;            /* input variables: 1, or 3 for x1, x2, x3 (0 reads as 1) */
+    /* batched data (nds > 0): dataset d is points [ds_off[d], ds_off[d] + ds_n[d])
+     * of the arrays (offsets multiples of 4), with normalising sum ds_ns[2d],
+     * ds_ns[2d+1] (2^-64 scale, double-float); chain c belongs to dataset
+     * c / chains_per_ds; chain groups are claimed dataset by dataset in the
+     * order ds_order (largest first); nd / nd_pad then give the largest */
+    int nds;
+    int chains_per_ds;
+    const int* ds_off;
+    const int* ds_n;
+    const float* ds_ns;
+    const int* ds_order;
+    /* captured block sequences: the block's seed is seed_src[seed_index]
+     * (device memory) when seed_src is set, else seed */
+    const uint32_t* seed_src;
+    int seed_index;
     int nd;
     int nd_pad;        /* multiple of 4                                       */
     float normsum_hi, normsum_lo;  /* 2^-64 * sum_d 0.5*(logf(2 PIf) + 2 logf(sd_d)), double-float */

@@ -659,6 +659,8 @@ struct DataView {
     const float* x[3];
     const float* y;
     const float* w;
+    int nd, nd_pad;           /* points, and the padded array length       */
+    float ns_hi, ns_lo;       /* 2^-64 * its normalising sum, double-float */
 };
 
 /* This lane's K points of one pass: the NV input variables, and which points
@@ -670,7 +672,7 @@ __device__ __forceinline__ uint32_t load_points(const DataView& dv, const KParam
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         const int i = base + 32 * k;
-        const bool v = i < p.nd;
+        const bool v = i < dv.nd;
 #pragma unroll
         for (int j = 0; j < NV; ++j) x[j][k] = v ? dv.x[j][i] : 0.0f;
         valid |= (v ? 1u : 0u) << k;
@@ -706,7 +708,7 @@ __device__ __forceinline__ float eval_pass(const uint2* prog, float* stk, float*
         valid = load_points<K, NV>(dv, p, base, x);
     }
     run_program<K, ROLLED, NV>(prog, x, acc, stk, scr, lane);
-    pts += ONEPASS ? p.nd : min(32 * K, p.nd - pass * 32 * K);
+    pts += ONEPASS ? dv.nd : min(32 * K, dv.nd - pass * 32 * K);
     float s = 0.0f;
     bad = false;
 #pragma unroll
@@ -735,7 +737,7 @@ __device__ __forceinline__ df eval_loglik(const uint2* prog, float* stk, float* 
     bool bad = false;
     const float* sy = dv.y;
     const float* sw = dv.w;
-    const int npass = ONEPASS ? 1 : (p.nd + 32 * K - 1) / (32 * K);
+    const int npass = ONEPASS ? 1 : (dv.nd + 32 * K - 1) / (32 * K);
 #pragma unroll 1
     for (int pass = 0; pass < npass; ++pass) {
         float x[NV][K], acc[K];
@@ -749,7 +751,7 @@ __device__ __forceinline__ df eval_loglik(const uint2* prog, float* stk, float* 
             valid = load_points<K, NV>(dv, p, base, x);
         }
         run_program<K, ROLLED, NV>(prog, x, acc, stk, scr, lane);
-        pts += ONEPASS ? p.nd : min(32 * K, p.nd - pass * 32 * K);
+        pts += ONEPASS ? dv.nd : min(32 * K, dv.nd - pass * 32 * K);
 #pragma unroll
         for (int k = 0; k < K; ++k) {
             if (valid & (1u << k)) {
@@ -764,7 +766,7 @@ __device__ __forceinline__ df eval_loglik(const uint2* prog, float* stk, float* 
     }
     df S = warp_sum_df(df_make(s, 0.0f));
     if (!isfinite(S.hi)) return df_make(-INFINITY, 0.0f);
-    return df_sub(df_neg(S), df_make(p.normsum_hi, p.normsum_lo));
+    return df_sub(df_neg(S), df_make(dv.ns_hi, dv.ns_lo));
 }
 
 /* Sum over all constants of lcauchypdf(C, 1) (main.cu:303-305, 537-540), each
@@ -941,31 +943,54 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) {
  * multivariate data. */
 __host__ __device__ __forceinline__ int data_arrays(const KParams& p) { return p.nv == 3 ? 5 : 3; }
 
-/* The dataset arrays in the order they are staged. */
+/* The dataset arrays in the order they are staged (device memory). */
 __device__ __forceinline__ const float* data_src(const KParams& p, int a) {
     return a == 0 ? p.dx : a == 1 ? p.dy : a == 2 ? p.dw : a == 3 ? p.dx2 : p.dx3;
 }
 
-/* The view of a dataset staged at dst (arrays of nd_pad floats, staging order)
- * or, streamed, of the device arrays. */
-__device__ __forceinline__ DataView data_view(const KParams& p, const float* dst, bool streamed) {
+/* Batched data (p.nds > 0): the dataset of chain `chain`. */
+__device__ __forceinline__ int chain_dataset(const KParams& p, int chain) {
+    return p.nds > 0 ? chain / p.chains_per_ds : -1;
+}
+
+/* The view of dataset d (-1: the single dataset): staged at dst (arrays of
+ * nd_pad floats, staging order; the region is sized for the largest dataset),
+ * or, streamed, the device arrays at the dataset's offset. */
+__device__ __forceinline__ DataView data_view(const KParams& p, const float* dst, bool streamed, int d = -1) {
     DataView dv;
-    if (streamed) {
-        dv.x[0] = p.dx; dv.y = p.dy; dv.w = p.dw; dv.x[1] = p.dx2; dv.x[2] = p.dx3;
+    size_t off = 0;
+    if (d < 0) {
+        dv.nd = p.nd; dv.nd_pad = p.nd_pad; dv.ns_hi = p.normsum_hi; dv.ns_lo = p.normsum_lo;
     } else {
-        const size_t n = (size_t)p.nd_pad;
+        off = (size_t)p.ds_off[d];
+        dv.nd = p.ds_n[d]; dv.nd_pad = (dv.nd + 3) & ~3;
+        dv.ns_hi = p.ds_ns[2 * d]; dv.ns_lo = p.ds_ns[2 * d + 1];
+    }
+    if (streamed) {
+        dv.x[0] = p.dx + off; dv.y = p.dy + off; dv.w = p.dw + off;
+        dv.x[1] = p.dx2 ? p.dx2 + off : nullptr; dv.x[2] = p.dx3 ? p.dx3 + off : nullptr;
+    } else {
+        const size_t n = (size_t)dv.nd_pad;
         dv.x[0] = dst; dv.y = dst + n; dv.w = dst + 2 * n; dv.x[1] = dst + 3 * n; dv.x[2] = dst + 4 * n;
     }
     return dv;
 }
 
-/* Stage the dataset into dst with one bulk TMA copy per array; bounded wait. */
-static __device__ void stage_dataset(float* dst, uint64_t* bar, const KParams& p) {
-    const uint32_t bytes = (uint32_t)p.nd_pad * 4u;
-    if (bytes == 0) return;
+/* Stage the dataset into dst with one bulk TMA copy per array; bounded wait.
+ * dv: the view it is staged for (its nd_pad); d: the dataset (-1: the single
+ * one).  Re-staging for another dataset (reinit) invalidates and
+ * re-initialises the barrier, so every thread must have left the previous
+ * wait (a __syncthreads) before.  Returns false, the same in every thread of
+ * the CTA, when the copy did not complete within the wait's limit. */
+static __device__ bool stage_dataset(float* dst, uint64_t* bar, const KParams& p, const DataView& dv, int d = -1,
+                                     bool reinit = false) {
+    const uint32_t bytes = (uint32_t)dv.nd_pad * 4u;
+    if (bytes == 0) return true;
+    const size_t off = d < 0 ? 0 : (size_t)p.ds_off[d];
     const int na = data_arrays(p);
     if (threadIdx.x == 0) {
         uint32_t b = smem_u32(bar);
+        if (reinit) asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(b) : "memory");
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -973,7 +998,7 @@ static __device__ void stage_dataset(float* dst, uint64_t* bar, const KParams& p
                      : "memory");
         for (int a = 0; a < na; ++a)
             asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                         ::"r"(smem_u32(dst + (size_t)a * p.nd_pad)), "l"(data_src(p, a)), "r"(bytes), "r"(b)
+                         ::"r"(smem_u32(dst + (size_t)a * dv.nd_pad)), "l"(data_src(p, a) + off), "r"(bytes), "r"(b)
                          : "memory");
     }
     __syncthreads();
@@ -986,6 +1011,7 @@ static __device__ void stage_dataset(float* dst, uint64_t* bar, const KParams& p
                      : "=r"(done) : "r"(b), "r"(0u) : "memory");
     }
     if (!done) atomicOr(p.err, 1);
+    return !__syncthreads_or(!done);
 }
 
 /* The accept rule of main.cu:728-740 / 790-802, in its exact evaluation order:
@@ -1064,14 +1090,18 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
 
-    /* CTA-shared dataset (or the device arrays when streamed) */
+    /* CTA-shared dataset (or the device arrays when streamed); with batched
+     * data, the dataset of the current chain group (staged per group) */
     uint64_t* bar = (uint64_t*)smem;
     float* fx = (float*)(smem + 16);
-    const DataView dv = data_view(p, fx, STREAM);
+    const bool batched = p.nds > 0;
+    DataView dv = data_view(p, fx, STREAM);
+    int staged_ds = -1;
+    bool bar_live = false;   /* the barrier has been initialised (batched restaging) */
     uint8_t* wbase = smem + 16;
     if (!STREAM) {
         wbase += align16((size_t)data_arrays(p) * p.nd_pad * 4);
-        stage_dataset(fx, bar, p);
+        if (!batched) stage_dataset(fx, bar, p, dv);
     }
     const size_t wbytes = warp_smem_bytes(p.PL, p.max_instr, p.levels, K);
     const WarpSmem ws = carve_warp<K>(wbase + (size_t)warp * wbytes, p.PL, p.max_instr, p.levels);
@@ -1082,13 +1112,14 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
 #pragma unroll
         for (int k = 0; k < K; ++k) {
             int i = lane + 32 * k;
-            bool v = i < p.nd;
+            bool v = i < dv.nd;
             ld.x[k] = v ? dv.x[0][i] : 0.0f;
             ld.valid |= (v ? 1u : 0u) << k;
         }
     }
     const int PL = p.PL;
     const LaneJump ljump = make_lane_jump(p, lane);
+    const uint32_t seed = p.seed_src ? p.seed_src[p.seed_index] : p.seed;
 
     __shared__ int s_group_base;
     const int nwarps = blockDim.x >> 5;
@@ -1102,8 +1133,8 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
     __shared__ int s_next;
     __shared__ float s_part_hi[8][GPR_MAX_PASSES];
     __shared__ float s_part_lo[8][GPR_MAX_PASSES];
-    const int npass = ONEPASS ? 1 : (p.nd + 32 * K - 1) / (32 * K);
-    const bool balanced = p.lockstep == 1 && npass <= GPR_MAX_PASSES;
+    int npass = ONEPASS ? 1 : (dv.nd + 32 * K - 1) / (32 * K);
+    bool balanced = p.lockstep == 1 && npass <= GPR_MAX_PASSES;
 
 #pragma unroll 1
     for (;;) {
@@ -1112,11 +1143,28 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
             /* CTA-wide chain groups: every warp of the CTA runs the same step at
              * the same time, so the warps share instruction-cache lines */
             __syncthreads();
-            if (threadIdx.x == 0) s_group_base = atomicAdd(p.next_chain, nwarps);
+            if (threadIdx.x == 0) {
+                int b = atomicAdd(p.next_chain, nwarps);
+                /* batched: claim groups in the host's order, largest datasets first */
+                if (batched && b < p.N) b = p.ds_order[b / p.chains_per_ds] * p.chains_per_ds + b % p.chains_per_ds;
+                s_group_base = b;
+            }
             __syncthreads();
             const int base = s_group_base;
             if (base >= p.N) break;
             chain = base + warp;
+            if (batched) {
+                const int d = chain_dataset(p, base);   /* a group never straddles datasets */
+                if (d != staged_ds) {
+                    dv = data_view(p, fx, STREAM, d);
+                    /* a copy that did not arrive leaves the CTA (the error flag is set) */
+                    if (!STREAM && !stage_dataset(fx, bar, p, dv, d, bar_live)) break;
+                    bar_live = bar_live || dv.nd_pad > 0;
+                    staged_ds = d;
+                    npass = (dv.nd + 32 * K - 1) / (32 * K);
+                    balanced = p.lockstep == 1 && npass <= GPR_MAX_PASSES;
+                }
+            }
         } else {
             if (lane == 0) chain = atomicAdd(p.next_chain, 1);
             chain = __shfl_sync(FULLMASK, chain, 0);
@@ -1142,9 +1190,9 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
         df forward = df_make(0.f, 0.f), backward = df_make(0.f, 0.f);
 
         Rng r;
-        r.key0 = p.seed; r.key1 = (uint32_t)chain; r.blk = 0xffffffffu; r.drawn = 0;
+        r.key0 = seed; r.key1 = (uint32_t)chain; r.blk = 0xffffffffu; r.drawn = 0;
         r.w0 = r.w1 = r.w2 = r.w3 = 0u;
-        r.s = (RNG == 0) ? ((p.seed + (uint32_t)chain) & 0x7fffffffu) : 0u;   /* rx = random_seed + idx */
+        r.s = (RNG == 0) ? ((seed + (uint32_t)chain) & 0x7fffffffu) : 0u;   /* rx = random_seed + idx */
         /* random-walk scale: the configured one, or this chain's own (adapted) */
         float rw_sd = (p.chain_scale && active) ? p.chain_scale[chain] : p.rw_sd;
         float log_sd = logf(rw_sd);
@@ -1243,7 +1291,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                     if (anybad) s_bad[w] = 1;
                 }
                 st_np += (unsigned long long)(s_count[w] + 4) *
-                         (unsigned)(ONEPASS ? p.nd : min(32 * K, p.nd - pass * 32 * K));
+                         (unsigned)(ONEPASS ? dv.nd : min(32 * K, dv.nd - pass * 32 * K));
             }
             __syncthreads();
             if (active) {
@@ -1253,7 +1301,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                     df S = df_make(0.0f, 0.0f);
                     for (int q = 0; q < npass; ++q) S = df_add(S, df_make(s_part_hi[warp][q], s_part_lo[warp][q]));
                     lik = !isfinite(S.hi) ? df_make(-INFINITY, 0.0f)
-                                          : df_sub(df_neg(S), df_make(p.normsum_hi, p.normsum_lo));
+                                          : df_sub(df_neg(S), df_make(dv.ns_hi, dv.ns_lo));
                 }
             }
           } else if (active) {

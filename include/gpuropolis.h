@@ -87,6 +87,28 @@ int gpr_set_data(gpr_handle* h, const float* x, const float* y, const float* sd,
 int gpr_set_data3(gpr_handle* h, const float* x1, const float* x2, const float* x3, const float* y,
                   const float* sd, int n);
 
+/* Batched data (no reference counterpart; the reference runs one dataset per
+ * process, main.cu:1143): n_datasets datasets in one launch, dataset d of
+ * sizes[d] points, the points concatenated in dataset order in x1 (and x2,
+ * x3 for three variables), y and sd.  The handle's chains split evenly:
+ * chain c fits dataset c / (n_chains / n_datasets), so n_chains must be a
+ * multiple of n_datasets.  Each chain's prior, likelihood and moves are
+ * exactly those of a handle holding its dataset alone (gpr_set_data).
+ * gpr_set_data / gpr_set_data3 return the handle to a single dataset. */
+int gpr_set_batched_data(gpr_handle* h, int n_datasets, const int* sizes, const float* x1, const float* x2,
+                         const float* x3, const float* y, const float* sd);
+
+/* Captured block sequence (no reference counterpart; it replaces the host
+ * loop's launches, main.cu:1156-1239): records n_blocks MH blocks of `steps`
+ * steps each, with the handle's current data, layout and moves, as one CUDA
+ * graph.  gpr_run_captured(h, seeds) replays it with seeds[0..n_blocks) as
+ * the blocks' random seeds (copied to the device inside the replay), with the
+ * chains identical to n_blocks gpr_run_block calls with those seeds; it waits
+ * for the previous replay to finish before writing the seeds.  Changing the
+ * data, layout or moves drops the capture (GPR_ERR_STATE on replay). */
+int gpr_capture_blocks(gpr_handle* h, int n_blocks, int steps);
+int gpr_run_captured(gpr_handle* h, const int* seeds);
+
 /* Upload chain state in the reference layout (main.cu:1144-1145, 1233-1234).
  * P holds program_length*N ints, C program_length*N floats (host memory). */
 int gpr_set_state(gpr_handle* h, const int32_t* P, const float* C);
