@@ -45,6 +45,10 @@ WORKLOADS = {
     # three input variables, 65536 points read from device memory in every pass
     "streamed-3var-16k": dict(N=16384, PL=127, nd=65536, data="multivar", ops="multi", rw_sd=0.1,
                               mh_steps=20, map_delta=0.0, blocks=1),
+    # 256 datasets of uneven size (log-uniform in [8, 4096] points), 512 chains
+    # each, in one launch; blocks replayed from a captured graph
+    "batched-256ds-131k": dict(N=131072, PL=47, nds=256, data="batched", ops="basic", rw_sd=0.1,
+                               mh_steps=200, blocks=5),
     # Hamiltonian moves on 8192 chains of the rational model: the case ncu captures
     "hmc-rational-8k-profile": dict(N=8192, PL=31, nd=1024, data="rational", ops="basic", rw_sd=0.0,
                                     mh_steps=20, map_delta=0.0, blocks=1),
@@ -359,6 +363,164 @@ def run_streamed(args, w):
                    "ops": "{+,-,*,/,sin,cos,exp,x1,x2,x3,const}", "launch": geo}}))
 
 
+def batched_datasets(g, nds, seed=2024):
+    """nds datasets: sizes log-uniform in [8, 4096], x ~ U[-5, 5], y = f(x) +
+    N(0, 0.01 std f(x)) with f a program of 3-15 nodes drawn from the prior
+    over the op set {+,-,*,/,exp,log,pow,x,const} (heap of 15 nodes, ops
+    uniform, Cauchy(0, 1) constants), redrawn until it is finite and not
+    constant on the dataset's x.  f is evaluated by the library's own
+    evaluator.  Returns the datasets and the generating programs."""
+    r = np.random.default_rng(seed)
+    sizes = np.round(np.exp(r.uniform(np.log(8), np.log(4096), nds))).astype(int)
+    M, PLg = 64, 15
+    ev = g.Sampler(M, program_length=PLg, ops=H.OPSET_BASIC)
+    out, gens = [], []
+    try:
+        for d in range(nds):
+            x = r.uniform(-5, 5, sizes[d]).astype(np.float32)
+            while True:
+                P, _ = H.random_programs(M, PLg, ops=H.OPSET_BASIC, seed=int(r.integers(1 << 30)),
+                                         shallow_frac=1.0)
+                C = r.standard_cauchy((PLg, M)).astype(np.float32)
+                ev.set_state(P, C)
+                vals, _, count = ev.eval_values(x)
+                with np.errstate(all="ignore"):
+                    sdv = np.std(vals.astype(np.float64), axis=1)
+                    ok = ((count >= 3) & (count <= 15) & np.all(np.isfinite(vals), axis=1)
+                          & (np.max(np.abs(vals), axis=1) < 1e6) & (sdv > 1e-3))
+                if ok.any():
+                    c = int(np.argmax(ok))
+                    break
+            f = vals[c].astype(np.float64)
+            noise = 0.01 * sdv[c]
+            y = (f + r.normal(0, noise, sizes[d])).astype(np.float32)
+            out.append((x, y, np.full(sizes[d], noise, np.float32)))
+            gens.append((P[:, c].copy(), C[:, c].copy(), int(count[c])))
+    finally:
+        ev.close()
+    return out, gens
+
+
+def run_batched(args, w):
+    """Batched uneven workload: 256 independent datasets (sizes log-uniform in
+    [8, 4096] points), 512 chains each (131072 chains), PROGRAM_LENGTH 47, op
+    set {+,-,*,/,exp,log,pow,x,const}, random-walk constants (sd 0.1) with the
+    reference's structure moves; the layout picked by the autotuner; one
+    timed step = one replay of a captured graph of 5 MH blocks of 200 steps
+    (1000 MH steps per chain).  Beside it, the same chains run as 256
+    separate handles (one launch per dataset per block)."""
+    import torch
+    import gpuropolis_gb300 as g
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    N, PL, nds, steps, nb = w["N"], w["PL"], w["nds"], w["mh_steps"], w["blocks"]
+    cpd = N // nds
+    sets, gens = batched_datasets(g, nds)
+    sizes = np.array([len(d[0]) for d in sets])
+    P0, C0 = H.random_programs(N, PL, ops=H.OPSET_BASIC, seed=99, shallow_frac=0.0)
+    s = g.Sampler(N, program_length=PL, ops=H.OPSET_BASIC, rng=g.RNG_LCG, const_proposal=g.CONST_RANDOM_WALK,
+                  rw_sd=w["rw_sd"], stream=stream.cuda_stream)
+    s.set_batched_data(sets)
+    s.set_state(P0, C0)
+    default_geo = s.launch_geometry()
+    for i in range(args.warmup):
+        s.run_block(steps, 11 + i)
+    tuned = None if args.no_autotune else s.autotune(steps=50, seed=4242)
+    geo = s.launch_geometry()
+    s.capture_blocks(nb, steps)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    s.run_captured([5 + b for b in range(nb)])   # the first replay uploads the graph
+    torch.cuda.synchronize()
+    s.reset_stats()
+    launches0 = s.launch_count()
+    evs = []
+    clk = ClockSampler(os.path.join(ROOT, "gpurun_out", "clocks_batched.csv")
+                       if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp/gpr_clocks_b.csv")
+    with clk:
+        for i in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            s.run_captured([1000 * (i + 1) + b for b in range(nb)])
+            e1.record(stream)
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
+    ms = float(sum(a.elapsed_time(b) for a, b in evs))
+    st = s.stats()
+    launches = s.launch_count() - launches0
+    value = N * steps * nb * args.steps / (ms / 1e3)
+
+    # end to end through the C ABI: pinned host state in, replay, state out
+    Ph = torch.empty((PL, N), dtype=torch.int32, pin_memory=True).numpy()
+    Ch = torch.empty((PL, N), dtype=torch.float32, pin_memory=True).numpy()
+    prh = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
+    lih = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
+    lib, ptr = s.lib, (lambda a: a.ctypes.data_as(g.ctypes.c_void_p))
+    lib.gpr_get_state(s.h, ptr(Ph), ptr(Ch), ptr(prh), ptr(lih))
+    seeds = np.arange(nb, dtype=np.int32) + 77
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_steps = max(1, min(args.steps, 2))
+    for i in range(e2e_steps):
+        lib.gpr_set_state(s.h, ptr(Ph), ptr(Ch))
+        lib.gpr_run_captured(s.h, ptr(seeds + i))
+        lib.gpr_get_state(s.h, ptr(Ph), ptr(Ch), ptr(prh), ptr(lih))
+    e2e = N * steps * nb * e2e_steps / (time.perf_counter() - t0)
+    Pw, Cw, _, _ = s.get_state()
+    s.close()
+
+    # the same chains as 256 separate handles, one block each, one launch per dataset
+    hs = []
+    try:
+        for d in range(nds):
+            h = g.Sampler(cpd, program_length=PL, ops=H.OPSET_BASIC, rng=g.RNG_LCG,
+                          const_proposal=g.CONST_RANDOM_WALK, rw_sd=w["rw_sd"], stream=stream.cuda_stream)
+            h.set_data(*sets[d])
+            h.set_state(Pw[:, d * cpd:(d + 1) * cpd], Cw[:, d * cpd:(d + 1) * cpd])
+            hs.append(h)
+        for h in hs:
+            h.run_block(steps, 3)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for h in hs:
+            h.run_block(steps, 4)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        sep = N * steps / (e0.elapsed_time(e1) / 1e3)
+    finally:
+        for h in hs:
+            h.close()
+
+    peaks = measured_peaks()
+    props = torch.cuda.get_device_properties(dev)
+    peak_tops = props.multi_processor_count * 128 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+    achieved = st["eval_node_points"] / (ms / 1e3) / 1e12
+    print(json.dumps({
+        "metric": "MH chain-steps/s, batched uneven datasets", "value": value, "unit": "chain-steps/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded)",
+        "point_evals_per_s": st["eval_points"] / (ms / 1e3),
+        "separate_handles": {"chain_steps_per_s": sep, "launches_per_block": nds,
+                             "batched_over_separate": value / sep},
+        "e2e": {"value": e2e, "unit": "chain-steps/s", "h2d_bytes_per_step": Ph.nbytes + Ch.nbytes,
+                "d2h_bytes_per_step": Ph.nbytes + Ch.nbytes + prh.nbytes + lih.nbytes, "steps": e2e_steps},
+        "gpu_launches": launches,
+        "roofline": {"bound": "fp32-issue", "achieved": achieved, "peak": peak_tops, "unit": "T-ops/s",
+                     "frac": achieved / peak_tops, "traffic": None},
+        "acceptance": {"structure": st["struct_accepted"] / max(1, st["struct_proposed"]),
+                       "constant": st["const_accepted"] / max(1, st["const_proposed"])},
+        "clocks": clk.summary(0),
+        "config": {"workload": args.workload, "N": N, "PL": PL, "datasets": nds, "chains_per_dataset": cpd,
+                   "points": {"total": int(sizes.sum()), "min": int(sizes.min()), "max": int(sizes.max()),
+                              "median": float(np.median(sizes))},
+                   "generator_nodes": {"min": min(c for _, _, c in gens), "max": max(c for _, _, c in gens)},
+                   "mh_steps_per_block": steps, "blocks_per_replay": nb, "rng": "lcg",
+                   "const_proposal": "rw:%g" % w["rw_sd"], "l2": "flushed between replays (256 MB write)",
+                   "launch_default": default_geo, "launch": geo, "autotuned": tuned}}))
+
+
 def cpu_reference_rate(w, P, C, x, y, sd, target_s=12.0, threads=0, chains=None):
     """chain-steps/s of the reference's own code (or its restatement) on the
     host cores, measured on chains [0, S) of the given state, S sized to
@@ -566,6 +728,9 @@ def main():
         return
     if args.workload == "streamed-3var-16k":
         run_streamed(args, w)
+        return
+    if args.workload == "batched-256ds-131k":
+        run_batched(args, w)
         return
     if args.impl == "reference":
         if int(os.environ.get("RANK", "0")) != 0:

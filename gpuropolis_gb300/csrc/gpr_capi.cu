@@ -716,12 +716,20 @@ int gpr_autotune(gpr_handle* h, int steps, int seed, int* K, int* onepass, int* 
     unsigned long long* sSt = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     int rc = GPR_OK;
-    struct Cand { int K, onepass, rolled; } cands[8];
+    /* staged layouts, then (unless the handle always streams) the streamed one,
+     * which reads the data from device memory / L2 and leaves shared memory to
+     * the warps; batched data and three variables take multi-pass layouts only */
+    struct Cand { int K, onepass, rolled, stream; } cands[10];
     int nc = 0;
+    const int saved_stream = h->stream_data;
+    const bool multi_only = h->kp.nds > 0 || h->kp.nv == 3;
     for (int Kc : {4, 8})
         for (int op = 1; op >= 0; --op)
             for (int ro = 0; ro <= 1; ++ro)
-                if (!op || h->nd <= 32 * Kc) cands[nc++] = {Kc, op, ro};
+                if ((!op || (h->nd <= 32 * Kc && !multi_only)) && !(h->kp.nv == 3 && Kc != 4))
+                    cands[nc++] = {Kc, op, ro, saved_stream};
+    if (!saved_stream)
+        for (int ro = 0; ro <= 1; ++ro) cands[nc++] = {4, 0, ro, 1};
     const gpr::LaunchCfg orig = h->lc;
     float best = 1e30f;
     gpr::LaunchCfg bestlc = orig;
@@ -763,7 +771,10 @@ int gpr_autotune(gpr_handle* h, int steps, int seed, int* K, int* onepass, int* 
         nc = 0;
     }
     for (int i = 0; i < nc; ++i) {
-        if (configure_launch(h, cands[i].K, cands[i].onepass, cands[i].rolled) != GPR_OK) continue;
+        h->stream_data = cands[i].stream;
+        const int crc = configure_launch(h, cands[i].K, cands[i].onepass, cands[i].rolled);
+        h->stream_data = saved_stream;
+        if (crc != GPR_OK || (cands[i].stream && !h->lc.stream)) continue;
         for (int rep = 0; rep < 2; ++rep) {   /* first run warms up, second is timed */
             AT_TRY(cudaMemcpyAsync(h->dP, sP, cnt * sizeof(int32_t), cudaMemcpyDeviceToDevice, h->stream));
             AT_TRY(cudaMemcpyAsync(h->dC, sC, cnt * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
@@ -784,7 +795,10 @@ int gpr_autotune(gpr_handle* h, int steps, int seed, int* K, int* onepass, int* 
         for (int pi = 0; pi < 3; ++pi)
             for (int wi = 0; wi < 2; ++wi) {
                 if (periods[pi] == base.lockstep && wpcs[wi] == base.warps_per_cta) continue;
-                if (configure_launch(h, base.K, base.onepass, base.rolled, periods[pi], wpcs[wi]) != GPR_OK) continue;
+                h->stream_data = base.stream ? 1 : saved_stream;
+                const int crc = configure_launch(h, base.K, base.onepass, base.rolled, periods[pi], wpcs[wi]);
+                h->stream_data = saved_stream;
+                if (crc != GPR_OK) continue;
                 for (int rep = 0; rep < 2; ++rep) {
                     AT_TRY(cudaMemcpyAsync(h->dP, sP, cnt * sizeof(int32_t), cudaMemcpyDeviceToDevice, h->stream));
                     AT_TRY(cudaMemcpyAsync(h->dC, sC, cnt * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));

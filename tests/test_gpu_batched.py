@@ -206,3 +206,65 @@ def test_captured_replay_over_batched_data():
     finally:
         a.close()
         b.close()
+
+
+@pytest.mark.parametrize("layout", [dict(K=8, onepass=0, rolled=0), dict(K=4, onepass=0, rolled=1),
+                                    dict(K=4, onepass=0, rolled=0, lockstep=5, warps_per_cta=4)],
+                         ids=["k8", "rolled", "lockstep5-wpc4"])
+def test_batched_layouts_equal_single_dataset_runs(layout):
+    kw = MODES["rw-philox"]
+    sets = _datasets([200, 33, 700], seed=17)
+    cpd = 64
+    N = cpd * len(sets)
+    P, C = g.host_init_chains(N, kw["program_length"], 21, ops=kw["ops"])
+    b = g.Sampler(N, **kw)
+    try:
+        b.set_batched_data(sets)
+        b.set_layout(**layout)
+        geo = b.launch_geometry()
+        assert geo["K"] == layout["K"] and geo["rolled"] == layout["rolled"]
+        b.set_state(P, C)
+        b.run_block(20, 5)
+        got = b.get_state()
+    finally:
+        b.close()
+    for d, ds in enumerate(sets):
+        s = g.Sampler(N, **kw)
+        try:
+            s.set_data(*ds)
+            s.set_layout(**{**layout, "lockstep": geo["lockstep"], "warps_per_cta": geo["warps_per_cta"]})
+            s.set_state(P, C)
+            s.run_block(20, 5)
+            lo, hi = d * cpd, (d + 1) * cpd
+            _same_state(_cols(got, lo, hi), _cols(s.get_state(), lo, hi), "dataset %d" % d)
+        finally:
+            s.close()
+
+
+@pytest.mark.parametrize("batched", [False, True])
+def test_autotune_leaves_the_state_and_sets_its_layout(batched):
+    """The autotuner's trial blocks (staged and streamed layouts) leave the
+    chains, scores and counters as they were, and the layout it reports is
+    the one the handle then runs."""
+    kw = MODES["rw-philox"]
+    N = 64 * 4
+    P, C = g.host_init_chains(N, kw["program_length"], 8, ops=kw["ops"])
+    s = g.Sampler(N, **kw)
+    try:
+        if batched:
+            s.set_batched_data(_datasets([90, 400, 12, 150], seed=2))
+        else:
+            s.set_data(*H.expdecay_data(250, seed=1))
+        s.set_state(P, C)
+        s.run_block(5, 1)
+        before, st0 = s.get_state(), s.stats()
+        t = s.autotune(steps=10, seed=3)
+        _same_state(before, s.get_state())
+        assert s.stats() == st0
+        geo = s.launch_geometry()
+        assert (geo["K"], geo["onepass"], geo["rolled"]) == (t["K"], t["onepass"], t["rolled"])
+        assert t["ms"] > 0
+        s.run_block(5, 2)
+        s.sync()
+    finally:
+        s.close()
