@@ -50,10 +50,14 @@ struct gpr_handle {
     int stream_data = 0;                   /* 1: always stream the dataset       */
     int* dds = nullptr;                    /* batched data: off | n | order      */
     float* dds_ns = nullptr;               /* batched data: normalising sums     */
-    /* a captured block sequence (gpr_capture_blocks) */
+    /* a captured block sequence (gpr_capture_blocks): the graph, and per block
+     * its kernel node with the node's launch parameters (the seed is set per
+     * replay) */
+    cudaGraph_t graph_src = nullptr;
     cudaGraphExec_t graph = nullptr;
-    uint32_t* dseeds = nullptr;
-    uint32_t* hseeds = nullptr;            /* pinned                             */
+    std::vector<cudaGraphNode_t> graph_nodes;
+    std::vector<cudaKernelNodeParams> graph_params;
+    std::vector<gpr::KParams> graph_kp;
     int graph_blocks = 0;
     unsigned long long* dkeys = nullptr;   /* N posterior keys                   */
     unsigned long long* dsel = nullptr;    /* [0] selected key                   */
@@ -130,7 +134,7 @@ static void free_all(gpr_handle* h) {
     cudaFree(h->dkeys); cudaFree(h->dsel); cudaFree(h->dseli); cudaFree(h->dtop); cudaFree(h->dscale);
     cudaFree(h->dds); cudaFree(h->dds_ns);
     if (h->graph) cudaGraphExecDestroy(h->graph);
-    cudaFree(h->dseeds); cudaFreeHost(h->hseeds);
+    if (h->graph_src) cudaGraphDestroy(h->graph_src);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
 }
 
@@ -274,6 +278,8 @@ int gpr_destroy(gpr_handle* h) {
  * data, layout or moves drops it. */
 static void drop_graph(gpr_handle* h) {
     if (h->graph) { cudaStreamSynchronize(h->stream); cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+    if (h->graph_src) { cudaGraphDestroy(h->graph_src); h->graph_src = nullptr; }
+    h->graph_nodes.clear(); h->graph_params.clear(); h->graph_kp.clear();
     h->graph_blocks = 0;
 }
 
@@ -334,7 +340,8 @@ static int configure_launch(gpr_handle* h, int K, int onepass, int rolled, int l
     drop_graph(h);
     gpr::LaunchCfg lc;
     lc.carveout = 0;
-    if (kp.nds > 0) {   /* batched: CTA groups within one dataset, staged per group */
+    if (kp.nds > 0) {   /* batched: CTA groups within one dataset, staged per group; K = 4 in passes */
+        K = 4;
         onepass = 0;
         if (lockstep < 1) lockstep = 1;
         wpc0 = batched_wpc(kp, wpc0);
@@ -523,33 +530,50 @@ int gpr_capture_blocks(gpr_handle* h, int n_blocks, int steps) {
     if (h->nd < 0) return fail(h, GPR_ERR_STATE, "gpr_set_data has not been called");
     CUDA_TRY(h, cudaSetDevice(h->device));
     drop_graph(h);
-    cudaFree(h->dseeds); cudaFreeHost(h->hseeds);
-    h->dseeds = nullptr; h->hseeds = nullptr;
-    CUDA_TRY(h, cudaMalloc(&h->dseeds, (size_t)n_blocks * sizeof(uint32_t)));
-    CUDA_TRY(h, cudaMallocHost(&h->hseeds, (size_t)n_blocks * sizeof(uint32_t)));
-    memset(h->hseeds, 0, (size_t)n_blocks * sizeof(uint32_t));
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
-    cudaGraph_t g = nullptr;
+    /* one counter reset and one kernel node per block; after each block the
+     * capture's single frontier node is that block's kernel */
+    std::vector<cudaGraphNode_t> nodes;
     CUDA_TRY(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    cudaError_t e = cudaMemcpyAsync(h->dseeds, h->hseeds, (size_t)n_blocks * sizeof(uint32_t),
-                                    cudaMemcpyHostToDevice, h->stream);
     int rc = GPR_OK;
-    for (int b = 0; b < n_blocks && e == cudaSuccess && rc == GPR_OK; ++b) {
-        h->kp.seed_src = h->dseeds;
-        h->kp.seed_index = b;
+    cudaError_t e = cudaSuccess;
+    for (int b = 0; b < n_blocks && rc == GPR_OK && e == cudaSuccess; ++b) {
         rc = run(h, steps, 0);
+        if (rc != GPR_OK) break;
+        cudaStreamCaptureStatus cs;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t ndeps = 0;
+        e = cudaStreamGetCaptureInfo(h->stream, &cs, nullptr, nullptr, &deps, nullptr, &ndeps);
+        if (e == cudaSuccess && ndeps != 1) e = cudaErrorStreamCaptureUnmatched;
+        if (e == cudaSuccess) nodes.push_back(deps[0]);
     }
-    h->kp.seed_src = nullptr;
-    h->kp.seed_index = 0;
+    cudaGraph_t g = nullptr;
     const cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
     if (e == cudaSuccess) e = e2;
-    if (e == cudaSuccess && rc == GPR_OK) e = cudaGraphInstantiate(&h->graph, g, 0);
-    if (g) cudaGraphDestroy(g);
-    if (rc != GPR_OK) return rc;
-    if (e != cudaSuccess) {
-        h->graph = nullptr;
+    std::vector<cudaKernelNodeParams> params(nodes.size());
+    std::vector<gpr::KParams> kps(nodes.size());
+    for (size_t b = 0; b < nodes.size() && e == cudaSuccess && rc == GPR_OK; ++b) {
+        cudaGraphNodeType t;
+        e = cudaGraphNodeGetType(nodes[b], &t);
+        if (e == cudaSuccess && t != cudaGraphNodeTypeKernel) e = cudaErrorStreamCaptureUnmatched;
+        if (e == cudaSuccess) e = cudaGraphKernelNodeGetParams(nodes[b], &params[b]);
+        if (e == cudaSuccess) {   /* the kernels take one argument, the KParams */
+            kps[b] = *(const gpr::KParams*)params[b].kernelParams[0];
+            params[b].extra = nullptr;
+        }
+    }
+    cudaGraphExec_t ex = nullptr;
+    if (e == cudaSuccess && rc == GPR_OK) e = cudaGraphInstantiate(&ex, g, 0);
+    if (rc != GPR_OK || e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        if (rc != GPR_OK) return rc;
         return fail(h, GPR_ERR_CUDA, "gpr_capture_blocks: %s", cudaGetErrorString(e));
     }
+    h->graph_src = g;
+    h->graph = ex;
+    h->graph_nodes = std::move(nodes);
+    h->graph_params = std::move(params);
+    h->graph_kp = std::move(kps);
     h->graph_blocks = n_blocks;
     return GPR_OK;
 }
@@ -558,9 +582,16 @@ int gpr_run_captured(gpr_handle* h, const int* seeds) {
     if (!h || !seeds) return GPR_ERR_ARG;
     if (!h->graph) return fail(h, GPR_ERR_STATE, "no captured block sequence (gpr_capture_blocks)");
     CUDA_TRY(h, cudaSetDevice(h->device));
-    /* the previous replay may still be reading the pinned seeds */
-    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
-    for (int b = 0; b < h->graph_blocks; ++b) h->hseeds[b] = (uint32_t)seeds[b];
+    /* the seeds go into the kernel nodes' parameters: the update applies to
+     * launches after it, not to a replay already enqueued */
+    for (int b = 0; b < h->graph_blocks; ++b) {
+        gpr::KParams kp = h->graph_kp[b];
+        kp.seed = (uint32_t)seeds[b];
+        cudaKernelNodeParams np = h->graph_params[b];
+        void* args[] = {(void*)&kp};
+        np.kernelParams = args;
+        CUDA_TRY(h, cudaGraphExecKernelNodeSetParams(h->graph, h->graph_nodes[b], &np));
+    }
     CUDA_TRY(h, cudaGraphLaunch(h->graph, h->stream));
     h->launches += h->graph_blocks;
     return GPR_OK;
@@ -726,7 +757,7 @@ int gpr_autotune(gpr_handle* h, int steps, int seed, int* K, int* onepass, int* 
     for (int Kc : {4, 8})
         for (int op = 1; op >= 0; --op)
             for (int ro = 0; ro <= 1; ++ro)
-                if ((!op || (h->nd <= 32 * Kc && !multi_only)) && !(h->kp.nv == 3 && Kc != 4))
+                if ((!op || (h->nd <= 32 * Kc && !multi_only)) && !(multi_only && Kc != 4))
                     cands[nc++] = {Kc, op, ro, saved_stream};
     if (!saved_stream)
         for (int ro = 0; ro <= 1; ++ro) cands[nc++] = {4, 0, ro, 1};
@@ -863,8 +894,9 @@ int gpr_set_layout2(gpr_handle* h, int K, int onepass, int rolled, int lockstep,
         (warps_per_cta != 1 && warps_per_cta != 2 && warps_per_cta != 4 && warps_per_cta != 8))
         return fail(h, GPR_ERR_ARG, "invalid layout K=%d onepass=%d lockstep=%d warps=%d for %d points", K,
                     onepass, lockstep, warps_per_cta, h->kp.nd);
-    if (h->kp.nv == 3 && (K != 4 || onepass))
-        return fail(h, GPR_ERR_ARG, "three input variables take K=4 in passes (got K=%d onepass=%d)", K, onepass);
+    if ((h->kp.nv == 3 || h->kp.nds > 0) && (K != 4 || onepass))
+        return fail(h, GPR_ERR_ARG, "%s take K=4 in passes (got K=%d onepass=%d)",
+                    h->kp.nds > 0 ? "batched datasets" : "three input variables", K, onepass);
     CUDA_TRY(h, cudaSetDevice(h->device));
     return configure_launch(h, K, onepass ? 1 : 0, rolled ? 1 : 0, lockstep, warps_per_cta);
 }

@@ -449,7 +449,7 @@ __global__ void __launch_bounds__(128) mh_hmc_kernel(const __grid_constant__ KPa
     const GradSmem ws = carve_grad(wbase + (size_t)warp * grad_warp_bytes(p.PL, p.max_instr), p.PL, p.max_instr);
     const int PL = p.PL;
     const bool adapt = p.chain_scale && p.adapt_target > 0.0f;
-    const uint32_t seed = p.seed_src ? p.seed_src[p.seed_index] : p.seed;
+    const uint32_t seed = p.seed;
     const float unscale = (float)GPR_DF_UNSCALE;
 
 #pragma unroll 1

@@ -13,7 +13,11 @@ size_t mh_smem_bytes(const KParams& p, int K, int warps_per_cta, int stream) {
            (size_t)warps_per_cta * warp_smem_bytes(p.PL, p.max_instr, p.levels, K);
 }
 
-static const void* pick_kernel(int K, int onepass, int rng, int rolled, int stream, int nv) {
+static const void* pick_kernel(int K, int onepass, int rng, int rolled, int stream, int nv, int batched) {
+    if (batched) {
+        if (K != 4 || onepass) return nullptr;
+        return nv == 3 ? mh_kernel_k4bv(rng, rolled, stream) : mh_kernel_k4b(rng, rolled, stream);
+    }
     if (nv == 3) return (K == 4 && !onepass) ? mh_kernel_k4v(rng, rolled, stream) : nullptr;
     if (stream) return (K == 4 && !onepass) ? mh_kernel_k4s(rng, rolled) : nullptr;
     if (K == 4) return onepass ? mh_kernel_k4(rng, rolled) : mh_kernel_k4m(rng, rolled);
@@ -31,7 +35,7 @@ void fill_lcg_jump_table(KParams& p) {
 }
 
 cudaError_t mh_occupancy(const KParams& p, const LaunchCfg& lc, int* ctas_per_sm) {
-    const void* f = pick_kernel(lc.K, lc.onepass, p.rng_mode, lc.rolled, lc.stream, p.nv);
+    const void* f = pick_kernel(lc.K, lc.onepass, p.rng_mode, lc.rolled, lc.stream, p.nv, p.nds > 0);
     if (!f) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lc.smem_bytes);
     if (e != cudaSuccess) return e;
@@ -39,7 +43,7 @@ cudaError_t mh_occupancy(const KParams& p, const LaunchCfg& lc, int* ctas_per_sm
 }
 
 cudaError_t launch_mh_block(const KParams& p, const LaunchCfg& lc, cudaStream_t st) {
-    const void* f = pick_kernel(lc.K, lc.onepass, p.rng_mode, lc.rolled, lc.stream, p.nv);
+    const void* f = pick_kernel(lc.K, lc.onepass, p.rng_mode, lc.rolled, lc.stream, p.nv, p.nds > 0);
     if (!f) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lc.smem_bytes);
     if (e != cudaSuccess) return e;

@@ -48,10 +48,6 @@ struct KParams {
     const int* ds_n;
     const float* ds_ns;
     const int* ds_order;
-    /* captured block sequences: the block's seed is seed_src[seed_index]
-     * (device memory) when seed_src is set, else seed */
-    const uint32_t* seed_src;
-    int seed_index;
     int nd;
     int nd_pad;        /* multiple of 4                                       */
     float normsum_hi, normsum_lo;  /* 2^-64 * sum_d 0.5*(logf(2 PIf) + 2 logf(sd_d)), double-float */
@@ -113,6 +109,8 @@ const void* mh_kernel_k8(int rng, int rolled);
 const void* mh_kernel_k8m(int rng, int rolled);
 const void* mh_kernel_k4s(int rng, int rolled);   /* dataset streamed from device memory */
 const void* mh_kernel_k4v(int rng, int rolled, int stream);   /* three input variables */
+const void* mh_kernel_k4b(int rng, int rolled, int stream);    /* batched data */
+const void* mh_kernel_k4bv(int rng, int rolled, int stream);   /* batched, three input variables */
 
 /* Launch geometry picked by the host (persistent grid). */
 struct LaunchCfg {

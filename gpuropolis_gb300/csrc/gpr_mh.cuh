@@ -1083,8 +1083,10 @@ __device__ __forceinline__ void structure_move(Rng& r, const uint8_t* oc, uint8_
 
 /* STREAM: the dataset is read from device memory (L2-resident for a few MB)
  * instead of being staged into each CTA's shared memory -- the layout for
- * datasets too large to stage. */
-template <int K, bool ONEPASS, int RNG, bool ROLLED, bool STREAM, int NV>
+ * datasets too large to stage.  BATCHED: many datasets (p.nds > 0), the view
+ * switched per chain group; a compile-time switch, so that the single-dataset
+ * kernel keeps its dataset view in constant memory rather than registers. */
+template <int K, bool ONEPASS, int RNG, bool ROLLED, bool STREAM, int NV, bool BATCHED>
 __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __grid_constant__ KParams p) {
     extern __shared__ __align__(128) uint8_t smem[];
     const int lane = threadIdx.x & 31;
@@ -1094,7 +1096,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
      * data, the dataset of the current chain group (staged per group) */
     uint64_t* bar = (uint64_t*)smem;
     float* fx = (float*)(smem + 16);
-    const bool batched = p.nds > 0;
+    constexpr bool batched = BATCHED;
     DataView dv = data_view(p, fx, STREAM);
     int staged_ds = -1;
     bool bar_live = false;   /* the barrier has been initialised (batched restaging) */
@@ -1119,7 +1121,6 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
     }
     const int PL = p.PL;
     const LaneJump ljump = make_lane_jump(p, lane);
-    const uint32_t seed = p.seed_src ? p.seed_src[p.seed_index] : p.seed;
 
     __shared__ int s_group_base;
     const int nwarps = blockDim.x >> 5;
@@ -1153,7 +1154,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
             const int base = s_group_base;
             if (base >= p.N) break;
             chain = base + warp;
-            if (batched) {
+            if constexpr (BATCHED) {
                 const int d = chain_dataset(p, base);   /* a group never straddles datasets */
                 if (d != staged_ds) {
                     dv = data_view(p, fx, STREAM, d);
@@ -1189,6 +1190,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
         df cur_cs = df_make(0.f, 0.f);
         df forward = df_make(0.f, 0.f), backward = df_make(0.f, 0.f);
 
+        const uint32_t seed = p.seed;
         Rng r;
         r.key0 = seed; r.key1 = (uint32_t)chain; r.blk = 0xffffffffu; r.drawn = 0;
         r.w0 = r.w1 = r.w2 = r.w3 = 0u;

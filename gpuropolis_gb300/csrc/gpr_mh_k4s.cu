@@ -5,12 +5,12 @@
 #include "gpr_mh.cuh"
 
 namespace gpr {
-template __global__ void mh_block_kernel<4, false, 0, false, true, 1>(const __grid_constant__ KParams p);
-template __global__ void mh_block_kernel<4, false, 1, false, true, 1>(const __grid_constant__ KParams p);
-template __global__ void mh_block_kernel<4, false, 0, true, true, 1>(const __grid_constant__ KParams p);
-template __global__ void mh_block_kernel<4, false, 1, true, true, 1>(const __grid_constant__ KParams p);
+template __global__ void mh_block_kernel<4, false, 0, false, true, 1, false>(const __grid_constant__ KParams p);
+template __global__ void mh_block_kernel<4, false, 1, false, true, 1, false>(const __grid_constant__ KParams p);
+template __global__ void mh_block_kernel<4, false, 0, true, true, 1, false>(const __grid_constant__ KParams p);
+template __global__ void mh_block_kernel<4, false, 1, true, true, 1, false>(const __grid_constant__ KParams p);
 const void* mh_kernel_k4s(int rng, int rolled) {
-    if (rolled) return rng ? (const void*)mh_block_kernel<4, false, 1, true, true, 1> : (const void*)mh_block_kernel<4, false, 0, true, true, 1>;
-    return rng ? (const void*)mh_block_kernel<4, false, 1, false, true, 1> : (const void*)mh_block_kernel<4, false, 0, false, true, 1>;
+    if (rolled) return rng ? (const void*)mh_block_kernel<4, false, 1, true, true, 1, false> : (const void*)mh_block_kernel<4, false, 0, true, true, 1, false>;
+    return rng ? (const void*)mh_block_kernel<4, false, 1, false, true, 1, false> : (const void*)mh_block_kernel<4, false, 0, false, true, 1, false>;
 }
 }  // namespace gpr

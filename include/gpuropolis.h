@@ -101,11 +101,11 @@ int gpr_set_batched_data(gpr_handle* h, int n_datasets, const int* sizes, const 
 /* Captured block sequence (no reference counterpart; it replaces the host
  * loop's launches, main.cu:1156-1239): records n_blocks MH blocks of `steps`
  * steps each, with the handle's current data, layout and moves, as one CUDA
- * graph.  gpr_run_captured(h, seeds) replays it with seeds[0..n_blocks) as
- * the blocks' random seeds (copied to the device inside the replay), with the
- * chains identical to n_blocks gpr_run_block calls with those seeds; it waits
- * for the previous replay to finish before writing the seeds.  Changing the
- * data, layout or moves drops the capture (GPR_ERR_STATE on replay). */
+ * graph.  gpr_run_captured(h, seeds) enqueues a replay with seeds[0..n_blocks)
+ * as the blocks' random seeds (set in the graph's kernel parameters before the
+ * launch, so replays may be queued back to back), with the chains identical
+ * to n_blocks gpr_run_block calls with those seeds.  Changing the data,
+ * layout or moves drops the capture (GPR_ERR_STATE on replay). */
 int gpr_capture_blocks(gpr_handle* h, int n_blocks, int steps);
 int gpr_run_captured(gpr_handle* h, const int* seeds);
 

@@ -208,9 +208,10 @@ def test_captured_replay_over_batched_data():
         b.close()
 
 
-@pytest.mark.parametrize("layout", [dict(K=8, onepass=0, rolled=0), dict(K=4, onepass=0, rolled=1),
-                                    dict(K=4, onepass=0, rolled=0, lockstep=5, warps_per_cta=4)],
-                         ids=["k8", "rolled", "lockstep5-wpc4"])
+@pytest.mark.parametrize("layout", [dict(K=4, onepass=0, rolled=1),
+                                    dict(K=4, onepass=0, rolled=0, lockstep=5, warps_per_cta=4),
+                                    dict(K=4, onepass=0, rolled=1, lockstep=0, warps_per_cta=2)],
+                         ids=["rolled", "lockstep5-wpc4", "free-wpc2"])
 def test_batched_layouts_equal_single_dataset_runs(layout):
     kw = MODES["rw-philox"]
     sets = _datasets([200, 33, 700], seed=17)
@@ -220,6 +221,8 @@ def test_batched_layouts_equal_single_dataset_runs(layout):
     b = g.Sampler(N, **kw)
     try:
         b.set_batched_data(sets)
+        with pytest.raises(g.GprError, match="K=4 in passes"):
+            b.set_layout(8, 0, 0)
         b.set_layout(**layout)
         geo = b.launch_geometry()
         assert geo["K"] == layout["K"] and geo["rolled"] == layout["rolled"]
