@@ -990,9 +990,9 @@ int gpr_loglik_grad(gpr_handle* h, double* grad, double* likelihood) {
     double* dl = nullptr;
     cudaError_t e = cudaMalloc(&dg, cnt * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&dl, (size_t)h->N * sizeof(double));
-    if (e == cudaSuccess)
-        e = gpr::launch_loglik_grad(h->kp, dg, dl, h->stream_data || gpr::grad_smem_bytes(h->kp, 4) > 227 * 1024,
-                                    h->stream);
+    /* batched data: every warp reads its chain's dataset from device memory */
+    const bool st = h->stream_data || h->kp.nds > 0 || gpr::grad_smem_bytes(h->kp, 4) > 227 * 1024;
+    if (e == cudaSuccess) e = gpr::launch_loglik_grad(h->kp, dg, dl, st, h->stream);
     if (e == cudaSuccess) {
         h->launches++;
         e = cudaMemcpyAsync(grad, dg, cnt * sizeof(double), cudaMemcpyDeviceToHost, h->stream);

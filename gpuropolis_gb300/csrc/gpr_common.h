@@ -45,18 +45,33 @@ enum gpr_opclass {
 #define GPR_HDI static inline
 #endif
 
+/* The class of op o: a 4-bit field per op, eight ops to a 32-bit word, so
+ * the lookup is a few integer operations with no branch or jump table. */
+#define GPR_CLS_AT(op, cls) ((uint32_t)(cls) << (4 * ((op) & 7)))
+#define GPR_CLS_WORD(w)                                                                               \
+    ((uint32_t)(GPR_CLS_FIELD((w) * 8 + 0) | GPR_CLS_FIELD((w) * 8 + 1) | GPR_CLS_FIELD((w) * 8 + 2) | \
+                GPR_CLS_FIELD((w) * 8 + 3) | GPR_CLS_FIELD((w) * 8 + 4) | GPR_CLS_FIELD((w) * 8 + 5) | \
+                GPR_CLS_FIELD((w) * 8 + 6) | GPR_CLS_FIELD((w) * 8 + 7)))
+#define GPR_CLS_FIELD(op) GPR_CLS_AT(op, gpr_op_class_slow(op))
+
+static constexpr int gpr_op_class_slow(int o) {
+    return (o == OP_ONE || o == OP_CONST || o == OP_X1 || o == OP_X2 || o == OP_X3) ? CLS_LEAF0
+         : o == OP_A ? CLS_PASS_A
+         : o == OP_B ? CLS_PASS_B
+         : (o == OP_INV || o == OP_LOG || o == OP_EXP || o == OP_SQRT || o == OP_SIN || o == OP_ASIN ||
+            o == OP_COS || o == OP_ACOS || o == OP_TAN || o == OP_ATAN || o == OP_ABS) ? CLS_UNARY
+         : (o == OP_CPLUS || o == OP_CTIMES || o == OP_CPOW || o == OP_CRPOW) ? CLS_CUNARY
+         : (o == OP_PLUS || o == OP_MINUS || o == OP_RMINUS || o == OP_TIMES || o == OP_DIV || o == OP_RDIV ||
+            o == OP_POW || o == OP_RPOW) ? CLS_BINARY
+         : CLS_INVALID;
+}
+
 GPR_HDI int gpr_op_class(int o) {
-    switch (o) {
-        case OP_ONE: case OP_CONST: case OP_X1: case OP_X2: case OP_X3: return CLS_LEAF0;
-        case OP_A: return CLS_PASS_A;
-        case OP_B: return CLS_PASS_B;
-        case OP_INV: case OP_LOG: case OP_EXP: case OP_SQRT: case OP_SIN: case OP_ASIN:
-        case OP_COS: case OP_ACOS: case OP_TAN: case OP_ATAN: case OP_ABS: return CLS_UNARY;
-        case OP_CPLUS: case OP_CTIMES: case OP_CPOW: case OP_CRPOW: return CLS_CUNARY;
-        case OP_PLUS: case OP_MINUS: case OP_RMINUS: case OP_TIMES: case OP_DIV: case OP_RDIV:
-        case OP_POW: case OP_RPOW: return CLS_BINARY;
-        default: return CLS_INVALID;
-    }
+    if ((unsigned)o >= 32u) return CLS_INVALID;
+    const int w = o >> 3;
+    const uint32_t word = w == 0 ? GPR_CLS_WORD(0) : w == 1 ? GPR_CLS_WORD(1) : w == 2 ? GPR_CLS_WORD(2)
+                                                                                    : GPR_CLS_WORD(3);
+    return (int)((word >> (4 * (o & 7))) & 15u);
 }
 
 /* ---- compiled program: a reachable-only postfix form of the heap tree ----

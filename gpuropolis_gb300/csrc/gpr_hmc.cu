@@ -30,6 +30,7 @@ static const void* grad_kernel_t(int stream, int nv) {
 
 cudaError_t launch_loglik_grad(const KParams& p, double* grad, double* lik, int stream, cudaStream_t st) {
     if (!grad_supported(p)) return cudaErrorInvalidValue;
+    if (p.nds > 0) stream = 1;   /* batched data are read per chain from device memory */
     const int wpc = 4;
     const size_t smem = grad_smem_bytes(p, wpc, stream);
     const void* f = p.max_instr <= 130 ? grad_kernel_t<130>(stream, p.nv) : grad_kernel_t<258>(stream, p.nv);
@@ -70,7 +71,7 @@ cudaError_t hmc_occupancy(const KParams& p, int warps_per_cta, size_t smem, int 
 }
 
 cudaError_t launch_hmc_block(const KParams& p, const LaunchCfg& lc, cudaStream_t st) {
-    if (!grad_supported(p)) return cudaErrorInvalidValue;
+    if (!grad_supported(p) || (p.nds > 0 && !lc.stream)) return cudaErrorInvalidValue;
     const void* f = hmc_kernel(p, lc.stream);
     cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lc.smem_bytes);
     if (e == cudaSuccess) e = set_carveout(f, lc.carveout);

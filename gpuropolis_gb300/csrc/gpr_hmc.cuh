@@ -320,11 +320,9 @@ __device__ __forceinline__ void backward_tape(const uint2* __restrict__ prog, in
  * g[i] = 2^-64 d loglik / d C[i] in FP32, at the bookkeeping scale like the
  * likelihood (0 for constants the program does not read).  The gradient is
  * meaningful only when the likelihood is finite. */
-template <int K, int MAXI, int NV>
+template <int K, int MAXI, int NV, bool STREAM>
 __device__ df eval_loglik_grad(const uint2* prog, int ninstr, const GradSmem& ws, const DataView& dv,
                                const KParams& p, int lane, int& pts, float* g) {
-    const float* sy = dv.y;
-    const float* sw = dv.w;
     const int PL = p.PL;
     Row<K> tape[MAXI];             /* thread-local: results of every instruction */
     Row<K> astk[GPR_ASTK_MAX];     /* adjoints of pushed values                  */
@@ -338,7 +336,7 @@ __device__ df eval_loglik_grad(const uint2* prog, int ninstr, const GradSmem& ws
     for (int pass = 0; pass < npass && !bad; ++pass) {
         float x[NV][K], adj[K];
         const int base = pass * 32 * K + lane;
-        const uint32_t valid = load_points<K, NV>(dv, p, base, x);
+        const uint32_t valid = load_points<K, NV, STREAM>(dv, p, base, x);
         forward_tape<K, NV>(prog, ninstr, ws.match, x, tape);
         pts += min(32 * K, dv.nd - pass * 32 * K);
         const Row<K> fres = tape[ninstr - 2];
@@ -348,11 +346,12 @@ __device__ df eval_loglik_grad(const uint2* prog, int ninstr, const GradSmem& ws
             if (valid & (1u << k)) {
                 const int i = base + 32 * k;
                 const float f = fres.v[k];
-                const float r = __fsub_rn(f, sy[i]);
+                const float wi = data_at<STREAM>(dv, DA_W, i);
+                const float r = __fsub_rn(f, data_at<STREAM>(dv, DA_Y, i));
                 const float q = __fmul_rn(r, r);
                 bad |= !(q <= FLT_MAX);
-                s = fmaf(q, sw[i], s);
-                adj[k] = __fmul_rn(__fmul_rn(-2.0f, sw[i]), r);
+                s = fmaf(q, wi, s);
+                adj[k] = __fmul_rn(__fmul_rn(-2.0f, wi), r);
             }
         }
         bad = __any_sync(FULLMASK, bad);
@@ -399,11 +398,11 @@ __device__ __forceinline__ float hmc_momentum(uint32_t seed, uint32_t chain, uin
  * device memory.  Returns where the per-warp regions start. */
 template <bool STREAM>
 __device__ __forceinline__ uint8_t* grad_dataset(uint8_t* smem, const KParams& p, DataView& dv) {
-    float* fx = (float*)(smem + 16);
+    float* fx = (float*)(smem + GPR_STAGED_OFFSET);
     dv = data_view(p, fx, STREAM);
-    if (STREAM) return smem + 16;
+    if (STREAM) return smem + GPR_STAGED_OFFSET;
     stage_dataset(fx, (uint64_t*)smem, p, dv);
-    return smem + 16 + align16((size_t)data_arrays(p) * p.nd_pad * 4);
+    return smem + GPR_STAGED_OFFSET + align16((size_t)data_arrays(p) * p.nd_pad * 4);
 }
 
 template <int K, int MAXI, bool STREAM, int NV>
@@ -417,7 +416,7 @@ __global__ void __launch_bounds__(128) loglik_grad_kernel(const __grid_constant_
     const GradSmem ws = carve_grad(wbase + (size_t)warp * grad_warp_bytes(p.PL, p.max_instr), p.PL, p.max_instr);
     const int chain = blockIdx.x * (blockDim.x >> 5) + warp;
     if (chain >= p.N) return;
-    if (p.nds > 0) dv = data_view(p, nullptr, true, chain_dataset(p, chain));   /* batched: streamed */
+    if (STREAM && p.nds > 0) dv = data_view(p, nullptr, true, chain_dataset(p, chain));   /* batched: streamed */
     const int PL = p.PL;
     for (int i = lane; i < PL; i += 32) {
         const int o = p.P[(size_t)i * p.N + chain];
@@ -425,12 +424,12 @@ __global__ void __launch_bounds__(128) loglik_grad_kernel(const __grid_constant_
         ws.Cs[0][i] = p.C[(size_t)i * p.N + chain];
     }
     __syncwarp();
-    const CompileOut co = compile_parallel(ws.ops[0], PL, ws.prog[0], compile_scratch(ws.gacc, PL), lane);
+    const CompileOut co = compile_parallel<NV>(ws.ops[0], PL, ws.prog[0], compile_scratch(ws.gacc, PL), lane);
     __syncwarp();
     build_eval_program(ws.prog[0], ws.Cs[0], co.ninstr, ws.eprog, lane);
     pop_match(ws.prog[0], co.ninstr, ws.match, lane);
     int pts = 0;
-    const df lik = eval_loglik_grad<K, MAXI, NV>(ws.eprog, co.ninstr, ws, dv, p, lane, pts, ws.gnew);
+    const df lik = eval_loglik_grad<K, MAXI, NV, STREAM>(ws.eprog, co.ninstr, ws, dv, p, lane, pts, ws.gnew);
     for (int i = lane; i < PL; i += 32) grad[(size_t)i * p.N + chain] = (double)ws.gnew[i] * GPR_DF_UNSCALE;
     if (lane == 0) lik_out[chain] = df_to_double_unscaled(lik);
 }
@@ -458,7 +457,7 @@ __global__ void __launch_bounds__(128) mh_hmc_kernel(const __grid_constant__ KPa
         if (lane == 0) chain = atomicAdd(p.next_chain, 1);
         chain = __shfl_sync(FULLMASK, chain, 0);
         if (chain >= p.N) break;
-        if (p.nds > 0) dv = data_view(p, nullptr, true, chain_dataset(p, chain));   /* batched: streamed */
+        if (STREAM && p.nds > 0) dv = data_view(p, nullptr, true, chain_dataset(p, chain));   /* batched: streamed */
 
         for (int i = lane; i < PL; i += 32) {
             const int o = p.P[(size_t)i * p.N + chain];
@@ -502,7 +501,7 @@ __global__ void __launch_bounds__(128) mh_hmc_kernel(const __grid_constant__ KPa
                     pbuf = cur ^ 1;
                 }
                 __syncwarp();
-                const CompileOut co = compile_parallel(ws.ops[pbuf], PL, ws.prog[pbuf],
+                const CompileOut co = compile_parallel<NV>(ws.ops[pbuf], PL, ws.prog[pbuf],
                                                        compile_scratch(ws.gacc, PL), lane);
                 __syncwarp();
                 const df backward = df_make(__fmul_rn(-p.logcount[co.count], GPR_DF_SCALE), 0.0f);
@@ -510,7 +509,7 @@ __global__ void __launch_bounds__(128) mh_hmc_kernel(const __grid_constant__ KPa
                 build_eval_program(ws.prog[pbuf], ws.Cs[ccur], co.ninstr, ws.eprog, lane);
                 pop_match(ws.prog[pbuf], co.ninstr, ws.match, lane);
                 int pe = 0;
-                const df lik = eval_loglik_grad<K, MAXI, NV>(ws.eprog, co.ninstr, ws, dv, p, lane, pe, ws.gnew);
+                const df lik = eval_loglik_grad<K, MAXI, NV, STREAM>(ws.eprog, co.ninstr, ws, dv, p, lane, pe, ws.gnew);
                 st_pts += (unsigned)pe;
                 const df prior = df_add(length_prior(co.length, p), cs);
                 const df post = df_add(prior, lik);
@@ -560,7 +559,7 @@ __global__ void __launch_bounds__(128) mh_hmc_kernel(const __grid_constant__ KPa
                         build_eval_program(ws.prog[cur], q, cur_ninstr, ws.eprog, lane);
                         __syncwarp();
                         int pe = 0;
-                        lik = eval_loglik_grad<K, MAXI, NV>(ws.eprog, cur_ninstr, ws, dv, p, lane, pe, ws.gnew);
+                        lik = eval_loglik_grad<K, MAXI, NV, STREAM>(ws.eprog, cur_ninstr, ws, dv, p, lane, pe, ws.gnew);
                         st_pts += (unsigned)pe;
                         st_evals++; st_nodes += (unsigned)cur_count;
                         st_np += (unsigned long long)(cur_count + 4) * (unsigned)pe;

@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(128) eval_values_kernel(const __grid_constant_
         ws.Cs[0][i] = p.C[(size_t)i * p.N + chain];
     }
     __syncwarp();
-    CompileOut co = compile_parallel(ws.ops[0], p.PL, ws.prog[0], compile_scratch(ws.stk, p.PL), lane);
+    CompileOut co = compile_parallel<3>(ws.ops[0], p.PL, ws.prog[0], compile_scratch(ws.stk, p.PL), lane);
     if (lane == 0) {
         length[chain] = co.length;
         count[chain] = co.count;

@@ -229,20 +229,23 @@ __device__ __forceinline__ int binary_bop(int o, int& swapped) {
 #define PL_X3 (-5)
 #define PL_C0 (-6)
 
+/* NV: input variables of the kernel; with one, x2 and x3 never occur (the
+ * host rejects them), and their cases are compiled out to keep the
+ * compiler's code small. */
+template <int NV>
 __device__ __forceinline__ uint32_t pl_load_instr(int r) {
     if (r == PL_X || r == PL_X1N) return I_LDX;
     if (r == PL_ONE) return I_LD1;
     if (r == PL_NAN) return I_LDNAN;
-    if (r == PL_X2) return I_LDX2;
-    if (r == PL_X3) return I_LDX3;
+    if (NV > 1 && (r == PL_X2 || r == PL_X3)) return r == PL_X2 ? I_LDX2 : I_LDX3;
     return I_LDC | ((uint32_t)(PL_C0 - r) << 8);
 }
+template <int NV>
 __device__ __forceinline__ uint32_t pl_bin_instr(int bop, int accleft, int r, bool pop) {
     if (pop) return GPR_BIN(bop, accleft, SRC_POP);
     if (r == PL_X || r == PL_X1N) return GPR_BIN(bop, accleft, SRC_X);
     if (r == PL_ONE) return GPR_BIN(bop, accleft, SRC_ONE);
-    if (r == PL_X2) return GPR_BIN(bop, accleft, SRC_X2);
-    if (r == PL_X3) return GPR_BIN(bop, accleft, SRC_X3);
+    if (NV > 1 && (r == PL_X2 || r == PL_X3)) return GPR_BIN(bop, accleft, r == PL_X2 ? SRC_X2 : SRC_X3);
     if (r == PL_NAN) return GPR_BIN(bop, accleft, SRC_C) | (255u << 8);
     return GPR_BIN(bop, accleft, SRC_C) | ((uint32_t)(PL_C0 - r) << 8);
 }
@@ -272,6 +275,7 @@ __device__ __forceinline__ int child_res(const CompileScratch& cs, int PL, int j
 __device__ __forceinline__ float leaf_len(int r) { return r == PL_NAN ? __int_as_float(0x7fc00000) : 1.0f; }
 __device__ __forceinline__ int leaf_cnt(int r) { return r == PL_X ? 0 : 1; }
 
+template <int NV>
 static __device__ CompileOut compile_parallel(const uint8_t* ops, int PL, uint32_t* prog, const CompileScratch& cs,
                                        int lane) {
     int D = 0;
@@ -289,9 +293,7 @@ static __device__ CompileOut compile_parallel(const uint8_t* ops, int PL, uint32
             else if (cls == CLS_PASS_B) r = child_res(cs, PL, 2 * j + 1);
             else if (o == OP_ONE) r = PL_ONE;
             else if (o == OP_CONST) r = PL_C0 - (j - 1);
-            else if (o == OP_X1) r = PL_X1N;
-            else if (o == OP_X2) r = PL_X2;
-            else if (o == OP_X3) r = PL_X3;
+            else if (o >= OP_X1 && o <= (NV > 1 ? OP_X3 : OP_X1)) r = PL_X1N - (o - OP_X1);   /* x1, x2, x3 */
             else if (cls == CLS_INVALID) r = PL_NAN;
             cs.res[j] = r;
             cs.start[j] = -1;
@@ -320,7 +322,7 @@ static __device__ CompileOut compile_parallel(const uint8_t* ops, int PL, uint32
     CompileOut out;
     const int r0 = PL >= 1 ? cs.res[1] : PL_X;
     if (r0 <= 0) {
-        if (lane == 0) { prog[0] = pl_load_instr(r0); prog[1] = I_END; }
+        if (lane == 0) { prog[0] = pl_load_instr<NV>(r0); prog[1] = I_END; }
         out.ninstr = 2; out.length = leaf_len(r0); out.count = leaf_cnt(r0);
         __syncwarp();
         return out;
@@ -350,26 +352,26 @@ static __device__ CompileOut compile_parallel(const uint8_t* ops, int PL, uint32
                 ui |= ((uint32_t)(j - 1) << 8);
                 const int L = child_res(cs, PL, 2 * j);
                 if (L > 0) { cs.start[L] = st; prog[st + cs.icnt[L]] = ui; }
-                else { prog[st] = pl_load_instr(L); prog[st + 1] = ui; }
+                else { prog[st] = pl_load_instr<NV>(L); prog[st + 1] = ui; }
             } else {
                 int sw;
                 const int bop = binary_bop(o, sw);
                 const int U = child_res(cs, PL, sw ? 2 * j + 1 : 2 * j);
                 const int V = child_res(cs, PL, sw ? 2 * j : 2 * j + 1);
                 if (U <= 0 && V <= 0) {
-                    prog[st] = pl_load_instr(U);
-                    prog[st + 1] = pl_bin_instr(bop, 1, V, false);
+                    prog[st] = pl_load_instr<NV>(U);
+                    prog[st + 1] = pl_bin_instr<NV>(bop, 1, V, false);
                 } else if (U > 0 && V <= 0) {
                     cs.start[U] = st;
-                    prog[st + cs.icnt[U]] = pl_bin_instr(bop, 1, V, false);
+                    prog[st + cs.icnt[U]] = pl_bin_instr<NV>(bop, 1, V, false);
                 } else if (U <= 0 && V > 0) {
                     cs.start[V] = st;
-                    prog[st + cs.icnt[V]] = pl_bin_instr(bop, 0, U, false);
+                    prog[st + cs.icnt[V]] = pl_bin_instr<NV>(bop, 0, U, false);
                 } else {
                     cs.start[U] = st;
                     prog[st + cs.icnt[U]] = I_PUSH;
                     cs.start[V] = st + cs.icnt[U] + 1;
-                    prog[st + cs.icnt[U] + 1 + cs.icnt[V]] = pl_bin_instr(bop, 0, 0, true);
+                    prog[st + cs.icnt[U] + 1 + cs.icnt[V]] = pl_bin_instr<NV>(bop, 0, 0, true);
                 }
             }
         }
@@ -526,18 +528,17 @@ __device__ __forceinline__ void run_program(const uint2* __restrict__ prog,
             }
             goto next_ins;
         }
+        if (NV > 1 && (code == I_LDX2 || code == I_LDX3)) {
+            const int vi = NV > 1 ? (code == I_LDX2 ? 1 : 2) : 0;
+#pragma unroll
+            for (int k = 0; k < K; ++k) acc[k] = x[vi][k];
+            goto next_ins;
+        }
         switch (code) {
             case I_LDX:
 #pragma unroll
                 for (int k = 0; k < K; ++k) acc[k] = x[0][k];
                 break;
-            case I_LDX2:
-            case I_LDX3: {
-                const int vi = NV > 1 ? (code == I_LDX2 ? 1 : 2) : 0;
-#pragma unroll
-                for (int k = 0; k < K; ++k) acc[k] = NV > 1 ? x[vi][k] : 0.0f;
-                break;
-            }
             case I_LDC:
 #pragma unroll
                 for (int k = 0; k < K; ++k) acc[k] = c;
@@ -653,7 +654,9 @@ __device__ __forceinline__ WarpSmem carve_warp(uint8_t* base, int PL, int max_in
     return w;
 }
 
-/* The dataset as the evaluators read it: the CTA's shared-memory copy, or the
+/* The dataset as the evaluators read it: the CTA's shared-memory copy
+ * (arrays of nd_pad floats in the staging order x1 | y | w | x2 | x3, 16
+ * bytes into the dynamic shared memory, after the staging barrier), or the
  * device arrays when streamed.  x[1], x[2] only for multivariate data. */
 struct DataView {
     const float* x[3];
@@ -663,9 +666,33 @@ struct DataView {
     float ns_hi, ns_lo;       /* 2^-64 * its normalising sum, double-float */
 };
 
+/* The dynamic shared memory of the kernel running (every extern __shared__
+ * array starts at its base).  Staged data are addressed from this symbol, so
+ * the loads are shared-memory loads at constant offsets. */
+extern __shared__ __align__(128) uint8_t gpr_dyn_smem[];
+#define GPR_STAGED_OFFSET 16
+
+/* Dataset array indices in the staging order. */
+#define DA_X1 0
+#define DA_Y 1
+#define DA_W 2
+#define DA_X2 3
+#define DA_X3 4
+
+/* Point i of dataset array a: from the staged copy in shared memory, or from
+ * the device arrays when streamed. */
+template <bool STREAM>
+__device__ __forceinline__ float data_at(const DataView& dv, int a, int i) {
+    if (STREAM) {
+        const float* q = a == DA_X1 ? dv.x[0] : a == DA_Y ? dv.y : a == DA_W ? dv.w : a == DA_X2 ? dv.x[1] : dv.x[2];
+        return q[i];
+    }
+    return ((const float*)(gpr_dyn_smem + GPR_STAGED_OFFSET))[a * dv.nd_pad + i];
+}
+
 /* This lane's K points of one pass: the NV input variables, and which points
  * exist (bit k). */
-template <int K, int NV>
+template <int K, int NV, bool STREAM>
 __device__ __forceinline__ uint32_t load_points(const DataView& dv, const KParams& p, int base,
                                                 float (&x)[NV][K]) {
     uint32_t valid = 0u;
@@ -674,7 +701,7 @@ __device__ __forceinline__ uint32_t load_points(const DataView& dv, const KParam
         const int i = base + 32 * k;
         const bool v = i < dv.nd;
 #pragma unroll
-        for (int j = 0; j < NV; ++j) x[j][k] = v ? dv.x[j][i] : 0.0f;
+        for (int j = 0; j < NV; ++j) x[j][k] = v ? data_at<STREAM>(dv, j == 0 ? DA_X1 : DA_X1 + 2 + j, i) : 0.0f;
         valid |= (v ? 1u : 0u) << k;
     }
     return valid;
@@ -691,21 +718,19 @@ struct LaneData {
  * of (f - y)^2 * w over its points, and whether any of its points is
  * invalid.  Used by the CTA-balanced evaluation, where any warp of the CTA may
  * evaluate any chain's pass. */
-template <int K, bool ONEPASS, bool ROLLED, int NV>
+template <int K, bool ONEPASS, bool ROLLED, int NV, bool STREAM>
 __device__ __forceinline__ float eval_pass(const uint2* prog, float* stk, float* scr,
                                            const LaneData<K>& ld, const DataView& dv, const KParams& p,
                                            int lane, int pass, bool& bad, int& pts) {
     float x[NV][K], acc[K];
     uint32_t valid;
     const int base = pass * 32 * K + lane;
-    const float* sy = dv.y;
-    const float* sw = dv.w;
     if (ONEPASS) {
 #pragma unroll
         for (int k = 0; k < K; ++k) x[0][k] = ld.x[k];
         valid = ld.valid;
     } else {
-        valid = load_points<K, NV>(dv, p, base, x);
+        valid = load_points<K, NV, STREAM>(dv, p, base, x);
     }
     run_program<K, ROLLED, NV>(prog, x, acc, stk, scr, lane);
     pts += ONEPASS ? dv.nd : min(32 * K, dv.nd - pass * 32 * K);
@@ -715,10 +740,10 @@ __device__ __forceinline__ float eval_pass(const uint2* prog, float* stk, float*
     for (int k = 0; k < K; ++k) {
         if (valid & (1u << k)) {
             const int i = base + 32 * k;
-            float r = __fsub_rn(acc[k], sy[i]);
+            float r = __fsub_rn(acc[k], data_at<STREAM>(dv, DA_Y, i));
             float q = __fmul_rn(r, r);
             bad |= !(q <= FLT_MAX);
-            s = fmaf(q, sw[i], s);
+            s = fmaf(q, data_at<STREAM>(dv, DA_W, i), s);
         }
     }
     return s;
@@ -729,14 +754,12 @@ __device__ __forceinline__ float eval_pass(const uint2* prog, float* stk, float*
  * invalid (main.cu:459,462).  Each lane sums its points in FP32; the 32 lane
  * sums are combined with error-free transforms (FP64 on GB300 runs at about
  * 1/70 of the FP32 rate, so no FP64 instruction is issued here). */
-template <int K, bool ONEPASS, bool ROLLED, int NV>
+template <int K, bool ONEPASS, bool ROLLED, int NV, bool STREAM>
 __device__ __forceinline__ df eval_loglik(const uint2* prog, float* stk, float* scr,
                                           const LaneData<K>& ld, const DataView& dv, const KParams& p,
                                           int lane, int& pts) {
     float s = 0.0f;
     bool bad = false;
-    const float* sy = dv.y;
-    const float* sw = dv.w;
     const int npass = ONEPASS ? 1 : (dv.nd + 32 * K - 1) / (32 * K);
 #pragma unroll 1
     for (int pass = 0; pass < npass; ++pass) {
@@ -748,7 +771,7 @@ __device__ __forceinline__ df eval_loglik(const uint2* prog, float* stk, float* 
             for (int k = 0; k < K; ++k) x[0][k] = ld.x[k];
             valid = ld.valid;
         } else {
-            valid = load_points<K, NV>(dv, p, base, x);
+            valid = load_points<K, NV, STREAM>(dv, p, base, x);
         }
         run_program<K, ROLLED, NV>(prog, x, acc, stk, scr, lane);
         pts += ONEPASS ? dv.nd : min(32 * K, dv.nd - pass * 32 * K);
@@ -756,10 +779,10 @@ __device__ __forceinline__ df eval_loglik(const uint2* prog, float* stk, float* 
         for (int k = 0; k < K; ++k) {
             if (valid & (1u << k)) {
                 const int i = base + 32 * k;
-                float r = __fsub_rn(acc[k], sy[i]);
+                float r = __fsub_rn(acc[k], data_at<STREAM>(dv, DA_Y, i));
                 float q = __fmul_rn(r, r);
                 bad |= !(q <= FLT_MAX);
-                s = fmaf(q, sw[i], s);
+                s = fmaf(q, data_at<STREAM>(dv, DA_W, i), s);
             }
         }
         if (__any_sync(FULLMASK, bad)) return df_make(-INFINITY, 0.0f);
@@ -1095,12 +1118,12 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
     /* CTA-shared dataset (or the device arrays when streamed); with batched
      * data, the dataset of the current chain group (staged per group) */
     uint64_t* bar = (uint64_t*)smem;
-    float* fx = (float*)(smem + 16);
+    float* fx = (float*)(smem + GPR_STAGED_OFFSET);
     constexpr bool batched = BATCHED;
     DataView dv = data_view(p, fx, STREAM);
     int staged_ds = -1;
     bool bar_live = false;   /* the barrier has been initialised (batched restaging) */
-    uint8_t* wbase = smem + 16;
+    uint8_t* wbase = smem + GPR_STAGED_OFFSET;
     if (!STREAM) {
         wbase += align16((size_t)data_arrays(p) * p.nd_pad * 4);
         if (!batched) stage_dataset(fx, bar, p, dv);
@@ -1115,7 +1138,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
         for (int k = 0; k < K; ++k) {
             int i = lane + 32 * k;
             bool v = i < dv.nd;
-            ld.x[k] = v ? dv.x[0][i] : 0.0f;
+            ld.x[k] = v ? data_at<STREAM>(dv, DA_X1, i) : 0.0f;
             ld.valid |= (v ? 1u : 0u) << k;
         }
     }
@@ -1234,7 +1257,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
             }
             __syncwarp();
             if (need_compile) {
-                const CompileOut co = compile_parallel(ws.ops[pbuf], PL, ws.prog[pbuf],
+                const CompileOut co = compile_parallel<NV>(ws.ops[pbuf], PL, ws.prog[pbuf],
                                                        compile_scratch(ws.stk, PL), lane);
                 len = co.length;
                 count = co.count;
@@ -1280,7 +1303,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                 const int w = __ffs(__ballot_sync(FULLMASK, my_rank == q)) - 1;
                 if (s_bad[w]) continue;
                 bool bad;
-                const float sl = eval_pass<K, ONEPASS, ROLLED, NV>(s_prog[w], ws.stk, ws.scr, ld, dv,
+                const float sl = eval_pass<K, ONEPASS, ROLLED, NV, STREAM>(s_prog[w], ws.stk, ws.scr, ld, dv,
                                                                p, lane, pass, bad, pts);
                 /* FP32 butterfly within the pass (terms are >= 0: <= 5 roundings),
                  * double-float across passes */
@@ -1307,7 +1330,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                 }
             }
           } else if (active) {
-            lik = eval_loglik<K, ONEPASS, ROLLED, NV>(ws.eprog, ws.stk, ws.scr, ld, dv, p, lane, pts);
+            lik = eval_loglik<K, ONEPASS, ROLLED, NV, STREAM>(ws.eprog, ws.stk, ws.scr, ld, dv, p, lane, pts);
             st_np += (unsigned long long)(count + 4) * (unsigned)pts;
           }
           st_pts += (unsigned)pts;
