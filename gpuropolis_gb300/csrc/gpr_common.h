@@ -54,7 +54,15 @@ enum gpr_opclass {
                 GPR_CLS_FIELD((w) * 8 + 6) | GPR_CLS_FIELD((w) * 8 + 7)))
 #define GPR_CLS_FIELD(op) GPR_CLS_AT(op, gpr_op_class_slow(op))
 
-static constexpr int gpr_op_class_slow(int o) {
+#if defined(__CUDACC__)
+#define GPR_HDC __host__ __device__ constexpr
+#else
+#define GPR_HDC static constexpr
+#endif
+
+/* The class of op o, written out; only evaluated at compile time, to build
+ * the table below. */
+GPR_HDC int gpr_op_class_slow(int o) {
     return (o == OP_ONE || o == OP_CONST || o == OP_X1 || o == OP_X2 || o == OP_X3) ? CLS_LEAF0
          : o == OP_A ? CLS_PASS_A
          : o == OP_B ? CLS_PASS_B
