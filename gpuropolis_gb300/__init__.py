@@ -102,6 +102,7 @@ def library():
     lib.gpr_loglik_grad.argtypes = [vp, vp, vp]
     lib.gpr_run_block_traced.argtypes = [vp, ip, ip, ip, vp]
     lib.gpr_set_batched_data.argtypes = [vp, ip, vp, vp, vp, vp, vp, vp]
+    lib.gpr_resample_datasets.argtypes = [vp, ip, dp, ctypes.c_uint32, vp, vp]
     lib.gpr_capture_blocks.argtypes = [vp, ip, ip]
     lib.gpr_run_captured.argtypes = [vp, vp]
     lib.gpr_resample.argtypes = [vp, ip, dp, ctypes.c_uint32, vp, vp]
@@ -332,6 +333,15 @@ class Sampler:
         self._check(self.lib.gpr_resample(self.h, int(mode), float(param), int(seed) & 0xffffffff,
                                           ctypes.byref(n), ctypes.byref(cut)))
         return n.value, cut.value
+
+    def resample_datasets(self, n_datasets, mode=0, param=0.5, seed=1):
+        """Per-dataset device resampling (gpr_resample_datasets): returns
+        (chains re-drawn, cutoffs, one per dataset)."""
+        n = ctypes.c_int()
+        cuts = np.zeros(max(1, int(n_datasets)), np.float64)
+        self._check(self.lib.gpr_resample_datasets(self.h, int(mode), float(param), int(seed) & 0xffffffff,
+                                                   ctypes.byref(n), _ptr(cuts)))
+        return n.value, cuts
 
     def top_chains(self, k, margin=0.0, capacity=None):
         """Candidate chains for the k best (gpr_top_chains): (chains, count, threshold)."""

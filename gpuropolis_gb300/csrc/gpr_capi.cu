@@ -16,6 +16,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <algorithm>
+#include <limits>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -60,7 +61,8 @@ struct gpr_handle {
     std::vector<gpr::KParams> graph_kp;
     int graph_blocks = 0;
     unsigned long long* dkeys = nullptr;   /* N posterior keys                   */
-    unsigned long long* dsel = nullptr;    /* [0] selected key                   */
+    unsigned long long* dsel = nullptr;    /* [0] selected key (per dataset)     */
+    int dsel_cap = 0;
     int* dseli = nullptr;                  /* [0] count, [1] first index         */
     int* dtop = nullptr;                   /* candidate chains, dtop_cap entries */
     int dtop_cap = 0;
@@ -1034,8 +1036,16 @@ int gpr_run_block_traced(gpr_handle* h, int steps, int random_seed, int trace_n,
 static int ensure_select(gpr_handle* h) {
     if (!h->dkeys) {
         CUDA_TRY(h, cudaMalloc(&h->dkeys, (size_t)h->N * sizeof(unsigned long long)));
-        CUDA_TRY(h, cudaMalloc(&h->dsel, 2 * sizeof(unsigned long long)));
         CUDA_TRY(h, cudaMalloc(&h->dseli, 4 * sizeof(int)));
+    }
+    const int need = std::max(2, h->kp.nds);   /* one selected key per dataset */
+    if (h->dsel_cap < need) {
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        cudaFree(h->dsel);
+        h->dsel = nullptr;
+        h->dsel_cap = 0;
+        CUDA_TRY(h, cudaMalloc(&h->dsel, (size_t)need * sizeof(unsigned long long)));
+        h->dsel_cap = need;
     }
     return GPR_OK;
 }
@@ -1053,37 +1063,54 @@ static int select_rank(gpr_handle* h, int rank, unsigned long long* key) {
     return GPR_OK;
 }
 
-int gpr_resample(gpr_handle* h, int mode, double param, uint32_t seed, int* n_redrawn, double* cutoff) {
+int gpr_resample_datasets(gpr_handle* h, int mode, double param, uint32_t seed, int* n_redrawn,
+                          double* cutoffs) {
     if (!h) return GPR_ERR_ARG;
     if (mode != 0 && mode != 1) return fail(h, GPR_ERR_ARG, "unknown resample mode %d", mode);
     if (h->cfg.n_ops < 2)
         return fail(h, GPR_ERR_ARG, "re-drawing ops needs at least 2 ops (random_int(n_ops - 1))");
-    int rank = h->N - 1;
+    const int nseg = h->kp.nds > 0 ? h->kp.nds : 1;
+    const int seg = h->N / nseg;
+    int rank = seg - 1;
     if (mode == 0) {
-        const double r = (double)h->N * param;
-        if (!(r >= 0.0 && r < (double)h->N)) return fail(h, GPR_ERR_ARG, "quantile %g is not in [0, 1)", param);
+        const double r = (double)seg * param;
+        if (!(r >= 0.0 && r < (double)seg)) return fail(h, GPR_ERR_ARG, "quantile %g is not in [0, 1)", param);
         rank = (int)r;
     } else if (!(param >= 0.0)) {
         return fail(h, GPR_ERR_ARG, "map-delta %g is not >= 0", param);
     }
     CUDA_TRY(h, cudaSetDevice(h->device));
-    int rc = select_rank(h, rank, nullptr);
+    int rc = ensure_select(h);
     if (rc != GPR_OK) return rc;
+    CUDA_TRY(h, gpr::launch_select(h->kp, rank, h->dkeys, h->dsel, h->stream, nseg));
+    h->launches += 2;
     CUDA_TRY(h, cudaMemsetAsync(h->dseli, 0, sizeof(int), h->stream));
     const gpr::Magic mops1 = magic_for(divisor_for(h->cfg.n_ops - 1));
     const gpr::Magic morder = magic_for(divisor_for(8));
-    CUDA_TRY(h, gpr::launch_redraw(h->kp, h->dsel, mode, param, seed, mops1, morder, h->dseli, h->stream));
+    CUDA_TRY(h, gpr::launch_redraw(h->kp, h->dsel, nseg > 1 ? seg : 0, mode, param, seed, mops1, morder, h->dseli,
+                                   h->stream));
     h->launches++;
-    if (n_redrawn || cutoff) {
-        unsigned long long key = 0;
+    if (n_redrawn || cutoffs) {
+        std::vector<unsigned long long> keys((size_t)nseg);
         int cnt = 0;
-        CUDA_TRY(h, cudaMemcpyAsync(&key, h->dsel, sizeof key, cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(h, cudaMemcpyAsync(keys.data(), h->dsel, (size_t)nseg * sizeof(unsigned long long),
+                                    cudaMemcpyDeviceToHost, h->stream));
         CUDA_TRY(h, cudaMemcpyAsync(&cnt, h->dseli, sizeof cnt, cudaMemcpyDeviceToHost, h->stream));
         CUDA_TRY(h, cudaStreamSynchronize(h->stream));
         if (n_redrawn) *n_redrawn = cnt;
-        if (cutoff) *cutoff = gpr_key_value(key) - (mode == 1 ? param : 0.0);
+        if (cutoffs)
+            for (int d = 0; d < nseg; ++d) cutoffs[d] = gpr_key_value(keys[d]) - (mode == 1 ? param : 0.0);
     }
     return GPR_OK;
+}
+
+int gpr_resample(gpr_handle* h, int mode, double param, uint32_t seed, int* n_redrawn, double* cutoff) {
+    if (!h) return GPR_ERR_ARG;
+    if (h->kp.nds > 0) {   /* batched data: per dataset; the cutoffs differ */
+        if (cutoff) *cutoff = std::numeric_limits<double>::quiet_NaN();
+        return gpr_resample_datasets(h, mode, param, seed, n_redrawn, nullptr);
+    }
+    return gpr_resample_datasets(h, mode, param, seed, n_redrawn, cutoff);
 }
 
 int gpr_top_chains(gpr_handle* h, int k, double margin, int* chains, int capacity, int* n, double* threshold) {

@@ -147,16 +147,18 @@ cudaError_t hmc_occupancy(const KParams& p, int warps_per_cta, size_t smem, int 
 cudaError_t launch_hmc_block(const KParams& p, const LaunchCfg& lc, cudaStream_t st);
 
 /* Selection over the chains' posteriors (gpr_resample.cu).  launch_select
- * writes one order-preserving key per chain (gpr_select.h) into keys and the
- * key of ascending rank `rank` into *out.  launch_redraw re-draws every chain
- * whose posterior is below the cutoff -- the value of *sel_key, minus delta
- * when map_delta -- from the initial distribution, counting them in
- * *n_redrawn.  launch_collect appends the chains with key >= kmin to out and
+ * writes one order-preserving key per chain (gpr_select.h) into keys and,
+ * for each of `segments` equal runs of chains, the key of ascending rank
+ * `rank` within the run into out[segment].  launch_redraw re-draws every
+ * chain whose posterior is below the cutoff -- the value of sel_key[chain /
+ * seg_len] (seg_len 0: sel_key[0]), minus delta when map_delta -- from the
+ * initial distribution, counting them in *n_redrawn.  launch_collect appends the chains with key >= kmin to out and
  * counts them; launch_first_index writes the smallest chain with key == k. */
 cudaError_t launch_select(const KParams& p, int rank, unsigned long long* keys, unsigned long long* out,
+                          cudaStream_t st, int segments = 1);
+cudaError_t launch_redraw(const KParams& p, const unsigned long long* sel_key, int seg_len, int map_delta,
+                          double delta, uint32_t seed, Magic mag_ops1, Magic mag_order, int* n_redrawn,
                           cudaStream_t st);
-cudaError_t launch_redraw(const KParams& p, const unsigned long long* sel_key, int map_delta, double delta,
-                          uint32_t seed, Magic mag_ops1, Magic mag_order, int* n_redrawn, cudaStream_t st);
 cudaError_t launch_collect(const unsigned long long* keys, int N, unsigned long long kmin, int* out, int cap,
                            int* count, cudaStream_t st);
 cudaError_t launch_first_index(const unsigned long long* keys, int N, const unsigned long long* k, int* out,

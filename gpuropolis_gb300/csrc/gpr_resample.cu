@@ -25,11 +25,15 @@ __global__ void post_key_kernel(const double* prior, const double* lik, int N, u
         keys[i] = gpr_post_key(prior[i] + lik[i]);
 }
 
-/* The key of rank `rank` (0-based, ascending) among keys[0..N).  One CTA:
- * per 8-bit digit, a shared histogram of the keys that match the digits fixed
- * so far, then warp 0 finds the bin that holds the rank. */
+/* The key of rank `rank` (0-based, ascending) among keys[0..N) of segment
+ * blockIdx.x (keys + blockIdx.x * N; one segment per dataset of a batched
+ * handle), into out[blockIdx.x].  One CTA per segment: per 8-bit digit, a
+ * shared histogram of the keys that match the digits fixed so far, then warp
+ * 0 finds the bin that holds the rank. */
 __global__ void __launch_bounds__(1024) select_rank_kernel(const unsigned long long* keys, int N, int rank,
                                                            unsigned long long* out) {
+    keys += (size_t)blockIdx.x * (size_t)N;
+    out += blockIdx.x;
     __shared__ unsigned int hist[256];
     __shared__ unsigned long long s_prefix;
     __shared__ int s_rank;
@@ -83,12 +87,14 @@ __global__ void __launch_bounds__(1024) select_rank_kernel(const unsigned long l
  * reference's order (all PL ops, then all PL constants; main.cu:1224-1228):
  * op = ops[random_int(n_ops - 1)], constant = 10^(random_int(8) - 4) *
  * random_normal().  Draws come from the Philox stream keyed by
- * (seed, chain | 2^31). */
-__global__ void redraw_kernel(const __grid_constant__ KParams p, const unsigned long long* sel_key, int map_delta,
-                              double delta, uint32_t seed, Magic mag_ops1, Magic mag_order, int* n_redrawn) {
+ * (seed, chain | 2^31).  seg_len > 0: chain c compares with the cutoff of
+ * its segment, sel_key[c / seg_len]. */
+__global__ void redraw_kernel(const __grid_constant__ KParams p, const unsigned long long* sel_key, int seg_len,
+                              int map_delta, double delta, uint32_t seed, Magic mag_ops1, Magic mag_order,
+                              int* n_redrawn) {
     const int chain = blockIdx.x * blockDim.x + threadIdx.x;
     if (chain >= p.N) return;
-    double cutoff = gpr_key_value(*sel_key);
+    double cutoff = gpr_key_value(sel_key[seg_len > 0 ? chain / seg_len : 0]);
     if (map_delta) cutoff -= delta;
     if (!(p.prior[chain] + p.lik[chain] < cutoff)) return;
     Rng r;
@@ -130,18 +136,20 @@ static int grid_for(int n, int threads) {
 }
 
 cudaError_t launch_select(const KParams& p, int rank, unsigned long long* keys, unsigned long long* out,
-                          cudaStream_t st) {
+                          cudaStream_t st, int segments) {
+    if (segments < 1 || p.N % segments) return cudaErrorInvalidValue;
     post_key_kernel<<<grid_for(p.N, 256), 256, 0, st>>>(p.prior, p.lik, p.N, keys);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    select_rank_kernel<<<1, 1024, 0, st>>>(keys, p.N, rank, out);
+    select_rank_kernel<<<segments, 1024, 0, st>>>(keys, p.N / segments, rank, out);
     return cudaGetLastError();
 }
 
-cudaError_t launch_redraw(const KParams& p, const unsigned long long* sel_key, int map_delta, double delta,
-                          uint32_t seed, Magic mag_ops1, Magic mag_order, int* n_redrawn, cudaStream_t st) {
-    redraw_kernel<<<(p.N + 127) / 128, 128, 0, st>>>(p, sel_key, map_delta, delta, seed, mag_ops1, mag_order,
-                                                       n_redrawn);
+cudaError_t launch_redraw(const KParams& p, const unsigned long long* sel_key, int seg_len, int map_delta,
+                          double delta, uint32_t seed, Magic mag_ops1, Magic mag_order, int* n_redrawn,
+                          cudaStream_t st) {
+    redraw_kernel<<<(p.N + 127) / 128, 128, 0, st>>>(p, sel_key, seg_len, map_delta, delta, seed, mag_ops1,
+                                                       mag_order, n_redrawn);
     return cudaGetLastError();
 }
 

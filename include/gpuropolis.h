@@ -262,6 +262,16 @@ int gpr_run_block_traced(gpr_handle* h, int steps, int random_seed, int trace_n,
  * non-NULL the call waits and reports them.  Needs n_ops >= 2. */
 int gpr_resample(gpr_handle* h, int mode, double param, uint32_t seed, int* n_redrawn, double* cutoff);
 
+/* gpr_resample per dataset (batched data, gpr_set_batched_data): each
+ * dataset's chains are resampled against the cutoff of their own posteriors,
+ * the rank rule applied to the N / n_datasets chains of the dataset;
+ * cutoffs (optional) receives one cutoff per dataset.  On a handle with one
+ * dataset it is gpr_resample.  gpr_resample on batched data does the same
+ * and reports a NaN cutoff.  gpr_top_chains and gpr_map_chain select over
+ * all chains of the handle. */
+int gpr_resample_datasets(gpr_handle* h, int mode, double param, uint32_t seed, int* n_redrawn,
+                          double* cutoffs);
+
 /* Candidates for the k best chains: every chain whose posterior is >= the
  * k-th largest posterior minus margin (NaN never; all non-NaN chains when
  * fewer than k are non-NaN).  Up to `capacity` chain indices are written to

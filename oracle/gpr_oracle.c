@@ -493,16 +493,20 @@ static int port_cmp_bayes(const void* a, const void* b) {
  * then all PL constants as powf(10, random_int(8) - 4) * random_normal() --
  * from the Philox stream keyed by (seed, chain | 2^31).  Returns the number of
  * chains re-drawn; *cutoff_out receives the cutoff. */
-int gpr_port_resample(const port_cfg* cfg, int N, int32_t* P, float* C, const double* prior, const double* lik,
-                      int mode, double param, uint32_t seed, double* cutoff_out) {
-    double* post = (double*)malloc((size_t)N * sizeof(double));
-    for (int h = 0; h < N; ++h) post[h] = prior[h] + lik[h];
-    qsort(post, (size_t)N, sizeof(double), port_cmp_bayes);
-    const double cutoff = mode == 1 ? post[N - 1] - param : post[(int)(N * param)];
+/* Resampling of chains [c0, c1) against their own cutoff (rank rule over
+ * the c1 - c0 chains); the streams are keyed by the global chain index. */
+static int port_resample_range(const port_cfg* cfg, int N, int c0, int c1, int32_t* P, float* C,
+                               const double* prior, const double* lik, int mode, double param, uint32_t seed,
+                               double* cutoff_out) {
+    const int n = c1 - c0;
+    double* post = (double*)malloc((size_t)(n > 0 ? n : 1) * sizeof(double));
+    for (int h = 0; h < n; ++h) post[h] = prior[c0 + h] + lik[c0 + h];
+    qsort(post, (size_t)n, sizeof(double), port_cmp_bayes);
+    const double cutoff = mode == 1 ? post[n - 1] - param : post[(int)(n * param)];
     free(post);
     int redrawn = 0;
     const int PL = cfg->program_length;
-    for (int h = 0; h < N; ++h) {
+    for (int h = c0; h < c1; ++h) {
         if (!(prior[h] + lik[h] < cutoff)) continue;
         port_rng r;
         r.rng = 1;
@@ -516,6 +520,23 @@ int gpr_port_resample(const port_cfg* cfg, int N, int32_t* P, float* C, const do
         ++redrawn;
     }
     if (cutoff_out) *cutoff_out = cutoff;
+    return redrawn;
+}
+
+int gpr_port_resample(const port_cfg* cfg, int N, int32_t* P, float* C, const double* prior, const double* lik,
+                      int mode, double param, uint32_t seed, double* cutoff_out) {
+    return port_resample_range(cfg, N, 0, N, P, C, prior, lik, mode, param, seed, cutoff_out);
+}
+
+/* Batched data: the same per dataset, chains [d*N/nseg, (d+1)*N/nseg) of
+ * dataset d resampled against that dataset's cutoff (cutoffs_out[d]). */
+int gpr_port_resample_segments(const port_cfg* cfg, int N, int nseg, int32_t* P, float* C, const double* prior,
+                               const double* lik, int mode, double param, uint32_t seed, double* cutoffs_out) {
+    const int seg = N / nseg;
+    int redrawn = 0;
+    for (int d = 0; d < nseg; ++d)
+        redrawn += port_resample_range(cfg, N, d * seg, (d + 1) * seg, P, C, prior, lik, mode, param, seed,
+                                       cutoffs_out ? cutoffs_out + d : NULL);
     return redrawn;
 }
 

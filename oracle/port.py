@@ -51,6 +51,8 @@ def lib():
         L.gpr_port_loglik_grad_f64_nv.argtypes = [vp, ip, ip, ip, vp, vp, ip, vp, vp]
         L.gpr_port_loglik_grad_f64_nv.restype = dp
         L.gpr_port_resample.argtypes = [ctypes.POINTER(PortCfg), ip, vp, vp, vp, vp, ip, dp, ctypes.c_uint, vp]
+        L.gpr_port_resample_segments.argtypes = [ctypes.POINTER(PortCfg), ip, ip, vp, vp, vp, vp, ip, dp,
+                                                 ctypes.c_uint, vp]
         assert L.gpr_port_sizeof_cfg() == ctypes.sizeof(PortCfg)
         _lib = L
     return _lib
@@ -155,6 +157,19 @@ def resample(c, P, C, prior, lik, mode, param, seed):
     n = lib().gpr_port_resample(ctypes.byref(c), N, _p(P), _p(C), _p(prior), _p(lik), mode, param, seed,
                                 ctypes.byref(cut))
     return n, cut.value
+
+
+def resample_segments(c, P, C, prior, lik, nseg, mode, param, seed):
+    """resample per dataset of a batched handle: chains [d*N/nseg, (d+1)*N/nseg)
+    against their own cutoff; returns (number re-drawn, cutoffs)."""
+    PL, N = P.shape
+    assert P.dtype == np.int32 and C.dtype == np.float32 and P.flags.c_contiguous and C.flags.c_contiguous
+    prior = np.ascontiguousarray(prior, np.float64)
+    lik = np.ascontiguousarray(lik, np.float64)
+    cuts = np.zeros(nseg, np.float64)
+    n = lib().gpr_port_resample_segments(ctypes.byref(c), N, nseg, _p(P), _p(C), _p(prior), _p(lik), mode,
+                                         param, seed, _p(cuts))
+    return n, cuts
 
 
 def loglik_f64(P, idx, Cd, x, y, sd):

@@ -271,3 +271,45 @@ def test_autotune_leaves_the_state_and_sets_its_layout(batched):
         s.sync()
     finally:
         s.close()
+
+
+@pytest.mark.parametrize("mode,param", [(0, 0.5), (0, 0.0), (0, 0.9), (1, 20.0), (1, 0.0)])
+def test_resample_per_dataset_matches_oracle(mode, param):
+    """Batched data: each dataset's chains are resampled against the cutoff of
+    their own posteriors; cutoffs, the chains re-drawn and their new programs
+    and constants equal the oracle's per-dataset restatement bit for bit."""
+    port = pytest.importorskip("oracle.port")
+    sets = _datasets([50, 700, 9, 260], seed=5)
+    cpd = 96
+    N = cpd * len(sets)
+    kw = MODES["rw-philox"]
+    P0, C0 = g.host_init_chains(N, kw["program_length"], 44, ops=kw["ops"])
+    s = g.Sampler(N, **kw)
+    try:
+        s.set_batched_data(sets)
+        s.set_state(P0, C0)
+        s.run_block(30, 7)
+        P, C, prior, lik = s.get_state()
+        n_dev, cuts_dev = s.resample_datasets(len(sets), mode, param, seed=2024)
+        P1, C1, _, _ = s.get_state()
+        # gpr_resample on batched data: the same per-dataset rule, NaN cutoff
+        s.set_state(P, C)
+        s.set_scores(prior, lik)
+        n2, cut2 = s.resample(mode, param, seed=2024)
+        P2, C2, _, _ = s.get_state()
+    finally:
+        s.close()
+    Pr, Cr = P.copy(), C.copy()
+    n_ref, cuts_ref = port.resample_segments(port.cfg(PL=kw["program_length"], ops=kw["ops"]), Pr, Cr, prior, lik,
+                                             len(sets), mode, param, 2024)
+    assert np.array_equal(cuts_dev, cuts_ref, equal_nan=True), (cuts_dev, cuts_ref)
+    assert n_dev == n_ref == n2 and np.isnan(cut2)
+    assert np.array_equal(P1, Pr) and np.array_equal(C1.view(np.uint32), Cr.view(np.uint32))
+    assert np.array_equal(P2, Pr) and np.array_equal(C2.view(np.uint32), Cr.view(np.uint32))
+    # per dataset, the cutoff is the rank rule over that dataset's chains alone
+    post = prior + lik
+    for d in range(len(sets)):
+        seg = post[d * cpd:(d + 1) * cpd]
+        srt = np.concatenate([seg[np.isnan(seg)], np.sort(seg[~np.isnan(seg)])])
+        want = srt[-1] - param if mode == 1 else srt[int(cpd * param)]
+        assert (np.isnan(want) and np.isnan(cuts_dev[d])) or want == cuts_dev[d]

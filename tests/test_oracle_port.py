@@ -137,3 +137,35 @@ def test_rational_program_reads_its_five_constants():
     f = np.array([port.call_f64(P, C, 0, v) for v in x])
     want = (b[0] + b[1] * x + b[2] * x ** 2) / (1 + b[3] * x + b[4] * x ** 2)
     assert np.allclose(f, want, rtol=1e-5, atol=1e-6)
+
+
+def test_resample_segments_restates_resample_per_dataset():
+    """The per-dataset restatement: one segment is the plain resample; with
+    several, each segment's cutoff is the rank rule over its own chains and
+    only its own chains below it are re-drawn (streams keyed by the global
+    chain index)."""
+    N, PL, nseg = 400, 31, 4
+    P, C = H.random_programs(N, PL, ops=H.OPSET_BASIC, seed=1)
+    prior, lik = H.mixed_scores(N, seed=3)
+    c = port.cfg(PL=PL, ops=H.OPSET_BASIC)
+    P1, C1 = P.copy(), C.copy()
+    n1, cut1 = port.resample(c, P1, C1, prior, lik, 0, 0.5, 9)
+    P2, C2 = P.copy(), C.copy()
+    n2, cuts2 = port.resample_segments(c, P2, C2, prior, lik, 1, 0, 0.5, 9)
+    assert n1 == n2 and cut1 == cuts2[0] and np.array_equal(P1, P2) and np.array_equal(C1, C2)
+    for mode, param in ((0, 0.3), (1, 5.0)):
+        P3, C3 = P.copy(), C.copy()
+        n3, cuts3 = port.resample_segments(c, P3, C3, prior, lik, nseg, mode, param, 9)
+        seg = N // nseg
+        post = prior + lik
+        total = 0
+        for d in range(nseg):
+            s = post[d * seg:(d + 1) * seg]
+            srt = np.concatenate([s[np.isnan(s)], np.sort(s[~np.isnan(s)])])
+            want = srt[-1] - param if mode == 1 else srt[int(seg * param)]
+            assert (np.isnan(want) and np.isnan(cuts3[d])) or want == cuts3[d]
+            below = s < cuts3[d]
+            total += int(below.sum())
+            changed = ~np.all(P3[:, d * seg:(d + 1) * seg] == P[:, d * seg:(d + 1) * seg], axis=0)
+            assert not (changed & ~below).any()
+        assert n3 == total
