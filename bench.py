@@ -57,6 +57,10 @@ WORKLOADS = {
                                 mh_steps=100, map_delta=20.0, blocks=1),
 }
 METRIC = "MH chain-steps/s & point-evals/s (1 GB300); ESS/s gradient vs random-walk MH"
+# DRAM bytes (read + write) of one mh_block_kernel launch of the plain-mh-131k workload, from
+# the ncu capture summarised in profiles/mh_block_kernel_dram_plain-mh-131k.md: the chain state
+# read and written once; the dataset lives in shared memory.
+MH_LAUNCH_DRAM_BYTES = 113.43e6
 
 
 def dataset(w):
@@ -407,8 +411,10 @@ def run_batched(args, w):
     set {+,-,*,/,exp,log,pow,x,const}, random-walk constants (sd 0.1) with the
     reference's structure moves; the layout picked by the autotuner; one
     timed step = one replay of a captured graph of 5 MH blocks of 200 steps
-    (1000 MH steps per chain).  Beside it, the same chains run as 256
-    separate handles (one launch per dataset per block)."""
+    (1000 MH steps per chain), then the device resampling per dataset
+    (chains more than 20 log-units below their dataset's MAP re-drawn).
+    Beside it, the same chains run as 256 separate handles (one launch per
+    dataset per block)."""
     import torch
     import gpuropolis_gb300 as g
     dev = torch.device("cuda", 0)
@@ -443,6 +449,7 @@ def run_batched(args, w):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
             s.run_captured([1000 * (i + 1) + b for b in range(nb)])
+            s.lib.gpr_resample_datasets(s.h, 1, 20.0, 77 + i, None, None)
             e1.record(stream)
             evs.append((e0, e1))
         torch.cuda.synchronize()
@@ -465,6 +472,7 @@ def run_batched(args, w):
     for i in range(e2e_steps):
         lib.gpr_set_state(s.h, ptr(Ph), ptr(Ch))
         lib.gpr_run_captured(s.h, ptr(seeds + i))
+        lib.gpr_resample_datasets(s.h, 1, 20.0, 99 + i, None, None)
         lib.gpr_get_state(s.h, ptr(Ph), ptr(Ch), ptr(prh), ptr(lih))
     e2e = N * steps * nb * e2e_steps / (time.perf_counter() - t0)
     Pw, Cw, _, _ = s.get_state()
@@ -517,6 +525,7 @@ def run_batched(args, w):
                               "median": float(np.median(sizes))},
                    "generator_nodes": {"min": min(c for _, _, c in gens), "max": max(c for _, _, c in gens)},
                    "mh_steps_per_block": steps, "blocks_per_replay": nb, "rng": "lcg",
+                   "resample": "per dataset, map-delta 20, on the device after each replay",
                    "const_proposal": "rw:%g" % w["rw_sd"], "l2": "flushed between replays (256 MB write)",
                    "launch_default": default_geo, "launch": geo, "autotuned": tuned}}))
 
@@ -697,7 +706,8 @@ def run_gpu(args, w):
                 "d2h_bytes_per_step": d2h, "blocks": e2e_blocks},
         "gpu_launches": launches,
         "roofline": {"bound": "fp32-issue", "achieved": achieved_tops, "peak": peak_tops,
-                     "unit": "T-ops/s", "frac": achieved_tops / peak_tops, "traffic": None,
+                     "unit": "T-ops/s", "frac": achieved_tops / peak_tops,
+                     "traffic": MH_LAUNCH_DRAM_BYTES if args.workload == "plain-mh-131k" else None,
                      "note": "algorithmic FP32 ops = (node count + 4) per point evaluated; peak = "
                              "SMs x 128 lanes x max SM clock (nominal, no measured FP32 peak)"},
         "stats": st,
