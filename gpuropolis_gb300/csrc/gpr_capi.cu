@@ -298,7 +298,7 @@ static int batched_wpc(const gpr::KParams& kp, int wpc) {
  * most ctas_per_sm CTAs per SM (0: as many as fit).  Capping the CTAs also
  * caps the shared-memory carveout, which leaves the rest of the SM's L1 to
  * the thread-local gradient tapes. */
-static int configure_hmc(gpr_handle* h, int wpc0 = 4, int ctas_per_sm = 0) {
+static int configure_hmc(gpr_handle* h, int wpc0 = 4, int ctas_per_sm = 0, int stream_mode = -1) {
     if (wpc0 < 1 || wpc0 > 4) wpc0 = 4;   /* the kernel is built for CTAs of at most 128 threads */
     drop_graph(h);
     gpr::KParams& kp = h->kp;
@@ -306,8 +306,14 @@ static int configure_hmc(gpr_handle* h, int wpc0 = 4, int ctas_per_sm = 0) {
         return fail(h, GPR_ERR_ARG, "gradient moves support program_length <= 127 (got %d)", kp.PL);
     gpr::LaunchCfg lc;
     lc.K = 4; lc.onepass = 0; lc.rolled = 0; lc.lockstep = 0; lc.carveout = 0;
-    /* batched data: each warp reads its own chain's dataset from device memory */
-    lc.stream = h->stream_data || kp.nds > 0 || gpr::grad_smem_bytes(kp, wpc0) > 227 * 1024;
+    /* Streamed when asked, for batched data (each warp reads its own chain's
+     * dataset from device memory), when staging does not fit, and when the
+     * staged copy would take over a quarter of the CTA's shared memory: the
+     * memory it frees goes to L1, which holds the gradient tapes (on the
+     * 1024-point rational model streaming measured 23% faster). */
+    const size_t staged = gpr::grad_smem_bytes(kp, wpc0, 0), streamed = gpr::grad_smem_bytes(kp, wpc0, 1);
+    lc.stream = h->stream_data || kp.nds > 0 || staged > 227 * 1024 ||
+                (stream_mode < 0 ? 4 * (staged - streamed) > staged : stream_mode > 0);
     int wpc = wpc0;
     size_t smem = gpr::grad_smem_bytes(kp, wpc, lc.stream);
     while (smem > 227 * 1024 && wpc > 1) smem = gpr::grad_smem_bytes(kp, wpc /= 2, lc.stream);
@@ -786,9 +792,13 @@ int gpr_autotune(gpr_handle* h, int steps, int seed, int* K, int* onepass, int* 
     /* the Hamiltonian kernel: CTA size and resident CTAs per SM, i.e. occupancy
      * against L1 left for the gradient tapes */
     if (hmc) {
-        const int shapes[5][2] = {{4, 0}, {4, 5}, {4, 4}, {2, 0}, {1, 0}};
-        for (int i = 0; i < 5; ++i) {
-            if (configure_hmc(h, shapes[i][0], shapes[i][1]) != GPR_OK) continue;
+        /* CTA size and residency cap, each with the data staged (unless the
+         * handle always streams) and streamed */
+        const int shapes[6][2] = {{4, 0}, {4, 7}, {4, 5}, {4, 4}, {2, 0}, {1, 0}};
+        for (int i = 0; i < 12; ++i) {
+            const int want_stream = i >= 6;
+            if (configure_hmc(h, shapes[i % 6][0], shapes[i % 6][1], want_stream) != GPR_OK) continue;
+            if (h->lc.stream != want_stream) continue;   /* forced one way: tried once */
             for (int rep = 0; rep < 2; ++rep) {
                 AT_TRY(cudaMemcpyAsync(h->dP, sP, cnt * sizeof(int32_t), cudaMemcpyDeviceToDevice, h->stream));
                 AT_TRY(cudaMemcpyAsync(h->dC, sC, cnt * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));

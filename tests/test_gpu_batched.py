@@ -244,16 +244,19 @@ def test_batched_layouts_equal_single_dataset_runs(layout):
             s.close()
 
 
+@pytest.mark.parametrize("mode", ["rw-philox", "hmc"])
 @pytest.mark.parametrize("batched", [False, True])
-def test_autotune_leaves_the_state_and_sets_its_layout(batched):
-    """The autotuner's trial blocks (staged and streamed layouts) leave the
-    chains, scores and counters as they were, and the layout it reports is
-    the one the handle then runs."""
-    kw = MODES["rw-philox"]
+def test_autotune_leaves_the_state_and_sets_its_layout(batched, mode):
+    """The autotuner's trial blocks (staged and streamed layouts; for
+    Hamiltonian moves CTA shapes and residency caps) leave the chains, scores
+    and counters as they were, and the layout it reports is the one the
+    handle then runs."""
+    kw = MODES[mode]
     N = 64 * 4
     P, C = g.host_init_chains(N, kw["program_length"], 8, ops=kw["ops"])
     s = g.Sampler(N, **kw)
     try:
+        _setup(s, mode)
         if batched:
             s.set_batched_data(_datasets([90, 400, 12, 150], seed=2))
         else:
