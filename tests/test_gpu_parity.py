@@ -31,7 +31,7 @@ def lib():
     return g.library()
 
 
-@pytest.mark.parametrize("PL", [31, 63])
+@pytest.mark.parametrize("PL", [1, 31, 63, 255])
 def test_eval_values_match_reference(lib, PL):
     _need_ref()
     N = 1024
@@ -114,13 +114,30 @@ def test_prior_likelihood_match_reference(lib, data):
 
 
 CASES = [
-    # (PL, opset, rng, const mode, rw_sd, data)
-    (31, None, g.RNG_LCG, g.CONST_REFERENCE, 0.0, "quad"),
-    (31, None, g.RNG_PHILOX, g.CONST_REFERENCE, 0.0, "quad"),
-    (31, H.OPSET_BASIC, g.RNG_LCG, g.CONST_RANDOM_WALK, 0.1, "quad"),
-    (63, H.OPSET_BASIC, g.RNG_LCG, g.CONST_RANDOM_WALK, 0.1, "expdecay"),
-    (63, None, g.RNG_PHILOX, g.CONST_REFERENCE, 0.0, "expdecay"),
+    # (N, PL, opset, rng, const mode, rw_sd, data)
+    (1024, 31, None, g.RNG_LCG, g.CONST_REFERENCE, 0.0, "quad"),
+    (1024, 31, None, g.RNG_PHILOX, g.CONST_REFERENCE, 0.0, "quad"),
+    (1024, 31, H.OPSET_BASIC, g.RNG_LCG, g.CONST_RANDOM_WALK, 0.1, "quad"),
+    (1024, 63, H.OPSET_BASIC, g.RNG_LCG, g.CONST_RANDOM_WALK, 0.1, "expdecay"),
+    (1024, 63, None, g.RNG_PHILOX, g.CONST_REFERENCE, 0.0, "expdecay"),
+    # edges: chain counts that leave a CTA's chain group partly empty, a single
+    # chain, the shortest and the longest programs, and an empty dataset
+    (13, 31, None, g.RNG_LCG, g.CONST_REFERENCE, 0.0, "quad"),
+    (1001, 31, H.OPSET_BASIC, g.RNG_LCG, g.CONST_RANDOM_WALK, 0.1, "quad"),
+    (1, 31, None, g.RNG_PHILOX, g.CONST_REFERENCE, 0.0, "quad"),
+    (256, 1, None, g.RNG_LCG, g.CONST_REFERENCE, 0.0, "quad"),
+    (96, 255, H.OPSET_BASIC, g.RNG_LCG, g.CONST_RANDOM_WALK, 0.1, "expdecay"),
+    (256, 31, H.OPSET_BASIC, g.RNG_LCG, g.CONST_RANDOM_WALK, 0.1, "empty"),
 ]
+
+
+def _case_data(data):
+    if data == "quad":
+        return H.quad_data()
+    if data == "expdecay":
+        return H.expdecay_data()
+    z = np.zeros(0, np.float32)
+    return z, z, z
 
 
 def _fragile(tr):
@@ -141,8 +158,8 @@ def _fragile(tr):
     return abs(np.log(max(u, 1e-30)) - acc) <= noise or abs(acc) <= noise
 
 
-@pytest.mark.parametrize("case", CASES, ids=lambda c: "pl%d-%s-%s-%s" % (
-    c[0], "basic" if c[1] else "ref", "philox" if c[2] else "lcg", "rw" if c[3] else "indep"))
+@pytest.mark.parametrize("case", CASES, ids=lambda c: "n%d-pl%d-%s-%s-%s-%s" % (
+    c[0], c[1], "basic" if c[2] else "ref", "philox" if c[3] else "lcg", "rw" if c[4] else "indep", c[6]))
 def test_mh_block_matches_reference(lib, case):
     """After a block, chains are bit-identical to the reference's; every chain
     that is not has, at or before its first differing step, an accept decision
@@ -150,9 +167,9 @@ def test_mh_block_matches_reference(lib, case):
     bit-exact)."""
     _need_ref()
     from oracle import port
-    PL, ops, rng, cmode, rw_sd, data = case
-    N, steps, seed = 1024, 25, 987654
-    x, y, sd = H.quad_data() if data == "quad" else H.expdecay_data()
+    N, PL, ops, rng, cmode, rw_sd, data = case
+    steps, seed = 25, 987654
+    x, y, sd = _case_data(data)
     P, C = H.random_programs(N, PL, ops=ops, seed=11)
     s = g.Sampler(N, program_length=PL, ops=ops, rng=rng, const_proposal=cmode, rw_sd=rw_sd)
     s.set_data(x, y, sd)
@@ -164,7 +181,9 @@ def test_mh_block_matches_reference(lib, case):
     Pr, Cr = P.copy(), C.copy()
     prior_r, lik_r = o.run_kernel(Pr, Cr, x, y, sd, steps, seed)
     same = np.all(Pg == Pr, axis=0) & np.all(Cg.view(np.int32) == Cr.view(np.int32), axis=0)
-    assert same.mean() >= 0.9, "bit-identical chains: %.4f" % same.mean()
+    # (with few chains the fraction is coarse; the explanation of every
+    # divergence below is the criterion that holds at any N)
+    assert same.mean() >= 0.9 or N < 100, "bit-identical chains: %.4f" % same.mean()
 
     # every divergence starts at a fragile decision of the reference
     c = port.cfg(PL, ops=o.ops, rng=int(rng == g.RNG_PHILOX), const_mode=cmode, rw_sd=rw_sd, project_math=1)
