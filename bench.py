@@ -28,11 +28,14 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
+# where the nvidia-smi clock samples of the timed regions are written
+CLOCKS_DIR = os.environ.get("GPR_CLOCKS_DIR", tempfile.gettempdir())
 sys.path.insert(0, ROOT)
 
 from tests import helpers as H  # noqa: E402  (seeded synthetic inputs)
@@ -441,8 +444,7 @@ def run_batched(args, w):
     s.reset_stats()
     launches0 = s.launch_count()
     evs = []
-    clk = ClockSampler(os.path.join(ROOT, "gpurun_out", "clocks_batched.csv")
-                       if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp/gpr_clocks_b.csv")
+    clk = ClockSampler(os.path.join(CLOCKS_DIR, "clocks_batched.csv"))
     with clk:
         for i in range(args.steps):
             flush.zero_()
@@ -623,8 +625,7 @@ def run_gpu(args, w):
 
     # device-resident timed loop: per block CUDA events around the kernel
     evs = []
-    clk = ClockSampler(os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")
-                       if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp/gpr_clocks.csv")
+    clk = ClockSampler(os.path.join(CLOCKS_DIR, "clocks_bench.csv"))
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()

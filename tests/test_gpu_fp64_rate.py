@@ -1,6 +1,6 @@
 """The reason the kernel issues no FP64 arithmetic in its step loop: on GB300,
 FP64 throughput is a small fraction of FP32.  Measured with cuBLAS GEMMs
-(DGEMM vs SGEMM without TF32), the printed rates are what the design doc cites."""
+(DGEMM vs SGEMM without TF32); the test prints both rates."""
 import time
 
 import pytest

@@ -14,7 +14,9 @@ from tests import helpers as H
 g = pytest.importorskip("gpuropolis_gb300")
 oref = pytest.importorskip("oracle.ref")
 
-NIST = "/root/reference/data-sources/NIST"
+from oracle import build_ref  # noqa: E402
+
+NIST = os.path.join(build_ref.REF_DIR, "data-sources", "NIST")
 
 
 def _need_ref():
