@@ -221,3 +221,40 @@ def test_mh_block_matches_reference(lib, case):
     bad = (rel > 1e-5) & (cond <= 1e-6)
     assert not bad.any(), list(zip(idx[bad][:5], rel[bad][:5], cond[bad][:5]))
     s.close()
+
+
+@pytest.mark.parametrize("cmode,rw_sd", [(g.CONST_RANDOM_WALK, 0.1), (g.CONST_REFERENCE, 0.0)],
+                         ids=["rw", "indep"])
+def test_posterior_distribution_matches_reference_ks(lib, cmode, rw_sd):
+    """Agreement in distribution over long runs, where FP32-fragile accept
+    decisions have long since made individual chains differ: 1024 chains
+    from the same starting programs, 1000 MH steps, the device with one seed
+    and the reference's own code with another; the chains' final
+    log-posteriors must agree under a two-sample Kolmogorov-Smirnov test, and
+    so must the node counts of the final programs."""
+    _need_ref()
+    from scipy import stats
+    N, PL, steps = 1024, 31, 1000
+    ops = H.OPSET_BASIC
+    x, y, sd = H.quad_data()
+    P, C = H.random_programs(N, PL, ops=ops, seed=21)
+    s = g.Sampler(N, program_length=PL, ops=ops, rng=g.RNG_LCG, const_proposal=cmode, rw_sd=rw_sd)
+    try:
+        s.set_data(x, y, sd)
+        s.set_state(P, C)
+        s.run_block(steps, 1234)
+        Pg, Cg, prior_g, lik_g = s.get_state()
+        _, _, count_g = s.eval_values(x[:1])
+    finally:
+        s.close()
+    o = oref.get(pl=PL, opset=1, philox=0, project_math=1, rw_sd=rw_sd)
+    Pr, Cr = P.copy(), C.copy()
+    prior_r, lik_r = o.run_kernel(Pr, Cr, x, y, sd, steps, 5678)
+    count_r = np.array([o.count_nodes(Pr, Cr, i) for i in range(N)])
+    post_g, post_r = prior_g + lik_g, prior_r + lik_r
+    fin_g, fin_r = post_g[np.isfinite(post_g)], post_r[np.isfinite(post_r)]
+    assert len(fin_g) > N // 2 and len(fin_r) > N // 2
+    ks = stats.ks_2samp(fin_g, fin_r)
+    assert ks.pvalue > 1e-3, (ks, np.median(fin_g), np.median(fin_r))
+    kc = stats.ks_2samp(count_g, count_r)
+    assert kc.pvalue > 1e-3, kc
