@@ -52,6 +52,9 @@ WORKLOADS = {
     # each, in one launch; blocks replayed from a captured graph
     "batched-256ds-131k": dict(N=131072, PL=47, nds=256, data="batched", ops="basic", rw_sd=0.1,
                                mh_steps=200, blocks=5),
+    # the streamed workload cut to 8192 chains x 5 steps: the case ncu captures
+    "streamed-3var-8k-profile": dict(N=8192, PL=127, nd=65536, data="multivar", ops="multi", rw_sd=0.1,
+                                     mh_steps=5, map_delta=0.0, blocks=1),
     # Hamiltonian moves on 8192 chains of the rational model: the case ncu captures
     "hmc-rational-8k-profile": dict(N=8192, PL=31, nd=1024, data="rational", ops="basic", rw_sd=0.0,
                                     mh_steps=20, map_delta=0.0, blocks=1),
@@ -737,7 +740,7 @@ def main():
     if args.workload == "hmc-rational-8k-profile":
         run_hmc_profile(args)
         return
-    if args.workload == "streamed-3var-16k":
+    if args.workload in ("streamed-3var-16k", "streamed-3var-8k-profile"):
         run_streamed(args, w)
         return
     if args.workload == "batched-256ds-131k":

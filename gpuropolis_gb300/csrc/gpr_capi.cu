@@ -386,6 +386,12 @@ static int configure_launch(gpr_handle* h, int K, int onepass, int rolled, int l
  * when the data fit, heavy ops unrolled (the fastest layout measured on the
  * 250-point, PROGRAM_LENGTH 63 workload; gpr_autotune re-checks per dataset). */
 static int choose_launch(gpr_handle* h) {
+    /* A dataset of more than GPR_MAX_PASSES passes cannot be split across a
+     * CTA's warps: each warp evaluates its own chain, and step barriers would
+     * make every warp wait for the CTA's longest program.  Free-running warps
+     * in 4-warp CTAs instead (65,536 points, PL 127: 1.06e6 against 6.0e5
+     * chain-steps/s).  Batched data keep their CTA chain groups. */
+    if ((h->kp.nd + 127) / 128 > GPR_MAX_PASSES && h->kp.nds == 0) return configure_launch(h, 4, 0, 0, 0, 4);
     /* three input variables: built for K = 4 in passes only */
     return configure_launch(h, 4, (h->kp.nd <= 128 && h->kp.nv != 3) ? 1 : 0, 0, 1, 8);
 }

@@ -116,6 +116,10 @@ enum gpr_stat {
     GPR_NSTATS
 };
 
+/* Passes (32*K points each) a CTA-balanced evaluation can split a dataset
+ * into; beyond it each warp evaluates its own chain. */
+#define GPR_MAX_PASSES 64
+
 /* Maximum compiled length for a program of PL heap nodes. */
 #define GPR_MAX_INSTR(PL) (2 * (PL) + 4)
 

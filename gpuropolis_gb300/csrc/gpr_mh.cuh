@@ -36,8 +36,6 @@
 namespace gpr {
 
 #define FULLMASK 0xffffffffu
-/* passes (32*K points each) a CTA-balanced evaluation can split a dataset into */
-#define GPR_MAX_PASSES 64
 
 __host__ __device__ __forceinline__ size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
 
