@@ -276,6 +276,19 @@ int gpr_destroy(gpr_handle* h) {
     return GPR_OK;
 }
 
+/* The handle has no dataset until a new one is fully uploaded: a failure
+ * while replacing the data leaves no pointer to freed device memory behind
+ * (gpr_run_block then reports that no data were set). */
+static void forget_data(gpr_handle* h) {
+    h->nd = -1;
+    h->nd_pad = 0;
+    gpr::KParams& kp = h->kp;
+    kp.nd = 0; kp.nd_pad = 0; kp.nds = 0;
+    kp.dx = kp.dy = kp.dw = kp.dx2 = kp.dx3 = nullptr;
+    kp.ds_off = kp.ds_n = kp.ds_order = nullptr;
+    kp.ds_ns = nullptr;
+}
+
 /* A captured block sequence bakes the launch parameters in: any change of
  * data, layout or moves drops it. */
 static void drop_graph(gpr_handle* h) {
@@ -426,8 +439,9 @@ static int set_data_impl(gpr_handle* h, const float* x, const float* x2, const f
         normsum += 0.5 * ((double)logf((float)(2.0 * PIf)) + 2.0 * (double)logf(sd[i]));
     }
     drop_graph(h);
-    h->kp.nds = 0;
-    if (h->ddata) { CUDA_TRY(h, cudaStreamSynchronize(h->stream)); cudaFree(h->ddata); h->ddata = nullptr; }
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    forget_data(h);
+    if (h->ddata) { cudaFree(h->ddata); h->ddata = nullptr; }
     if (nd_pad > 0) {
         CUDA_TRY(h, cudaMalloc(&h->ddata, host.size() * sizeof(float)));
         CUDA_TRY(h, cudaMemcpyAsync(h->ddata, host.data(), host.size() * sizeof(float),
@@ -509,7 +523,9 @@ int gpr_set_batched_data(gpr_handle* h, int n_datasets, const int* sizes, const 
     for (int d = 0; d < n_datasets; ++d) order[d] = d;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return sizes[a] > sizes[b]; });
     for (int d = 0; d < n_datasets; ++d) meta[2 * n_datasets + d] = order[d];
-    if (h->ddata) { CUDA_TRY(h, cudaStreamSynchronize(h->stream)); cudaFree(h->ddata); h->ddata = nullptr; }
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    forget_data(h);
+    if (h->ddata) { cudaFree(h->ddata); h->ddata = nullptr; }
     cudaFree(h->dds); cudaFree(h->dds_ns);
     h->dds = nullptr; h->dds_ns = nullptr;
     CUDA_TRY(h, cudaMalloc(&h->ddata, host.size() * sizeof(float)));
