@@ -113,6 +113,41 @@ def test_prior_likelihood_match_reference(lib, data):
     s.close()
 
 
+
+@pytest.mark.parametrize("data,PL,ops", [("quad", 31, None), ("expdecay", 63, H.OPSET_BASIC)],
+                         ids=["quad-pl31-ref", "expdecay-pl63-basic"])
+def test_loglik_error_vs_fp64(lib, data, PL, ops):
+    """The device log-likelihood (FP32 evaluation, double-float accumulation,
+    no FP64 instruction) against the FP64 evaluation of the same programs:
+    within 1e-5 relative wherever the program's FP32 evaluation is itself
+    determined to 1e-6 (the reference's FP32 result, compiled for the host,
+    lies within 1e-6 of FP64); chains outside that are counted, not judged."""
+    _need_ref()
+    from oracle import port
+    N = 2048
+    x, y, sd = H.quad_data() if data == "quad" else H.expdecay_data()
+    P, C = H.random_programs(N, PL, ops=ops, seed=17)
+    s = g.Sampler(N, program_length=PL, ops=ops)
+    try:
+        s.set_data(x, y, sd)
+        s.set_state(P, C)
+        _, lik = s.evaluate()
+    finally:
+        s.close()
+    o = oref.get(pl=PL, opset=1 if ops else 0, project_math=1)
+    rlik = np.array([o.likelihood(P, C, i, x, y, sd) for i in range(N)])
+    f64 = np.array([port.likelihood(P, C, i, x, y, sd, f64=True) for i in range(N)])
+    with np.errstate(all="ignore"):
+        cond = np.abs(rlik - f64) / np.maximum(np.abs(f64), 1.0)
+        err = np.abs(lik - f64) / np.maximum(np.abs(f64), 1.0)
+    ok = np.isfinite(f64) & np.isfinite(rlik) & (cond <= 1e-6)
+    assert ok.sum() > N // 10, ok.sum()
+    assert np.all(np.isfinite(lik[ok]))
+    assert err[ok].max() <= 1e-5, (err[ok].max(), np.where(ok)[0][np.argmax(err[ok])])
+    print("loglik rel. error vs FP64 (%d well-conditioned chains of %d): median %.2e, max %.2e"
+          % (ok.sum(), N, np.median(err[ok]), err[ok].max()))
+
+
 CASES = [
     # (N, PL, opset, rng, const mode, rw_sd, data)
     (1024, 31, None, g.RNG_LCG, g.CONST_REFERENCE, 0.0, "quad"),
