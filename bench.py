@@ -664,11 +664,14 @@ def run_gpu(args, w):
     e2e_blocks = max(1, min(args.steps, 5))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    # the drop-in's block loop through the C ABI, as the CLI runs it with --device-resample:
+    # state in from pinned host buffers, the block, the MAP-delta resampling on the device,
+    # state out to pinned host buffers (where samples.txt is written from)
     for i in range(e2e_blocks):
         lib.gpr_set_state(s.h, ptr(Ph), ptr(Ch))
         lib.gpr_run_block(s.h, w["mh_steps"], 7919 * (i + 1))
+        lib.gpr_resample(s.h, 1, w["map_delta"], 31 * (i + 1), None, None)
         lib.gpr_get_state(s.h, ptr(Ph), ptr(Ch), ptr(prh), ptr(lih))
-        resample_host(Ph, Ch, prh, lih, w["map_delta"], ops, hostrng)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     e2e_value = world * w["N"] * w["mh_steps"] * e2e_blocks / e2e_s
@@ -707,7 +710,9 @@ def run_gpu(args, w):
                    "l2": "flushed between blocks (256 MB write)", "parallelism": "replicas" if world > 1 else "1 GPU",
                    "launch": geo, "autotuned": tuned},
         "e2e": {"value": e2e_value, "unit": "chain-steps/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "blocks": e2e_blocks},
+                "d2h_bytes_per_step": d2h, "blocks": e2e_blocks,
+                "loop": "gpr_set_state (pinned host), gpr_run_block, gpr_resample (device, map-delta), "
+                        "gpr_get_state (pinned host)"},
         "gpu_launches": launches,
         "roofline": {"bound": "fp32-issue", "achieved": achieved_tops, "peak": peak_tops,
                      "unit": "T-ops/s", "frac": achieved_tops / peak_tops,
