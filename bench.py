@@ -373,6 +373,22 @@ def run_streamed(args, w):
                    "ops": "{+,-,*,/,sin,cos,exp,x1,x2,x3,const}", "launch": geo}}))
 
 
+def hbm_roofline(point_evals, seconds, peaks, traffic):
+    """The MH kernel against the HBM roof: algorithmic bytes = 12 per
+    point-eval (x, y and the weight of one point), over the timed launches.
+    The kernel reads them from shared memory or registers, not HBM (its DRAM
+    traffic per launch is `traffic`, the chain state); what bounds it is the
+    interpreter's instruction latency (roofline_fp32_issue, profiles/)."""
+    peak = peaks.get("hbm_gbs")
+    achieved = point_evals * 12 / seconds / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak if peak else None, "traffic": traffic,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if peak else None,
+            "note": "12 algorithmic bytes per point-eval, served from shared memory (staged layout) or "
+                    "L1/L2 (streamed layout), not HBM; DRAM traffic per launch (traffic) is the chain state. "
+                    "The kernel is latency-bound, not HBM-bound."}
+
+
 def batched_datasets(g, nds, seed=2024):
     """nds datasets: sizes log-uniform in [8, 4096], x ~ U[-5, 5], y = f(x) +
     N(0, 0.01 std f(x)) with f a program of 3-15 nodes drawn from the prior
@@ -520,8 +536,9 @@ def run_batched(args, w):
         "e2e": {"value": e2e, "unit": "chain-steps/s", "h2d_bytes_per_step": Ph.nbytes + Ch.nbytes,
                 "d2h_bytes_per_step": Ph.nbytes + Ch.nbytes + prh.nbytes + lih.nbytes, "steps": e2e_steps},
         "gpu_launches": launches,
-        "roofline": {"bound": "fp32-issue", "achieved": achieved, "peak": peak_tops, "unit": "T-ops/s",
-                     "frac": achieved / peak_tops, "traffic": None},
+        "roofline": hbm_roofline(st["eval_points"], ms / 1e3, peaks, None),
+        "roofline_fp32_issue": {"bound": "fp32-issue", "achieved": achieved, "peak": peak_tops,
+                                "unit": "T-ops/s", "frac": achieved / peak_tops},
         "acceptance": {"structure": st["struct_accepted"] / max(1, st["struct_proposed"]),
                        "constant": st["const_accepted"] / max(1, st["const_proposed"])},
         "clocks": clk.summary(0),
@@ -714,11 +731,12 @@ def run_gpu(args, w):
                 "loop": "gpr_set_state (pinned host), gpr_run_block, gpr_resample (device, map-delta), "
                         "gpr_get_state (pinned host)"},
         "gpu_launches": launches,
-        "roofline": {"bound": "fp32-issue", "achieved": achieved_tops, "peak": peak_tops,
-                     "unit": "T-ops/s", "frac": achieved_tops / peak_tops,
-                     "traffic": MH_LAUNCH_DRAM_BYTES if args.workload == "plain-mh-131k" else None,
-                     "note": "algorithmic FP32 ops = (node count + 4) per point evaluated; peak = "
-                             "SMs x 128 lanes x max SM clock (nominal, no measured FP32 peak)"},
+        "roofline": hbm_roofline(st["eval_points"], kernel_ms / 1e3, peaks,
+                                 MH_LAUNCH_DRAM_BYTES if args.workload == "plain-mh-131k" else None),
+        "roofline_fp32_issue": {"bound": "fp32-issue", "achieved": achieved_tops, "peak": peak_tops,
+                                "unit": "T-ops/s", "frac": achieved_tops / peak_tops,
+                                "note": "algorithmic FP32 ops = (node count + 4) per point evaluated; peak = "
+                                        "SMs x 128 lanes x max SM clock (nominal, no measured FP32 peak)"},
         "stats": st,
         "acceptance": {"structure": st["struct_accepted"] / max(1, st["struct_proposed"]),
                        "constant": st["const_accepted"] / max(1, st["const_proposed"])},
