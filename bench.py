@@ -629,7 +629,16 @@ def run_gpu(args, w):
     def block(i):
         s.run_block(w["mh_steps"], 1000003 * (i + 1) + rank)
 
+    nres = [0]
+
     def resample():
+        if world > 1:
+            # one population over all ranks: the MAP-delta cutoff over every rank's chains
+            # (one all_reduce), each rank re-drawing its own chains on its device
+            from gpuropolis_gb300 import population
+            nres[0] += 1
+            population.resample_population(s, 1, w["map_delta"], 4242 + nres[0])
+            return
         P, C, prior, lik = s.get_state()
         resample_host(P, C, prior, lik, w["map_delta"], ops, hostrng)
         s.set_state(P, C)
@@ -724,7 +733,9 @@ def run_gpu(args, w):
         "point_evals_per_s": value * w["nd"],
         "config": {"workload": args.workload, **{k: w[k] for k in ("N", "PL", "nd", "mh_steps", "map_delta")},
                    "ops": w["ops"], "const_proposal": "rw:%g" % w["rw_sd"], "rng": "lcg",
-                   "l2": "flushed between blocks (256 MB write)", "parallelism": "replicas" if world > 1 else "1 GPU",
+                   "l2": "flushed between blocks (256 MB write)",
+                   "parallelism": "one population over %d GPUs (resampling cutoff exchanged per block, "
+                                  "outside the timed region)" % world if world > 1 else "1 GPU",
                    "launch": geo, "autotuned": tuned},
         "e2e": {"value": e2e_value, "unit": "chain-steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "blocks": e2e_blocks,

@@ -103,6 +103,7 @@ def library():
     lib.gpr_run_block_traced.argtypes = [vp, ip, ip, ip, vp]
     lib.gpr_set_batched_data.argtypes = [vp, ip, vp, vp, vp, vp, vp, vp]
     lib.gpr_resample_datasets.argtypes = [vp, ip, dp, ctypes.c_uint32, vp, vp]
+    lib.gpr_resample_below.argtypes = [vp, dp, ctypes.c_uint32, ip, vp]
     lib.gpr_capture_blocks.argtypes = [vp, ip, ip]
     lib.gpr_run_captured.argtypes = [vp, vp]
     lib.gpr_resample.argtypes = [vp, ip, dp, ctypes.c_uint32, vp, vp]
@@ -221,6 +222,13 @@ class Sampler:
         C = np.ascontiguousarray(C, np.float32).reshape(self.PL, self.N)
         self._check(self.lib.gpr_set_state(self.h, _ptr(P), _ptr(C)))
 
+    def get_scores(self):
+        """(prior, likelihood) of every chain, without the programs."""
+        prior = np.empty(self.N, np.float64)
+        lik = np.empty(self.N, np.float64)
+        self._check(self.lib.gpr_get_state(self.h, None, None, _ptr(prior), _ptr(lik)))
+        return prior, lik
+
     def get_state(self):
         P = np.empty((self.PL, self.N), np.int32)
         C = np.empty((self.PL, self.N), np.float32)
@@ -333,6 +341,14 @@ class Sampler:
         self._check(self.lib.gpr_resample(self.h, int(mode), float(param), int(seed) & 0xffffffff,
                                           ctypes.byref(n), ctypes.byref(cut)))
         return n.value, cut.value
+
+    def resample_below(self, cutoff, seed=1, chain_offset=0):
+        """Re-draw the chains below an explicit cutoff (gpr_resample_below);
+        returns the number re-drawn."""
+        n = ctypes.c_int()
+        self._check(self.lib.gpr_resample_below(self.h, float(cutoff), int(seed) & 0xffffffff, int(chain_offset),
+                                                ctypes.byref(n)))
+        return n.value
 
     def resample_datasets(self, n_datasets, mode=0, param=0.5, seed=1):
         """Per-dataset device resampling (gpr_resample_datasets): returns

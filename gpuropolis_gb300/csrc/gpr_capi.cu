@@ -1145,6 +1145,31 @@ int gpr_resample(gpr_handle* h, int mode, double param, uint32_t seed, int* n_re
     return gpr_resample_datasets(h, mode, param, seed, n_redrawn, cutoff);
 }
 
+int gpr_resample_below(gpr_handle* h, double cutoff, uint32_t seed, int chain_offset, int* n_redrawn) {
+    if (!h) return GPR_ERR_ARG;
+    if (h->cfg.n_ops < 2)
+        return fail(h, GPR_ERR_ARG, "re-drawing ops needs at least 2 ops (random_int(n_ops - 1))");
+    if (chain_offset < 0) return fail(h, GPR_ERR_ARG, "chain_offset must be >= 0 (got %d)", chain_offset);
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    int rc = ensure_select(h);
+    if (rc != GPR_OK) return rc;
+    /* the cutoff as a selected key (gpr_select.h keys round-trip every value) */
+    const unsigned long long key = gpr_post_key(cutoff);
+    CUDA_TRY(h, cudaMemcpyAsync(h->dsel, &key, sizeof key, cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaMemsetAsync(h->dseli, 0, sizeof(int), h->stream));
+    const gpr::Magic mops1 = magic_for(divisor_for(h->cfg.n_ops - 1));
+    const gpr::Magic morder = magic_for(divisor_for(8));
+    CUDA_TRY(h, gpr::launch_redraw(h->kp, h->dsel, 0, 0, 0.0, seed, mops1, morder, h->dseli, h->stream,
+                                   (uint32_t)chain_offset));
+    h->launches++;
+    /* the key's host copy must outlive the asynchronous copy: wait here */
+    int cnt = 0;
+    CUDA_TRY(h, cudaMemcpyAsync(&cnt, h->dseli, sizeof cnt, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    if (n_redrawn) *n_redrawn = cnt;
+    return GPR_OK;
+}
+
 int gpr_top_chains(gpr_handle* h, int k, double margin, int* chains, int capacity, int* n, double* threshold) {
     if (!h) return GPR_ERR_ARG;
     if (k < 1 || k > h->N) return fail(h, GPR_ERR_ARG, "k = %d is not in [1, %d]", k, h->N);

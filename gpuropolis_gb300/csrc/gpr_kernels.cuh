@@ -158,7 +158,7 @@ cudaError_t launch_select(const KParams& p, int rank, unsigned long long* keys, 
                           cudaStream_t st, int segments = 1);
 cudaError_t launch_redraw(const KParams& p, const unsigned long long* sel_key, int seg_len, int map_delta,
                           double delta, uint32_t seed, Magic mag_ops1, Magic mag_order, int* n_redrawn,
-                          cudaStream_t st);
+                          cudaStream_t st, uint32_t chain_offset = 0);
 cudaError_t launch_collect(const unsigned long long* keys, int N, unsigned long long kmin, int* out, int cap,
                            int* count, cudaStream_t st);
 cudaError_t launch_first_index(const unsigned long long* keys, int N, const unsigned long long* k, int* out,

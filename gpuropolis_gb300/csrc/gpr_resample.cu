@@ -87,18 +87,20 @@ __global__ void __launch_bounds__(1024) select_rank_kernel(const unsigned long l
  * reference's order (all PL ops, then all PL constants; main.cu:1224-1228):
  * op = ops[random_int(n_ops - 1)], constant = 10^(random_int(8) - 4) *
  * random_normal().  Draws come from the Philox stream keyed by
- * (seed, chain | 2^31).  seg_len > 0: chain c compares with the cutoff of
+ * (seed, (chain + chain_offset) | 2^31): with the offset of a handle's first
+ * chain in a population spread over several handles or GPUs, every chain of
+ * the population has its own stream.  seg_len > 0: chain c compares with the cutoff of
  * its segment, sel_key[c / seg_len]. */
 __global__ void redraw_kernel(const __grid_constant__ KParams p, const unsigned long long* sel_key, int seg_len,
-                              int map_delta, double delta, uint32_t seed, Magic mag_ops1, Magic mag_order,
-                              int* n_redrawn) {
+                              int map_delta, double delta, uint32_t seed, uint32_t chain_offset, Magic mag_ops1,
+                              Magic mag_order, int* n_redrawn) {
     const int chain = blockIdx.x * blockDim.x + threadIdx.x;
     if (chain >= p.N) return;
     double cutoff = gpr_key_value(sel_key[seg_len > 0 ? chain / seg_len : 0]);
     if (map_delta) cutoff -= delta;
     if (!(p.prior[chain] + p.lik[chain] < cutoff)) return;
     Rng r;
-    r.s = 0u; r.key0 = seed; r.key1 = (uint32_t)chain | 0x80000000u; r.blk = 0xffffffffu; r.drawn = 0u;
+    r.s = 0u; r.key0 = seed; r.key1 = ((uint32_t)chain + chain_offset) | 0x80000000u; r.blk = 0xffffffffu; r.drawn = 0u;
     r.w0 = r.w1 = r.w2 = r.w3 = 0u;
     const size_t N = (size_t)p.N;
 #pragma unroll 1
@@ -147,9 +149,9 @@ cudaError_t launch_select(const KParams& p, int rank, unsigned long long* keys, 
 
 cudaError_t launch_redraw(const KParams& p, const unsigned long long* sel_key, int seg_len, int map_delta,
                           double delta, uint32_t seed, Magic mag_ops1, Magic mag_order, int* n_redrawn,
-                          cudaStream_t st) {
-    redraw_kernel<<<(p.N + 127) / 128, 128, 0, st>>>(p, sel_key, seg_len, map_delta, delta, seed, mag_ops1,
-                                                       mag_order, n_redrawn);
+                          cudaStream_t st, uint32_t chain_offset) {
+    redraw_kernel<<<(p.N + 127) / 128, 128, 0, st>>>(p, sel_key, seg_len, map_delta, delta, seed, chain_offset,
+                                                       mag_ops1, mag_order, n_redrawn);
     return cudaGetLastError();
 }
 

@@ -272,6 +272,17 @@ int gpr_resample(gpr_handle* h, int mode, double param, uint32_t seed, int* n_re
 int gpr_resample_datasets(gpr_handle* h, int mode, double param, uint32_t seed, int* n_redrawn,
                           double* cutoffs);
 
+/* The re-draw of gpr_resample against a cutoff the caller supplies: every
+ * chain whose posterior is strictly below `cutoff` is re-drawn, chain c from
+ * the stream keyed by (seed, chain_offset + c).  For one population of chains
+ * spread over several handles or GPUs: the cutoff is computed over the whole
+ * population (the largest posterior minus delta, or the posterior at the
+ * quantile's rank, reference comparator order), and each handle passes the
+ * index of its first chain, so that the handles together re-draw exactly what
+ * one handle holding every chain would (gpr_resample with that cutoff).  Waits
+ * for the re-draw; *n_redrawn (optional) receives the count. */
+int gpr_resample_below(gpr_handle* h, double cutoff, uint32_t seed, int chain_offset, int* n_redrawn);
+
 /* Candidates for the k best chains: every chain whose posterior is >= the
  * k-th largest posterior minus margin (NaN never; all non-NaN chains when
  * fewer than k are non-NaN).  Up to `capacity` chain indices are written to

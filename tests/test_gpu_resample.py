@@ -105,3 +105,54 @@ def test_selection_rejects_bad_arguments():
             s.resample(0, 0.5)
     finally:
         s.close()
+
+
+@pytest.mark.parametrize("mode,param", [(0, 0.5), (1, 20.0), (0, 0.0)])
+def test_population_split_over_handles_equals_one_handle(mode, param):
+    """One population of 4096 chains held by two handles (chains [0, 2048)
+    and [2048, 4096)): the cutoff over both halves (population.py) and each
+    half's re-draw below it with its chain offset (gpr_resample_below) give,
+    bit for bit, the programs and constants of one handle holding every chain
+    and resampling with gpr_resample.  This is the exchange a population
+    spread over several GPUs makes once per block."""
+    from gpuropolis_gb300 import population as pop
+    N, PL, half = 4096, 31, 2048
+    P0, C0 = H.random_programs(N, PL, seed=3)
+    prior, lik = H.mixed_scores(N, seed=4)
+    full = g.Sampler(N, program_length=PL)
+    parts = [g.Sampler(half, program_length=PL) for _ in range(2)]
+    try:
+        full.set_state(P0, C0)
+        full.set_scores(prior, lik)
+        n_full, cut_full = full.resample(mode, param, seed=777)
+        Pf, Cf, _, _ = full.get_state()
+        cut = pop.population_cutoff(prior + lik, mode, param)
+        assert (np.isnan(cut) and np.isnan(cut_full)) or cut == cut_full
+        n_parts = 0
+        Ps, Cs = [], []
+        for k, s in enumerate(parts):
+            sl = slice(k * half, (k + 1) * half)
+            s.set_state(np.ascontiguousarray(P0[:, sl]), np.ascontiguousarray(C0[:, sl]))
+            s.set_scores(prior[sl], lik[sl])
+            pr, li = s.get_scores()
+            assert np.array_equal(pr, prior[sl], equal_nan=True) and np.array_equal(li, lik[sl], equal_nan=True)
+            n_parts += s.resample_below(cut, seed=777, chain_offset=k * half)
+            P, C, _, _ = s.get_state()
+            Ps.append(P)
+            Cs.append(C)
+    finally:
+        full.close()
+        for s in parts:
+            s.close()
+    assert n_parts == n_full
+    assert np.array_equal(np.concatenate(Ps, axis=1), Pf)
+    assert np.array_equal(np.concatenate(Cs, axis=1).view(np.uint32), Cf.view(np.uint32))
+
+
+def test_resample_below_rejects_bad_arguments():
+    s = g.Sampler(16, program_length=31)
+    try:
+        with pytest.raises(g.GprError):
+            s.resample_below(0.0, 1, -1)
+    finally:
+        s.close()
