@@ -111,6 +111,7 @@ def library():
     lib.gpr_map_chain.argtypes = [vp, vp, vp]
     # host side (include/gpuropolis_host.h)
     lib.gpr_load_data_file.argtypes = [ctypes.c_char_p, fp, ip, ip, P(vp), P(vp), P(vp), P(ip)]
+    lib.gpr_load_data_file3.argtypes = [ctypes.c_char_p, fp, ip, ip, P(vp), P(vp), P(vp), P(vp), P(vp), P(ip)]
     lib.gpr_free.argtypes = [vp]
     lib.gpr_host_last_error.restype = ctypes.c_char_p
     lib.gpr_format_expression.argtypes = [vp, vp, ip, ip, ip, ctypes.c_char_p, ip, ctypes.c_char_p, ip]
@@ -399,6 +400,24 @@ def load_data_file(path, sdscale=1.0, first_half=False, even_half=False):
         lib.gpr_free(p)
     return tuple(out)
 
+
+
+def load_data_file3(path, sdscale=1.0, first_half=False, even_half=False):
+    """Data with three input variables, lines "x1 x2 x3 y sd" (the reference's
+    loader rules, main.cu:319-363); returns (x1, x2, x3, y, sd)."""
+    lib = library()
+    ptrs = [ctypes.c_void_p() for _ in range(5)]
+    n = ctypes.c_int()
+    rc = lib.gpr_load_data_file3(path.encode(), sdscale, int(first_half), int(even_half),
+                                 *[ctypes.byref(p) for p in ptrs], ctypes.byref(n))
+    if rc != 0:
+        raise GprError(rc, lib.gpr_host_last_error().decode(errors="replace"))
+    out = []
+    for p in ptrs:
+        a = np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ctypes.c_float)), shape=(max(n.value, 1),))
+        out.append(a[:n.value].copy())
+        lib.gpr_free(p)
+    return tuple(out)
 
 def format_expression(P, C, idx, cfmt="C", latex=False):
     lib = library()

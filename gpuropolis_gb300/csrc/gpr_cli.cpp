@@ -20,7 +20,9 @@
  * (resample on the GPU from a Philox stream keyed by the block seed, without
  * copying the state back and forth), --tops=K (write tops.txt: the K
  * lines of this run's samples.txt that `sort -g -k3 | tail -n K`, run-all.sh:45,
- * selects, found with the device's top-k instead of an external sort).
+ * selects, found with the device's top-k instead of an external sort),
+ * --vars=3 (data lines "x1 x2 x3 y sd"; the op set then also holds the leaves
+ * x1, x2, x3, op codes 27-29, unless --ops gives one).
  */
 #include <getopt.h>
 #include <stdio.h>
@@ -44,9 +46,11 @@ static int hmc_steps = 8, struct_every = 5;
 static int resample_mode = GPR_RESAMPLE_QUANTILE;
 static double resample_param = 0.5;
 static int device_resample = 0, tops_k = 0;
+static int n_vars = 1, ops_given = 0;
 static std::vector<int> ops;
 
-enum { OPT_PL = 1000, OPT_MAXLEN, OPT_OPS, OPT_RNG, OPT_CONST, OPT_RESAMPLE, OPT_THREADS, OPT_DEVRES, OPT_TOPS, OPT_STRUCT };
+enum { OPT_PL = 1000, OPT_MAXLEN, OPT_OPS, OPT_RNG, OPT_CONST, OPT_RESAMPLE, OPT_THREADS, OPT_DEVRES, OPT_TOPS, OPT_STRUCT,
+       OPT_VARS };
 
 static struct option long_options[] = {
     {"in", required_argument, NULL, 'd'},
@@ -74,6 +78,7 @@ static struct option long_options[] = {
     {"device-resample", no_argument, NULL, OPT_DEVRES},
     {"tops", required_argument, NULL, OPT_TOPS},
     {"struct-every", required_argument, NULL, OPT_STRUCT},
+    {"vars", required_argument, NULL, OPT_VARS},
     {NULL, 0, 0, 0}};
 
 static int parse_ops(const char* s) {
@@ -113,7 +118,8 @@ static int process_arguments(int argc, char** argv) {
             case '_': break;
             case OPT_PL: PL = atoi(optarg); break;
             case OPT_MAXLEN: PL = atoi(optarg) - 1; break;
-            case OPT_OPS: if (parse_ops(optarg)) return 1; break;
+            case OPT_OPS: if (parse_ops(optarg)) return 1; ops_given = 1; break;
+            case OPT_VARS: n_vars = atoi(optarg); if (n_vars != 1 && n_vars != 3) return 1; break;
             case OPT_RNG:
                 if (!strcmp(optarg, "lcg")) rng_mode = GPR_RNG_LCG;
                 else if (!strcmp(optarg, "philox")) rng_mode = GPR_RNG_PHILOX;
@@ -183,8 +189,11 @@ int main(int argc, char** argv) {
     if (!(burn >= 0)) FAIL("burn must be >= 0");
     if (!(thin >= 1)) FAIL("thin must be >= 1");
 
+    if (n_vars == 3 && !ops_given)
+        for (int o = 27; o <= 29; ++o) ops.push_back(o);   /* the reference's ops and x1, x2, x3 */
     gpr_config cfg;
     gpr_default_config(&cfg);
+    cfg.n_vars = n_vars;
     cfg.program_length = PL;
     cfg.n_ops = (int)ops.size();
     if (cfg.n_ops > GPR_MAX_OPS) FAIL("too many ops");
@@ -210,9 +219,12 @@ int main(int argc, char** argv) {
     std::string LOG_PATH = out_path + "/log.txt";
     if (seed == -1) seed = (int)time(NULL);
 
-    float *x = nullptr, *y = nullptr, *sd = nullptr;
+    float *x = nullptr, *y = nullptr, *sd = nullptr, *x2 = nullptr, *x3 = nullptr;
     int ndata = 0;
-    int rc = gpr_load_data_file(in_file_path.c_str(), sdscale, FIRST_HALF_DATA, EVEN_HALF_DATA, &x, &y, &sd, &ndata);
+    int rc = n_vars == 3
+        ? gpr_load_data_file3(in_file_path.c_str(), sdscale, FIRST_HALF_DATA, EVEN_HALF_DATA, &x, &x2, &x3, &y, &sd,
+                              &ndata)
+        : gpr_load_data_file(in_file_path.c_str(), sdscale, FIRST_HALF_DATA, EVEN_HALF_DATA, &x, &y, &sd, &ndata);
     if (rc != GPR_HOST_OK) { fprintf(stderr, "*** ERROR: %s\n", gpr_host_last_error()); gpr_destroy(h); return 1; }
 
     FILE* fp = fopen(SAMPLE_PATH.c_str(), "a");
@@ -226,7 +238,10 @@ int main(int argc, char** argv) {
     fprintf(hs, "# -----------------------------------------------------------------\n");
     fprintf(hs, "# -- Data:\n");
     fprintf(hs, "# -----------------------------------------------------------------\n");
-    for (int i = 0; i < ndata; i++) fprintf(hs, "# \t%f\t%f\t%f\n", x[i], y[i], sd[i]);
+    for (int i = 0; i < ndata; i++) {
+        if (n_vars == 3) fprintf(hs, "# \t%f\t%f\t%f\t%f\t%f\n", x[i], x2[i], x3[i], y[i], sd[i]);
+        else fprintf(hs, "# \t%f\t%f\t%f\n", x[i], y[i], sd[i]);
+    }
     fprintf(hs, "#\n#\n");
     fclose(hs);
     fwrite(head, 1, head_len, fp);
@@ -255,7 +270,8 @@ int main(int argc, char** argv) {
     std::vector<double> prior(N), lik(N);
     gpr_host_init_chains(P.data(), C.data(), N, PL, ops.data(), (int)ops.size());   /* main.cu:1133-1137 */
 
-    if (gpr_set_data(h, x, y, sd, ndata) != GPR_OK || gpr_set_state(h, P.data(), C.data()) != GPR_OK) {
+    const int drc = n_vars == 3 ? gpr_set_data3(h, x, x2, x3, y, sd, ndata) : gpr_set_data(h, x, y, sd, ndata);
+    if (drc != GPR_OK || gpr_set_state(h, P.data(), C.data()) != GPR_OK) {
         fprintf(stderr, "%s\n", gpr_last_error(h));
         gpr_destroy(h);
         return 1;
@@ -330,7 +346,7 @@ int main(int argc, char** argv) {
                 (double)N * steps * outer / (s > 0 ? s : 1e-9));
         fclose(lg);
     }
-    gpr_free(x); gpr_free(y); gpr_free(sd);
+    gpr_free(x); gpr_free(y); gpr_free(sd); gpr_free(x2); gpr_free(x3);
     gpr_destroy(h);
     return 0;
 }

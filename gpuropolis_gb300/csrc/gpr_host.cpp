@@ -36,25 +36,34 @@
 namespace {
 
 /* ---------------------------------------------------------------- data --- */
+/* nx = 1: the reference's "x y sd" lines; nx = 3: "x1 x2 x3 y sd" (the
+ * variables in front, the same rules).  xs holds the nx variables of each
+ * point in turn. */
 int load_impl(const char* path, float sdscale, int first_half, int even_half, std::vector<float>& xs,
-              std::vector<float>& ys, std::vector<float>& sds, std::string& err) {
+              std::vector<float>& ys, std::vector<float>& sds, std::string& err, int nx = 1) {
     FILE* fp = fopen(path, "r");
     if (!fp) { err = std::string("Cannot open file:\t") + path; return GPR_HOST_ERR_IO; }
     char* line = nullptr;
     size_t len = 0;
-    double x, y, sd;
+    double x, y, sd, x2 = 0.0, x3 = 0.0;
     int rc = GPR_HOST_OK;
     while (getline(&line, &len, fp) != -1) {
         if (line[0] == '#') continue;                                        /* main.cu:328 */
-        if (sscanf(line, "%lf\t%lf\t%lf\n", &x, &y, &sd) == 3 ||
-            sscanf(line, "%le\t%le\t%le\n", &x, &y, &sd) == 3) {            /* main.cu:329-338 */
+        const bool parsed = nx == 3
+            ? (sscanf(line, "%lf\t%lf\t%lf\t%lf\t%lf\n", &x, &x2, &x3, &y, &sd) == 5 ||
+               sscanf(line, "%le\t%le\t%le\t%le\t%le\n", &x, &x2, &x3, &y, &sd) == 5)
+            : (sscanf(line, "%lf\t%lf\t%lf\n", &x, &y, &sd) == 3 ||
+               sscanf(line, "%le\t%le\t%le\n", &x, &y, &sd) == 3);        /* main.cu:329-338 */
+        if (parsed) {
             sd = sdscale * sd;
             if (!((float)sd > 0.0f)) {                                      /* main.cu:332 */
                 err = std::string("sd must be > 0 in line: ") + line;
                 rc = GPR_HOST_ERR_DATA;
                 break;
             }
-            xs.push_back((float)x); ys.push_back((float)y); sds.push_back((float)sd);
+            xs.push_back((float)x);
+            if (nx == 3) { xs.push_back((float)x2); xs.push_back((float)x3); }
+            ys.push_back((float)y); sds.push_back((float)sd);
         } else if (strspn(line, " \r\n\t") == strlen(line)) {               /* main.cu:339 */
             continue;
         } else {
@@ -67,12 +76,15 @@ int load_impl(const char* path, float sdscale, int first_half, int even_half, st
     fclose(fp);
     if (rc != GPR_HOST_OK) return rc;
     if (first_half) {                                   /* keep the first size/2 points, main.cu:350-355 */
-        size_t mid = xs.size() / 2;
-        xs.resize(mid); ys.resize(mid); sds.resize(mid);
+        size_t mid = ys.size() / 2;
+        xs.resize(mid * nx); ys.resize(mid); sds.resize(mid);
     }
     if (even_half) {                                    /* drop even 0-based indices, main.cu:356-360 */
         std::vector<float> a, b, c;
-        for (size_t i = 1; i < xs.size(); i += 2) { a.push_back(xs[i]); b.push_back(ys[i]); c.push_back(sds[i]); }
+        for (size_t i = 1; i < ys.size(); i += 2) {
+            for (int k = 0; k < nx; ++k) a.push_back(xs[i * nx + k]);
+            b.push_back(ys[i]); c.push_back(sds[i]);
+        }
         xs.swap(a); ys.swap(b); sds.swap(c);
     }
     return GPR_HOST_OK;
@@ -304,6 +316,31 @@ int gpr_load_data_file(const char* path, float sdscale, int first_half, int even
     *sd = (float*)malloc((m + 1) * sizeof(float));
     if (!*x || !*y || !*sd) return GPR_HOST_ERR_ARG;
     std::copy(xs.begin(), xs.end(), *x);
+    std::copy(ys.begin(), ys.end(), *y);
+    std::copy(sds.begin(), sds.end(), *sd);
+    *n = (int)m;
+    return GPR_HOST_OK;
+}
+
+int gpr_load_data_file3(const char* path, float sdscale, int first_half, int even_half, float** x1, float** x2,
+                        float** x3, float** y, float** sd, int* n) {
+    if (!path || !x1 || !x2 || !x3 || !y || !sd || !n) return GPR_HOST_ERR_ARG;
+    std::vector<float> xs, ys, sds;
+    int rc = load_impl(path, sdscale, first_half, even_half, xs, ys, sds, g_host_err, 3);
+    if (rc != GPR_HOST_OK) return rc;
+    const size_t m = ys.size();
+    float** outs[5] = {x1, x2, x3, y, sd};
+    for (float** o : outs) *o = nullptr;
+    for (float** o : outs) {
+        *o = (float*)malloc((m + 1) * sizeof(float));
+        if (!*o) {
+            for (float** q : outs) { free(*q); *q = nullptr; }
+            return GPR_HOST_ERR_ARG;
+        }
+    }
+    for (size_t i = 0; i < m; ++i) {
+        (*x1)[i] = xs[3 * i]; (*x2)[i] = xs[3 * i + 1]; (*x3)[i] = xs[3 * i + 2];
+    }
     std::copy(ys.begin(), ys.end(), *y);
     std::copy(sds.begin(), sds.end(), *sd);
     *n = (int)m;

@@ -25,6 +25,13 @@ enum { GPR_RESAMPLE_QUANTILE = 0, GPR_RESAMPLE_MAP_DELTA = 1 };
  * GPR_HOST_ERR_* code (the reference exits) and set gpr_host_last_error(). */
 int gpr_load_data_file(const char* path, float sdscale, int first_half, int even_half,
                        float** x, float** y, float** sd, int* n);
+
+/* Data with three input variables (no reference counterpart): lines
+ * "x1 x2 x3 y sd", the variables in front of the reference's y and sd, with
+ * the same parse rules, sdscale and trims as gpr_load_data_file.  On success
+ * *x1, *x2, *x3, *y, *sd are malloc'ed arrays of *n floats. */
+int gpr_load_data_file3(const char* path, float sdscale, int first_half, int even_half, float** x1, float** x2,
+                        float** x3, float** y, float** sd, int* n);
 void gpr_free(void* p);
 const char* gpr_host_last_error(void);
 

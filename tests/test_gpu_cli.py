@@ -165,3 +165,34 @@ def test_cli_gradient_moves_constants_only(tmp_path):
     assert "hmc:0.001:4" in log and "Structure move every: 0" in log
     r = subprocess.run([g.CLI_PATH, "--const-proposal=hmc:x"], capture_output=True, text=True, timeout=60)
     assert r.returncode == 1
+
+
+def test_cli_three_variables(tmp_path):
+    """--vars=3: data lines "x1 x2 x3 y sd" (the header echoes all five
+    columns), the op set holding the leaves x1, x2, x3 (printed X, Y, Z in
+    the op-code string and x1, x2, x3 in expressions); programs that read x2
+    and x3 appear and score finite posteriors."""
+    if not os.path.exists(g.CLI_PATH):
+        pytest.skip("CLI not built")
+    x1, x2, x3, y, sd = H.multivar_data(150, seed=6)
+    data = tmp_path / "data3.txt"
+    with open(data, "w") as f:
+        f.write("# x1\tx2\tx3\ty\tsd\n")
+        for row in zip(x1, x2, x3, y, sd):
+            f.write("\t".join("%.9g" % v for v in row) + "\n")
+    out = _run_cli(tmp_path, "v3", ["--in=%s" % data, "--vars=3", "--N=512", "--steps=50", "--outer=3",
+                                    "--seed=11", "--quiet", "--ops=1,3,4,5,6,9,11,20,22,27,28,29,14",
+                                    "--resample=map-delta:20"])
+    head, lines = _lines(out / "samples.txt")
+    data_rows = [h for h in head if h.startswith("# \t") and h.count("\t") == 5]
+    assert len(data_rows) == 150
+    assert len(lines) > 0
+    fields = [l.split("\t") for l in lines]
+    codes = [f[10] for f in fields]
+    assert any("Y" in c or "Z" in c for c in codes)
+    exprs = [f[7] for f in fields]
+    assert any("x2" in e or "x3" in e for e in exprs)
+    post = np.array([float(f[2]) for f in fields])
+    assert np.isfinite(post).any()
+    r = subprocess.run([g.CLI_PATH, "--vars=2"], capture_output=True, text=True, timeout=60)
+    assert r.returncode != 0

@@ -107,6 +107,52 @@ def test_data_loader_errors(tmp_path):
     np.testing.assert_array_equal(sd, np.float32([0.5, 0.2]))
 
 
+@pytest.mark.parametrize("trim", [(False, False), (True, False), (False, True), (True, True)])
+def test_three_variable_loader(tmp_path, trim):
+    """Lines "x1 x2 x3 y sd" under the reference's parse rules (comment and
+    blank lines skipped, sd scaled and > 0, first-half / even-half trims in
+    the reference's order), checked against the same rules written out in
+    Python, and against the single-variable loader on its x1, y, sd columns."""
+    _lib()
+    r = np.random.default_rng(4)
+    n = 37
+    cols = r.normal(size=(5, n))
+    cols[4] = np.abs(cols[4]) + 0.1
+    lines = ["# header", ""]
+    for i in range(n):
+        lines.append("\t".join("%.6g" % v for v in cols[:, i]))
+        if i % 9 == 0:
+            lines.append("   ")
+    p = tmp_path / "d3.txt"
+    p.write_text("\n".join(lines) + "\n")
+    got = g.load_data_file3(str(p), 2.0, *trim)
+    want = np.array([[float("%.6g" % v) for v in c] for c in cols])
+    want[4] *= 2.0
+    idx = np.arange(n)
+    if trim[0]:
+        idx = idx[: n // 2]
+    if trim[1]:
+        idx = idx[1::2]
+    for k in range(5):
+        np.testing.assert_array_equal(got[k], want[k][idx].astype(np.float32))
+    p1 = tmp_path / "d1.txt"
+    p1.write_text("\n".join(["\t".join("%.6g" % cols[k, i] for k in (0, 3, 4)) for i in range(n)]) + "\n")
+    one = g.load_data_file(str(p1), 2.0, *trim)
+    for a, b in zip(one, (got[0], got[3], got[4])):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_three_variable_loader_errors(tmp_path):
+    _lib()
+    p = tmp_path / "bad3.txt"
+    p.write_text("1 2 3 4 0.5\n1 2 3\n")           # a three-column line is not five columns
+    with pytest.raises(g.GprError):
+        g.load_data_file3(str(p))
+    p.write_text("1 2 3 4 0\n")
+    with pytest.raises(g.GprError, match="sd must be > 0"):
+        g.load_data_file3(str(p))
+
+
 @pytest.mark.parametrize("opset", [0, 1])
 def test_host_init_matches_reference(opset):
     _need_ref(); _lib()
