@@ -52,6 +52,10 @@ WORKLOADS = {
     # each, in one launch; blocks replayed from a captured graph
     "batched-256ds-131k": dict(N=131072, PL=47, nds=256, data="batched", ops="basic", rw_sd=0.1,
                                mh_steps=200, blocks=5),
+    # the batched workload cut to 64 datasets x 128 chains, the streamed layout, no
+    # comparison handles: the case ncu captures
+    "batched-64ds-8k-profile": dict(N=8192, PL=47, nds=64, data="batched", ops="basic", rw_sd=0.1,
+                                    mh_steps=50, blocks=1, stream=True, compare=False),
     # the streamed workload cut to 8192 chains x 5 steps: the case ncu captures
     "streamed-3var-8k-profile": dict(N=8192, PL=127, nd=65536, data="multivar", ops="multi", rw_sd=0.1,
                                      mh_steps=5, map_delta=0.0, blocks=1),
@@ -450,6 +454,8 @@ def run_batched(args, w):
     s = g.Sampler(N, program_length=PL, ops=H.OPSET_BASIC, rng=g.RNG_LCG, const_proposal=g.CONST_RANDOM_WALK,
                   rw_sd=w["rw_sd"], stream=stream.cuda_stream)
     s.set_batched_data(sets)
+    if w.get("stream"):
+        s.set_streaming(True)
     s.set_state(P0, C0)
     default_geo = s.launch_geometry()
     for i in range(args.warmup):
@@ -501,23 +507,25 @@ def run_batched(args, w):
 
     # the same chains as 256 separate handles, one block each, one launch per dataset
     hs = []
+    sep = float("nan")
     try:
-        for d in range(nds):
+        for d in range(nds if w.get("compare", True) else 0):
             h = g.Sampler(cpd, program_length=PL, ops=H.OPSET_BASIC, rng=g.RNG_LCG,
                           const_proposal=g.CONST_RANDOM_WALK, rw_sd=w["rw_sd"], stream=stream.cuda_stream)
             h.set_data(*sets[d])
             h.set_state(Pw[:, d * cpd:(d + 1) * cpd], Cw[:, d * cpd:(d + 1) * cpd])
             hs.append(h)
-        for h in hs:
-            h.run_block(steps, 3)
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for h in hs:
-            h.run_block(steps, 4)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        sep = N * steps / (e0.elapsed_time(e1) / 1e3)
+        if hs:
+            for h in hs:
+                h.run_block(steps, 3)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for h in hs:
+                h.run_block(steps, 4)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            sep = N * steps / (e0.elapsed_time(e1) / 1e3)
     finally:
         for h in hs:
             h.close()
@@ -532,7 +540,7 @@ def run_batched(args, w):
         "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded)",
         "point_evals_per_s": st["eval_points"] / (ms / 1e3),
         "separate_handles": {"chain_steps_per_s": sep, "launches_per_block": nds,
-                             "batched_over_separate": value / sep},
+                             "batched_over_separate": value / sep} if sep == sep else None,
         "e2e": {"value": e2e, "unit": "chain-steps/s", "h2d_bytes_per_step": Ph.nbytes + Ch.nbytes,
                 "d2h_bytes_per_step": Ph.nbytes + Ch.nbytes + prh.nbytes + lih.nbytes, "steps": e2e_steps},
         "gpu_launches": launches,
@@ -777,7 +785,7 @@ def main():
     if args.workload in ("streamed-3var-16k", "streamed-3var-8k-profile"):
         run_streamed(args, w)
         return
-    if args.workload == "batched-256ds-131k":
+    if args.workload in ("batched-256ds-131k", "batched-64ds-8k-profile"):
         run_batched(args, w)
         return
     if args.impl == "reference":
