@@ -17,6 +17,7 @@
 #include <string.h>
 #include <algorithm>
 #include <limits>
+#include <new>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -411,7 +412,22 @@ static int choose_launch(gpr_handle* h) {
 
 /* Device layout of a dataset: x1 | y | w | sd | x2 | x3, nd_pad floats each
  * (x2, x3 only for three input variables). */
+static int set_data_body(gpr_handle* h, const float* x, const float* x2, const float* x3, const float* y,
+                         const float* sd, int n);
+
+/* The host staging copies of a dataset can exceed host memory; no C++
+ * exception may leave a C entry point, so allocation failures become error
+ * codes. */
 static int set_data_impl(gpr_handle* h, const float* x, const float* x2, const float* x3, const float* y,
+                         const float* sd, int n) {
+    try {
+        return set_data_body(h, x, x2, x3, y, sd, n);
+    } catch (const std::bad_alloc&) {
+        return fail(h, GPR_ERR_ARG, "not enough host memory to stage %d points", n);
+    }
+}
+
+static int set_data_body(gpr_handle* h, const float* x, const float* x2, const float* x3, const float* y,
                          const float* sd, int n) {
     if (n < 0) return fail(h, GPR_ERR_ARG, "n must be >= 0");
     if (n > 0 && (!x || !y || !sd)) return fail(h, GPR_ERR_ARG, "x, y, sd must be non-NULL");
@@ -472,9 +488,21 @@ int gpr_set_data(gpr_handle* h, const float* x, const float* y, const float* sd,
     return set_data_impl(h, x, nullptr, nullptr, y, sd, n);
 }
 
+static int set_batched_body(gpr_handle* h, int n_datasets, const int* sizes, const float* x1, const float* x2,
+                            const float* x3, const float* y, const float* sd);
+
 int gpr_set_batched_data(gpr_handle* h, int n_datasets, const int* sizes, const float* x1, const float* x2,
                          const float* x3, const float* y, const float* sd) {
     if (!h) return GPR_ERR_ARG;
+    try {
+        return set_batched_body(h, n_datasets, sizes, x1, x2, x3, y, sd);
+    } catch (const std::bad_alloc&) {
+        return fail(h, GPR_ERR_ARG, "not enough host memory to stage %d datasets", n_datasets);
+    }
+}
+
+static int set_batched_body(gpr_handle* h, int n_datasets, const int* sizes, const float* x1, const float* x2,
+                            const float* x3, const float* y, const float* sd) {
     if (n_datasets < 1 || !sizes) return fail(h, GPR_ERR_ARG, "n_datasets must be >= 1 with sizes");
     if (h->N % n_datasets) return fail(h, GPR_ERR_ARG, "%d chains do not split evenly into %d datasets",
                                        h->N, n_datasets);
@@ -989,13 +1017,26 @@ int gpr_adapt_scales(gpr_handle* h, float target_accept) {
         return fail(h, GPR_ERR_ARG, "the reference's constant proposals have no scale to adapt");
     CUDA_TRY(h, cudaSetDevice(h->device));
     if (!h->dscale) {
-        CUDA_TRY(h, cudaMalloc(&h->dscale, (size_t)h->N * sizeof(float)));
+        /* the scales become the handle's only once they hold the start value */
+        float* d = nullptr;
+        CUDA_TRY(h, cudaMalloc(&d, (size_t)h->N * sizeof(float)));
         const float s0 = h->kp.const_mode == GPR_CONST_HMC ? h->kp.hmc_eps : h->kp.rw_sd;
-        std::vector<float> init((size_t)h->N, s0);
-        CUDA_TRY(h, cudaMemcpyAsync(h->dscale, init.data(), init.size() * sizeof(float), cudaMemcpyHostToDevice,
-                                    h->stream));
-        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
-        h->kp.chain_scale = h->dscale;
+        std::vector<float> init;
+        try {
+            init.assign((size_t)h->N, s0);
+        } catch (const std::bad_alloc&) {
+            cudaFree(d);
+            return fail(h, GPR_ERR_ARG, "not enough host memory for %d chain scales", h->N);
+        }
+        cudaError_t e = cudaMemcpyAsync(d, init.data(), init.size() * sizeof(float), cudaMemcpyHostToDevice,
+                                        h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) {
+            cudaFree(d);
+            return fail(h, GPR_ERR_CUDA, "gpr_adapt_scales: %s", cudaGetErrorString(e));
+        }
+        h->dscale = d;
+        h->kp.chain_scale = d;
     }
     drop_graph(h);
     h->kp.adapt_target = target_accept;
