@@ -188,6 +188,8 @@ int main(int argc, char** argv) {
     if (!(N > 0)) FAIL("N must be > 0");
     if (!(burn >= 0)) FAIL("burn must be >= 0");
     if (!(thin >= 1)) FAIL("thin must be >= 1");
+    if (resample_mode == GPR_RESAMPLE_QUANTILE ? !(resample_param >= 0.0 && resample_param < 1.0) : !(resample_param >= 0.0))
+        FAIL("--resample: the quantile must be in [0, 1), the MAP delta >= 0");
 
     if (n_vars == 3 && !ops_given)
         for (int o = 27; o <= 29; ++o) ops.push_back(o);   /* the reference's ops and x1, x2, x3 */
@@ -321,8 +323,12 @@ int main(int argc, char** argv) {
                 return 1;
             }
         } else {
-            gpr_host_resample(P.data(), C.data(), prior.data(), lik.data(), N, PL, ops.data(), (int)ops.size(),
-                              resample_mode, resample_param);
+            if (gpr_host_resample(P.data(), C.data(), prior.data(), lik.data(), N, PL, ops.data(), (int)ops.size(),
+                                  resample_mode, resample_param) < 0) {
+                fprintf(stderr, "*** ERROR: %s\n", gpr_host_last_error());
+                gpr_destroy(h);
+                return 1;
+            }
             if (gpr_set_state(h, P.data(), C.data()) != GPR_OK) {
                 fprintf(stderr, "CUDA error: %s\n", gpr_last_error(h));
                 gpr_destroy(h);

@@ -304,11 +304,23 @@ thread_local std::string g_host_err;
 
 extern "C" {
 
+/* load_impl with host-memory exhaustion as an error code (no exception may
+ * leave a C entry point) */
+static int load_guarded(const char* path, float sdscale, int first_half, int even_half, std::vector<float>& xs,
+                        std::vector<float>& ys, std::vector<float>& sds, int nx) {
+    try {
+        return load_impl(path, sdscale, first_half, even_half, xs, ys, sds, g_host_err, nx);
+    } catch (const std::bad_alloc&) {
+        g_host_err = std::string("not enough host memory to load ") + path;
+        return GPR_HOST_ERR_DATA;
+    }
+}
+
 int gpr_load_data_file(const char* path, float sdscale, int first_half, int even_half,
                        float** x, float** y, float** sd, int* n) {
     if (!path || !x || !y || !sd || !n) return GPR_HOST_ERR_ARG;
     std::vector<float> xs, ys, sds;
-    int rc = load_impl(path, sdscale, first_half, even_half, xs, ys, sds, g_host_err);
+    int rc = load_guarded(path, sdscale, first_half, even_half, xs, ys, sds, 1);
     if (rc != GPR_HOST_OK) return rc;
     size_t m = xs.size();
     *x = (float*)malloc((m + 1) * sizeof(float));
@@ -326,7 +338,7 @@ int gpr_load_data_file3(const char* path, float sdscale, int first_half, int eve
                         float** x3, float** y, float** sd, int* n) {
     if (!path || !x1 || !x2 || !x3 || !y || !sd || !n) return GPR_HOST_ERR_ARG;
     std::vector<float> xs, ys, sds;
-    int rc = load_impl(path, sdscale, first_half, even_half, xs, ys, sds, g_host_err, 3);
+    int rc = load_guarded(path, sdscale, first_half, even_half, xs, ys, sds, 3);
     if (rc != GPR_HOST_OK) return rc;
     const size_t m = ys.size();
     float** outs[5] = {x1, x2, x3, y, sd};
@@ -375,9 +387,22 @@ float gpr_polynomial_degree(const int32_t* P, const float* C, int N, int PL, int
     return degree_of(t, 1);
 }
 
+static int64_t format_samples_body(const int32_t* P, const float* C, const double* prior, const double* lik,
+                                   int N, int PL, int block, int show_constants, int nthreads, char** out);
+
 int64_t gpr_format_samples(const int32_t* P, const float* C, const double* prior, const double* lik,
                            int N, int PL, int block, int show_constants, int nthreads, char** out) {
     if (!P || !C || !prior || !lik || !out || N <= 0) return -1;
+    try {
+        return format_samples_body(P, C, prior, lik, N, PL, block, show_constants, nthreads, out);
+    } catch (const std::exception&) {   /* host memory, or a thread that could not start */
+        g_host_err = "gpr_format_samples: out of host resources";
+        return -1;
+    }
+}
+
+static int64_t format_samples_body(const int32_t* P, const float* C, const double* prior, const double* lik,
+                                   int N, int PL, int block, int show_constants, int nthreads, char** out) {
     int T = nthreads > 0 ? nthreads : (int)std::max(1u, std::thread::hardware_concurrency());
     T = std::min(T, N);
     std::vector<std::string> parts(T);
@@ -416,7 +441,22 @@ void gpr_host_init_chains(int32_t* P, float* C, int N, int PL, const int* ops, i
 
 int gpr_host_resample(int32_t* P, float* C, const double* prior, const double* lik, int N, int PL,
                       const int* ops, int n_ops, int mode, double param) {
-    std::vector<double> post((size_t)N);
+    if (!P || !C || !prior || !lik || !ops || N <= 0 || PL <= 0 || n_ops < 2) {
+        g_host_err = "gpr_host_resample: bad arguments";
+        return -1;
+    }
+    if (mode == GPR_RESAMPLE_QUANTILE ? !((double)N * param >= 0.0 && (double)N * param < (double)N)
+                                      : (mode != GPR_RESAMPLE_MAP_DELTA || !(param >= 0.0))) {
+        g_host_err = "gpr_host_resample: mode must be quantile with param in [0, 1) or map-delta with param >= 0";
+        return -1;
+    }
+    std::vector<double> post;
+    try {
+        post.resize((size_t)N);
+    } catch (const std::bad_alloc&) {
+        g_host_err = "gpr_host_resample: not enough host memory";
+        return -1;
+    }
     for (int h = 0; h < N; ++h) post[h] = prior[h] + lik[h];
     qsort(post.data(), (size_t)N, sizeof(double), cmp_bayes);          /* main.cu:1216-1218 */
     double cutoff;

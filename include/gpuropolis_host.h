@@ -65,7 +65,9 @@ void gpr_host_init_chains(int32_t* P, float* C, int N, int PL, const int* ops, i
  * comparator; cutoff = sorted[(int)(N*param)] (GPR_RESAMPLE_QUANTILE, param
  * 0.5 in the reference) or max - param (GPR_RESAMPLE_MAP_DELTA); chains
  * strictly below the cutoff are re-drawn like the initialisation, in chain
- * order.  Returns the number of chains re-drawn. */
+ * order.  Returns the number of chains re-drawn, or -1 (gpr_host_last_error)
+ * for bad arguments: N or PL < 1, fewer than 2 ops (the re-draw takes
+ * random_int(n_ops - 1)), a quantile outside [0, 1) or a negative delta. */
 int gpr_host_resample(int32_t* P, float* C, const double* prior, const double* lik, int N, int PL,
                       const int* ops, int n_ops, int mode, double param);
 

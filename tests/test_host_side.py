@@ -270,3 +270,16 @@ def test_variable_leaves_need_three_variables():
     assert g.format_expression(P, C, 0) == "(x2+x3)"
     line = g.format_samples(P, C, np.zeros(1), np.zeros(1), 1)
     assert '"+YZ1111"' in line
+
+
+def test_host_resample_rejects_bad_arguments():
+    """The host resampling returns -1 instead of reading past the sorted
+    posteriors (a quantile of 1 or more) or dividing by zero (one op)."""
+    _lib()
+    N, PL = 64, 31
+    P, C = H.random_programs(N, PL, seed=1)
+    prior, lik = H.mixed_scores(N, seed=2)
+    for mode, param, ops in ((0, 1.0, None), (0, -0.1, None), (1, -1.0, None), (2, 0.5, None), (0, 0.5, [1])):
+        assert g.host_resample(P.copy(), C.copy(), prior, lik, ops=ops, mode=mode, param=param) == -1
+        assert "gpr_host_resample" in g.library().gpr_host_last_error().decode()
+    assert g.host_resample(P.copy(), C.copy(), prior, lik, mode=0, param=0.5) >= 0
