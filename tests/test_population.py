@@ -45,6 +45,63 @@ def _worker(rank, port, out_dir):
         dist.destroy_process_group()
 
 
+class _RecordingSampler:
+    """Stands in for a Sampler on a rank without a GPU: the scores it holds,
+    and the (cutoff, seed, chain offset) of the re-draw it is asked for."""
+
+    def __init__(self, prior, lik):
+        self.prior, self.lik = prior, lik
+        self.N = len(prior)
+        self.calls = []
+
+    def get_scores(self):
+        return self.prior, self.lik
+
+    def resample_below(self, cutoff, seed, chain_offset):
+        self.calls.append((cutoff, seed, chain_offset))
+        return int(np.sum(self.prior + self.lik < cutoff))
+
+
+def _resample_worker(rank, port, out_dir):
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=2)
+    try:
+        post = _posteriors(rank, SIZES[rank], "mixed")
+        s = _RecordingSampler(post * 0.25, post * 0.75)
+        res = {}
+        for mode, param in CASES:
+            n, cut = pop.resample_population(s, mode, param, seed=99)
+            res["%d-%g" % (mode, param)] = (n, cut, s.calls[-1])
+        np.save(os.path.join(out_dir, "res%d.npy" % rank), res, allow_pickle=True)
+    finally:
+        dist.destroy_process_group()
+
+
+def test_resample_population_over_two_gloo_ranks(tmp_path):
+    """Each rank asks its own handle for the re-draw below the population's
+    cutoff, with the shared seed and its first chain's population index; the
+    ranks' re-draw counts add up to the population's count below the cutoff."""
+    import torch.multiprocessing as mp
+    mp.start_processes(_resample_worker, args=(_free_port(), str(tmp_path)), nprocs=2, join=True,
+                       start_method="spawn")
+    got = [np.load(tmp_path / ("res%d.npy" % r), allow_pickle=True).item() for r in range(2)]
+    allpost = np.concatenate([_posteriors(r, SIZES[r], "mixed") for r in range(2)])
+    # the ranks' scores are 0.25 and 0.75 of these posteriors: their sums, as the sampler adds them
+    allsum = np.concatenate([p * 0.25 + p * 0.75 for p in (_posteriors(r, SIZES[r], "mixed") for r in range(2))])
+    for mode, param in CASES:
+        key = "%d-%g" % (mode, param)
+        cut = pop.local_cutoff(allsum, mode, param)
+        total = 0
+        for r in range(2):
+            n, c, (call_cut, call_seed, call_off) = got[r][key]
+            assert (np.isnan(cut) and np.isnan(c)) or c == cut, (key, r, c, cut)
+            assert call_seed == 99 and call_off == (0 if r == 0 else SIZES[0])
+            total += n
+        assert total == int(np.sum(allsum < cut)), key
+    assert len(allpost) == sum(SIZES)
+
+
 def _free_port():
     with socket.socket() as s:
         s.bind(("127.0.0.1", 0))
