@@ -22,7 +22,9 @@
  * lines of this run's samples.txt that `sort -g -k3 | tail -n K`, run-all.sh:45,
  * selects, found with the device's top-k instead of an external sort),
  * --vars=3 (data lines "x1 x2 x3 y sd"; the op set then also holds the leaves
- * x1, x2, x3, op codes 27-29, unless --ops gives one).
+ * x1, x2, x3, op codes 27-29, unless --ops gives one), --adapt=T (random-walk
+ * and gradient moves: each chain's own scale adapted toward acceptance T
+ * during the blocks not written out, 0..burn, then kept).
  */
 #include <getopt.h>
 #include <stdio.h>
@@ -47,10 +49,11 @@ static int resample_mode = GPR_RESAMPLE_QUANTILE;
 static double resample_param = 0.5;
 static int device_resample = 0, tops_k = 0;
 static int n_vars = 1, ops_given = 0;
+static float adapt_target = 0.0f;
 static std::vector<int> ops;
 
 enum { OPT_PL = 1000, OPT_MAXLEN, OPT_OPS, OPT_RNG, OPT_CONST, OPT_RESAMPLE, OPT_THREADS, OPT_DEVRES, OPT_TOPS, OPT_STRUCT,
-       OPT_VARS };
+       OPT_VARS, OPT_ADAPT };
 
 static struct option long_options[] = {
     {"in", required_argument, NULL, 'd'},
@@ -79,6 +82,7 @@ static struct option long_options[] = {
     {"tops", required_argument, NULL, OPT_TOPS},
     {"struct-every", required_argument, NULL, OPT_STRUCT},
     {"vars", required_argument, NULL, OPT_VARS},
+    {"adapt", required_argument, NULL, OPT_ADAPT},
     {NULL, 0, 0, 0}};
 
 static int parse_ops(const char* s) {
@@ -120,6 +124,10 @@ static int process_arguments(int argc, char** argv) {
             case OPT_MAXLEN: PL = atoi(optarg) - 1; break;
             case OPT_OPS: if (parse_ops(optarg)) return 1; ops_given = 1; break;
             case OPT_VARS: n_vars = atoi(optarg); if (n_vars != 1 && n_vars != 3) return 1; break;
+            case OPT_ADAPT:
+                adapt_target = (float)atof(optarg);
+                if (!(adapt_target > 0.0f && adapt_target < 1.0f)) return 1;
+                break;
             case OPT_RNG:
                 if (!strcmp(optarg, "lcg")) rng_mode = GPR_RNG_LCG;
                 else if (!strcmp(optarg, "philox")) rng_mode = GPR_RNG_PHILOX;
@@ -190,6 +198,8 @@ int main(int argc, char** argv) {
     if (!(thin >= 1)) FAIL("thin must be >= 1");
     if (resample_mode == GPR_RESAMPLE_QUANTILE ? !(resample_param >= 0.0 && resample_param < 1.0) : !(resample_param >= 0.0))
         FAIL("--resample: the quantile must be in [0, 1), the MAP delta >= 0");
+    if (adapt_target > 0.0f && const_mode == GPR_CONST_REFERENCE)
+        FAIL("--adapt needs --const-proposal=rw:SD, hmc:EPS:L or mala:EPS (the reference's proposals have no scale)");
 
     if (n_vars == 3 && !ops_given)
         for (int o = 27; o <= 29; ++o) ops.push_back(o);   /* the reference's ops and x1, x2, x3 */
@@ -260,6 +270,7 @@ int main(int argc, char** argv) {
         if (const_mode == GPR_CONST_RANDOM_WALK) fprintf(lg, "%g", rw_sd);
         if (const_mode == GPR_CONST_HMC) fprintf(lg, "%g:%d", hmc_eps, hmc_steps);
         fprintf(lg, "\n# \tStructure move every: %d steps", struct_every);
+        if (adapt_target > 0.0f) fprintf(lg, "\n# \tAdapt: per-chain scales toward acceptance %g in blocks 0..%d", adapt_target, burn);
         fprintf(lg, "\n# \tResample: %s:%g%s\n# \tOps:", resample_mode == GPR_RESAMPLE_MAP_DELTA ? "map-delta" : "quantile",
                 resample_param, device_resample ? " (device)" : "");
         for (int o : ops) fprintf(lg, " %d", o);
@@ -282,7 +293,18 @@ int main(int argc, char** argv) {
     struct timespec t0, t1;
     clock_gettime(CLOCK_MONOTONIC, &t0);
     std::vector<int> cand(tops ? (size_t)N : 0);
+    float adapting = 0.0f;
     for (int o = 0; o < outer; o++) {
+        /* per-chain scales adapt while the blocks are not written out, then stay */
+        const float want = (adapt_target > 0.0f && o <= burn) ? adapt_target : 0.0f;
+        if (want != adapting || (o == 0 && want > 0.0f)) {
+            if (gpr_adapt_scales(h, want) != GPR_OK) {
+                fprintf(stderr, "%s\n", gpr_last_error(h));
+                gpr_destroy(h);
+                return 1;
+            }
+            adapting = want;
+        }
         int block_seed = gpr_host_rand();                /* main.cu:1160 */
         const bool write = o > burn && o % thin == 0;    /* main.cu:1170 */
         if (gpr_run_block(h, steps, block_seed) != GPR_OK ||

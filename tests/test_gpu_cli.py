@@ -196,3 +196,26 @@ def test_cli_three_variables(tmp_path):
     assert np.isfinite(post).any()
     r = subprocess.run([g.CLI_PATH, "--vars=2"], capture_output=True, text=True, timeout=60)
     assert r.returncode != 0
+
+
+def test_cli_adapt(tmp_path):
+    """--adapt=T: per-chain scales adapt during the blocks that are not
+    written (0..burn) and are kept afterwards; log.txt records it; the run
+    writes the blocks after burn-in; --adapt needs a proposal with a scale."""
+    if not os.path.exists(g.CLI_PATH):
+        pytest.skip("CLI not built")
+    x, y, sd = H.quad_data(80, seed=8)
+    data = tmp_path / "data.txt"
+    _write_data(data, x, y, sd)
+    out = _run_cli(tmp_path, "adapt", ["--in=%s" % data, "--N=256", "--steps=100", "--outer=4", "--burn=1",
+                                       "--seed=4", "--quiet", "--ops=basic", "--const-proposal=rw:0.5",
+                                       "--adapt=0.3"])
+    log = (out / "log.txt").read_text()
+    assert "Adapt: per-chain scales toward acceptance 0.3 in blocks 0..1" in log
+    _, lines = _lines(out / "samples.txt")
+    blocks = sorted({int(l.split("\t")[1]) for l in lines})
+    assert blocks == [2, 3] and len(lines) == 2 * 256
+    for bad in (["--adapt=0"], ["--adapt=1.5"], ["--adapt=0.5"]):   # the last: reference proposals
+        r = subprocess.run([g.CLI_PATH, "--in=%s" % data, "--N=64", "--steps=5", "--outer=1", "--quiet",
+                            "--out=%s" % (tmp_path / "x")] + bad, capture_output=True, text=True, timeout=60)
+        assert r.returncode != 0, bad
