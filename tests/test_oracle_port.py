@@ -16,7 +16,7 @@ def _need_ref():
         pytest.skip("reference oracle source not available")
 
 
-@pytest.mark.parametrize("PL", [31, 63])
+@pytest.mark.parametrize("PL", [1, 31, 63, 255])
 def test_port_folds_match_reference(PL):
     _need_ref()
     P, C = H.random_programs(300, PL, seed=21)
@@ -49,14 +49,22 @@ MH_CASES = [
     dict(PL=31, opset=0, rng=1, rw=0.0, pm=1),
     dict(PL=31, opset=1, rng=0, rw=0.1, pm=1),
     dict(PL=63, opset=1, rng=1, rw=0.1, pm=1),
+    # program-length edges, and an empty dataset
+    dict(PL=1, opset=0, rng=0, rw=0.0, pm=1),
+    dict(PL=255, opset=1, rng=0, rw=0.1, pm=1),
+    dict(PL=31, opset=1, rng=0, rw=0.1, pm=1, data="empty"),
 ]
 
 
-@pytest.mark.parametrize("case", MH_CASES, ids=lambda c: "pl%(PL)d-o%(opset)d-r%(rng)d-rw%(rw)g-m%(pm)d" % c)
+@pytest.mark.parametrize("case", MH_CASES,
+                         ids=lambda c: "pl%(PL)d-o%(opset)d-r%(rng)d-rw%(rw)g-m%(pm)d" % c + c.get("data", ""))
 def test_port_mh_block_matches_reference(case):
     _need_ref()
     ops = H.OPSET_BASIC if case["opset"] else None
-    x, y, sd = H.quad_data() if case["PL"] == 31 else H.expdecay_data()
+    if case.get("data") == "empty":
+        x = y = sd = np.zeros(0, np.float32)
+    else:
+        x, y, sd = H.quad_data() if case["PL"] in (1, 31) else H.expdecay_data()
     P, C = H.random_programs(256, case["PL"], ops=ops, seed=23)
     o = oref.get(pl=case["PL"], opset=case["opset"], philox=case["rng"], project_math=case["pm"],
                  rw_sd=case["rw"])
