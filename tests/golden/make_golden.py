@@ -1,6 +1,7 @@
 """Generate the golden vectors in tests/golden/ from the reference's own code
 (main.cu compiled for the host by oracle/build_ref.py).  Run in a checkout
-that has the reference mounted:  python tests/golden/make_golden.py
+that has the reference mounted:  python tests/golden/make_golden.py [case ...]
+(all cases when none is named)
 
 Each case stores a seeded initial state, the dataset, the block seed and what
 the reference's MH_simple_kernel (main.cu:679-813) produced after `steps`
@@ -22,14 +23,23 @@ CASES = {
     "pl31_ref_lcg_indep": dict(PL=31, opset=0, philox=0, rw=0.0, data="quad", N=48, steps=30, seed=31337),
     "pl31_ref_philox_indep": dict(PL=31, opset=0, philox=1, rw=0.0, data="quad", N=48, steps=30, seed=4711),
     "pl63_basic_lcg_rw": dict(PL=63, opset=1, philox=0, rw=0.1, data="expdecay", N=48, steps=30, seed=2718),
+    # edges: the shortest and the longest programs, an empty dataset
+    "pl1_ref_lcg_indep": dict(PL=1, opset=0, philox=0, rw=0.0, data="quad", N=48, steps=30, seed=99),
+    "pl255_basic_lcg_rw": dict(PL=255, opset=1, philox=0, rw=0.1, data="expdecay", N=16, steps=20, seed=1234),
+    "pl31_basic_lcg_rw_empty": dict(PL=31, opset=1, philox=0, rw=0.1, data="empty", N=48, steps=30, seed=555),
 }
 XS = np.float32([-1.5, 0.0, 0.25, 2.0, 7.5])
 
 
-def main():
+def main(names=None):
     for name, c in CASES.items():
+        if names and name not in names:
+            continue
         ops = H.OPSET_BASIC if c["opset"] else None
-        x, y, sd = (H.quad_data(101, seed=5) if c["data"] == "quad" else H.expdecay_data(250, seed=5))
+        if c["data"] == "empty":
+            x = y = sd = np.zeros(0, np.float32)
+        else:
+            x, y, sd = (H.quad_data(101, seed=5) if c["data"] == "quad" else H.expdecay_data(250, seed=5))
         P0, C0 = H.random_programs(c["N"], c["PL"], ops=ops, seed=77)
         o = oref.get(pl=c["PL"], opset=c["opset"], philox=c["philox"], project_math=1, rw_sd=c["rw"])
         prior0 = np.array([o.prior(P0, C0, i) for i in range(c["N"])])
@@ -51,4 +61,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])
