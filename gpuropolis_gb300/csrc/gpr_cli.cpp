@@ -24,7 +24,10 @@
  * --vars=3 (data lines "x1 x2 x3 y sd"; the op set then also holds the leaves
  * x1, x2, x3, op codes 27-29, unless --ops gives one), --adapt=T (random-walk
  * and gradient moves: each chain's own scale adapted toward acceptance T
- * during the blocks not written out, 0..burn, then kept).
+ * during the blocks not written out, 0..burn, then kept), --checkpoint=FILE
+ * (after every block: the chains, the seed and the host stream's position)
+ * and --resume=FILE (continue from such a file, appending to samples.txt:
+ * the continued run writes what the uninterrupted one would have).
  */
 #include <getopt.h>
 #include <stdio.h>
@@ -32,6 +35,7 @@
 #include <string.h>
 #include <time.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -50,10 +54,11 @@ static double resample_param = 0.5;
 static int device_resample = 0, tops_k = 0;
 static int n_vars = 1, ops_given = 0;
 static float adapt_target = 0.0f;
+static std::string ckpt_path, resume_path;
 static std::vector<int> ops;
 
 enum { OPT_PL = 1000, OPT_MAXLEN, OPT_OPS, OPT_RNG, OPT_CONST, OPT_RESAMPLE, OPT_THREADS, OPT_DEVRES, OPT_TOPS, OPT_STRUCT,
-       OPT_VARS, OPT_ADAPT };
+       OPT_VARS, OPT_ADAPT, OPT_CKPT, OPT_RESUME };
 
 static struct option long_options[] = {
     {"in", required_argument, NULL, 'd'},
@@ -83,6 +88,8 @@ static struct option long_options[] = {
     {"struct-every", required_argument, NULL, OPT_STRUCT},
     {"vars", required_argument, NULL, OPT_VARS},
     {"adapt", required_argument, NULL, OPT_ADAPT},
+    {"checkpoint", required_argument, NULL, OPT_CKPT},
+    {"resume", required_argument, NULL, OPT_RESUME},
     {NULL, 0, 0, 0}};
 
 static int parse_ops(const char* s) {
@@ -124,6 +131,8 @@ static int process_arguments(int argc, char** argv) {
             case OPT_MAXLEN: PL = atoi(optarg) - 1; break;
             case OPT_OPS: if (parse_ops(optarg)) return 1; ops_given = 1; break;
             case OPT_VARS: n_vars = atoi(optarg); if (n_vars != 1 && n_vars != 3) return 1; break;
+            case OPT_CKPT: ckpt_path = optarg; break;
+            case OPT_RESUME: resume_path = optarg; break;
             case OPT_ADAPT:
                 adapt_target = (float)atof(optarg);
                 if (!(adapt_target > 0.0f && adapt_target < 1.0f)) return 1;
@@ -186,6 +195,55 @@ static void write_params(FILE* fp, int ndata, int wgpu) {   /* main.cu:1090-1104
 
 #define FAIL(...) do { fprintf(stderr, __VA_ARGS__); fprintf(stderr, "\n"); return 1; } while (0)
 
+/* Checkpoint file: "GPRCKPT1", int32 {version 1, N, PL, n_vars, n_ops, last
+ * block done, seed, 0}, uint64 host rand() calls, int32 ops[n_ops], int32
+ * P[N*PL], float C[N*PL] (the reference layout). */
+static const char CKPT_MAGIC[8] = {'G', 'P', 'R', 'C', 'K', 'P', 'T', '1'};
+
+static bool write_checkpoint(const std::string& path, int block, const std::vector<int32_t>& P,
+                             const std::vector<float>& C) {
+    const std::string tmp = path + ".tmp";
+    FILE* f = fopen(tmp.c_str(), "wb");
+    if (!f) return false;
+    const int32_t hdr[8] = {1, N, PL, n_vars, (int32_t)ops.size(), block, seed, 0};
+    const uint64_t calls = gpr_host_rand_calls();
+    bool ok = fwrite(CKPT_MAGIC, 1, 8, f) == 8 && fwrite(hdr, sizeof hdr, 1, f) == 1 &&
+              fwrite(&calls, sizeof calls, 1, f) == 1 &&
+              fwrite(ops.data(), sizeof(int32_t), ops.size(), f) == ops.size() &&
+              fwrite(P.data(), sizeof(int32_t), P.size(), f) == P.size() &&
+              fwrite(C.data(), sizeof(float), C.size(), f) == C.size();
+    ok = (fclose(f) == 0) && ok;
+    return ok && rename(tmp.c_str(), path.c_str()) == 0;   /* a crash mid-write keeps the last good one */
+}
+
+/* Reads a checkpoint written with the same chains, program length, variables
+ * and op set; returns the last block done (or -1) and sets seed and the stream
+ * position. */
+static int read_checkpoint(const std::string& path, std::vector<int32_t>& P, std::vector<float>& C,
+                           uint64_t* calls, std::string& err) {
+    FILE* f = fopen(path.c_str(), "rb");
+    if (!f) { err = "cannot open checkpoint " + path; return -1; }
+    char magic[8];
+    int32_t hdr[8];
+    std::vector<int32_t> ck_ops;
+    bool ok = fread(magic, 1, 8, f) == 8 && !memcmp(magic, CKPT_MAGIC, 8) && fread(hdr, sizeof hdr, 1, f) == 1 &&
+              hdr[0] == 1 && fread(calls, sizeof *calls, 1, f) == 1;
+    if (ok && (hdr[1] != N || hdr[2] != PL || hdr[3] != n_vars || hdr[4] != (int32_t)ops.size()))
+        { err = "checkpoint was written for other chains, program length, variables or op set"; ok = false; }
+    if (ok) {
+        ck_ops.resize((size_t)hdr[4]);
+        ok = fread(ck_ops.data(), sizeof(int32_t), ck_ops.size(), f) == ck_ops.size() &&
+             std::equal(ck_ops.begin(), ck_ops.end(), ops.begin());
+        if (!ok) err = "checkpoint was written for another op set";
+    }
+    if (ok) ok = fread(P.data(), sizeof(int32_t), P.size(), f) == P.size() &&
+                 fread(C.data(), sizeof(float), C.size(), f) == C.size();
+    fclose(f);
+    if (!ok) { if (err.empty()) err = "checkpoint " + path + " is truncated or not a checkpoint"; return -1; }
+    seed = hdr[6];
+    return hdr[5];
+}
+
 int main(int argc, char** argv) {
     for (int i = 0; i < 27; ++i) ops.push_back(i);
     if (process_arguments(argc, argv) == 1) {
@@ -198,6 +256,8 @@ int main(int argc, char** argv) {
     if (!(thin >= 1)) FAIL("thin must be >= 1");
     if (resample_mode == GPR_RESAMPLE_QUANTILE ? !(resample_param >= 0.0 && resample_param < 1.0) : !(resample_param >= 0.0))
         FAIL("--resample: the quantile must be in [0, 1), the MAP delta >= 0");
+    if (adapt_target > 0.0f && (!ckpt_path.empty() || !resume_path.empty()))
+        FAIL("--checkpoint / --resume do not keep the adaptation's state; run --adapt without them");
     if (adapt_target > 0.0f && const_mode == GPR_CONST_REFERENCE)
         FAIL("--adapt needs --const-proposal=rw:SD, hmc:EPS:L or mala:EPS (the reference's proposals have no scale)");
 
@@ -227,6 +287,20 @@ int main(int argc, char** argv) {
         return 1;
     }
     const int wgpu = WHICH_GPU;
+    /* a resumed run takes its chains, seed and host-stream position from the checkpoint */
+    const size_t cnt = (size_t)N * PL;
+    std::vector<int32_t> ckP;
+    std::vector<float> ckC;
+    uint64_t ck_calls = 0;
+    int o_start = 0;
+    if (!resume_path.empty()) {
+        ckP.resize(cnt);
+        ckC.resize(cnt);
+        std::string err;
+        const int last = read_checkpoint(resume_path, ckP, ckC, &ck_calls, err);
+        if (last < 0) { fprintf(stderr, "*** ERROR: %s\n", err.c_str()); gpr_destroy(h); return 1; }
+        o_start = last + 1;
+    }
     std::string SAMPLE_PATH = out_path + "/samples.txt";
     std::string LOG_PATH = out_path + "/log.txt";
     if (seed == -1) seed = (int)time(NULL);
@@ -256,10 +330,10 @@ int main(int argc, char** argv) {
     }
     fprintf(hs, "#\n#\n");
     fclose(hs);
-    fwrite(head, 1, head_len, fp);
+    if (resume_path.empty()) fwrite(head, 1, head_len, fp);   /* a resumed run appends to its samples */
     fclose(fp);
     gpr_tops* tops = tops_k > 0 ? gpr_tops_new(tops_k) : nullptr;
-    if (tops) gpr_tops_add_text(tops, head, (int64_t)head_len);
+    if (tops && resume_path.empty()) gpr_tops_add_text(tops, head, (int64_t)head_len);
     free(head);
 
     FILE* lg = fopen(LOG_PATH.c_str(), "a");
@@ -275,13 +349,19 @@ int main(int argc, char** argv) {
                 resample_param, device_resample ? " (device)" : "");
         for (int o : ops) fprintf(lg, " %d", o);
         fprintf(lg, "\n# \tLibrary: %s\n", gpr_version());
+        if (!resume_path.empty()) fprintf(lg, "# \tResumed from %s after block %d\n", resume_path.c_str(), o_start - 1);
     }
 
-    const size_t cnt = (size_t)N * PL;
     std::vector<int32_t> P(cnt);
     std::vector<float> C(cnt);
     std::vector<double> prior(N), lik(N);
     gpr_host_init_chains(P.data(), C.data(), N, PL, ops.data(), (int)ops.size());   /* main.cu:1133-1137 */
+    if (!resume_path.empty()) {
+        P.swap(ckP);
+        C.swap(ckC);
+        gpr_host_srand((unsigned)seed);                 /* the host stream where the checkpoint left it */
+        gpr_host_rand_skip(ck_calls);
+    }
 
     const int drc = n_vars == 3 ? gpr_set_data3(h, x, x2, x3, y, sd, ndata) : gpr_set_data(h, x, y, sd, ndata);
     if (drc != GPR_OK || gpr_set_state(h, P.data(), C.data()) != GPR_OK) {
@@ -294,7 +374,7 @@ int main(int argc, char** argv) {
     clock_gettime(CLOCK_MONOTONIC, &t0);
     std::vector<int> cand(tops ? (size_t)N : 0);
     float adapting = 0.0f;
-    for (int o = 0; o < outer; o++) {
+    for (int o = o_start; o < outer; o++) {
         /* per-chain scales adapt while the blocks are not written out, then stay */
         const float want = (adapt_target > 0.0f && o <= burn) ? adapt_target : 0.0f;
         if (want != adapting || (o == 0 && want > 0.0f)) {
@@ -357,6 +437,15 @@ int main(int argc, char** argv) {
                 return 1;
             }
         }
+        if (!ckpt_path.empty()) {
+            /* the device resampling leaves the host copy behind: refresh it first */
+            if ((device_resample && gpr_get_state(h, P.data(), C.data(), nullptr, nullptr) != GPR_OK) ||
+                !write_checkpoint(ckpt_path, o, P, C)) {
+                fprintf(stderr, "*** ERROR: cannot write checkpoint %s (%s)\n", ckpt_path.c_str(), gpr_last_error(h));
+                gpr_destroy(h);
+                return 1;
+            }
+        }
         if (!QUIET) progress_bar(float(o) / float(outer));
     }
     if (tops) {
@@ -371,7 +460,7 @@ int main(int argc, char** argv) {
     if (lg) {
         double s = (t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec);
         fprintf(lg, "# \tSampling wall time (s): %.3f\n# \tChain-steps/s: %.4g\n", s,
-                (double)N * steps * outer / (s > 0 ? s : 1e-9));
+                (double)N * steps * (outer - o_start) / (s > 0 ? s : 1e-9));
         fclose(lg);
     }
     gpr_free(x); gpr_free(y); gpr_free(sd); gpr_free(x2); gpr_free(x3);

@@ -265,14 +265,23 @@ void format_line(std::string& out, const int32_t* P, const float* C, const doubl
 }
 
 /* ---------------------------------------------------------- host RNG --- */
+/* Every host draw goes through counted_rand(): the number of rand() calls
+ * since srand() is the whole state a checkpoint needs to continue the stream
+ * (re-seed, then skip that many draws). */
+uint64_t g_rand_calls = 0;
+int counted_rand() {
+    ++g_rand_calls;
+    return rand();
+}
+
 /* host random_int / random_float / random_normal (main.cu:262-284) */
 int host_random_int(int limit) {
     int divisor = RAND_MAX / limit;
     int retval;
-    do { retval = rand() / divisor; } while (retval > limit - 1);
+    do { retval = counted_rand() / divisor; } while (retval > limit - 1);
     return retval;
 }
-float host_random_float() { return float(rand()) / RAND_MAX; }
+float host_random_float() { return float(counted_rand()) / RAND_MAX; }
 float host_random_normal() {
     float u = host_random_float();
     float v = host_random_float();
@@ -427,8 +436,15 @@ static int64_t format_samples_body(const int32_t* P, const float* C, const doubl
     return (int64_t)total;
 }
 
-void gpr_host_srand(unsigned seed) { srand(seed); }
-int gpr_host_rand(void) { return rand(); }
+void gpr_host_srand(unsigned seed) {
+    srand(seed);
+    g_rand_calls = 0;
+}
+int gpr_host_rand(void) { return counted_rand(); }
+uint64_t gpr_host_rand_calls(void) { return g_rand_calls; }
+void gpr_host_rand_skip(uint64_t n) {
+    for (uint64_t i = 0; i < n; ++i) counted_rand();
+}
 
 void gpr_host_init_chains(int32_t* P, float* C, int N, int PL, const int* ops, int n_ops) {
     /* main.cu:1133-1137: every op first (in memory order), then every constant */

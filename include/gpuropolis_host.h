@@ -56,6 +56,11 @@ int64_t gpr_format_samples(const int32_t* P, const float* C, const double* prior
 /* The host random stream: srand/rand of the C library (main.cu:1107,1160). */
 void gpr_host_srand(unsigned seed);
 int gpr_host_rand(void);
+/* The host stream's position: rand() calls since gpr_host_srand (every host
+ * draw of this library counts).  gpr_host_srand(seed) then
+ * gpr_host_rand_skip(n) puts the stream back where a run left it. */
+uint64_t gpr_host_rand_calls(void);
+void gpr_host_rand_skip(uint64_t n);
 
 /* Initial chains (main.cu:1133-1137): every op ops[random_int(n_ops-1)] in
  * memory order, then every constant 10^U{-4..3} * N(0,1), host rand(). */

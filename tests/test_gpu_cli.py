@@ -219,3 +219,33 @@ def test_cli_adapt(tmp_path):
         r = subprocess.run([g.CLI_PATH, "--in=%s" % data, "--N=64", "--steps=5", "--outer=1", "--quiet",
                             "--out=%s" % (tmp_path / "x")] + bad, capture_output=True, text=True, timeout=60)
         assert r.returncode != 0, bad
+
+
+@pytest.mark.parametrize("extra", [[], ["--device-resample"]], ids=["host-resample", "device-resample"])
+def test_cli_checkpoint_resume(tmp_path, extra):
+    """A run stopped after block 2 with --checkpoint and continued with
+    --resume writes, after the first run's lines, exactly the lines the
+    uninterrupted run writes for blocks 3 and 4 (chains, seed and the host
+    stream's position all come back)."""
+    if not os.path.exists(g.CLI_PATH):
+        pytest.skip("CLI not built")
+    x, y, sd = H.quad_data(70, seed=9)
+    data = tmp_path / "data.txt"
+    _write_data(data, x, y, sd)
+    base = ["--in=%s" % data, "--N=256", "--steps=20", "--seed=13", "--quiet", "--ops=basic",
+            "--const-proposal=rw:0.1", "--resample=quantile:0.5"] + extra
+    whole = _run_cli(tmp_path, "whole", base + ["--outer=5"])
+    ck = tmp_path / "state.ckpt"
+    part = _run_cli(tmp_path, "part", base + ["--outer=3", "--checkpoint=%s" % ck])
+    r = subprocess.run([g.CLI_PATH] + base + ["--outer=5", "--resume=%s" % ck, "--out=%s" % part],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    hw, lw = _lines(whole / "samples.txt")
+    hp, lp = _lines(part / "samples.txt")
+    assert lp == lw and len(lw) == 4 * 256      # blocks 1..4 are written (block 0 is not: o > burn)
+    assert "Resumed from" in (part / "log.txt").read_text()
+    # a checkpoint for other chains is refused
+    r = subprocess.run([g.CLI_PATH] + base + ["--N=128", "--outer=5", "--resume=%s" % ck,
+                                              "--out=%s" % (tmp_path / "bad")], capture_output=True, text=True,
+                       timeout=60)
+    assert r.returncode != 0 and "checkpoint" in r.stderr

@@ -293,3 +293,33 @@ def test_posterior_distribution_matches_reference_ks(lib, cmode, rw_sd):
     assert ks.pvalue > 1e-3, (ks, np.median(fin_g), np.median(fin_r))
     kc = stats.ks_2samp(count_g, count_r)
     assert kc.pvalue > 1e-3, kc
+
+
+@pytest.mark.parametrize("where", ["y", "x"])
+def test_nan_data_matches_reference(lib, where):
+    """A data point with NaN y makes every program's likelihood -inf
+    (main.cu:459-462); with NaN x, exactly the programs that read x at that
+    point are -inf, constant programs stay finite: the device agrees with the
+    reference chain by chain."""
+    _need_ref()
+    N, PL = 1024, 31
+    x, y, sd = H.quad_data()
+    x, y = x.copy(), y.copy()
+    (y if where == "y" else x)[17] = np.nan
+    P, C = H.random_programs(N, PL, seed=29)
+    s = g.Sampler(N, program_length=PL)
+    try:
+        s.set_data(x, y, sd)
+        s.set_state(P, C)
+        _, lik = s.evaluate()
+    finally:
+        s.close()
+    o = oref.get(pl=PL, project_math=1)
+    rlik = np.array([o.likelihood(P, C, i, x, y, sd) for i in range(N)])
+    if where == "y":
+        assert np.all(rlik == -np.inf) and np.all(lik == -np.inf)
+        return
+    assert np.array_equal(np.isneginf(lik), np.isneginf(rlik))
+    fin = np.isfinite(lik) & np.isfinite(rlik)
+    assert fin.any()
+    assert H.rel_err(lik[fin], rlik[fin]).max() <= 1e-4
