@@ -67,9 +67,9 @@ WORKLOADS = {
                                 mh_steps=100, map_delta=20.0, blocks=1),
 }
 METRIC = "MH chain-steps/s & point-evals/s (1 GB300); ESS/s gradient vs random-walk MH"
-# DRAM bytes (read + write) of one mh_block_kernel launch of the plain-mh-131k workload, from
-# the ncu capture summarised in profiles/mh_block_kernel_dram_plain-mh-131k.md: the chain state
-# read and written once; the dataset lives in shared memory.
+# DRAM bytes (read + write) of one mh_block_kernel launch of the plain-mh-131k workload, taken
+# from an ncu capture of that launch (dram__bytes_read.sum + dram__bytes_write.sum), not measured
+# in this run: the chain state read and written once; the dataset lives in shared memory.
 MH_LAUNCH_DRAM_BYTES = 113.43e6
 
 

@@ -85,6 +85,7 @@ def library():
     lib.gpr_stream.argtypes = [vp]
     lib.gpr_stream.restype = vp
     lib.gpr_debug_math.argtypes = [vp, ip, vp, vp, vp, ip]
+    lib.gpr_debug_phase_profile.argtypes = [vp, ip, ip, vp, ip]
     lib.gpr_autotune.argtypes = [vp, ip, ip, vp, vp, vp, vp]
     lib.gpr_set_layout.argtypes = [vp, ip, ip, ip]
     lib.gpr_layout_rolled.argtypes = [vp]
@@ -268,6 +269,20 @@ class Sampler:
         out = np.empty_like(a)
         self._check(self.lib.gpr_debug_math(self.h, code, _ptr(a), _ptr(b), _ptr(out), len(a)))
         return out
+
+    PHASE_NAMES = ("claim", "load", "step_barrier", "structure_proposal", "constant_proposal", "compile",
+                   "cauchy_prior", "eval_program", "barrier1", "rank", "evaluation", "barrier2", "combine",
+                   "accept", "store")
+
+    def phase_profile(self, steps, seed):
+        """One block of MH steps through the phase-timed build of the current
+        layout (same results as run_block): clock64 cycles per phase summed
+        over warps, plus the evaluation passes and program instructions
+        interpreted."""
+        out = np.zeros(len(self.PHASE_NAMES) + 2, np.uint64)
+        self._check(self.lib.gpr_debug_phase_profile(self.h, int(steps), int(seed), _ptr(out), len(out)))
+        d = {n: int(v) for n, v in zip(self.PHASE_NAMES, out)}
+        return {"cycles": d, "passes": int(out[-2]), "instructions": int(out[-1])}
 
     def autotune(self, steps=50, seed=1):
         """Pick the fastest evaluation layout on the current state and data."""

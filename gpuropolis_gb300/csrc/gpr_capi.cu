@@ -77,7 +77,10 @@ struct gpr_handle {
     std::string err;
 };
 
-static std::string g_create_error;
+/* Failures with no handle to hold them (gpr_create, gpr_run_block_noalloc):
+ * one message per host thread, so that calls failing at once on different
+ * threads do not race on it. */
+static thread_local std::string g_create_error;
 
 static int fail(gpr_handle* h, int code, const char* fmt, ...) {
     char buf[512];
@@ -795,6 +798,35 @@ int gpr_debug_math(gpr_handle* h, int op, const float* a, const float* b, float*
     return GPR_OK;
 }
 
+int gpr_debug_phase_profile(gpr_handle* h, int steps, int random_seed, uint64_t* out, int n) {
+    if (!h) return GPR_ERR_ARG;
+    if (steps < 0 || n < 0 || (n > 0 && !out)) return fail(h, GPR_ERR_ARG, "bad arguments");
+    if (h->nd < 0) return fail(h, GPR_ERR_STATE, "gpr_set_data has not been called");
+    if (h->kp.const_mode == GPR_CONST_HMC || h->kp.nv == 3 || h->kp.nds > 0 || h->lc.rolled ||
+        h->kp.rng_mode != GPR_RNG_LCG || !gpr::mh_kernel_prof(h->lc.K, h->lc.onepass, 0, h->lc.stream))
+        return fail(h, GPR_ERR_ARG, "no phase-timed build of this layout");
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    unsigned long long* d = nullptr;
+    CUDA_TRY(h, cudaMalloc(&d, GPR_PH_SLOTS * sizeof(unsigned long long)));
+    unsigned long long tmp[GPR_PH_SLOTS] = {};
+    gpr::KParams kp = h->kp;
+    kp.steps = steps;
+    kp.seed = (uint32_t)random_seed;
+    kp.phase = d;
+    cudaError_t e = cudaMemsetAsync(d, 0, sizeof tmp, h->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->dcounter, 0, sizeof(int), h->stream);
+    if (e == cudaSuccess) e = gpr::launch_mh_block_prof(kp, h->lc, h->stream);
+    if (e == cudaSuccess) {
+        h->launches++;
+        e = cudaMemcpyAsync(tmp, d, sizeof tmp, cudaMemcpyDeviceToHost, h->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return fail(h, GPR_ERR_CUDA, "gpr_debug_phase_profile: %s", cudaGetErrorString(e));
+    for (int i = 0; i < n && i < GPR_PH_SLOTS; ++i) out[i] = tmp[i];
+    return gpr_sync(h);
+}
+
 int gpr_autotune(gpr_handle* h, int steps, int seed, int* K, int* onepass, int* rolled, float* best_ms) {
     if (!h || steps <= 0) return fail(h, GPR_ERR_ARG, "bad arguments");
     if (h->nd < 0) return fail(h, GPR_ERR_STATE, "gpr_set_data has not been called");
@@ -1292,7 +1324,6 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
 
 enum { kNoallocMaxDevices = 64 };
 static std::mutex g_noalloc_mu;
-static unsigned char* g_noalloc_addr[kNoallocMaxDevices];
 static int g_noalloc_sms[kNoallocMaxDevices];
 
 /* The weights of gpr_set_data, computed in place from sd on the device (the
@@ -1309,23 +1340,25 @@ static __global__ void noalloc_data_kernel(float* x, float* y, float* w, int n, 
     }
 }
 
-/* One-time per device (device current): the scratch's device address and the
- * SM count. */
+/* Per call, with the device current: the scratch array's device address,
+ * looked up every time (cudaGetSymbolAddress allocates nothing, and an
+ * address kept from an earlier call would be stale after the context was
+ * reset and the module reloaded), and the SM count, cached per device (a
+ * reset does not change it). */
 static int noalloc_setup(int device, unsigned char** scratch, int* sms) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess)
+        return fail(nullptr, GPR_ERR_CUDA, "cudaGetSymbolAddress(scratch) failed: %s", cudaGetErrorString(e));
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_addr[device]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess)
-            return fail(nullptr, GPR_ERR_CUDA, "cudaGetSymbolAddress(scratch) failed: %s", cudaGetErrorString(e));
+    if (!g_noalloc_sms[device]) {
         int n = 0;
         e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, device);
         if (e != cudaSuccess)
             return fail(nullptr, GPR_ERR_CUDA, "cudaDeviceGetAttribute failed: %s", cudaGetErrorString(e));
         g_noalloc_sms[device] = n;
-        g_noalloc_addr[device] = (unsigned char*)p;
     }
-    *scratch = g_noalloc_addr[device];
+    *scratch = (unsigned char*)p;
     *sms = g_noalloc_sms[device];
     return GPR_OK;
 }
@@ -1336,6 +1369,7 @@ static void noalloc_params(gpr::KParams& kp, const gpr_config* cfg, int n_chains
     const int PL = cfg->program_length;
     memset(&kp, 0, sizeof kp);
     kp.N = n_chains; kp.PL = PL;
+    kp.nv = 1;                          /* one input variable, as gpr_create's default */
     kp.rng_mode = cfg->rng;
     kp.const_mode = cfg->const_proposal;
     kp.rw_sd = cfg->rw_sd;
@@ -1382,6 +1416,9 @@ extern "C" int gpr_run_block_noalloc(const gpr_config* cfg, int n_chains, int32_
                     GPR_MAX_PROGRAM_LENGTH, PL);
     if (cfg->n_ops < 1 || cfg->n_ops > GPR_MAX_OPS)
         return fail(nullptr, GPR_ERR_ARG, "n_ops must be in [1, %d] (got %d)", GPR_MAX_OPS, cfg->n_ops);
+    if (cfg->n_vars != 0 && cfg->n_vars != 1)
+        return fail(nullptr, GPR_ERR_ARG, "gpr_run_block_noalloc takes one input variable (n_vars 0 or 1, got %d)",
+                    cfg->n_vars);
     for (int i = 0; i < cfg->n_ops; ++i)
         if (cfg->ops[i] < 0 || cfg->ops[i] >= OP_NREF)
             return fail(nullptr, GPR_ERR_ARG, "ops[%d] = %d is not an op code", i, cfg->ops[i]);

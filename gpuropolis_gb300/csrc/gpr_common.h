@@ -116,6 +116,32 @@ enum gpr_stat {
     GPR_NSTATS
 };
 
+/* Phases of one chain's block that the instrumented MH kernel times
+ * (gpr_debug_phase_profile): clock64 cycles of each warp between phase
+ * boundaries, summed over warps.  After the phases, two counts: evaluation
+ * passes run, and program instructions interpreted (summed over passes). */
+enum gpr_phase {
+    GPR_PH_CLAIM = 0,  /* claiming the next chain (group barrier + counter)       */
+    GPR_PH_LOAD,       /* chain state in from device memory                        */
+    GPR_PH_STEPBAR,    /* step barrier of the free-running / periodic layouts      */
+    GPR_PH_STRUCT,     /* structure proposal (main.cu:699-742)                     */
+    GPR_PH_CONST,      /* constant proposal (main.cu:743-806)                      */
+    GPR_PH_COMPILE,    /* heap tree -> postfix program                             */
+    GPR_PH_CAUCHY,     /* Cauchy prior over all constants                          */
+    GPR_PH_EPROG,      /* evaluation program (instructions paired with constants)  */
+    GPR_PH_BAR1,       /* publishing the program + the first step barrier          */
+    GPR_PH_RANK,       /* ranking the CTA's programs by length                     */
+    GPR_PH_EVAL,       /* evaluation passes and their reductions                   */
+    GPR_PH_BAR2,       /* the second step barrier                                  */
+    GPR_PH_COMBINE,    /* combining a chain's pass sums into its likelihood        */
+    GPR_PH_ACCEPT,     /* prior, posterior, accept rule, bookkeeping               */
+    GPR_PH_STORE,      /* chain state and scores out                               */
+    GPR_NPHASES,
+    GPR_PH_NPASSES = GPR_NPHASES,   /* count: evaluation passes                    */
+    GPR_PH_NINSTR,                  /* count: instructions interpreted             */
+    GPR_PH_SLOTS
+};
+
 /* Passes (32*K points each) a CTA-balanced evaluation can split a dataset
  * into; beyond it each warp evaluates its own chain. */
 #define GPR_MAX_PASSES 64

@@ -92,6 +92,7 @@ struct KParams {
                            * leapfrog step (Hamiltonian moves), else rw_sd / hmc_eps */
     float adapt_target;   /* > 0: adapt chain_scale toward this acceptance rate
                            * during the block and write it back at its end */
+    unsigned long long* phase;   /* instrumented kernels only: GPR_PH_SLOTS sums */
 
     /* the reference LCG (main.cu:215) advanced 2^b steps is the affine map
      * x -> lcgA[b]*x + lcgC[b] (mod 2^32, then masked to 31 bits) */
@@ -127,6 +128,11 @@ struct LaunchCfg {
 
 size_t mh_smem_bytes(const KParams& p, int K, int warps_per_cta, int stream = 0);
 cudaError_t launch_mh_block(const KParams& p, const LaunchCfg& lc, cudaStream_t st);
+/* The phase-timed instantiation of the same layout (gpr_mh_prof.cu); p.phase
+ * must point at GPR_PH_SLOTS zeroed counters.  Single dataset, one input
+ * variable, LCG or Philox, heavy ops unrolled; other layouts are refused. */
+cudaError_t launch_mh_block_prof(const KParams& p, const LaunchCfg& lc, cudaStream_t st);
+const void* mh_kernel_prof(int K, int onepass, int rng, int stream);
 cudaError_t mh_occupancy(const KParams& p, const LaunchCfg& lc, int* ctas_per_sm);
 
 /* Diagnostics: evaluate every chain's program at nx points, and report the

@@ -1107,11 +1107,34 @@ __device__ __forceinline__ void structure_move(Rng& r, const uint8_t* oc, uint8_
  * datasets too large to stage.  BATCHED: many datasets (p.nds > 0), the view
  * switched per chain group; a compile-time switch, so that the single-dataset
  * kernel keeps its dataset view in constant memory rather than registers. */
-template <int K, bool ONEPASS, int RNG, bool ROLLED, bool STREAM, int NV, bool BATCHED>
+/* PROF: the phase-timed variant (gpr_mh_prof.cu only): lane 0 of each warp
+ * adds the clock64 cycles between phase boundaries (gpr_phase) to a
+ * per-warp shared counter, flushed to p.phase when the warp leaves. */
+template <int K, bool ONEPASS, int RNG, bool ROLLED, bool STREAM, int NV, bool BATCHED, bool PROF = false>
 __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __grid_constant__ KParams p) {
     extern __shared__ __align__(128) uint8_t smem[];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
+    __shared__ unsigned long long s_ph[PROF ? 8 : 1][PROF ? GPR_PH_SLOTS : 1];
+    long long ph_t = 0;
+    if constexpr (PROF) {
+        for (int i = threadIdx.x; i < 8 * GPR_PH_SLOTS; i += blockDim.x) (&s_ph[0][0])[i] = 0ull;
+        __syncthreads();
+        ph_t = clock64();
+    }
+    /* close the current phase: its cycles go to counter `i` */
+#define GPR_PH(i)                                                                  \
+    do {                                                                           \
+        if constexpr (PROF) {                                                      \
+            const long long t_ = clock64();                                        \
+            if (lane == 0) s_ph[warp][(i)] += (unsigned long long)(t_ - ph_t);      \
+            ph_t = t_;                                                             \
+        }                                                                          \
+    } while (0)
+#define GPR_PH_COUNT(i, v)                                                         \
+    do {                                                                           \
+        if constexpr (PROF) { if (lane == 0) s_ph[warp][(i)] += (unsigned long long)(v); } \
+    } while (0)
 
     /* CTA-shared dataset (or the device arrays when streamed); with batched
      * data, the dataset of the current chain group (staged per group) */
@@ -1158,6 +1181,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
     int npass = ONEPASS ? 1 : (dv.nd + 32 * K - 1) / (32 * K);
     bool balanced = p.lockstep == 1 && npass <= GPR_MAX_PASSES;
 
+    GPR_PH(GPR_PH_CLAIM);
 #pragma unroll 1
     for (;;) {
         int chain = 0;
@@ -1193,6 +1217,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
             if (chain >= p.N) break;
         }
         const bool active = chain < p.N;
+        GPR_PH(GPR_PH_CLAIM);
 
         /* load the chain (reference layout) into buffer 0 */
         if (active)
@@ -1228,9 +1253,11 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
          * are the MH iterations (main.cu:697-808).  One call site each for
          * compile, prior and likelihood keeps the kernel's hot code small. */
         int cur_ninstr = 0;
+        GPR_PH(GPR_PH_LOAD);
 #pragma unroll 1
         for (int step = -1; step < p.steps; ++step) {
           if (!balanced && p.lockstep > 0 && (step + 1) % p.lockstep == 0) __syncthreads();
+          GPR_PH(GPR_PH_STEPBAR);
           const bool init = step < 0;
           const bool structural = !init && p.struct_every > 0 && (step % p.struct_every == 0);
           int pbuf = cur, cbuf = ccur;
@@ -1245,6 +1272,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                 structure_move<RNG>(r, ws.ops[cur], ws.ops[cur ^ 1], df_invalid(cur_post), p, lane);
                 pbuf = cur ^ 1;
                 need_compile = true;
+                GPR_PH(GPR_PH_STRUCT);
             } else if (!init) {
                 /* ---- constant move (main.cu:743-806) ---- */
                 df fws, bws;
@@ -1252,6 +1280,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                 if (p.const_mode == 0) { forward = df_add(forward, fws); backward = df_add(backward, bws); }
                 cbuf = ccur ^ 1;
                 need_cauchy = true;
+                GPR_PH(GPR_PH_CONST);
             }
             __syncwarp();
             if (need_compile) {
@@ -1261,11 +1290,13 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                 count = co.count;
                 ninstr = co.ninstr;
                 __syncwarp();
+                GPR_PH(GPR_PH_COMPILE);
             }
-            if (need_cauchy) cs = cauchy_sum(ws.Cs[cbuf], p, lane);
+            if (need_cauchy) { cs = cauchy_sum(ws.Cs[cbuf], p, lane); GPR_PH(GPR_PH_CAUCHY); }
             if (structural) backward = df_make(__fmul_rn(-p.logcount[count], GPR_DF_SCALE), 0.0f);
             build_eval_program(ws.prog[pbuf], ws.Cs[cbuf], ninstr, ws.eprog, lane);
             __syncwarp();
+            GPR_PH(GPR_PH_EPROG);
           }
           df lik = df_make(0.0f, 0.0f);
           int pts = 0;
@@ -1278,6 +1309,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
             }
             if (threadIdx.x == 0) s_next = 0;
             __syncthreads();
+            GPR_PH(GPR_PH_BAR1);
             /* rank of this lane's chain (lane < nwarps) by program length, longest first */
             int my_rank = 64, nact = 0;
             {
@@ -1291,6 +1323,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                 if (cl >= 0) my_rank = rk;
             }
             const int ntasks = nact * npass;
+            GPR_PH(GPR_PH_RANK);
 #pragma unroll 1
             for (;;) {
                 int t = 0;
@@ -1315,8 +1348,12 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                 }
                 st_np += (unsigned long long)(s_count[w] + 4) *
                          (unsigned)(ONEPASS ? dv.nd : min(32 * K, dv.nd - pass * 32 * K));
+                GPR_PH_COUNT(GPR_PH_NPASSES, 1);
+                GPR_PH_COUNT(GPR_PH_NINSTR, s_cost[w]);
             }
+            GPR_PH(GPR_PH_EVAL);
             __syncthreads();
+            GPR_PH(GPR_PH_BAR2);
             if (active) {
                 if (s_bad[warp]) {
                     lik = df_make(-INFINITY, 0.0f);
@@ -1327,9 +1364,13 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                                           : df_sub(df_neg(S), df_make(dv.ns_hi, dv.ns_lo));
                 }
             }
+            GPR_PH(GPR_PH_COMBINE);
           } else if (active) {
             lik = eval_loglik<K, ONEPASS, ROLLED, NV, STREAM>(ws.eprog, ws.stk, ws.scr, ld, dv, p, lane, pts);
             st_np += (unsigned long long)(count + 4) * (unsigned)pts;
+            GPR_PH_COUNT(GPR_PH_NPASSES, ONEPASS ? 1 : (dv.nd + 32 * K - 1) / (32 * K));
+            GPR_PH_COUNT(GPR_PH_NINSTR, (unsigned long long)ninstr * (ONEPASS ? 1 : (dv.nd + 32 * K - 1) / (32 * K)));
+            GPR_PH(GPR_PH_EVAL);
           }
           st_pts += (unsigned)pts;
           if (active) {
@@ -1355,6 +1396,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
             if (p.trace && !init && lane < p.trace_n)
                 p.trace[((size_t)chain * p.steps + step) * p.trace_n + lane] = ws.Cs[ccur][lane];
           }
+          GPR_PH(GPR_PH_ACCEPT);
         }
 
         /* write back (main.cu:811-812 and the in-place P, C) */
@@ -1384,7 +1426,14 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
             }
         }
         __syncwarp();
+        GPR_PH(GPR_PH_STORE);
     }
+    if constexpr (PROF) {
+        if (lane == 0 && p.phase)
+            for (int i = 0; i < GPR_PH_SLOTS; ++i) atomicAdd(&p.phase[i], s_ph[warp][i]);
+    }
+#undef GPR_PH
+#undef GPR_PH_COUNT
 }
 
 }  // namespace gpr

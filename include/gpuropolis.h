@@ -142,8 +142,8 @@ int gpr_device_state(gpr_handle* h, int32_t** P, float** C, double** prior, doub
 /* Kernel launches issued by this handle since creation (evidence counter). */
 int64_t gpr_launch_count(gpr_handle* h);
 
-/* Human-readable description of the last error on h (or of the last failed
- * gpr_create when h is NULL). */
+/* Human-readable description of the last error on h (or, when h is NULL, of
+ * the calling thread's last failed gpr_create or gpr_run_block_noalloc). */
 const char* gpr_last_error(gpr_handle* h);
 
 /* Library version string. */
@@ -161,6 +161,17 @@ int gpr_debug_eval_values(gpr_handle* h, const float* xs, int nx, float* out, fl
 /* The evaluator's exp (op 0), log (op 1) and pow (op 2, second operand b)
  * applied elementwise to n host values (for accuracy tests against FP64). */
 int gpr_debug_math(gpr_handle* h, int op, const float* a, const float* b, float* out, int n);
+
+/* Run one block of `steps` MH steps (as gpr_run_block, same results) with the
+ * phase-timed build of the handle's current layout, and copy min(n, 17)
+ * counters to out: [0..14] clock64 cycles spent per phase, summed over the
+ * warps (claim, load, step barrier, structure proposal, constant proposal,
+ * compile, Cauchy prior, evaluation program, first barrier, ranking,
+ * evaluation, second barrier, combine, accept, store), [15] evaluation
+ * passes, [16] program instructions interpreted.  Only single-dataset,
+ * one-variable, LCG handles whose layout has heavy ops unrolled are
+ * instrumented; others return GPR_ERR_ARG. */
+int gpr_debug_phase_profile(gpr_handle* h, int steps, int random_seed, uint64_t* out, int n);
 
 /* Layout autotuner (no reference counterpart): times one block of `steps`
  * MH steps under each valid evaluation layout -- K = 4 or 8 points per lane,
@@ -325,11 +336,14 @@ int gpr_map_chain(gpr_handle* h, int* chain, double* posterior);
  * array per device.  Each call writes all of them on its stream before its
  * launch, so the caller zeroes nothing.  Two calls that overlap on one device
  * (from other threads, or on other streams) share that array and race:
- * serialise them.  Runs on cfg->stream (NULL: the default stream) and returns
- * when the block has finished, reporting kernel error flags as gpr_sync does.
- * The first call on each device does one-time setup (looks up the scratch's
- * address and loads the device code): make it before any stream capture.
- * Failures are described by gpr_last_error(NULL). */
+ * serialise them.  Runs on cfg->stream (NULL: the default stream), waits for
+ * that stream to finish the block before returning, and reports kernel error
+ * flags as gpr_sync does.  Every call looks up the scratch array's device
+ * address with cudaGetSymbolAddress (which allocates nothing), so a context
+ * reset between calls is harmless; the first call on each device also loads
+ * the library's device code there: make that first call before any stream
+ * capture.  cfg->n_vars must be 0 or 1 (one input variable).  Failures are
+ * described by gpr_last_error(NULL), per host thread. */
 int gpr_run_block_noalloc(const gpr_config* cfg, int n_chains, int32_t* P, float* C,
                           double* prior, double* likelihood, const float* x, const float* y,
                           const float* sd, int ndata, int steps, int random_seed);

@@ -62,6 +62,20 @@ def test_rejects_dataset_larger_than_scratch():
     assert rc == 1 and "device pointers" in msg, (rc, msg)
 
 
+def test_rejects_three_variable_config():
+    """The entry point runs one input variable only: a configuration asking
+    for three (or an invalid count) is refused, not run as univariate."""
+    x = np.zeros(8, np.float32)
+    sd = np.ones(8, np.float32)
+    dummy = np.zeros(64 * 31, np.float64)
+    p = g._ptr(dummy)
+    for nv in (2, 3):
+        cfg = g.make_config()
+        cfg.n_vars = nv
+        rc, msg = _call(cfg, 64, (p, p, p, p), x, x, sd, 1, 1)
+        assert rc == 1 and "n_vars" in msg, (nv, rc, msg)
+
+
 def _device_state(s):
     ptrs = [ctypes.c_void_p() for _ in range(4)]
     s._check(s.lib.gpr_device_state(s.h, *[ctypes.byref(p) for p in ptrs]))
