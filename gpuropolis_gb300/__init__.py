@@ -91,6 +91,8 @@ def library():
     lib.gpr_layout_rolled.argtypes = [vp]
     lib.gpr_layout_lockstep.argtypes = [vp]
     lib.gpr_set_layout2.argtypes = [vp, ip, ip, ip, ip, ip]
+    lib.gpr_set_layout3.argtypes = [vp, ip, ip, ip, ip, ip, ip]
+    lib.gpr_layout_pipelined.argtypes = [vp]
     lib.gpr_get_stats.argtypes = [vp, vp, ip]
     lib.gpr_reset_stats.argtypes = [vp]
     lib.gpr_set_scores.argtypes = [vp, vp, vp]
@@ -292,8 +294,11 @@ class Sampler:
                                           ctypes.byref(ro), ctypes.byref(ms)))
         return dict(K=k.value, onepass=op.value, rolled=ro.value, ms=ms.value)
 
-    def set_layout(self, K, onepass, rolled, lockstep=1, warps_per_cta=8):
-        self._check(self.lib.gpr_set_layout2(self.h, K, int(onepass), int(rolled), lockstep, warps_per_cta))
+    def set_layout(self, K, onepass, rolled, lockstep=1, warps_per_cta=8, pipe=0):
+        """pipe=1: the pipelined kernel (two chains per warp); otherwise the
+        lockstep kernel with CTA barriers every `lockstep` steps (0: none)."""
+        self._check(self.lib.gpr_set_layout3(self.h, K, int(onepass), int(rolled), lockstep, warps_per_cta,
+                                             int(pipe)))
 
     def launch_geometry(self):
         v = [ctypes.c_int() for _ in range(4)] + [ctypes.c_int64()]
@@ -301,6 +306,7 @@ class Sampler:
         return dict(K=v[0].value, onepass=v[1].value, warps_per_cta=v[2].value,
                     ctas=v[3].value, smem_bytes=v[4].value, rolled=int(self.lib.gpr_layout_rolled(self.h)),
                     lockstep=int(self.lib.gpr_layout_lockstep(self.h)),
+                    pipe=int(self.lib.gpr_layout_pipelined(self.h)),
                     stream=int(self.lib.gpr_layout_streamed(self.h)))
 
     STAT_NAMES = ("evals", "eval_nodes", "eval_points", "eval_node_points", "struct_proposed",

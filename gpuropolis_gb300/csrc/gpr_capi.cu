@@ -49,6 +49,9 @@ struct gpr_handle {
     float* ddata = nullptr;    /* x | y | w | sd, each nd_pad floats */
     /* selection scratch, allocated by the first gpr_resample/gpr_top_chains/gpr_map_chain */
     float* dscale = nullptr;               /* per-chain proposal scales          */
+    float* dpart = nullptr;                /* chunk sums of the pipelined kernel for large datasets */
+    size_t dpart_floats = 0;
+    double* dds_ns64 = nullptr;            /* batched data: unscaled normalising sums */
     int stream_data = 0;                   /* 1: always stream the dataset       */
     int* dds = nullptr;                    /* batched data: off | n | order      */
     float* dds_ns = nullptr;               /* batched data: normalising sums     */
@@ -112,6 +115,43 @@ static gpr::Magic magic_for(uint32_t d) {
 /* divisor of random_int(n), main.cu:220 */
 static uint32_t divisor_for(int n) { return (uint32_t)(2147483647 / (n + 1)); }
 
+/* The exponent e of the likelihood weights 2^-e / (2 sd^2): the largest is
+ * at most 2^-8, so the FP32 sum of a 128-point chunk of terms (each at most
+ * FLT_MAX times its weight) cannot overflow; e is clamped to [-62, 191] so
+ * that 2^(e-64) is a normal float. */
+static int weight_exponent(const float* sd, size_t n) {
+    double maxw = 0.0;
+    for (size_t i = 0; i < n; ++i) {
+        const double s = (double)sd[i];
+        const double w = 1.0 / (2.0 * s * s);
+        if (w > maxw) maxw = w;
+    }
+    if (!(maxw > 0.0) || !std::isfinite(maxw)) return 0;
+    int x = 0;
+    frexp(maxw, &x);                    /* maxw <= 2^x */
+    return std::min(191, std::max(-62, x + 8));
+}
+
+/* The per-point weight of a point with standard deviation sd. */
+static float point_weight(float sd, int e) {
+    const double s = (double)sd;
+    return (float)(ldexp(1.0, -e) / (2.0 * s * s));
+}
+
+/* The scale fields of the kernel parameters for weight exponent e. */
+static void set_weight_scale(gpr::KParams& kp, int e) {
+    kp.lik_unscale = ldexp(1.0, e);
+    kp.w_to_df = (float)ldexp(1.0, e - 64);
+}
+
+/* The FP64 prior constants: log(NOPS + 1) (main.cu:536) and PL logf(PIf),
+ * the constant part of the Cauchy sum (main.cu:304, 537-540). */
+static void set_prior_constants(gpr::KParams& kp, int n_ops, int PL) {
+    const double PIf = 3.141592653589;                             /* main.cu:194 */
+    kp.ln1_64 = log((double)n_ops + 1);
+    kp.cauchy_c64 = (double)PL * (double)logf((float)PIf);
+}
+
 extern "C" {
 
 void gpr_default_config(gpr_config* cfg) {
@@ -138,7 +178,7 @@ static void free_all(gpr_handle* h) {
     cudaFree(h->dP); cudaFree(h->dC); cudaFree(h->dprior); cudaFree(h->dlik);
     cudaFree(h->dlogcount); cudaFree(h->dcounter); cudaFree(h->ddata); cudaFree(h->dstats);
     cudaFree(h->dkeys); cudaFree(h->dsel); cudaFree(h->dseli); cudaFree(h->dtop); cudaFree(h->dscale);
-    cudaFree(h->dds); cudaFree(h->dds_ns);
+    cudaFree(h->dds); cudaFree(h->dds_ns); cudaFree(h->dds_ns64); cudaFree(h->dpart);
     if (h->graph) cudaGraphExecDestroy(h->graph);
     if (h->graph_src) cudaGraphDestroy(h->graph_src);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
@@ -250,6 +290,8 @@ int gpr_create(const gpr_config* cfg, int n_chains, gpr_handle** out) {
     kp.logpi_f = logf(PI_INT);                 /* log(PROPOSE_INT) binds to the float overload */
     kp.log1mpi_f = (float)log(1.0 - (double)PI_INT);
     kp.geom_logr = gpr_rng_logf(R);
+    set_prior_constants(kp, cfg->n_ops, PL);
+    set_weight_scale(kp, 0);
     kp.logcount = h->dlogcount;
     kp.next_chain = h->dcounter;
     kp.err = h->dcounter + 1;
@@ -291,6 +333,7 @@ static void forget_data(gpr_handle* h) {
     kp.dx = kp.dy = kp.dw = kp.dx2 = kp.dx3 = nullptr;
     kp.ds_off = kp.ds_n = kp.ds_order = nullptr;
     kp.ds_ns = nullptr;
+    kp.ds_ns64 = nullptr;
 }
 
 /* A captured block sequence bakes the launch parameters in: any change of
@@ -302,11 +345,13 @@ static void drop_graph(gpr_handle* h) {
     h->graph_blocks = 0;
 }
 
-/* Largest CTA size (warps) that divides the chains of one dataset, so that
- * a CTA's chain group never straddles two datasets. */
-static int batched_wpc(const gpr::KParams& kp, int wpc) {
+/* Largest CTA size (warps) whose chain group (one chain per warp, two for
+ * the pipelined kernel) divides the chains of one dataset, so that a group
+ * never straddles two datasets. */
+static int batched_wpc(const gpr::KParams& kp, int wpc, int pipe = 0) {
     if (kp.nds <= 0) return wpc;
-    while (wpc > 1 && kp.chains_per_ds % wpc) wpc /= 2;
+    const int per = pipe ? 2 : 1;
+    while (wpc > 1 && kp.chains_per_ds % (per * wpc)) wpc /= 2;
     return wpc;
 }
 
@@ -358,32 +403,43 @@ static int configure_hmc(gpr_handle* h, int wpc0 = 4, int ctas_per_sm = 0, int s
 
 /* A dataset is streamed from device memory when the caller asks for it, or
  * when staging it beside a full CTA of warps would not fit in shared memory;
- * streaming uses K = 4 points per lane in passes. */
-static int configure_launch(gpr_handle* h, int K, int onepass, int rolled, int lockstep = 1, int wpc0 = 8) {
+ * streaming uses K = 4 points per lane in passes.  pipe: the pipelined kernel
+ * (two chains per warp, one barrier per half-step; lockstep is then unused);
+ * it needs heavy ops unrolled, and for batched data chain groups of
+ * 2 x warps_per_cta chains within one dataset. */
+static int configure_launch(gpr_handle* h, int K, int onepass, int rolled, int lockstep = 1, int wpc0 = 8,
+                            int pipe = 1) {
     gpr::KParams& kp = h->kp;
     if (kp.const_mode == GPR_CONST_HMC) return configure_hmc(h);
     drop_graph(h);
     gpr::LaunchCfg lc;
     lc.carveout = 0;
+    if (pipe && rolled) return fail(h, GPR_ERR_ARG, "the pipelined kernel runs heavy ops unrolled only");
+    if (pipe && kp.nds > 0 && kp.chains_per_ds % 2)
+        pipe = 0;   /* an odd number of chains per dataset cannot pair up within one dataset */
     if (kp.nds > 0) {   /* batched: CTA groups within one dataset, staged per group; K = 4 in passes */
         K = 4;
         onepass = 0;
         if (lockstep < 1) lockstep = 1;
-        wpc0 = batched_wpc(kp, wpc0);
+        wpc0 = batched_wpc(kp, wpc0, pipe);
     }
-    lc.stream = h->stream_data || gpr::mh_smem_bytes(kp, K, wpc0) > 227 * 1024;
+    auto smem_of = [&](int k, int w, int st) {
+        return pipe ? gpr::pipe_smem_bytes(kp, k, w, st) : gpr::mh_smem_bytes(kp, k, w, st);
+    };
+    lc.stream = h->stream_data || smem_of(K, wpc0, 0) > 227 * 1024;
     if (lc.stream) { K = 4; onepass = 0; }
     lc.K = K;
     lc.onepass = onepass;
     lc.rolled = rolled;
     lc.lockstep = lockstep;
+    lc.pipe = pipe;
     int wpc = wpc0;
-    size_t smem = gpr::mh_smem_bytes(kp, lc.K, wpc, lc.stream);
+    size_t smem = smem_of(lc.K, wpc, lc.stream);
     while (smem > 227 * 1024 && wpc > 1) {
         wpc /= 2;
-        smem = gpr::mh_smem_bytes(kp, lc.K, wpc, lc.stream);
+        smem = smem_of(lc.K, wpc, lc.stream);
     }
-    if (kp.nds > 0) wpc = batched_wpc(kp, wpc);
+    if (kp.nds > 0) wpc = batched_wpc(kp, wpc, pipe);
     if (smem > 227 * 1024)
         return fail(h, GPR_ERR_ARG, "programs of length %d do not fit in shared memory", kp.PL);
     lc.warps_per_cta = wpc;
@@ -392,25 +448,37 @@ static int configure_launch(gpr_handle* h, int K, int onepass, int rolled, int l
     CUDA_TRY(h, gpr::mh_occupancy(kp, lc, &per_sm));
     if (per_sm < 1) return fail(h, GPR_ERR_ARG, "kernel cannot be resident (smem %zu)", smem);
     long long ctas = (long long)h->num_sms * per_sm;
-    long long need = (h->N + wpc - 1) / wpc;
+    const int per_cta = pipe ? 2 * wpc : wpc;
+    long long need = (h->N + per_cta - 1) / per_cta;
     if (ctas > need) ctas = need;
     lc.ctas = (int)ctas;
+    /* chunk sums beyond the pipelined kernel's shared-memory board: one row
+     * per (CTA, group, warp) in device memory */
+    kp.part_stride = 0;
+    const int stride = pipe ? gpr::pipe_part_stride(kp.nd) : 0;
+    if (stride > 0) {
+        const size_t need_f = (size_t)lc.ctas * 16 * (size_t)stride;
+        if (h->dpart_floats < need_f) {
+            CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+            cudaFree(h->dpart);
+            h->dpart = nullptr;
+            h->dpart_floats = 0;
+            CUDA_TRY(h, cudaMalloc(&h->dpart, need_f * sizeof(float)));
+            h->dpart_floats = need_f;
+        }
+        kp.part = h->dpart;
+        kp.part_stride = stride;
+    }
     h->lc = lc;
     return GPR_OK;
 }
 
-/* Default layout before any autotuning: K = 4 points per lane, one pass
- * when the data fit, heavy ops unrolled (the fastest layout measured on the
- * 250-point, PROGRAM_LENGTH 63 workload; gpr_autotune re-checks per dataset). */
+/* Default layout before any autotuning: the pipelined kernel, K = 4 points
+ * per lane, one pass when the data fit, heavy ops unrolled; three input
+ * variables and batched data take K = 4 in passes (gpr_autotune re-checks
+ * per dataset). */
 static int choose_launch(gpr_handle* h) {
-    /* A dataset of more than GPR_MAX_PASSES passes cannot be split across a
-     * CTA's warps: each warp evaluates its own chain, and step barriers would
-     * make every warp wait for the CTA's longest program.  Free-running warps
-     * in 4-warp CTAs instead (65,536 points, PL 127: 1.06e6 against 6.0e5
-     * chain-steps/s).  Batched data keep their CTA chain groups. */
-    if ((h->kp.nd + 127) / 128 > GPR_MAX_PASSES && h->kp.nds == 0) return configure_launch(h, 4, 0, 0, 0, 4);
-    /* three input variables: built for K = 4 in passes only */
-    return configure_launch(h, 4, (h->kp.nd <= 128 && h->kp.nv != 3) ? 1 : 0, 0, 1, 8);
+    return configure_launch(h, 4, (h->kp.nd <= 128 && h->kp.nv != 3 && h->kp.nds == 0) ? 1 : 0, 0, 1, 8, 1);
 }
 
 /* Device layout of a dataset: x1 | y | w | sd | x2 | x3, nd_pad floats each
@@ -448,11 +516,11 @@ static int set_data_body(gpr_handle* h, const float* x, const float* x2, const f
         }
     double normsum = 0.0;
     const double PIf = 3.141592653589;
+    const int we = weight_exponent(sd, (size_t)n);
     for (int i = 0; i < n; ++i) {
         host[i] = x[i];
         host[nd_pad + i] = y[i];
-        double s = (double)sd[i];
-        host[2 * (size_t)nd_pad + i] = (float)(0x1p-64 / (2.0 * s * s));
+        host[2 * (size_t)nd_pad + i] = point_weight(sd[i], we);
         host[3 * (size_t)nd_pad + i] = sd[i];
         /* the constant part of lnormalpdf (main.cu:300), per point */
         normsum += 0.5 * ((double)logf((float)(2.0 * PIf)) + 2.0 * (double)logf(sd[i]));
@@ -477,6 +545,8 @@ static int set_data_body(gpr_handle* h, const float* x, const float* x2, const f
         kp.normsum_hi = (float)ns;
         kp.normsum_lo = (float)(ns - (double)kp.normsum_hi);
     }
+    kp.normsum64 = normsum;
+    set_weight_scale(kp, we);
     kp.dx = h->ddata;
     kp.dy = h->ddata ? h->ddata + nd_pad : nullptr;
     kp.dw = h->ddata ? h->ddata + 2 * (size_t)nd_pad : nullptr;
@@ -529,7 +599,9 @@ static int set_batched_body(gpr_handle* h, int n_datasets, const int* sizes, con
     std::vector<float> host((three ? 6 : 4) * T + 4, 0.0f);
     std::vector<int> meta(3 * (size_t)n_datasets);
     std::vector<float> ns(2 * (size_t)n_datasets);
+    std::vector<double> ns64((size_t)n_datasets);
     const double PIf = 3.141592653589;
+    const int we = weight_exponent(sd, (size_t)total);
     size_t off = 0, src = 0;
     for (int d = 0; d < n_datasets; ++d) {
         meta[d] = (int)off;
@@ -538,12 +610,12 @@ static int set_batched_body(gpr_handle* h, int n_datasets, const int* sizes, con
         for (int i = 0; i < sizes[d]; ++i, ++src) {
             host[off + i] = x1[src];
             host[T + off + i] = y[src];
-            const double sdd = (double)sd[src];
-            host[2 * T + off + i] = (float)(0x1p-64 / (2.0 * sdd * sdd));
+            host[2 * T + off + i] = point_weight(sd[src], we);
             host[3 * T + off + i] = sd[src];
             if (three) { host[4 * T + off + i] = x2[src]; host[5 * T + off + i] = x3[src]; }
             normsum += 0.5 * ((double)logf((float)(2.0 * PIf)) + 2.0 * (double)logf(sd[src]));   /* main.cu:300 */
         }
+        ns64[d] = normsum;
         const double nsd = normsum * 0x1p-64;
         ns[2 * d] = (float)nsd;
         ns[2 * d + 1] = (float)(nsd - (double)ns[2 * d]);
@@ -557,20 +629,25 @@ static int set_batched_body(gpr_handle* h, int n_datasets, const int* sizes, con
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     forget_data(h);
     if (h->ddata) { cudaFree(h->ddata); h->ddata = nullptr; }
-    cudaFree(h->dds); cudaFree(h->dds_ns);
-    h->dds = nullptr; h->dds_ns = nullptr;
+    cudaFree(h->dds); cudaFree(h->dds_ns); cudaFree(h->dds_ns64);
+    h->dds = nullptr; h->dds_ns = nullptr; h->dds_ns64 = nullptr;
     CUDA_TRY(h, cudaMalloc(&h->ddata, host.size() * sizeof(float)));
     CUDA_TRY(h, cudaMalloc(&h->dds, meta.size() * sizeof(int)));
     CUDA_TRY(h, cudaMalloc(&h->dds_ns, ns.size() * sizeof(float)));
+    CUDA_TRY(h, cudaMalloc(&h->dds_ns64, ns64.size() * sizeof(double)));
     CUDA_TRY(h, cudaMemcpyAsync(h->ddata, host.data(), host.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
     CUDA_TRY(h, cudaMemcpyAsync(h->dds, meta.data(), meta.size() * sizeof(int), cudaMemcpyHostToDevice, h->stream));
     CUDA_TRY(h, cudaMemcpyAsync(h->dds_ns, ns.data(), ns.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(h->dds_ns64, ns64.data(), ns64.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                h->stream));
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     gpr::KParams& kp = h->kp;
     h->nd = (int)maxn;
     h->nd_pad = (int)((maxn + 3) & ~3);
     kp.nd = h->nd; kp.nd_pad = h->nd_pad;
     kp.normsum_hi = kp.normsum_lo = 0.0f;
+    kp.normsum64 = 0.0;
+    set_weight_scale(kp, we);
     kp.dx = h->ddata; kp.dy = h->ddata + T; kp.dw = h->ddata + 2 * T;
     kp.dx2 = three ? h->ddata + 4 * T : nullptr;
     kp.dx3 = three ? h->ddata + 5 * T : nullptr;
@@ -580,6 +657,7 @@ static int set_batched_body(gpr_handle* h, int n_datasets, const int* sizes, con
     kp.ds_n = h->dds + n_datasets;
     kp.ds_order = h->dds + 2 * n_datasets;
     kp.ds_ns = h->dds_ns;
+    kp.ds_ns64 = h->dds_ns64;
     return choose_launch(h);
 }
 
@@ -803,7 +881,7 @@ int gpr_debug_phase_profile(gpr_handle* h, int steps, int random_seed, uint64_t*
     if (steps < 0 || n < 0 || (n > 0 && !out)) return fail(h, GPR_ERR_ARG, "bad arguments");
     if (h->nd < 0) return fail(h, GPR_ERR_STATE, "gpr_set_data has not been called");
     if (h->kp.const_mode == GPR_CONST_HMC || h->kp.nv == 3 || h->kp.nds > 0 || h->lc.rolled ||
-        h->kp.rng_mode != GPR_RNG_LCG || !gpr::mh_kernel_prof(h->lc.K, h->lc.onepass, 0, h->lc.stream))
+        h->kp.rng_mode != GPR_RNG_LCG || !gpr::prof_kernel(h->lc))
         return fail(h, GPR_ERR_ARG, "no phase-timed build of this layout");
     CUDA_TRY(h, cudaSetDevice(h->device));
     unsigned long long* d = nullptr;
@@ -839,18 +917,21 @@ int gpr_autotune(gpr_handle* h, int steps, int seed, int* K, int* onepass, int* 
     int rc = GPR_OK;
     /* staged layouts, then (unless the handle always streams) the streamed one,
      * which reads the data from device memory / L2 and leaves shared memory to
-     * the warps; batched data and three variables take multi-pass layouts only */
-    struct Cand { int K, onepass, rolled, stream; } cands[10];
+     * the warps; batched data and three variables take multi-pass layouts only;
+     * each with the pipelined kernel (heavy ops unrolled) and the lockstep one */
+    struct Cand { int K, onepass, rolled, stream, pipe; } cands[24];
     int nc = 0;
     const int saved_stream = h->stream_data;
     const bool multi_only = h->kp.nds > 0 || h->kp.nv == 3;
-    for (int Kc : {4, 8})
-        for (int op = 1; op >= 0; --op)
-            for (int ro = 0; ro <= 1; ++ro)
-                if ((!op || (h->nd <= 32 * Kc && !multi_only)) && !(multi_only && Kc != 4))
-                    cands[nc++] = {Kc, op, ro, saved_stream};
+    for (int pi = 1; pi >= 0; --pi)
+        for (int Kc : {4, 8})
+            for (int op = 1; op >= 0; --op)
+                for (int ro = 0; ro <= (pi ? 0 : 1); ++ro)
+                    if ((!op || (h->nd <= 32 * Kc && !multi_only)) && !(multi_only && Kc != 4))
+                        cands[nc++] = {Kc, op, ro, saved_stream, pi};
     if (!saved_stream)
-        for (int ro = 0; ro <= 1; ++ro) cands[nc++] = {4, 0, ro, 1};
+        for (int pi = 1; pi >= 0; --pi)
+            for (int ro = 0; ro <= (pi ? 0 : 1); ++ro) cands[nc++] = {4, 0, ro, 1, pi};
     const gpr::LaunchCfg orig = h->lc;
     float best = 1e30f;
     gpr::LaunchCfg bestlc = orig;
@@ -897,9 +978,9 @@ int gpr_autotune(gpr_handle* h, int steps, int seed, int* K, int* onepass, int* 
     }
     for (int i = 0; i < nc; ++i) {
         h->stream_data = cands[i].stream;
-        const int crc = configure_launch(h, cands[i].K, cands[i].onepass, cands[i].rolled);
+        const int crc = configure_launch(h, cands[i].K, cands[i].onepass, cands[i].rolled, 1, 8, cands[i].pipe);
         h->stream_data = saved_stream;
-        if (crc != GPR_OK || (cands[i].stream && !h->lc.stream)) continue;
+        if (crc != GPR_OK || (cands[i].stream && !h->lc.stream) || h->lc.pipe != cands[i].pipe) continue;
         for (int rep = 0; rep < 2; ++rep) {   /* first run warms up, second is timed */
             AT_TRY(cudaMemcpyAsync(h->dP, sP, cnt * sizeof(int32_t), cudaMemcpyDeviceToDevice, h->stream));
             AT_TRY(cudaMemcpyAsync(h->dC, sC, cnt * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
@@ -912,16 +993,17 @@ int gpr_autotune(gpr_handle* h, int steps, int seed, int* K, int* onepass, int* 
         AT_TRY(cudaEventElapsedTime(&ms, e0, e1));
         if (ms < best) { best = ms; bestlc = h->lc; }
     }
-    /* second stage: barrier period and CTA size for the best layout */
+    /* second stage: barrier period (lockstep kernel) and CTA size for the best layout */
     if (!hmc) {
         const gpr::LaunchCfg base = bestlc;
         const int periods[3] = {1, 5, 0};
         const int wpcs[2] = {8, 4};
-        for (int pi = 0; pi < 3; ++pi)
+        for (int pi = 0; pi < (base.pipe ? 1 : 3); ++pi)
             for (int wi = 0; wi < 2; ++wi) {
                 if (periods[pi] == base.lockstep && wpcs[wi] == base.warps_per_cta) continue;
                 h->stream_data = base.stream ? 1 : saved_stream;
-                const int crc = configure_launch(h, base.K, base.onepass, base.rolled, periods[pi], wpcs[wi]);
+                const int crc = configure_launch(h, base.K, base.onepass, base.rolled, periods[pi], wpcs[wi],
+                                                 base.pipe);
                 h->stream_data = saved_stream;
                 if (crc != GPR_OK) continue;
                 for (int rep = 0; rep < 2; ++rep) {
@@ -937,7 +1019,16 @@ int gpr_autotune(gpr_handle* h, int steps, int seed, int* K, int* onepass, int* 
                 if (ms < best) { best = ms; bestlc = h->lc; }
             }
     }
-    h->lc = bestlc;
+    if (!hmc) {
+        /* re-derive the chosen layout (and its scratch) rather than copying it */
+        h->stream_data = bestlc.stream ? 1 : saved_stream;
+        rc = configure_launch(h, bestlc.K, bestlc.onepass, bestlc.rolled, bestlc.lockstep, bestlc.warps_per_cta,
+                              bestlc.pipe);
+        h->stream_data = saved_stream;
+        if (rc != GPR_OK) goto done;
+    } else {
+        h->lc = bestlc;
+    }
     AT_TRY(cudaMemcpyAsync(h->dP, sP, cnt * sizeof(int32_t), cudaMemcpyDeviceToDevice, h->stream));
     AT_TRY(cudaMemcpyAsync(h->dC, sC, cnt * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
     AT_TRY(cudaMemcpyAsync(h->dprior, sPr, h->N * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
@@ -982,7 +1073,12 @@ int gpr_set_layout(gpr_handle* h, int K, int onepass, int rolled) {
 }
 
 int gpr_set_layout2(gpr_handle* h, int K, int onepass, int rolled, int lockstep, int warps_per_cta) {
+    return gpr_set_layout3(h, K, onepass, rolled, lockstep, warps_per_cta, 0);
+}
+
+int gpr_set_layout3(gpr_handle* h, int K, int onepass, int rolled, int lockstep, int warps_per_cta, int pipe) {
     if (!h) return GPR_ERR_ARG;
+    if (pipe && rolled) return fail(h, GPR_ERR_ARG, "the pipelined kernel runs heavy ops unrolled only");
     if (h->kp.const_mode == GPR_CONST_HMC) return fail(h, GPR_ERR_ARG, "the HMC kernel has a single layout");
     if ((K != 4 && K != 8) || (onepass && h->kp.nd > 32 * K) || lockstep < 0 ||
         (warps_per_cta != 1 && warps_per_cta != 2 && warps_per_cta != 4 && warps_per_cta != 8))
@@ -992,7 +1088,7 @@ int gpr_set_layout2(gpr_handle* h, int K, int onepass, int rolled, int lockstep,
         return fail(h, GPR_ERR_ARG, "%s take K=4 in passes (got K=%d onepass=%d)",
                     h->kp.nds > 0 ? "batched datasets" : "three input variables", K, onepass);
     CUDA_TRY(h, cudaSetDevice(h->device));
-    return configure_launch(h, K, onepass ? 1 : 0, rolled ? 1 : 0, lockstep, warps_per_cta);
+    return configure_launch(h, K, onepass ? 1 : 0, rolled ? 1 : 0, lockstep, warps_per_cta, pipe ? 1 : 0);
 }
 
 int gpr_launch_geometry(gpr_handle* h, int* K, int* onepass, int* warps_per_cta, int* ctas, int64_t* smem) {
@@ -1009,6 +1105,7 @@ void* gpr_stream(gpr_handle* h) { return h ? (void*)h->stream : nullptr; }
 
 int gpr_layout_rolled(gpr_handle* h) { return h ? h->lc.rolled : 0; }
 int gpr_layout_lockstep(gpr_handle* h) { return h ? h->lc.lockstep : 0; }
+int gpr_layout_pipelined(gpr_handle* h) { return h ? h->lc.pipe : 0; }
 
 int gpr_get_stats(gpr_handle* h, uint64_t* out, int n) {
     if (!h || !out || n < 0) return GPR_ERR_ARG;
@@ -1313,7 +1410,8 @@ int gpr_map_chain(gpr_handle* h, int* chain, double* posterior) {
  *                 on its stream before the launch.
  *   [256, ...)    logf(k) for k = 0 .. program_length + 1 (Hastings terms).
  *   [1536, ...)   x | y | w, GPR_NOALLOC_MAX_POINTS floats each, w being the
- *                 per-point likelihood weight 2^-64 / (2 sd^2).
+ *                 per-point likelihood weight 2^-e / (2 sd^2), e set by the
+ *                 dataset's smallest sd (as gpr_set_data sets it).
  * Every call rewrites the table and the dataset before its launch, so nothing
  * left by an earlier call is read.  Two calls in flight on one device at once
  * share the array and race. */
@@ -1329,12 +1427,12 @@ static int g_noalloc_sms[kNoallocMaxDevices];
 /* The weights of gpr_set_data, computed in place from sd on the device (the
  * same IEEE double operations and rounding as the host code), and zero
  * padding up to nd_pad, which the kernel stages with the data. */
-static __global__ void noalloc_data_kernel(float* x, float* y, float* w, int n, int nd_pad) {
+static __global__ void noalloc_data_kernel(float* x, float* y, float* w, int n, int nd_pad, double wscale) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nd_pad) return;
     if (i < n) {
         const double s = (double)w[i];
-        w[i] = (float)(0x1p-64 / (2.0 * s * s));
+        w[i] = (float)(wscale / (2.0 * s * s));
     } else {
         x[i] = 0.0f; y[i] = 0.0f; w[i] = 0.0f;
     }
@@ -1391,6 +1489,7 @@ static void noalloc_params(gpr::KParams& kp, const gpr_config* cfg, int n_chains
     kp.logpi_f = logf(PI_INT);
     kp.log1mpi_f = (float)log(1.0 - (double)PI_INT);
     kp.geom_logr = gpr_rng_logf(R);
+    set_prior_constants(kp, cfg->n_ops, PL);
     kp.lockstep = 1;
     kp.struct_every = 5;
     kp.hmc_eps = 0.01f;
@@ -1491,6 +1590,9 @@ extern "C" int gpr_run_block_noalloc(const gpr_config* cfg, int n_chains, int32_
     const double ns = normsum * 0x1p-64;
     kp.normsum_hi = (float)ns;
     kp.normsum_lo = (float)(ns - (double)kp.normsum_hi);
+    kp.normsum64 = normsum;
+    const int we = weight_exponent(sd, (size_t)ndata);
+    set_weight_scale(kp, we);
     kp.dx = sx; kp.dy = sy; kp.dw = sw;
 
     auto report = [&](int code) { g_create_error = h.err; return code; };
@@ -1506,7 +1608,7 @@ extern "C" int gpr_run_block_noalloc(const gpr_config* cfg, int n_chains, int32_
         NA_TRY(cudaMemcpyAsync(sx, x, ndata * sizeof(float), cudaMemcpyHostToDevice, h.stream));
         NA_TRY(cudaMemcpyAsync(sy, y, ndata * sizeof(float), cudaMemcpyHostToDevice, h.stream));
         NA_TRY(cudaMemcpyAsync(sw, sd, ndata * sizeof(float), cudaMemcpyHostToDevice, h.stream));
-        noalloc_data_kernel<<<(nd_pad + 255) / 256, 256, 0, h.stream>>>(sx, sy, sw, ndata, nd_pad);
+        noalloc_data_kernel<<<(nd_pad + 255) / 256, 256, 0, h.stream>>>(sx, sy, sw, ndata, nd_pad, ldexp(1.0, -we));
         NA_TRY(cudaGetLastError());
     }
 #undef NA_TRY

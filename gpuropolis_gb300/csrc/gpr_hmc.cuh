@@ -346,7 +346,8 @@ __device__ df eval_loglik_grad(const uint2* prog, int ninstr, const GradSmem& ws
             if (valid & (1u << k)) {
                 const int i = base + 32 * k;
                 const float f = fres.v[k];
-                const float wi = data_at<STREAM>(dv, DA_W, i);
+                /* the 2^-64-scaled weight: dw carries 2^-e; the factor 2^(e-64) is exact */
+                const float wi = __fmul_rn(data_at<STREAM>(dv, DA_W, i), p.w_to_df);
                 const float r = __fsub_rn(f, data_at<STREAM>(dv, DA_Y, i));
                 const float q = __fmul_rn(r, r);
                 bad |= !(q <= FLT_MAX);

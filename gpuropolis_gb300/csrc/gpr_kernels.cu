@@ -3,7 +3,7 @@
  * (gpr_mh.cuh, instantiated in gpr_mh_k*.cu) and the diagnostics kernel that
  * evaluates compiled programs point by point for the parity tests.
  */
-#include "gpr_mh.cuh"
+#include "gpr_pipe.cuh"
 
 namespace gpr {
 
@@ -13,7 +13,26 @@ size_t mh_smem_bytes(const KParams& p, int K, int warps_per_cta, int stream) {
            (size_t)warps_per_cta * warp_smem_bytes(p.PL, p.max_instr, p.levels, K);
 }
 
-static const void* pick_kernel(int K, int onepass, int rng, int rolled, int stream, int nv, int batched) {
+size_t pipe_smem_bytes(const KParams& p, int K, int warps_per_cta, int stream) {
+    return 16 + (stream ? 0 : align16((size_t)data_arrays(p) * p.nd_pad * 4)) +
+           (size_t)warps_per_cta * pipe_warp_bytes(p.PL, p.max_instr, p.levels, K);
+}
+
+int pipe_part_stride(int nd) {
+    const int nch = (nd + GPR_CHUNK_POINTS - 1) / GPR_CHUNK_POINTS;
+    return nch <= GPR_PIPE_CHUNKS ? 0 : nch;
+}
+
+static const void* pick_pipe(int K, int onepass, int rng, int rolled, int stream, int nv, int batched) {
+    if (batched) return (K == 4 && !onepass) ? pipe_kernel_k4b(rng, rolled, stream, nv) : nullptr;
+    if (nv == 3) return (K == 4 && !onepass) ? pipe_kernel_k4v(rng, rolled, stream) : nullptr;
+    if (K == 4) return pipe_kernel_k4(rng, rolled, onepass, stream);
+    if (K == 8) return stream ? nullptr : pipe_kernel_k8(rng, rolled, onepass);
+    return nullptr;
+}
+
+static const void* pick_kernel(int K, int onepass, int rng, int rolled, int stream, int nv, int batched, int pipe) {
+    if (pipe) return pick_pipe(K, onepass, rng, rolled, stream, nv, batched);
     if (batched) {
         if (K != 4 || onepass) return nullptr;
         return nv == 3 ? mh_kernel_k4bv(rng, rolled, stream) : mh_kernel_k4b(rng, rolled, stream);
@@ -35,7 +54,7 @@ void fill_lcg_jump_table(KParams& p) {
 }
 
 cudaError_t mh_occupancy(const KParams& p, const LaunchCfg& lc, int* ctas_per_sm) {
-    const void* f = pick_kernel(lc.K, lc.onepass, p.rng_mode, lc.rolled, lc.stream, p.nv, p.nds > 0);
+    const void* f = pick_kernel(lc.K, lc.onepass, p.rng_mode, lc.rolled, lc.stream, p.nv, p.nds > 0, lc.pipe);
     if (!f) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lc.smem_bytes);
     if (e != cudaSuccess) return e;
@@ -43,7 +62,7 @@ cudaError_t mh_occupancy(const KParams& p, const LaunchCfg& lc, int* ctas_per_sm
 }
 
 cudaError_t launch_mh_block(const KParams& p, const LaunchCfg& lc, cudaStream_t st) {
-    const void* f = pick_kernel(lc.K, lc.onepass, p.rng_mode, lc.rolled, lc.stream, p.nv, p.nds > 0);
+    const void* f = pick_kernel(lc.K, lc.onepass, p.rng_mode, lc.rolled, lc.stream, p.nv, p.nds > 0, lc.pipe);
     if (!f) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lc.smem_bytes);
     if (e != cudaSuccess) return e;

@@ -50,7 +50,20 @@ struct KParams {
     const int* ds_order;
     int nd;
     int nd_pad;        /* multiple of 4                                       */
-    float normsum_hi, normsum_lo;  /* 2^-64 * sum_d 0.5*(logf(2 PIf) + 2 logf(sd_d)), double-float */
+    float normsum_hi, normsum_lo;  /* 2^-64 * sum_d 0.5*(logf(2 PIf) + 2 logf(sd_d)), double-float
+                                    * (the Hamiltonian kernel's bookkeeping)  */
+    /* The weights dw are 2^-e / (2 sd^2), e chosen per handle so that the
+     * FP32 sum of a 128-point chunk cannot overflow (every weight <= 2^-8).
+     * The MH kernels keep every Bayes quantity in FP64, unscaled. */
+    double lik_unscale;     /* 2^e                                            */
+    float w_to_df;          /* 2^(e-64): dw * w_to_df is the Hamiltonian kernel's 2^-64-scaled weight */
+    double normsum64;       /* sum_d 0.5*(logf(2 PIf) + 2 logf(sd_d))          */
+    const double* ds_ns64;  /* batched: the same per dataset                   */
+    double ln1_64;          /* log((double)NOPS + 1)          (main.cu:536)     */
+    double cauchy_c64;      /* PL * logf(PIf): the constant part of the Cauchy prior (main.cu:304, 537-540) */
+    float* part;            /* chunk sums of the pipelined kernel when a dataset has more
+                             * chunks than its shared-memory board holds      */
+    int part_stride;        /* floats per (CTA, group, warp) in part          */
 
     /* proposals */
     int rng_mode;      /* 0 LCG, 1 Philox                                     */
@@ -121,18 +134,28 @@ struct LaunchCfg {
     int lockstep;      /* CTA barrier period in MH steps (0: warps run freely)   */
     int warps_per_cta;
     int ctas;
+    int pipe;          /* the pipelined kernel: two chains per warp, one barrier per half-step */
     size_t smem_bytes;
     int carveout;      /* shared-memory share of L1 in percent, 0 = the driver's choice */
     int stream;        /* dataset read from device memory, not staged per CTA   */
 };
 
 size_t mh_smem_bytes(const KParams& p, int K, int warps_per_cta, int stream = 0);
+size_t pipe_smem_bytes(const KParams& p, int K, int warps_per_cta, int stream = 0);
+/* Chunk-sum floats the pipelined kernel needs in p.part for nd points (0:
+ * its shared-memory board suffices), per (CTA, group, warp). */
+int pipe_part_stride(int nd);
+const void* pipe_kernel_k4(int rng, int rolled, int onepass, int stream);
+const void* pipe_kernel_k8(int rng, int rolled, int onepass);
+const void* pipe_kernel_k4v(int rng, int rolled, int stream);
+const void* pipe_kernel_k4b(int rng, int rolled, int stream, int nv);
 cudaError_t launch_mh_block(const KParams& p, const LaunchCfg& lc, cudaStream_t st);
 /* The phase-timed instantiation of the same layout (gpr_mh_prof.cu); p.phase
  * must point at GPR_PH_SLOTS zeroed counters.  Single dataset, one input
  * variable, LCG or Philox, heavy ops unrolled; other layouts are refused. */
 cudaError_t launch_mh_block_prof(const KParams& p, const LaunchCfg& lc, cudaStream_t st);
 const void* mh_kernel_prof(int K, int onepass, int rng, int stream);
+const void* prof_kernel(const LaunchCfg& lc);   /* the LCG phase-timed build of lc, or nullptr */
 cudaError_t mh_occupancy(const KParams& p, const LaunchCfg& lc, int* ctas_per_sm);
 
 /* Diagnostics: evaluate every chain's program at nx points, and report the

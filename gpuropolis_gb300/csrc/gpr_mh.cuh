@@ -455,20 +455,36 @@ __device__ __forceinline__ void heavy_staged(float (&acc)[K], const float (&w)[K
  * code, one value at a time); otherwise they are unrolled over K in registers
  * (more code, full ILP).  Which is faster depends on how much of the kernel
  * the instruction cache holds; gpr_autotune measures it. */
-template <int K, bool ROLLED, int NV>
-__device__ __forceinline__ void run_program(const uint2* __restrict__ prog,
+/* Where the interpreter fetches instruction i and the constant it reads:
+ * an evaluation program of (instruction, constant) pairs, or (PCProg) the
+ * compiled program and the chain's constants array, the constant of heap node
+ * n being cs[n] (NaN for the invalid-op marker 255). */
+struct PCProg {
+    const uint32_t* p;
+    const float* cs;
+};
+__device__ __forceinline__ uint2 prog_at(const uint2* e, int i) { return e[i]; }
+__device__ __forceinline__ uint2 prog_at(const PCProg& q, int i) {
+    const uint32_t ins = q.p[i];
+    const uint32_t node = (ins >> 8) & 0xffu;
+    const float c = node == 255u ? __int_as_float(0x7fc00000) : q.cs[node];
+    return make_uint2(ins, __float_as_uint(c));
+}
+
+template <int K, bool ROLLED, int NV, class PR>
+__device__ __forceinline__ void run_program(const PR prog,
                                             const float (&x)[NV][K], float (&acc)[K],
                                             float* __restrict__ stk, float* __restrict__ scr,
                                             int lane) {
     int sp = 0;
     int pc = 0;
-    uint2 insw = prog[0];
+    uint2 insw = prog_at(prog, 0);
 #pragma unroll 1
     for (;;) {
         const uint32_t ins = insw.x;
         const uint32_t code = ins & 0xffu;
         if (code == I_END) break;
-        const uint2 nxt = prog[pc + 1];      /* the program ends with I_END: always in bounds */
+        const uint2 nxt = prog_at(prog, pc + 1);   /* the program ends with I_END: always in bounds */
         ++pc;
         const float c = __uint_as_float(insw.y);
         if (code >= I_BIN0) {
@@ -661,7 +677,8 @@ struct DataView {
     const float* y;
     const float* w;
     int nd, nd_pad;           /* points, and the padded array length       */
-    float ns_hi, ns_lo;       /* 2^-64 * its normalising sum, double-float */
+    float ns_hi, ns_lo;       /* 2^-64 * its normalising sum, double-float (Hamiltonian kernel) */
+    double ns64;              /* its normalising sum (MH kernels)          */
 };
 
 /* The dynamic shared memory of the kernel running (every extern __shared__
@@ -712,14 +729,27 @@ struct LaneData {
     uint32_t valid;  /* bit k: point lane + 32k exists */
 };
 
-/* One pass (32*K points) of the likelihood of a program: this lane's FP32 sum
- * of (f - y)^2 * w over its points, and whether any of its points is
- * invalid.  Used by the CTA-balanced evaluation, where any warp of the CTA may
- * evaluate any chain's pass. */
-template <int K, bool ONEPASS, bool ROLLED, int NV, bool STREAM>
-__device__ __forceinline__ float eval_pass(const uint2* prog, float* stk, float* scr,
-                                           const LaneData<K>& ld, const DataView& dv, const KParams& p,
-                                           int lane, int pass, bool& bad, int& pts) {
+/* ---- the likelihood's reduction tree ----
+ * Fixed by point index, so that every layout (points per lane, data staged
+ * or streamed, chains balanced over a CTA or not) gives the same bits: the
+ * points are taken in chunks of 128 (chunk c = points 128c .. 128c+127, lane
+ * l holding points 128c + l + 32k, k = 0..3); each lane sums its four terms
+ * (f - y)^2 w in FP32 in k order, the 32 lane sums are combined by an FP32
+ * xor butterfly, and the chunk sums are added in FP64 in chunk order
+ * (main.cu:454-468 sums every point in double).  A chunk sum cannot
+ * overflow: every weight is at most 2^-8 (KParams::lik_unscale). */
+#define GPR_CHUNK_POINTS 128
+
+__device__ __forceinline__ int chunk_count(int nd) { return (nd + GPR_CHUNK_POINTS - 1) / GPR_CHUNK_POINTS; }
+
+/* One pass of a program over this lane's K points (pass q covers points
+ * [32Kq, 32K(q+1)), lane l holding points 32Kq + l + 32k): the FP32 sums of
+ * the pass's K/4 chunks, the same in every lane, and whether any point is
+ * invalid (main.cu:459,462), the same in every lane. */
+template <int K, bool ONEPASS, bool ROLLED, int NV, bool STREAM, class PR>
+__device__ __forceinline__ bool eval_pass_chunks(const PR prog, float* stk, float* scr, const LaneData<K>& ld,
+                                                 const DataView& dv, const KParams& p, int lane, int pass,
+                                                 float (&cs)[K / 4]) {
     float x[NV][K], acc[K];
     uint32_t valid;
     const int base = pass * 32 * K + lane;
@@ -731,63 +761,101 @@ __device__ __forceinline__ float eval_pass(const uint2* prog, float* stk, float*
         valid = load_points<K, NV, STREAM>(dv, p, base, x);
     }
     run_program<K, ROLLED, NV>(prog, x, acc, stk, scr, lane);
-    pts += ONEPASS ? dv.nd : min(32 * K, dv.nd - pass * 32 * K);
-    float s = 0.0f;
-    bad = false;
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        if (valid & (1u << k)) {
-            const int i = base + 32 * k;
-            float r = __fsub_rn(acc[k], data_at<STREAM>(dv, DA_Y, i));
-            float q = __fmul_rn(r, r);
-            bad |= !(q <= FLT_MAX);
-            s = fmaf(q, data_at<STREAM>(dv, DA_W, i), s);
-        }
-    }
-    return s;
-}
-
-/* Log-likelihood of one program, as a double-float at the bookkeeping scale
- * 2^-64 (the per-point weights w carry the scale).  -inf when any point is
- * invalid (main.cu:459,462).  Each lane sums its points in FP32; the 32 lane
- * sums are combined with error-free transforms (FP64 on GB300 runs at about
- * 1/70 of the FP32 rate, so no FP64 instruction is issued here). */
-template <int K, bool ONEPASS, bool ROLLED, int NV, bool STREAM>
-__device__ __forceinline__ df eval_loglik(const uint2* prog, float* stk, float* scr,
-                                          const LaneData<K>& ld, const DataView& dv, const KParams& p,
-                                          int lane, int& pts) {
-    float s = 0.0f;
     bool bad = false;
-    const int npass = ONEPASS ? 1 : (dv.nd + 32 * K - 1) / (32 * K);
-#pragma unroll 1
-    for (int pass = 0; pass < npass; ++pass) {
-        float x[NV][K], acc[K];
-        uint32_t valid;
-        const int base = pass * 32 * K + lane;
-        if (ONEPASS) {
 #pragma unroll
-            for (int k = 0; k < K; ++k) x[0][k] = ld.x[k];
-            valid = ld.valid;
-        } else {
-            valid = load_points<K, NV, STREAM>(dv, p, base, x);
-        }
-        run_program<K, ROLLED, NV>(prog, x, acc, stk, scr, lane);
-        pts += ONEPASS ? dv.nd : min(32 * K, dv.nd - pass * 32 * K);
+    for (int j = 0; j < K / 4; ++j) {
+        float s = 0.0f;
 #pragma unroll
-        for (int k = 0; k < K; ++k) {
+        for (int kk = 0; kk < 4; ++kk) {
+            const int k = 4 * j + kk;
             if (valid & (1u << k)) {
                 const int i = base + 32 * k;
-                float r = __fsub_rn(acc[k], data_at<STREAM>(dv, DA_Y, i));
-                float q = __fmul_rn(r, r);
+                const float r = __fsub_rn(acc[k], data_at<STREAM>(dv, DA_Y, i));
+                const float q = __fmul_rn(r, r);
                 bad |= !(q <= FLT_MAX);
-                s = fmaf(q, data_at<STREAM>(dv, DA_W, i), s);
+                s = __fmaf_rn(q, data_at<STREAM>(dv, DA_W, i), s);
             }
         }
-        if (__any_sync(FULLMASK, bad)) return df_make(-INFINITY, 0.0f);
+        cs[j] = s;
     }
-    df S = warp_sum_df(df_make(s, 0.0f));
-    if (!isfinite(S.hi)) return df_make(-INFINITY, 0.0f);
-    return df_sub(df_neg(S), df_make(dv.ns_hi, dv.ns_lo));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int j = 0; j < K / 4; ++j) cs[j] = __fadd_rn(cs[j], __shfl_xor_sync(FULLMASK, cs[j], o));
+    return __any_sync(FULLMASK, bad);
+}
+
+/* The log-likelihood from the FP64 sum of a program's chunk sums:
+ * -(sum) 2^e - the normalising sum. */
+__device__ __forceinline__ double finish_loglik(double S, const DataView& dv, const KParams& p) {
+    return (0.0 - S * p.lik_unscale) - dv.ns64;
+}
+
+/* Log-likelihood of one program evaluated by one warp (main.cu:454-468):
+ * -inf when any point is invalid (main.cu:459,462). */
+template <int K, bool ONEPASS, bool ROLLED, int NV, bool STREAM, class PR>
+__device__ __forceinline__ double eval_loglik64(const PR prog, float* stk, float* scr, const LaneData<K>& ld,
+                                                const DataView& dv, const KParams& p, int lane, int& pts) {
+    const int npass = ONEPASS ? 1 : (dv.nd + 32 * K - 1) / (32 * K);
+    const int nch = chunk_count(dv.nd);
+    double S = 0.0;
+#pragma unroll 1
+    for (int pass = 0; pass < npass; ++pass) {
+        float cs[K / 4];
+        const bool bad = eval_pass_chunks<K, ONEPASS, ROLLED, NV, STREAM>(prog, stk, scr, ld, dv, p, lane, pass, cs);
+        pts += ONEPASS ? dv.nd : min(32 * K, dv.nd - pass * 32 * K);
+        if (bad) return -INFINITY;
+#pragma unroll
+        for (int j = 0; j < K / 4; ++j)
+            if (pass * (K / 4) + j < nch) S += (double)cs[j];
+    }
+    return finish_loglik(S, dv, p);
+}
+
+/* Prior of a program (main.cu:529-544) in FP64: -length log(NOPS + 1) plus
+ * the Cauchy sum over all constants. */
+__device__ __forceinline__ double prior64(float length, double cauchy, const KParams& p) {
+    return (double)(-length) * p.ln1_64 + cauchy;
+}
+
+/* Sum over all constants of lcauchypdf(C, 1) (main.cu:303-305, 537-540) in
+ * FP64: the -log(1 + C^2) terms are FP32 (the reference's logf), added
+ * exactly as double-floats across the warp; the constant part is added once. */
+__device__ __forceinline__ double cauchy_sum64(const float* Cs, const KParams& p, int lane) {
+    df s = df_make(0.0f, 0.0f);
+#pragma unroll 1
+    for (int c = lane; c < p.PL; c += 32) {
+        const float x = Cs[c];
+        s = df_add(s, df_make(-gx_log(__fadd_rn(1.0f, __fmul_rn(x, x))), 0.0f));
+    }
+    s = warp_sum_df(s);
+    return ((double)s.hi + (double)s.lo) - p.cauchy_c64;
+}
+
+/* The accept rule of main.cu:728-740 / 790-802 in FP64, in its exact
+ * evaluation order: acceptance = proposal - current + backward - forward;
+ * the uniform draw is consumed only when the proposal is valid and
+ * acceptance <= 0; an invalid current state accepts anything. */
+template <int RNG>
+__device__ __forceinline__ bool mh_accept64(double ppost, double cur_post, double backward, double forward, Rng& r,
+                                            const KParams& p) {
+    const double acc = ((ppost - cur_post) + backward) - forward;
+    bool accept = false;
+    if (isfinite(ppost)) {
+        if (acc > 0.0) accept = true;
+        else accept = random_float<RNG>(r, p) < expf((float)acc);
+    }
+    if (!isfinite(cur_post)) accept = true;
+    return accept;
+}
+
+/* min(1, exp(acceptance)) of the rule above, for step-size adaptation only. */
+__device__ __forceinline__ float accept_prob64(double ppost, double cur_post, double backward, double forward) {
+    if (!isfinite(cur_post)) return 1.0f;
+    if (!isfinite(ppost)) return 0.0f;
+    const double acc = ((ppost - cur_post) + backward) - forward;
+    if (acc > 0.0) return 1.0f;
+    return expf((float)acc);
 }
 
 /* Sum over all constants of lcauchypdf(C, 1) (main.cu:303-305, 537-540), each
@@ -947,8 +1015,8 @@ __device__ void constant_move(Rng& r, const WarpSmem& w, const float* Cold, floa
     if (p.const_mode != 0) { fw_sum = f; bw_sum = b; return; }   /* random walk: symmetric, no terms */
     #pragma unroll 1
     for (int c = lane; c < PL; c += 32) {
-        f = df_add(f, df_make(__fmul_rn(w.fw[c], GPR_DF_SCALE), 0.0f));
-        b = df_add(b, df_make(__fmul_rn(w.bw[c], GPR_DF_SCALE), 0.0f));
+        f = df_add(f, df_make(w.fw[c], 0.0f));
+        b = df_add(b, df_make(w.bw[c], 0.0f));
     }
     fw_sum = warp_sum_df(f);
     bw_sum = warp_sum_df(b);
@@ -982,10 +1050,12 @@ __device__ __forceinline__ DataView data_view(const KParams& p, const float* dst
     size_t off = 0;
     if (d < 0) {
         dv.nd = p.nd; dv.nd_pad = p.nd_pad; dv.ns_hi = p.normsum_hi; dv.ns_lo = p.normsum_lo;
+        dv.ns64 = p.normsum64;
     } else {
         off = (size_t)p.ds_off[d];
         dv.nd = p.ds_n[d]; dv.nd_pad = (dv.nd + 3) & ~3;
         dv.ns_hi = p.ds_ns[2 * d]; dv.ns_lo = p.ds_ns[2 * d + 1];
+        dv.ns64 = p.ds_ns64[d];
     }
     if (streamed) {
         dv.x[0] = p.dx + off; dv.y = p.dy + off; dv.w = p.dw + off;
@@ -1102,14 +1172,44 @@ __device__ __forceinline__ void structure_move(Rng& r, const uint8_t* oc, uint8_
 #define GPR_MIN_CTAS 3
 #endif
 
+/* Phase timing of the instrumented builds (PROF): lane 0 of each warp adds
+ * the clock64 cycles since the last mark to the warp's counter `i`. */
+#define GPR_PH(i)                                                                     \
+    do {                                                                              \
+        if constexpr (PROF) {                                                         \
+            const long long t_ = clock64();                                           \
+            if (lane == 0) s_ph[warp][(i)] += (unsigned long long)(t_ - ph_t);         \
+            ph_t = t_;                                                                \
+        }                                                                             \
+    } while (0)
+#define GPR_PH_COUNT(i, v)                                                            \
+    do {                                                                              \
+        if constexpr (PROF) {                                                         \
+            if (lane == 0) s_ph[warp][(i)] += (unsigned long long)(v);                \
+        }                                                                             \
+    } while (0)
+
+/* A chain's random stream at the start of a block (rx = random_seed + idx,
+ * main.cu:691; Philox keyed by (seed, chain)). */
+template <int RNG>
+__device__ __forceinline__ Rng rng_start(uint32_t seed, int chain) {
+    Rng r;
+    r.key0 = seed; r.key1 = (uint32_t)chain; r.blk = 0xffffffffu; r.drawn = 0;
+    r.w0 = r.w1 = r.w2 = r.w3 = 0u;
+    r.s = (RNG == 0) ? ((seed + (uint32_t)chain) & 0x7fffffffu) : 0u;
+    return r;
+}
+
 /* STREAM: the dataset is read from device memory (L2-resident for a few MB)
  * instead of being staged into each CTA's shared memory -- the layout for
  * datasets too large to stage.  BATCHED: many datasets (p.nds > 0), the view
  * switched per chain group; a compile-time switch, so that the single-dataset
- * kernel keeps its dataset view in constant memory rather than registers. */
-/* PROF: the phase-timed variant (gpr_mh_prof.cu only): lane 0 of each warp
- * adds the clock64 cycles between phase boundaries (gpr_phase) to a
- * per-warp shared counter, flushed to p.phase when the warp leaves. */
+ * kernel keeps its dataset view in constant memory rather than registers.
+ * PROF: the phase-timed variant (gpr_mh_prof.cu only).
+ *
+ * Chains advance in one of three ways, by p.lockstep: 1, the CTA's warps step
+ * together and share the evaluation of every proposal (CTA-balanced: two
+ * barriers per step); k > 1, they realign every k steps; 0, they run freely. */
 template <int K, bool ONEPASS, int RNG, bool ROLLED, bool STREAM, int NV, bool BATCHED, bool PROF = false>
 __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __grid_constant__ KParams p) {
     extern __shared__ __align__(128) uint8_t smem[];
@@ -1122,19 +1222,6 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
         __syncthreads();
         ph_t = clock64();
     }
-    /* close the current phase: its cycles go to counter `i` */
-#define GPR_PH(i)                                                                  \
-    do {                                                                           \
-        if constexpr (PROF) {                                                      \
-            const long long t_ = clock64();                                        \
-            if (lane == 0) s_ph[warp][(i)] += (unsigned long long)(t_ - ph_t);      \
-            ph_t = t_;                                                             \
-        }                                                                          \
-    } while (0)
-#define GPR_PH_COUNT(i, v)                                                         \
-    do {                                                                           \
-        if constexpr (PROF) { if (lane == 0) s_ph[warp][(i)] += (unsigned long long)(v); } \
-    } while (0)
 
     /* CTA-shared dataset (or the device arrays when streamed); with batched
      * data, the dataset of the current chain group (staged per group) */
@@ -1170,18 +1257,18 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
     const int nwarps = blockDim.x >> 5;
     /* CTA-balanced evaluation (lockstep == 1): each warp publishes its chain's
      * program; all warps then pull (chain, pass) tasks, longest programs
-     * first, and leave per-pass partial sums here. */
+     * first, and leave the chunk sums of each pass here. */
     __shared__ const uint2* s_prog[8];
     __shared__ int s_cost[8];
     __shared__ int s_count[8];
     __shared__ int s_bad[8];
     __shared__ int s_next;
-    __shared__ float s_part_hi[8][GPR_MAX_PASSES];
-    __shared__ float s_part_lo[8][GPR_MAX_PASSES];
+    __shared__ float s_part[8][2 * GPR_MAX_PASSES];
     int npass = ONEPASS ? 1 : (dv.nd + 32 * K - 1) / (32 * K);
+    int nch = chunk_count(dv.nd);
     bool balanced = p.lockstep == 1 && npass <= GPR_MAX_PASSES;
-
     GPR_PH(GPR_PH_CLAIM);
+
 #pragma unroll 1
     for (;;) {
         int chain = 0;
@@ -1208,6 +1295,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                     bar_live = bar_live || dv.nd_pad > 0;
                     staged_ds = d;
                     npass = (dv.nd + 32 * K - 1) / (32 * K);
+                    nch = chunk_count(dv.nd);
                     balanced = p.lockstep == 1 && npass <= GPR_MAX_PASSES;
                 }
             }
@@ -1232,15 +1320,10 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
         int ccur = 0;          /* constants buffer of the current state */
         float cur_len = 0.0f;
         int cur_count = 0;
-        df cur_prior = df_make(0.f, 0.f), cur_lik = df_make(0.f, 0.f), cur_post = df_make(0.f, 0.f);
-        df cur_cs = df_make(0.f, 0.f);
-        df forward = df_make(0.f, 0.f), backward = df_make(0.f, 0.f);
+        double cur_prior = 0.0, cur_lik = 0.0, cur_post = 0.0, cur_cs = 0.0;
+        double forward = 0.0, backward = 0.0;
 
-        const uint32_t seed = p.seed;
-        Rng r;
-        r.key0 = seed; r.key1 = (uint32_t)chain; r.blk = 0xffffffffu; r.drawn = 0;
-        r.w0 = r.w1 = r.w2 = r.w3 = 0u;
-        r.s = (RNG == 0) ? ((seed + (uint32_t)chain) & 0x7fffffffu) : 0u;   /* rx = random_seed + idx */
+        Rng r = rng_start<RNG>(p.seed, chain);
         /* random-walk scale: the configured one, or this chain's own (adapted) */
         float rw_sd = (p.chain_scale && active) ? p.chain_scale[chain] : p.rw_sd;
         float log_sd = logf(rw_sd);
@@ -1263,13 +1346,13 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
           int pbuf = cur, cbuf = ccur;
           float len = cur_len;
           int count = cur_count, ninstr = cur_ninstr;
-          df cs = cur_cs;
+          double cs = cur_cs;
           if (active) {
             bool need_compile = init, need_cauchy = init;
             if (structural) {
                 /* ---- structure move (main.cu:699-742) ---- */
-                forward = df_make(__fmul_rn(-p.logcount[cur_count], GPR_DF_SCALE), 0.0f);
-                structure_move<RNG>(r, ws.ops[cur], ws.ops[cur ^ 1], df_invalid(cur_post), p, lane);
+                forward = -(double)p.logcount[cur_count];
+                structure_move<RNG>(r, ws.ops[cur], ws.ops[cur ^ 1], !isfinite(cur_post), p, lane);
                 pbuf = cur ^ 1;
                 need_compile = true;
                 GPR_PH(GPR_PH_STRUCT);
@@ -1277,7 +1360,10 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                 /* ---- constant move (main.cu:743-806) ---- */
                 df fws, bws;
                 constant_move<RNG>(r, ws, ws.Cs[ccur], ws.Cs[ccur ^ 1], fws, bws, p, ljump, lane, rw_sd);
-                if (p.const_mode == 0) { forward = df_add(forward, fws); backward = df_add(backward, bws); }
+                if (p.const_mode == 0) {
+                    forward += (double)fws.hi + (double)fws.lo;
+                    backward += (double)bws.hi + (double)bws.lo;
+                }
                 cbuf = ccur ^ 1;
                 need_cauchy = true;
                 GPR_PH(GPR_PH_CONST);
@@ -1292,13 +1378,13 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                 __syncwarp();
                 GPR_PH(GPR_PH_COMPILE);
             }
-            if (need_cauchy) { cs = cauchy_sum(ws.Cs[cbuf], p, lane); GPR_PH(GPR_PH_CAUCHY); }
-            if (structural) backward = df_make(__fmul_rn(-p.logcount[count], GPR_DF_SCALE), 0.0f);
+            if (need_cauchy) { cs = cauchy_sum64(ws.Cs[cbuf], p, lane); GPR_PH(GPR_PH_CAUCHY); }
+            if (structural) backward = -(double)p.logcount[count];
             build_eval_program(ws.prog[pbuf], ws.Cs[cbuf], ninstr, ws.eprog, lane);
             __syncwarp();
             GPR_PH(GPR_PH_EPROG);
           }
-          df lik = df_make(0.0f, 0.0f);
+          double lik = 0.0;
           int pts = 0;
           if (balanced) {
             if (lane == 0) {
@@ -1333,21 +1419,17 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                 const int q = t / npass, pass = t - q * npass;
                 const int w = __ffs(__ballot_sync(FULLMASK, my_rank == q)) - 1;
                 if (s_bad[w]) continue;
-                bool bad;
-                const float sl = eval_pass<K, ONEPASS, ROLLED, NV, STREAM>(s_prog[w], ws.stk, ws.scr, ld, dv,
-                                                               p, lane, pass, bad, pts);
-                /* FP32 butterfly within the pass (terms are >= 0: <= 5 roundings),
-                 * double-float across passes */
-                const float Sp = warp_sum(sl);
-                const df S = df_make(Sp, 0.0f);
-                const bool anybad = __any_sync(FULLMASK, bad);
+                float csum[K / 4];
+                const bool anybad = eval_pass_chunks<K, ONEPASS, ROLLED, NV, STREAM>(s_prog[w], ws.stk, ws.scr, ld,
+                                                                                   dv, p, lane, pass, csum);
+                const int np = ONEPASS ? dv.nd : min(32 * K, dv.nd - pass * 32 * K);
+                pts += np;
                 if (lane == 0) {
-                    s_part_hi[w][pass] = S.hi;
-                    s_part_lo[w][pass] = S.lo;
+#pragma unroll
+                    for (int j = 0; j < K / 4; ++j) s_part[w][pass * (K / 4) + j] = csum[j];
                     if (anybad) s_bad[w] = 1;
                 }
-                st_np += (unsigned long long)(s_count[w] + 4) *
-                         (unsigned)(ONEPASS ? dv.nd : min(32 * K, dv.nd - pass * 32 * K));
+                st_np += (unsigned long long)(s_count[w] + 4) * (unsigned)np;
                 GPR_PH_COUNT(GPR_PH_NPASSES, 1);
                 GPR_PH_COUNT(GPR_PH_NINSTR, s_cost[w]);
             }
@@ -1356,35 +1438,34 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
             GPR_PH(GPR_PH_BAR2);
             if (active) {
                 if (s_bad[warp]) {
-                    lik = df_make(-INFINITY, 0.0f);
+                    lik = -INFINITY;
                 } else {
-                    df S = df_make(0.0f, 0.0f);
-                    for (int q = 0; q < npass; ++q) S = df_add(S, df_make(s_part_hi[warp][q], s_part_lo[warp][q]));
-                    lik = !isfinite(S.hi) ? df_make(-INFINITY, 0.0f)
-                                          : df_sub(df_neg(S), df_make(dv.ns_hi, dv.ns_lo));
+                    double S = 0.0;
+                    for (int c = 0; c < nch; ++c) S += (double)s_part[warp][c];
+                    lik = finish_loglik(S, dv, p);
                 }
             }
             GPR_PH(GPR_PH_COMBINE);
           } else if (active) {
-            lik = eval_loglik<K, ONEPASS, ROLLED, NV, STREAM>(ws.eprog, ws.stk, ws.scr, ld, dv, p, lane, pts);
+            lik = eval_loglik64<K, ONEPASS, ROLLED, NV, STREAM>(ws.eprog, ws.stk, ws.scr, ld, dv, p, lane, pts);
             st_np += (unsigned long long)(count + 4) * (unsigned)pts;
-            GPR_PH_COUNT(GPR_PH_NPASSES, ONEPASS ? 1 : (dv.nd + 32 * K - 1) / (32 * K));
-            GPR_PH_COUNT(GPR_PH_NINSTR, (unsigned long long)ninstr * (ONEPASS ? 1 : (dv.nd + 32 * K - 1) / (32 * K)));
+            GPR_PH_COUNT(GPR_PH_NPASSES, npass);
+            GPR_PH_COUNT(GPR_PH_NINSTR, (unsigned long long)ninstr * npass);
             GPR_PH(GPR_PH_EVAL);
           }
           st_pts += (unsigned)pts;
           if (active) {
-            const df prior = df_add(length_prior(len, p), cs);
-            const df post = df_add(prior, lik);
+            const double prior = prior64(len, cs, p);
+            const double post = prior + lik;
             st_evals++; st_nodes += (unsigned)count;
             bool accept = true;
             if (!init) {
                 if (!structural && p.adapt_target > 0.0f && p.const_mode == 1) {
-                    log_sd = rm_update(log_sd, accept_prob(post, cur_post, backward, forward), p.adapt_target,
+                    log_sd = rm_update(log_sd, accept_prob64(post, cur_post, backward, forward), p.adapt_target,
                                        n_cmoves++);
                     rw_sd = expf(log_sd);
                 }
-                accept = mh_accept<RNG>(post, cur_post, backward, forward, r, p);
+                accept = mh_accept64<RNG>(post, cur_post, backward, forward, r, p);
                 if (structural) { st_sp++; st_sa += accept; } else { st_cp++; st_ca += accept; }
             }
             if (accept) {
@@ -1407,8 +1488,8 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
             p.C[(size_t)i * p.N + chain] = ws.Cs[ccur][i];
         }
         if (active && lane == 0) {
-            p.prior[chain] = df_to_double_unscaled(cur_prior);
-            p.lik[chain] = df_to_double_unscaled(cur_lik);
+            p.prior[chain] = cur_prior;
+            p.lik[chain] = cur_lik;
             if (p.chain_scale && p.adapt_target > 0.0f && p.const_mode == 1) p.chain_scale[chain] = rw_sd;
         }
         if (lane == 0 && p.stats) {
@@ -1432,8 +1513,6 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
         if (lane == 0 && p.phase)
             for (int i = 0; i < GPR_PH_SLOTS; ++i) atomicAdd(&p.phase[i], s_ph[warp][i]);
     }
-#undef GPR_PH
-#undef GPR_PH_COUNT
 }
 
 }  // namespace gpr

@@ -1,8 +1,8 @@
-/* The phase-timed instantiations of the MH block kernel (PROF = true) for the
+/* The phase-timed instantiations of the MH kernels (PROF = true) for the
  * single-dataset, one-variable, LCG layouts with heavy ops unrolled: a
  * diagnostics build that adds clock64 reads at phase boundaries
  * (gpr_debug_phase_profile).  The product kernels carry none of it. */
-#include "gpr_mh.cuh"
+#include "gpr_pipe.cuh"
 
 namespace gpr {
 template __global__ void mh_block_kernel<4, true, 0, false, false, 1, false, true>(const __grid_constant__ KParams p);
@@ -10,6 +10,17 @@ template __global__ void mh_block_kernel<4, false, 0, false, false, 1, false, tr
 template __global__ void mh_block_kernel<4, false, 0, false, true, 1, false, true>(const __grid_constant__ KParams p);
 template __global__ void mh_block_kernel<8, true, 0, false, false, 1, false, true>(const __grid_constant__ KParams p);
 template __global__ void mh_block_kernel<8, false, 0, false, false, 1, false, true>(const __grid_constant__ KParams p);
+template __global__ void mh_pipe_kernel<4, false, 0, false, false, 1, false, true>(const __grid_constant__ KParams p);
+template __global__ void mh_pipe_kernel<4, false, 0, false, true, 1, false, true>(const __grid_constant__ KParams p);
+template __global__ void mh_pipe_kernel<8, true, 0, false, false, 1, false, true>(const __grid_constant__ KParams p);
+
+static const void* pipe_prof(int K, int onepass, int rng, int stream) {
+    if (rng != 0) return nullptr;
+    if (K == 4 && !onepass) return stream ? (const void*)mh_pipe_kernel<4, false, 0, false, true, 1, false, true>
+                                          : (const void*)mh_pipe_kernel<4, false, 0, false, false, 1, false, true>;
+    if (K == 8 && onepass && !stream) return (const void*)mh_pipe_kernel<8, true, 0, false, false, 1, false, true>;
+    return nullptr;
+}
 
 const void* mh_kernel_prof(int K, int onepass, int rng, int stream) {
     if (rng != 0) return nullptr;
@@ -22,9 +33,14 @@ const void* mh_kernel_prof(int K, int onepass, int rng, int stream) {
     return nullptr;
 }
 
+const void* prof_kernel(const LaunchCfg& lc) {
+    return lc.pipe ? pipe_prof(lc.K, lc.onepass, 0, lc.stream) : mh_kernel_prof(lc.K, lc.onepass, 0, lc.stream);
+}
+
 cudaError_t launch_mh_block_prof(const KParams& p, const LaunchCfg& lc, cudaStream_t st) {
     if (p.nv == 3 || p.nds > 0 || lc.rolled || !p.phase) return cudaErrorInvalidValue;
-    const void* f = mh_kernel_prof(lc.K, lc.onepass, p.rng_mode, lc.stream);
+    const void* f = lc.pipe ? pipe_prof(lc.K, lc.onepass, p.rng_mode, lc.stream)
+                            : mh_kernel_prof(lc.K, lc.onepass, p.rng_mode, lc.stream);
     if (!f) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lc.smem_bytes);
     if (e != cudaSuccess) return e;
@@ -37,8 +53,10 @@ cudaError_t launch_mh_block_prof(const KParams& p, const LaunchCfg& lc, cudaStre
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
     if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
     long long ctas = (long long)nsm * per_sm;
-    const long long need = (p.N + lc.warps_per_cta - 1) / lc.warps_per_cta;
+    const int per_cta = lc.pipe ? 2 * lc.warps_per_cta : lc.warps_per_cta;
+    const long long need = (p.N + per_cta - 1) / per_cta;
     if (ctas > need) ctas = need;
+    if (ctas > lc.ctas) ctas = lc.ctas;   /* p.part holds rows for lc.ctas CTAs */
     KParams pp = p;
     pp.lockstep = lc.lockstep;
     void* args[] = {(void*)&pp};

@@ -174,20 +174,26 @@ int gpr_debug_math(gpr_handle* h, int op, const float* a, const float* b, float*
 int gpr_debug_phase_profile(gpr_handle* h, int steps, int random_seed, uint64_t* out, int n);
 
 /* Layout autotuner (no reference counterpart): times one block of `steps`
- * MH steps under each valid evaluation layout -- K = 4 or 8 points per lane,
- * data held in registers (one pass) or read from shared memory in passes,
- * transcendental/division ops unrolled or through a compact loop -- then,
- * for the best of those, each CTA barrier period (1, 5 steps, none) and CTA
- * size (8 or 4 chains), on the handle's current state and data; keeps the
- * fastest and restores the state, scores and counters.  Call after
- * gpr_set_data/gpr_set_state. */
+ * MH steps under each valid evaluation layout -- the pipelined kernel (two
+ * chains per warp) or the lockstep one (one chain per warp), K = 4 or 8
+ * points per lane, data held in registers (one pass), read from shared
+ * memory in passes or streamed from device memory, transcendental/division
+ * ops unrolled or (lockstep kernel) through a compact loop -- then, for the
+ * best of those, the CTA size (8 or 4 warps) and, for the lockstep kernel,
+ * the CTA barrier period (1, 5 steps, none), on the handle's current state and
+ * data; keeps the fastest and restores the state, scores and counters.  Every
+ * layout gives the same chains bit for bit, so the choice changes speed only.
+ * Call after gpr_set_data/gpr_set_state. */
 int gpr_autotune(gpr_handle* h, int steps, int seed, int* K, int* onepass, int* rolled, float* best_ms);
 
-/* Select an evaluation layout explicitly (K 4 or 8; onepass needs n <= 32K).
- * gpr_set_layout2 also sets the CTA barrier period in MH steps (0 = none)
- * and the warps (chains) per CTA (1, 2, 4 or 8). */
+/* Select an evaluation layout explicitly (K 4 or 8; onepass needs n <= 32K)
+ * on the lockstep kernel.  gpr_set_layout2 also sets the CTA barrier period
+ * in MH steps (0 = none) and the warps (chains) per CTA (1, 2, 4 or 8);
+ * gpr_set_layout3 also selects the pipelined kernel (pipe = 1: two chains per
+ * warp, heavy ops unrolled, the barrier period unused). */
 int gpr_set_layout(gpr_handle* h, int K, int onepass, int rolled);
 int gpr_set_layout2(gpr_handle* h, int K, int onepass, int rolled, int lockstep, int warps_per_cta);
+int gpr_set_layout3(gpr_handle* h, int K, int onepass, int rolled, int lockstep, int warps_per_cta, int pipe);
 
 /* Read the dataset from device memory in every pass (always = 1) instead of
  * staging it into each CTA's shared memory; 0 (default) streams only when
@@ -215,6 +221,11 @@ void* gpr_stream(gpr_handle* h);
  * current CTA barrier period. */
 int gpr_layout_rolled(gpr_handle* h);
 int gpr_layout_lockstep(gpr_handle* h);
+/* 1 when the current layout runs the pipelined kernel: two chains per warp,
+ * the chains of a CTA in two groups taking turns (one group draws and
+ * compiles its proposals while every warp evaluates the other group's), one
+ * CTA barrier per half-step, the evaluation of a chain split over all warps. */
+int gpr_layout_pipelined(gpr_handle* h);
 
 /* Counters accumulated by the MH kernel since the last reset (no reference
  * counterpart): [0] likelihood evaluations, [1] sum of evaluated node counts,

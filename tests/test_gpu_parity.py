@@ -117,8 +117,8 @@ def test_prior_likelihood_match_reference(lib, data):
 @pytest.mark.parametrize("data,PL,ops", [("quad", 31, None), ("expdecay", 63, H.OPSET_BASIC)],
                          ids=["quad-pl31-ref", "expdecay-pl63-basic"])
 def test_loglik_error_vs_fp64(lib, data, PL, ops):
-    """The device log-likelihood (FP32 evaluation, double-float accumulation,
-    no FP64 instruction) against the FP64 evaluation of the same programs:
+    """The device log-likelihood (FP32 evaluation, FP32 sums within 128-point
+    chunks, FP64 across chunks) against the FP64 evaluation of the same programs:
     within 1e-5 relative wherever the program's FP32 evaluation is itself
     determined to 1e-6 (the reference's FP32 result, compiled for the host,
     lies within 1e-6 of FP64); chains outside that are counted, not judged."""
@@ -322,4 +322,13 @@ def test_nan_data_matches_reference(lib, where):
     assert np.array_equal(np.isneginf(lik), np.isneginf(rlik))
     fin = np.isfinite(lik) & np.isfinite(rlik)
     assert fin.any()
-    assert H.rel_err(lik[fin], rlik[fin]).max() <= 1e-4
+    # 1e-5 wherever the program's FP32 evaluation is determined to 1e-6 (the
+    # reference's FP32 result within 1e-6 of FP64 on the same data), as the
+    # other parity tests judge
+    from oracle import port
+    f64 = np.array([port.likelihood(P, C, i, x, y, sd, f64=True) if fin[i] else np.nan for i in range(N)])
+    with np.errstate(all="ignore"):
+        cond = np.abs(rlik - f64) / np.maximum(np.abs(f64), 1.0)
+    judged = fin & np.isfinite(f64) & (cond <= 1e-6)
+    assert judged.sum() > fin.sum() // 2, (judged.sum(), fin.sum())
+    assert H.rel_err(lik[judged], rlik[judged]).max() <= 1e-5
