@@ -117,8 +117,10 @@ static uint32_t divisor_for(int n) { return (uint32_t)(2147483647 / (n + 1)); }
 
 /* The exponent e of the likelihood weights 2^-e / (2 sd^2): the largest is
  * at most 2^-8, so the FP32 sum of a 128-point chunk of terms (each at most
- * FLT_MAX times its weight) cannot overflow; e is clamped to [-62, 191] so
- * that 2^(e-64) is a normal float. */
+ * FLT_MAX times its weight) cannot overflow; e is clamped to [-62, 252]
+ * (2^-e stays a normal double, 2^(e-64) a normal float up to e = 191: beyond,
+ * for sd below about 5e-30, the Hamiltonian kernel's 2^-64-scaled weights
+ * overflow as they always have). */
 static int weight_exponent(const float* sd, size_t n) {
     double maxw = 0.0;
     for (size_t i = 0; i < n; ++i) {
@@ -129,7 +131,7 @@ static int weight_exponent(const float* sd, size_t n) {
     if (!(maxw > 0.0) || !std::isfinite(maxw)) return 0;
     int x = 0;
     frexp(maxw, &x);                    /* maxw <= 2^x */
-    return std::min(191, std::max(-62, x + 8));
+    return std::min(252, std::max(-62, x + 8));
 }
 
 /* The per-point weight of a point with standard deviation sd. */
