@@ -116,11 +116,12 @@ static gpr::Magic magic_for(uint32_t d) {
 static uint32_t divisor_for(int n) { return (uint32_t)(2147483647 / (n + 1)); }
 
 /* The exponent e of the likelihood weights 2^-e / (2 sd^2): the largest is
- * at most 2^-8, so the FP32 sum of a 128-point chunk of terms (each at most
- * FLT_MAX times its weight) cannot overflow; e is clamped to [-62, 252]
- * (2^-e stays a normal double, 2^(e-64) a normal float up to e = 191: beyond,
- * for sd below about 5e-30, the Hamiltonian kernel's 2^-64-scaled weights
- * overflow as they always have). */
+ * at most 2^-32, so a term (at most FLT_MAX times its weight) is at most
+ * 2^96 and the FP32 sum of up to 2^31 terms cannot overflow.  e is clamped to
+ * [-100, 250] (2^e is then a product of two normal floats): datasets with an
+ * sd below 1e-33 could overflow at the clamp.  The Hamiltonian kernel, which
+ * keeps its own 2^-64 scale, holds weights up to sd of about 5e-30 only, as
+ * it always has. */
 static int weight_exponent(const float* sd, size_t n) {
     double maxw = 0.0;
     for (size_t i = 0; i < n; ++i) {
@@ -131,7 +132,7 @@ static int weight_exponent(const float* sd, size_t n) {
     if (!(maxw > 0.0) || !std::isfinite(maxw)) return 0;
     int x = 0;
     frexp(maxw, &x);                    /* maxw <= 2^x */
-    return std::min(252, std::max(-62, x + 8));
+    return std::min(250, std::max(-100, x + 32));
 }
 
 /* The per-point weight of a point with standard deviation sd. */
@@ -143,15 +144,23 @@ static float point_weight(float sd, int e) {
 /* The scale fields of the kernel parameters for weight exponent e. */
 static void set_weight_scale(gpr::KParams& kp, int e) {
     kp.lik_unscale = ldexp(1.0, e);
+    kp.lik_e = e;
+    const int e1 = std::min(127, std::max(-126, e));
+    kp.unscale1 = (float)ldexp(1.0, e1);
+    kp.unscale2 = (float)ldexp(1.0, e - e1);
     kp.w_to_df = (float)ldexp(1.0, e - 64);
 }
 
-/* The FP64 prior constants: log(NOPS + 1) (main.cu:536) and PL logf(PIf),
- * the constant part of the Cauchy sum (main.cu:304, 537-540). */
+/* The prior's constants as double-floats: log(NOPS + 1) (main.cu:536) and
+ * PL logf(PIf), the constant part of the Cauchy sum (main.cu:304, 537-540). */
 static void set_prior_constants(gpr::KParams& kp, int n_ops, int PL) {
     const double PIf = 3.141592653589;                             /* main.cu:194 */
-    kp.ln1_64 = log((double)n_ops + 1);
-    kp.cauchy_c64 = (double)PL * (double)logf((float)PIf);
+    const double ln1 = log((double)n_ops + 1);
+    kp.ln1u_hi = (float)ln1;
+    kp.ln1u_lo = (float)(ln1 - (double)kp.ln1u_hi);
+    const double cc = (double)PL * (double)logf((float)PIf);
+    kp.cauchy_c_hi = (float)cc;
+    kp.cauchy_c_lo = (float)(cc - (double)kp.cauchy_c_hi);
 }
 
 extern "C" {

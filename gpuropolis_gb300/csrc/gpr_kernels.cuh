@@ -52,15 +52,20 @@ struct KParams {
     int nd_pad;        /* multiple of 4                                       */
     float normsum_hi, normsum_lo;  /* 2^-64 * sum_d 0.5*(logf(2 PIf) + 2 logf(sd_d)), double-float
                                     * (the Hamiltonian kernel's bookkeeping)  */
-    /* The weights dw are 2^-e / (2 sd^2), e chosen per handle so that the
-     * FP32 sum of a 128-point chunk cannot overflow (every weight <= 2^-8).
-     * The MH kernels keep every Bayes quantity in FP64, unscaled. */
+    /* The weights dw are 2^-e / (2 sd^2), e chosen per handle so that every
+     * weight is at most 2^-32: the sum S of a chain's terms (f - y)^2 w then
+     * cannot overflow FP32, chunk by chunk or in total.  The MH kernels keep
+     * S as a double-float at that scale; the likelihood is -S 2^e - the
+     * normalising sum, formed in FP64 only when a block's scores are written. */
     double lik_unscale;     /* 2^e                                            */
+    int lik_e;              /* e                                              */
+    float unscale1, unscale2;   /* 2^e as a product of two floats             */
     float w_to_df;          /* 2^(e-64): dw * w_to_df is the Hamiltonian kernel's 2^-64-scaled weight */
     double normsum64;       /* sum_d 0.5*(logf(2 PIf) + 2 logf(sd_d))          */
     const double* ds_ns64;  /* batched: the same per dataset                   */
-    double ln1_64;          /* log((double)NOPS + 1)          (main.cu:536)     */
-    double cauchy_c64;      /* PL * logf(PIf): the constant part of the Cauchy prior (main.cu:304, 537-540) */
+    float ln1u_hi, ln1u_lo; /* log((double)NOPS + 1) as a double-float (main.cu:536) */
+    float cauchy_c_hi, cauchy_c_lo;   /* PL * logf(PIf), the constant part of the
+                                       * Cauchy prior (main.cu:304, 537-540), double-float */
     float* part;            /* chunk sums of the pipelined kernel when a dataset has more
                              * chunks than its shared-memory board holds      */
     int part_stride;        /* floats per (CTA, group, warp) in part          */

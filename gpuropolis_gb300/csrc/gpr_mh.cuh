@@ -735,9 +735,10 @@ struct LaneData {
  * points are taken in chunks of 128 (chunk c = points 128c .. 128c+127, lane
  * l holding points 128c + l + 32k, k = 0..3); each lane sums its four terms
  * (f - y)^2 w in FP32 in k order, the 32 lane sums are combined by an FP32
- * xor butterfly, and the chunk sums are added in FP64 in chunk order
- * (main.cu:454-468 sums every point in double).  A chunk sum cannot
- * overflow: every weight is at most 2^-8 (KParams::lik_unscale). */
+ * xor butterfly, and the chunk sums are added as double-floats in chunk
+ * order (main.cu:454-468 sums every point in double).  The weights carry the
+ * factor 2^-e (KParams::lik_unscale), so S, the sum of a chain's terms, is a
+ * double-float at the scale 2^-e that cannot overflow. */
 #define GPR_CHUNK_POINTS 128
 
 __device__ __forceinline__ int chunk_count(int nd) { return (nd + GPR_CHUNK_POINTS - 1) / GPR_CHUNK_POINTS; }
@@ -785,43 +786,53 @@ __device__ __forceinline__ bool eval_pass_chunks(const PR prog, float* stk, floa
     return __any_sync(FULLMASK, bad);
 }
 
-/* The log-likelihood from the FP64 sum of a program's chunk sums:
- * -(sum) 2^e - the normalising sum. */
-__device__ __forceinline__ double finish_loglik(double S, const DataView& dv, const KParams& p) {
-    return (0.0 - S * p.lik_unscale) - dv.ns64;
-}
+/* S of an invalid likelihood (-inf, main.cu:459,462). */
+__device__ __forceinline__ df lik_invalid() { return df_make(INFINITY, 0.0f); }
 
-/* Log-likelihood of one program evaluated by one warp (main.cu:454-468):
- * -inf when any point is invalid (main.cu:459,462). */
+/* S of one program evaluated by one warp: the double-float sum of its chunk
+ * sums in chunk order, or +inf when any point is invalid. */
 template <int K, bool ONEPASS, bool ROLLED, int NV, bool STREAM, class PR>
-__device__ __forceinline__ double eval_loglik64(const PR prog, float* stk, float* scr, const LaneData<K>& ld,
-                                                const DataView& dv, const KParams& p, int lane, int& pts) {
+__device__ __forceinline__ df eval_loglik_S(const PR prog, float* stk, float* scr, const LaneData<K>& ld,
+                                            const DataView& dv, const KParams& p, int lane, int& pts) {
     const int npass = ONEPASS ? 1 : (dv.nd + 32 * K - 1) / (32 * K);
     const int nch = chunk_count(dv.nd);
-    double S = 0.0;
+    df S = df_make(0.0f, 0.0f);
 #pragma unroll 1
     for (int pass = 0; pass < npass; ++pass) {
         float cs[K / 4];
         const bool bad = eval_pass_chunks<K, ONEPASS, ROLLED, NV, STREAM>(prog, stk, scr, ld, dv, p, lane, pass, cs);
         pts += ONEPASS ? dv.nd : min(32 * K, dv.nd - pass * 32 * K);
-        if (bad) return -INFINITY;
+        if (bad) return lik_invalid();
 #pragma unroll
         for (int j = 0; j < K / 4; ++j)
-            if (pass * (K / 4) + j < nch) S += (double)cs[j];
+            if (pass * (K / 4) + j < nch) S = df_add(S, df_make(cs[j], 0.0f));
     }
-    return finish_loglik(S, dv, p);
+    return S;
 }
 
-/* Prior of a program (main.cu:529-544) in FP64: -length log(NOPS + 1) plus
- * the Cauchy sum over all constants. */
-__device__ __forceinline__ double prior64(float length, double cauchy, const KParams& p) {
-    return (double)(-length) * p.ln1_64 + cauchy;
+/* The log-likelihood (main.cu:454-468) of a chain with sum S, in FP64, for
+ * the scores a block writes: -S 2^e - the normalising sum. */
+__device__ __forceinline__ double lik_of(df S, const DataView& dv, const KParams& p) {
+    if (!isfinite(S.hi)) return -INFINITY;
+    return (0.0 - ((double)S.hi + (double)S.lo) * p.lik_unscale) - dv.ns64;
 }
 
-/* Sum over all constants of lcauchypdf(C, 1) (main.cu:303-305, 537-540) in
- * FP64: the -log(1 + C^2) terms are FP32 (the reference's logf), added
- * exactly as double-floats across the warp; the constant part is added once. */
-__device__ __forceinline__ double cauchy_sum64(const float* Cs, const KParams& p, int lane) {
+/* -length log(NOPS + 1) (main.cu:536): the exact product of the
+ * integer-valued length with the double-float constant. */
+__device__ __forceinline__ df length_prior_u(float length, const KParams& p) {
+    const float L = -length;
+    const float ph = __fmul_rn(L, p.ln1u_hi);
+    float e = __fmaf_rn(L, p.ln1u_hi, -ph);
+    e = __fmaf_rn(L, p.ln1u_lo, e);
+    if (!isfinite(ph)) return df_make(ph, 0.0f);
+    const float h = __fadd_rn(ph, e);
+    return df_make(h, __fsub_rn(e, __fsub_rn(h, ph)));
+}
+
+/* Sum over all constants of lcauchypdf(C, 1) (main.cu:303-305, 537-540): the
+ * -log(1 + C^2) terms are FP32 (the reference's logf), added exactly as
+ * double-floats across the warp; the constant part PL log(PIf) once. */
+__device__ __forceinline__ df cauchy_sum_u(const float* Cs, const KParams& p, int lane) {
     df s = df_make(0.0f, 0.0f);
 #pragma unroll 1
     for (int c = lane; c < p.PL; c += 32) {
@@ -829,46 +840,86 @@ __device__ __forceinline__ double cauchy_sum64(const float* Cs, const KParams& p
         s = df_add(s, df_make(-gx_log(__fadd_rn(1.0f, __fmul_rn(x, x))), 0.0f));
     }
     s = warp_sum_df(s);
-    return ((double)s.hi + (double)s.lo) - p.cauchy_c64;
+    return df_sub(s, df_make(p.cauchy_c_hi, p.cauchy_c_lo));
 }
 
-/* The accept rule of main.cu:728-740 / 790-802 in FP64, in its exact
- * evaluation order: acceptance = proposal - current + backward - forward;
- * the uniform draw is consumed only when the proposal is valid and
- * acceptance <= 0; an invalid current state accepts anything. */
-template <int RNG>
-__device__ __forceinline__ bool mh_accept64(double ppost, double cur_post, double backward, double forward, Rng& r,
-                                            const KParams& p) {
-    const double acc = ((ppost - cur_post) + backward) - forward;
-    bool accept = false;
-    if (isfinite(ppost)) {
-        if (acc > 0.0) accept = true;
-        else accept = random_float<RNG>(r, p) < expf((float)acc);
-    }
-    if (!isfinite(cur_post)) accept = true;
-    return accept;
-}
-
-/* min(1, exp(acceptance)) of the rule above, for step-size adaptation only. */
-__device__ __forceinline__ float accept_prob64(double ppost, double cur_post, double backward, double forward) {
-    if (!isfinite(cur_post)) return 1.0f;
-    if (!isfinite(ppost)) return 0.0f;
-    const double acc = ((ppost - cur_post) + backward) - forward;
-    if (acc > 0.0) return 1.0f;
-    return expf((float)acc);
-}
-
-/* Sum over all constants of lcauchypdf(C, 1) (main.cu:303-305, 537-540), each
- * FP32 term added exactly (double-float), at the bookkeeping scale. */
+/* The same sum at the Hamiltonian kernel's bookkeeping scale 2^-64, each
+ * FP32 term added exactly (double-float). */
 __device__ __forceinline__ df cauchy_sum(const float* Cs, const KParams& p, int lane) {
     df s = df_make(0.0f, 0.0f);
-    #pragma unroll 1
+#pragma unroll 1
     for (int c = lane; c < p.PL; c += 32) {
-        float x = Cs[c];
-        float a = __fadd_rn(1.0f, __fmul_rn(x, x));
+        const float x = Cs[c];
+        const float a = __fadd_rn(1.0f, __fmul_rn(x, x));
         s = df_add(s, df_make(__fmul_rn(__fsub_rn(-p.lpi_f, gx_log(a)), GPR_DF_SCALE), 0.0f));
     }
     return warp_sum_df(s);
+}
+
+/* The prior (main.cu:529-544) of a program with this length and Cauchy sum. */
+__device__ __forceinline__ df prior_u(float length, df cauchy, const KParams& p) {
+    return df_add(length_prior_u(length, p), cauchy);
+}
+
+/* The acceptance log-ratio of main.cu:728 / 790,
+ *   ((proposal posterior - current posterior) + backward) - forward,
+ * for two valid states, from the prior difference and the difference of the
+ * likelihood sums (the normalising sum cancels): ((dprior - dS 2^e) + bw) - fw
+ * as a double-float.  Sets huge when |dS 2^e| >= 2^100 while the other terms
+ * are finite: the ratio's sign is then that of -dS and its exponential 0
+ * (only that sign is returned). */
+__device__ __forceinline__ df accept_ratio(df prior_p, df S_p, df prior_c, df S_c, df bw, df fw, const KParams& p,
+                                           bool& huge) {
+    const df dS = df_sub(S_p, S_c);
+    const df dprior = df_sub(prior_p, prior_c);
+    /* |dS.hi| < 2^ex (an upper bound for subnormals too) */
+    const int ex = (int)((__float_as_uint(dS.hi) >> 23) & 0xffu) - 126;
+    huge = dS.hi != 0.0f && ex + p.lik_e > 100;
+    if (huge) {
+        const df rest = df_sub(df_add(dprior, bw), fw);
+        if (isfinite(rest.hi)) return df_make(dS.hi > 0.0f ? -1.0f : 1.0f, 0.0f);
+        huge = false;
+    }
+    /* dS 2^e, exact: two power-of-two factors, no overflow (|result| < 2^100) */
+    const df L = df_make(__fmul_rn(__fmul_rn(dS.hi, p.unscale1), p.unscale2),
+                         __fmul_rn(__fmul_rn(dS.lo, p.unscale1), p.unscale2));
+    return df_sub(df_add(df_sub(dprior, L), bw), fw);
+}
+
+/* The accept rule of main.cu:728-740 / 790-802, in its exact evaluation
+ * order: the uniform draw is consumed only when the proposal is valid and the
+ * acceptance ratio is not > 0; an invalid current state accepts anything.  A
+ * posterior is NaN when its prior is (an invalid op's length), -inf when its
+ * prior or likelihood is -inf; a NaN current posterior makes the ratio NaN (a
+ * draw, then acceptance), a -inf one makes it +inf (acceptance, no draw).
+ * prob, when given, receives min(1, exp(ratio)) for step-size adaptation. */
+template <int RNG>
+__device__ __forceinline__ bool mh_accept_u(df prior_p, df S_p, df prior_c, df S_c, df bw, df fw, Rng& r,
+                                            const KParams& p, float* prob = nullptr) {
+    const bool pp_valid = isfinite(prior_p.hi) && isfinite(S_p.hi);
+    const bool cp_nan = isnan(prior_c.hi);
+    const bool cp_valid = isfinite(prior_c.hi) && isfinite(S_c.hi);
+    if (!pp_valid) {
+        if (prob) *prob = cp_valid ? 0.0f : 1.0f;
+        return !cp_valid;
+    }
+    if (!cp_valid) {
+        if (prob) *prob = 1.0f;
+        if (cp_nan) (void)random_float<RNG>(r, p);
+        return true;
+    }
+    bool huge;
+    const df a = accept_ratio(prior_p, S_p, prior_c, S_c, bw, fw, p, huge);
+    if (huge) {
+        if (a.hi > 0.0f) { if (prob) *prob = 1.0f; return true; }
+        if (prob) *prob = 0.0f;
+        (void)random_float<RNG>(r, p);
+        return false;
+    }
+    if (df_gt0(a)) { if (prob) *prob = 1.0f; return true; }
+    const float e = expf(a.hi);
+    if (prob) *prob = e;
+    return random_float<RNG>(r, p) < e;
 }
 
 /* lnormalpdf(x, 1.0) (main.cu:299-301) */
@@ -1320,8 +1371,10 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
         int ccur = 0;          /* constants buffer of the current state */
         float cur_len = 0.0f;
         int cur_count = 0;
-        double cur_prior = 0.0, cur_lik = 0.0, cur_post = 0.0, cur_cs = 0.0;
-        double forward = 0.0, backward = 0.0;
+        /* the current state's prior, likelihood sum S (scale 2^-e) and Cauchy
+         * sum; the forward/backward terms (main.cu:702,723,761-775) */
+        df cur_prior = df_make(0.f, 0.f), cur_S = df_make(0.f, 0.f), cur_cs = df_make(0.f, 0.f);
+        df forward = df_make(0.f, 0.f), backward = df_make(0.f, 0.f);
 
         Rng r = rng_start<RNG>(p.seed, chain);
         /* random-walk scale: the configured one, or this chain's own (adapted) */
@@ -1346,13 +1399,14 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
           int pbuf = cur, cbuf = ccur;
           float len = cur_len;
           int count = cur_count, ninstr = cur_ninstr;
-          double cs = cur_cs;
+          df cs = cur_cs;
           if (active) {
             bool need_compile = init, need_cauchy = init;
             if (structural) {
                 /* ---- structure move (main.cu:699-742) ---- */
-                forward = -(double)p.logcount[cur_count];
-                structure_move<RNG>(r, ws.ops[cur], ws.ops[cur ^ 1], !isfinite(cur_post), p, lane);
+                forward = df_make(-p.logcount[cur_count], 0.0f);
+                const bool cur_invalid = !(isfinite(cur_prior.hi) && isfinite(cur_S.hi));
+                structure_move<RNG>(r, ws.ops[cur], ws.ops[cur ^ 1], cur_invalid, p, lane);
                 pbuf = cur ^ 1;
                 need_compile = true;
                 GPR_PH(GPR_PH_STRUCT);
@@ -1360,10 +1414,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                 /* ---- constant move (main.cu:743-806) ---- */
                 df fws, bws;
                 constant_move<RNG>(r, ws, ws.Cs[ccur], ws.Cs[ccur ^ 1], fws, bws, p, ljump, lane, rw_sd);
-                if (p.const_mode == 0) {
-                    forward += (double)fws.hi + (double)fws.lo;
-                    backward += (double)bws.hi + (double)bws.lo;
-                }
+                if (p.const_mode == 0) { forward = df_add(forward, fws); backward = df_add(backward, bws); }
                 cbuf = ccur ^ 1;
                 need_cauchy = true;
                 GPR_PH(GPR_PH_CONST);
@@ -1378,13 +1429,13 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                 __syncwarp();
                 GPR_PH(GPR_PH_COMPILE);
             }
-            if (need_cauchy) { cs = cauchy_sum64(ws.Cs[cbuf], p, lane); GPR_PH(GPR_PH_CAUCHY); }
-            if (structural) backward = -(double)p.logcount[count];
+            if (need_cauchy) { cs = cauchy_sum_u(ws.Cs[cbuf], p, lane); GPR_PH(GPR_PH_CAUCHY); }
+            if (structural) backward = df_make(-p.logcount[count], 0.0f);
             build_eval_program(ws.prog[pbuf], ws.Cs[cbuf], ninstr, ws.eprog, lane);
             __syncwarp();
             GPR_PH(GPR_PH_EPROG);
           }
-          double lik = 0.0;
+          df S = df_make(0.0f, 0.0f);
           int pts = 0;
           if (balanced) {
             if (lane == 0) {
@@ -1438,16 +1489,14 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
             GPR_PH(GPR_PH_BAR2);
             if (active) {
                 if (s_bad[warp]) {
-                    lik = -INFINITY;
+                    S = lik_invalid();
                 } else {
-                    double S = 0.0;
-                    for (int c = 0; c < nch; ++c) S += (double)s_part[warp][c];
-                    lik = finish_loglik(S, dv, p);
+                    for (int c = 0; c < nch; ++c) S = df_add(S, df_make(s_part[warp][c], 0.0f));
                 }
             }
             GPR_PH(GPR_PH_COMBINE);
           } else if (active) {
-            lik = eval_loglik64<K, ONEPASS, ROLLED, NV, STREAM>(ws.eprog, ws.stk, ws.scr, ld, dv, p, lane, pts);
+            S = eval_loglik_S<K, ONEPASS, ROLLED, NV, STREAM>(ws.eprog, ws.stk, ws.scr, ld, dv, p, lane, pts);
             st_np += (unsigned long long)(count + 4) * (unsigned)pts;
             GPR_PH_COUNT(GPR_PH_NPASSES, npass);
             GPR_PH_COUNT(GPR_PH_NINSTR, (unsigned long long)ninstr * npass);
@@ -1455,23 +1504,22 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
           }
           st_pts += (unsigned)pts;
           if (active) {
-            const double prior = prior64(len, cs, p);
-            const double post = prior + lik;
+            const df prior = prior_u(len, cs, p);
             st_evals++; st_nodes += (unsigned)count;
             bool accept = true;
             if (!init) {
+                float prob;
+                accept = mh_accept_u<RNG>(prior, S, cur_prior, cur_S, backward, forward, r, p, &prob);
                 if (!structural && p.adapt_target > 0.0f && p.const_mode == 1) {
-                    log_sd = rm_update(log_sd, accept_prob64(post, cur_post, backward, forward), p.adapt_target,
-                                       n_cmoves++);
+                    log_sd = rm_update(log_sd, prob, p.adapt_target, n_cmoves++);
                     rw_sd = expf(log_sd);
                 }
-                accept = mh_accept64<RNG>(post, cur_post, backward, forward, r, p);
                 if (structural) { st_sp++; st_sa += accept; } else { st_cp++; st_ca += accept; }
             }
             if (accept) {
                 cur = pbuf; ccur = cbuf;
                 cur_len = len; cur_count = count; cur_ninstr = ninstr; cur_cs = cs;
-                cur_prior = prior; cur_lik = lik; cur_post = post;
+                cur_prior = prior; cur_S = S;
             }
             __syncwarp();
             if (p.trace && !init && lane < p.trace_n)
@@ -1488,8 +1536,8 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
             p.C[(size_t)i * p.N + chain] = ws.Cs[ccur][i];
         }
         if (active && lane == 0) {
-            p.prior[chain] = cur_prior;
-            p.lik[chain] = cur_lik;
+            p.prior[chain] = (double)cur_prior.hi + (double)cur_prior.lo;
+            p.lik[chain] = lik_of(cur_S, dv, p);
             if (p.chain_scale && p.adapt_target > 0.0f && p.const_mode == 1) p.chain_scale[chain] = rw_sd;
         }
         if (lane == 0 && p.stats) {

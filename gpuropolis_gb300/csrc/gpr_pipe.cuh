@@ -32,19 +32,20 @@ namespace gpr {
 /* Most tasks one chain's evaluation is split into. */
 #define GPR_PIPE_TASKS 32
 
-/* A chain's state between its warp's turns (shared memory). */
+/* A chain's state between its warp's turns (shared memory; a turn reads the
+ * fields into registers and lane 0 writes them back). */
 struct PipeSlot {
-    double cur_prior, cur_lik, cur_post, cur_cs;  /* the current state's scores             */
-    double prior, cs, fw, bw;     /* the proposal in flight: prior, Cauchy sum; the
-                                   * forward/backward terms (main.cu:702,723,761-775)       */
-    int chain;                    /* >= p.N: no chain in this slot                          */
-    int cur, ccur, pbuf, cbuf;    /* ops/program and constants buffers: current, proposal   */
+    df cur_prior, cur_S, cur_cs;  /* the current state: prior, likelihood sum (scale 2^-e), Cauchy sum */
+    df prior, cs;                 /* the proposal in flight: prior, Cauchy sum                           */
+    df fw, bw;                    /* forward/backward terms (main.cu:702,723,761-775)                    */
+    int chain;                    /* >= p.N: no chain in this slot                                       */
+    int cur, ccur, pbuf, cbuf;    /* ops/program and constants buffers: current, proposal                */
     int ninstr, count, cur_ninstr, cur_count;
     float len, cur_len;
-    uint32_t rs, rblk, rw0, rw1, rw2, rw3;   /* the chain's random stream              */
-    float rw_sd, log_sd;          /* random-walk scale and its adaptation state            */
+    uint32_t rs, rblk, rw0, rw1, rw2, rw3;   /* the chain's random stream                           */
+    float rw_sd, log_sd;          /* random-walk scale and its adaptation state                         */
     int n_cmoves;
-    int structural;               /* the proposal in flight is a structure move             */
+    int structural;               /* the proposal in flight is a structure move                          */
 };
 
 /* Per-warp dynamic shared memory: per slot the op, constant and program
@@ -193,134 +194,148 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_pipe_kernel(const __grid
 
             /* ---- this warp's turn on its group-g chain ---- */
             {
-                PipeSlot S = s_slot[g][warp];
+                PipeSlot& SS = s_slot[g][warp];
+                const int chain = SS.chain;
                 const int step = (h - g) / 2 - 1;   /* the step proposed now: -1 the loaded state */
                 const WarpSmem wg = carve_pipe<K>(mybase, PL, p.max_instr, p.levels, g);
                 int publish = -1;
-                if (S.chain < p.N && step <= p.steps) {
+                int pbuf = 0, cbuf = 0, count = 0;
+                if (chain < p.N) {
+                    /* the chain's state, into registers */
+                    df cur_prior = SS.cur_prior, cur_S = SS.cur_S, cur_cs = SS.cur_cs;
+                    df prior = SS.prior, cs = SS.cs, fw = SS.fw, bw = SS.bw;
+                    int cur = SS.cur, ccur = SS.ccur;
+                    pbuf = SS.pbuf; cbuf = SS.cbuf;
+                    int ninstr = SS.ninstr, cur_ninstr = SS.cur_ninstr, cur_count = SS.cur_count;
+                    count = SS.count;
+                    float len = SS.len, cur_len = SS.cur_len;
+                    float rw_sd = SS.rw_sd, log_sd = SS.log_sd;
+                    int n_cmoves = SS.n_cmoves;
+                    bool structural = SS.structural != 0;
                     Rng r;
-                    r.key0 = p.seed; r.key1 = (uint32_t)S.chain; r.drawn = 0;
-                    r.s = S.rs; r.blk = S.rblk; r.w0 = S.rw0; r.w1 = S.rw1; r.w2 = S.rw2; r.w3 = S.rw3;
+                    r.key0 = p.seed; r.key1 = (uint32_t)chain; r.drawn = 0;
+                    r.s = SS.rs; r.blk = SS.rblk; r.w0 = SS.rw0; r.w1 = SS.rw1; r.w2 = SS.rw2; r.w3 = SS.rw3;
                     if (step >= 0) {
                         /* the accept rule for the proposal of step - 1 (the loaded state when step == 0) */
                         const bool init = step == 0;
-                        double lik;
+                        df S;
                         if (s_bad[g][warp]) {
-                            lik = -INFINITY;
+                            S = lik_invalid();
                         } else {
                             const float* pr = part_row(g, warp);
-                            double Sx = 0.0;
-                            for (int c = 0; c < nch; ++c) Sx += (double)pr[c];
-                            lik = finish_loglik(Sx, dv, p);
+                            S = df_make(0.0f, 0.0f);
+                            for (int c = 0; c < nch; ++c) S = df_add(S, df_make(pr[c], 0.0f));
                         }
                         GPR_PH(GPR_PH_COMBINE);
-                        const double post = S.prior + lik;
                         bool accept = true;
                         if (!init) {
-                            if (!S.structural && p.adapt_target > 0.0f && p.const_mode == 1) {
-                                S.log_sd = rm_update(S.log_sd, accept_prob64(post, S.cur_post, S.bw, S.fw),
-                                                     p.adapt_target, S.n_cmoves++);
-                                S.rw_sd = expf(S.log_sd);
+                            float prob;
+                            accept = mh_accept_u<RNG>(prior, S, cur_prior, cur_S, bw, fw, r, p, &prob);
+                            if (!structural && p.adapt_target > 0.0f && p.const_mode == 1) {
+                                log_sd = rm_update(log_sd, prob, p.adapt_target, n_cmoves++);
+                                rw_sd = expf(log_sd);
                             }
-                            accept = mh_accept64<RNG>(post, S.cur_post, S.bw, S.fw, r, p);
-                            if (S.structural) { st_sp++; st_sa += accept; } else { st_cp++; st_ca += accept; }
+                            if (structural) { st_sp++; st_sa += accept; } else { st_cp++; st_ca += accept; }
                         }
-                        st_evals++; st_nodes += (unsigned)S.count;
+                        st_evals++; st_nodes += (unsigned)count;
                         if (accept) {
-                            S.cur = S.pbuf; S.ccur = S.cbuf;
-                            S.cur_len = S.len; S.cur_count = S.count; S.cur_ninstr = S.ninstr; S.cur_cs = S.cs;
-                            S.cur_prior = S.prior; S.cur_lik = lik; S.cur_post = post;
+                            cur = pbuf; ccur = cbuf;
+                            cur_len = len; cur_count = count; cur_ninstr = ninstr; cur_cs = cs;
+                            cur_prior = prior; cur_S = S;
                         }
                         if (p.trace && !init && lane < p.trace_n)
-                            p.trace[((size_t)S.chain * p.steps + (step - 1)) * p.trace_n + lane] = wg.Cs[S.ccur][lane];
+                            p.trace[((size_t)chain * p.steps + (step - 1)) * p.trace_n + lane] = wg.Cs[ccur][lane];
                         GPR_PH(GPR_PH_ACCEPT);
                     }
                     if (step < 0) {
                         /* load the chain (reference layout, main.cu:683-685) */
                         for (int i = lane; i < PL; i += 32) {
-                            const int o = p.P[(size_t)i * p.N + S.chain];
+                            const int o = p.P[(size_t)i * p.N + chain];
                             wg.ops[0][i] = (uint8_t)((o >= 0 && o < OP_NALL) ? o : 255);
-                            wg.Cs[0][i] = p.C[(size_t)i * p.N + S.chain];
+                            wg.Cs[0][i] = p.C[(size_t)i * p.N + chain];
                         }
                         __syncwarp();
-                        r = rng_start<RNG>(p.seed, S.chain);
-                        S.cur = S.ccur = S.pbuf = S.cbuf = 0;
-                        S.cur_ninstr = S.cur_count = 0; S.cur_len = 0.0f;
-                        S.cur_prior = S.cur_lik = S.cur_post = S.cur_cs = 0.0;
-                        S.fw = S.bw = 0.0;
-                        S.rw_sd = p.chain_scale ? p.chain_scale[S.chain] : p.rw_sd;
-                        S.log_sd = logf(S.rw_sd);
-                        S.n_cmoves = 0;
-                        S.structural = 0;
+                        r = rng_start<RNG>(p.seed, chain);
+                        cur = ccur = pbuf = cbuf = 0;
+                        cur_ninstr = cur_count = 0; cur_len = 0.0f;
+                        cur_prior = cur_S = cur_cs = df_make(0.0f, 0.0f);
+                        fw = bw = df_make(0.0f, 0.0f);
+                        rw_sd = p.chain_scale ? p.chain_scale[chain] : p.rw_sd;
+                        log_sd = logf(rw_sd);
+                        n_cmoves = 0;
                         GPR_PH(GPR_PH_LOAD);
                     }
                     if (step < p.steps) {
                         const bool init = step < 0;
-                        const bool structural = !init && p.struct_every > 0 && (step % p.struct_every == 0);
+                        structural = !init && p.struct_every > 0 && (step % p.struct_every == 0);
                         bool need_compile = init;
                         if (structural) {
                             /* ---- structure move (main.cu:699-742) ---- */
-                            S.fw = -(double)p.logcount[S.cur_count];
-                            structure_move<RNG>(r, wg.ops[S.cur], wg.ops[S.cur ^ 1], !isfinite(S.cur_post), p, lane);
-                            S.pbuf = S.cur ^ 1; S.cbuf = S.ccur;
+                            fw = df_make(-p.logcount[cur_count], 0.0f);
+                            const bool cur_invalid = !(isfinite(cur_prior.hi) && isfinite(cur_S.hi));
+                            structure_move<RNG>(r, wg.ops[cur], wg.ops[cur ^ 1], cur_invalid, p, lane);
+                            pbuf = cur ^ 1; cbuf = ccur;
                             need_compile = true;
                             GPR_PH(GPR_PH_STRUCT);
                         } else if (!init) {
                             /* ---- constant move (main.cu:743-806) ---- */
                             df fws, bws;
-                            constant_move<RNG>(r, wg, wg.Cs[S.ccur], wg.Cs[S.ccur ^ 1], fws, bws, p, ljump, lane,
-                                               S.rw_sd);
-                            if (p.const_mode == 0) {
-                                S.fw += (double)fws.hi + (double)fws.lo;
-                                S.bw += (double)bws.hi + (double)bws.lo;
-                            }
-                            S.pbuf = S.cur; S.cbuf = S.ccur ^ 1;
-                            S.len = S.cur_len; S.count = S.cur_count; S.ninstr = S.cur_ninstr;
+                            constant_move<RNG>(r, wg, wg.Cs[ccur], wg.Cs[ccur ^ 1], fws, bws, p, ljump, lane, rw_sd);
+                            if (p.const_mode == 0) { fw = df_add(fw, fws); bw = df_add(bw, bws); }
+                            pbuf = cur; cbuf = ccur ^ 1;
+                            len = cur_len; count = cur_count; ninstr = cur_ninstr;
                             GPR_PH(GPR_PH_CONST);
                         }
                         __syncwarp();
                         if (need_compile) {
-                            const CompileOut co = compile_parallel<NV>(wg.ops[S.pbuf], PL, wg.prog[S.pbuf],
+                            const CompileOut co = compile_parallel<NV>(wg.ops[pbuf], PL, wg.prog[pbuf],
                                                                    compile_scratch(wg.stk, PL), lane);
-                            S.len = co.length; S.count = co.count; S.ninstr = co.ninstr;
+                            len = co.length; count = co.count; ninstr = co.ninstr;
                             __syncwarp();
                             GPR_PH(GPR_PH_COMPILE);
                         }
                         if (structural) {
-                            S.bw = -(double)p.logcount[S.count];
-                            S.cs = S.cur_cs;
+                            bw = df_make(-p.logcount[count], 0.0f);
+                            cs = cur_cs;
                         } else {
-                            S.cs = cauchy_sum64(wg.Cs[S.cbuf], p, lane);
+                            cs = cauchy_sum_u(wg.Cs[cbuf], p, lane);
                             GPR_PH(GPR_PH_CAUCHY);
                         }
-                        S.prior = prior64(S.len, S.cs, p);
-                        S.structural = structural;
-                        publish = S.ninstr;
+                        prior = prior_u(len, cs, p);
+                        publish = ninstr;
                     } else {
                         /* write back (main.cu:811-812 and the in-place P, C) */
                         for (int i = lane; i < PL; i += 32) {
-                            const uint8_t o = wg.ops[S.cur][i];
-                            if (o != 255) p.P[(size_t)i * p.N + S.chain] = (int32_t)o;
-                            p.C[(size_t)i * p.N + S.chain] = wg.Cs[S.ccur][i];
+                            const uint8_t o = wg.ops[cur][i];
+                            if (o != 255) p.P[(size_t)i * p.N + chain] = (int32_t)o;
+                            p.C[(size_t)i * p.N + chain] = wg.Cs[ccur][i];
                         }
                         if (lane == 0) {
-                            p.prior[S.chain] = S.cur_prior;
-                            p.lik[S.chain] = S.cur_lik;
-                            if (p.chain_scale && p.adapt_target > 0.0f && p.const_mode == 1)
-                                p.chain_scale[S.chain] = S.rw_sd;
+                            p.prior[chain] = (double)cur_prior.hi + (double)cur_prior.lo;
+                            p.lik[chain] = lik_of(cur_S, dv, p);
+                            if (p.chain_scale && p.adapt_target > 0.0f && p.const_mode == 1) p.chain_scale[chain] = rw_sd;
                         }
                         GPR_PH(GPR_PH_STORE);
                     }
-                    S.rs = r.s; S.rblk = r.blk; S.rw0 = r.w0; S.rw1 = r.w1; S.rw2 = r.w2; S.rw3 = r.w3;
+                    __syncwarp();
+                    if (lane == 0) {
+                        SS.cur_prior = cur_prior; SS.cur_S = cur_S; SS.cur_cs = cur_cs;
+                        SS.prior = prior; SS.cs = cs; SS.fw = fw; SS.bw = bw;
+                        SS.cur = cur; SS.ccur = ccur; SS.pbuf = pbuf; SS.cbuf = cbuf;
+                        SS.ninstr = ninstr; SS.count = count; SS.cur_ninstr = cur_ninstr; SS.cur_count = cur_count;
+                        SS.len = len; SS.cur_len = cur_len;
+                        SS.rs = r.s; SS.rblk = r.blk; SS.rw0 = r.w0; SS.rw1 = r.w1; SS.rw2 = r.w2; SS.rw3 = r.w3;
+                        SS.rw_sd = rw_sd; SS.log_sd = log_sd; SS.n_cmoves = n_cmoves;
+                        SS.structural = structural ? 1 : 0;
+                    }
                 }
                 __syncwarp();
                 if (lane == 0) {
-                    s_slot[g][warp] = S;
                     s_cost[g][warp] = publish;
-                    s_cnt[g][warp] = S.count;
+                    s_cnt[g][warp] = count;
                     s_bad[g][warp] = 0;
-                    s_pp[g][warp] = wg.prog[S.pbuf & 1];
-                    s_pc[g][warp] = wg.Cs[S.cbuf & 1];
+                    s_pp[g][warp] = wg.prog[pbuf & 1];
+                    s_pc[g][warp] = wg.Cs[cbuf & 1];
                 }
                 __syncwarp();
             }

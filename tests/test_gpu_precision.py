@@ -3,16 +3,21 @@
 The evaluation is FP32; the likelihood's per-point terms (f - y)^2 w are
 summed in FP32 within a 128-point chunk (four fused multiply-adds per lane,
 then a five-level butterfly: at most nine roundings, every term >= 0, so the
-chunk sum is within 9 u = 9 * 2^-24 of its exact value, relatively) and the
-chunk sums are added in FP64 in chunk order; the weight w = 2^-e/(2 sd^2) is
-the float nearest to the exact one (one more u).  So against the reference's
-double sum of the same FP32 residuals (main.cu:454-468) the quadratic part of
-the likelihood is within 10 u = 6.0e-7 relative, whatever the number of
-points.  Prior, posterior and the acceptance ratio
-((proposal - current) + backward) - forward (main.cu:728, 790) are FP64, so the
-ratio inherits only the two likelihoods' errors.  The weight's scale 2^-e is
-chosen from the data so that no chunk sum can overflow: posteriors are valid
-over the reference's whole range (there is no floor at -6e57)."""
+chunk sum is within 9 u = 9 * 2^-24 of its exact value, relatively); the
+chunk sums are added as double-floats in chunk order (error about 2^-47 of
+the running sum per chunk: 4e-12 relative at 512 chunks); the weight
+w = 2^-e/(2 sd^2) is the float nearest to the exact one (one more u).  So
+against the reference's double sum of the same FP32 residuals
+(main.cu:454-468) the quadratic part of the likelihood is within 10 u = 6.0e-7
+relative, whatever the number of points.  The prior and the acceptance ratio
+((proposal - current) + backward) - forward (main.cu:728, 790) are
+double-floats formed from the prior difference and the difference of the two
+likelihood sums (the normalising sum cancels), so the ratio carries the two
+likelihoods' 10 u each and nothing measurable besides; FP64 -- on GB300 one
+warp-wide FP64 add costs about 64 FP32 adds of issue time -- is used only
+when a block writes its scores.  The weight's scale 2^-e is chosen from the
+data so that no sum can overflow: posteriors are valid over the reference's
+whole range (there is no floor at -6e57)."""
 import numpy as np
 import pytest
 
