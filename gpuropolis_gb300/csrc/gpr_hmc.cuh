@@ -451,6 +451,7 @@ __global__ void __launch_bounds__(128) mh_hmc_kernel(const __grid_constant__ KPa
     const bool adapt = p.chain_scale && p.adapt_target > 0.0f;
     const uint32_t seed = p.seed;
     const float unscale = (float)GPR_DF_UNSCALE;
+    const LaneJump ljump = make_lane_jump(p, lane);
 
 #pragma unroll 1
     for (;;) {
@@ -498,7 +499,7 @@ __global__ void __launch_bounds__(128) mh_hmc_kernel(const __grid_constant__ KPa
                 df forward = df_make(0.f, 0.f);
                 if (!init) {
                     forward = df_make(__fmul_rn(-p.logcount[cur_count], GPR_DF_SCALE), 0.0f);
-                    structure_move<RNG>(r, ws.ops[cur], ws.ops[cur ^ 1], df_invalid(cur_post), p, lane);
+                    structure_move<RNG>(r, ws.ops[cur], ws.ops[cur ^ 1], df_invalid(cur_post), p, ljump, lane);
                     pbuf = cur ^ 1;
                 }
                 __syncwarp();

@@ -639,26 +639,30 @@ __host__ __device__ __forceinline__ size_t shared_region_bytes(int PL, int level
     return align16(m);
 }
 
-__host__ __device__ __forceinline__ size_t warp_smem_bytes(int PL, int max_instr, int levels, int K) {
+/* eprog: with an evaluation program of (instruction, constant) pairs; the MH
+ * kernels interpret program and constants in place and have none. */
+__host__ __device__ __forceinline__ size_t warp_smem_bytes(int PL, int max_instr, int levels, int K,
+                                                           bool eprog = true) {
     size_t plp = align16((size_t)PL);
     size_t b = 0;
     b += 2 * plp;                                /* ops */
     b += align16(2 * plp * 4);                   /* Cs */
     b += align16(2 * (size_t)max_instr * 4);     /* prog */
-    b += align16((size_t)max_instr * 8);         /* eprog */
+    if (eprog) b += align16((size_t)max_instr * 8);   /* eprog */
     b += shared_region_bytes(PL, levels, K);     /* stack + scratch | constant-move records */
     return align16(b);
 }
 
 template <int K>
-__device__ __forceinline__ WarpSmem carve_warp(uint8_t* base, int PL, int max_instr, int levels) {
+__device__ __forceinline__ WarpSmem carve_warp(uint8_t* base, int PL, int max_instr, int levels, bool eprog = true) {
     WarpSmem w;
     size_t plp = align16((size_t)PL);
     uint8_t* p = base;
     w.ops[0] = p; w.ops[1] = p + plp; p += 2 * plp;
     w.Cs[0] = (float*)p; w.Cs[1] = (float*)p + plp; p += align16(2 * plp * 4);
     w.prog[0] = (uint32_t*)p; w.prog[1] = (uint32_t*)p + max_instr; p += align16(2 * (size_t)max_instr * 4);
-    w.eprog = (uint2*)p; p += align16((size_t)max_instr * 8);
+    w.eprog = nullptr;
+    if (eprog) { w.eprog = (uint2*)p; p += align16((size_t)max_instr * 8); }
     w.stk = (float*)p;
     w.scr = w.stk + (size_t)levels * K * 32;
     w.off = (int*)p;
@@ -981,6 +985,7 @@ __device__ __forceinline__ void propose_constant(Rng& r, float old, float& nc, f
 struct LaneJump {
     uint32_t a, c;     /* state -> state after nominal*lane draws        */
     uint32_t sa, sc;   /* state -> state after nominal*32 draws          */
+    uint32_t da, dc;   /* state -> state after lane+1 draws              */
 };
 
 __device__ __forceinline__ void affine_power(uint32_t k, const KParams& p, uint32_t& A, uint32_t& C) {
@@ -995,6 +1000,7 @@ __device__ __forceinline__ LaneJump make_lane_jump(const KParams& p, int lane) {
     LaneJump j;
     affine_power(nominal * (uint32_t)lane, p, j.a, j.c);
     affine_power(nominal * 32u, p, j.sa, j.sc);
+    affine_power((uint32_t)lane + 1u, p, j.da, j.dc);
     return j;
 }
 
@@ -1006,6 +1012,9 @@ __device__ void constant_move(Rng& r, const WarpSmem& w, const float* Cold, floa
     const int nominal = (p.const_mode == 0) ? 4 : 3;
     /* first pass: every constant at its nominal offset, streams positioned by
      * one affine map each (LCG) or a counter offset (Philox) */
+    /* the LCG state after the last constant's draws: the stream's state once
+     * the offsets have converged */
+    uint32_t endst = 0u;
     {
         uint32_t st = (lj.a * r.s + lj.c) & 0x7fffffffu;
 #pragma unroll 1
@@ -1018,6 +1027,7 @@ __device__ void constant_move(Rng& r, const WarpSmem& w, const float* Cold, floa
             propose_constant<RNG>(rc, Cold[c], nc, dfw, dbw, p, rw_sd);
             Cnew[c] = nc; w.fw[c] = dfw; w.bw[c] = dbw; w.ndr[c] = (int)rc.drawn;
             w.off[c] = nominal * c;
+            if (c == PL - 1) endst = rc.s;
             st = (lj.sa * st + lj.sc) & 0x7fffffffu;
         }
     }
@@ -1035,6 +1045,7 @@ __device__ void constant_move(Rng& r, const WarpSmem& w, const float* Cold, floa
             float nc, dfw, dbw;
             propose_constant<RNG>(rc, Cold[c], nc, dfw, dbw, p, rw_sd);
             Cnew[c] = nc; w.fw[c] = dfw; w.bw[c] = dbw; w.ndr[c] = (int)rc.drawn;
+            if (c == PL - 1) endst = rc.s;
         }
         __syncwarp();
         /* exclusive prefix sum of draw counts, 32 constants at a time */
@@ -1056,7 +1067,8 @@ __device__ void constant_move(Rng& r, const WarpSmem& w, const float* Cold, floa
         }
         __syncwarp();
         if (!__any_sync(FULLMASK, changed)) {
-            rng_jump<RNG>(r, (uint32_t)base, p);
+            if (RNG == 0) r.s = __shfl_sync(FULLMASK, endst, (PL - 1) & 31);
+            else rng_jump<RNG>(r, (uint32_t)base, p);
             converged = true;
         }
     }
@@ -1192,30 +1204,77 @@ __device__ __forceinline__ float rm_update(float log_s, float alpha, float targe
     return fminf(fmaxf(__fadd_rn(log_s, __fmul_rn(gain, __fsub_rn(alpha, target))), -30.0f), 10.0f);
 }
 
+/* The value of Philox draw number ctr of a chain's stream (rng_next). */
+__device__ __forceinline__ uint32_t philox_draw(uint32_t key0, uint32_t key1, uint32_t ctr) {
+    uint32_t c[4] = {ctr >> 2, 0u, 0u, 0u};
+    gpr_philox4x32_10(c, key0, key1);
+    const uint32_t i = ctr & 3u;
+    const uint32_t v = (i == 0) ? c[0] : (i == 1) ? c[1] : (i == 2) ? c[2] : c[3];
+    return v >> 1;
+}
+
 /* Structure proposal (main.cu:699-742): a node n uniform in [0, PL) -- the
  * root when the current state is invalid -- and every node of its subtree
- * redrawn from the op set, in heap order level by level.  opn receives the
- * proposal, a copy of oc with that subtree replaced. */
+ * redrawn from the op set in increasing heap order (is_descendant,
+ * main.cu:660-677, 711-720), each a random_int(NOPS) with its rejection
+ * loop (main.cu:218-228).  The draws are made 32 stream positions at a time,
+ * one per lane (the LCG jumped by per-lane affine maps, Philox by counter);
+ * the accepted ones, ranked by a ballot, go to the subtree's nodes in order,
+ * and the stream is left after the draw that filled the last node -- the
+ * sequence of values and the stream position a one-draw-at-a-time loop gives.
+ * opn receives the proposal, a copy of oc with that subtree replaced. */
 template <int RNG>
 __device__ __forceinline__ void structure_move(Rng& r, const uint8_t* oc, uint8_t* opn, bool cur_invalid,
-                                               const KParams& p, int lane) {
+                                               const KParams& p, const LaneJump& lj, int lane) {
     const int PL = p.PL;
     const int n = cur_invalid ? 0 : random_int<RNG>(r, PL, p.mag_pl);
 #pragma unroll 1
     for (int i = lane; i < PL; i += 32) opn[i] = oc[i];
     __syncwarp();
-    const int m = n + 1;
+    const int m = n + 1;                          /* subtree root, 1-based */
+    int T = 0;                                    /* nodes in the subtree  */
 #pragma unroll 1
-    for (int d = 0;; ++d) {
-        const int lo = m << d;
-        if (lo > PL) break;
-        const int hi = min(lo + (1 << d) - 1, PL);
+    for (int d = 0; (m << d) <= PL; ++d) T += min((m << d) + (1 << d) - 1, PL) - (m << d) + 1;
+    const uint32_t lt = (1u << lane) - 1u;
+    uint32_t s = r.s;          /* LCG: the state before this round; Philox: the counter of its first draw */
+    uint32_t consumed = 0u;
+    int filled = 0;
 #pragma unroll 1
-        for (int j = lo; j <= hi; ++j) {
-            const int k = random_int<RNG>(r, p.nops, p.mag_nops);
-            if (lane == 0) opn[j - 1] = (uint8_t)p.opmap[k];
+    while (filled < T) {
+        const uint32_t x = (RNG == 0) ? ((lj.da * s + lj.dc) & 0x7fffffffu) : philox_draw(r.key0, r.key1, s + lane);
+        const uint32_t v = magic_div(x, p.mag_nops);
+        const bool ok = v < (uint32_t)p.nops;
+        const uint32_t bal = __ballot_sync(FULLMASK, ok);
+        const int rank = filled + __popc(bal & lt);
+        if (ok && rank < T) {
+            int t = rank, idx = m;
+#pragma unroll 1
+            for (int d = 0;; ++d) {
+                const int lo = m << d;
+                const int cnt = min(lo + (1 << d) - 1, PL) - lo + 1;
+                if (t < cnt) { idx = lo + t; break; }
+                t -= cnt;
+            }
+            opn[idx - 1] = (uint8_t)p.opmap[v];
+        }
+        const int got = __popc(bal);
+        if (filled + got >= T) {
+            /* the lane that drew the subtree's last node */
+            const uint32_t hit = __ballot_sync(FULLMASK, ok && rank == T - 1);
+            const int last = __ffs(hit) - 1;
+            consumed += (uint32_t)last + 1u;
+            if (RNG == 0) s = __shfl_sync(FULLMASK, x, last);
+            filled = T;
+        } else {
+            consumed += 32u;
+            if (RNG == 0) s = (p.lcgA[5] * s + p.lcgC[5]) & 0x7fffffffu;   /* 2^5 = 32 draws */
+            else s += 32u;
+            filled += got;
         }
     }
+    if (RNG == 0) r.s = s;
+    else r.s += consumed;
+    r.drawn += consumed;
 }
 
 /* Resident CTAs (of 8 warps) per SM the register allocation is sized for. */
@@ -1287,8 +1346,8 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
         wbase += align16((size_t)data_arrays(p) * p.nd_pad * 4);
         if (!batched) stage_dataset(fx, bar, p, dv);
     }
-    const size_t wbytes = warp_smem_bytes(p.PL, p.max_instr, p.levels, K);
-    const WarpSmem ws = carve_warp<K>(wbase + (size_t)warp * wbytes, p.PL, p.max_instr, p.levels);
+    const size_t wbytes = warp_smem_bytes(p.PL, p.max_instr, p.levels, K, false);
+    const WarpSmem ws = carve_warp<K>(wbase + (size_t)warp * wbytes, p.PL, p.max_instr, p.levels, false);
 
     LaneData<K> ld;
     if (ONEPASS) {
@@ -1309,15 +1368,17 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
     /* CTA-balanced evaluation (lockstep == 1): each warp publishes its chain's
      * program; all warps then pull (chain, pass) tasks, longest programs
      * first, and leave the chunk sums of each pass here. */
-    __shared__ const uint2* s_prog[8];
+    __shared__ const uint32_t* s_pp[8];   /* the published program ...   */
+    __shared__ const float* s_pc[8];      /* ... and its constants       */
     __shared__ int s_cost[8];
     __shared__ int s_count[8];
     __shared__ int s_bad[8];
     __shared__ int s_next;
-    __shared__ float s_part[8][2 * GPR_MAX_PASSES];
+    __shared__ float s_part[8][GPR_MAX_PASSES * (K / 4)];
     int npass = ONEPASS ? 1 : (dv.nd + 32 * K - 1) / (32 * K);
     int nch = chunk_count(dv.nd);
     bool balanced = p.lockstep == 1 && npass <= GPR_MAX_PASSES;
+    float inv_npass = __frcp_rn((float)max(npass, 1));
     GPR_PH(GPR_PH_CLAIM);
 
 #pragma unroll 1
@@ -1348,6 +1409,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                     npass = (dv.nd + 32 * K - 1) / (32 * K);
                     nch = chunk_count(dv.nd);
                     balanced = p.lockstep == 1 && npass <= GPR_MAX_PASSES;
+                    inv_npass = __frcp_rn((float)max(npass, 1));
                 }
             }
         } else {
@@ -1406,7 +1468,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                 /* ---- structure move (main.cu:699-742) ---- */
                 forward = df_make(-p.logcount[cur_count], 0.0f);
                 const bool cur_invalid = !(isfinite(cur_prior.hi) && isfinite(cur_S.hi));
-                structure_move<RNG>(r, ws.ops[cur], ws.ops[cur ^ 1], cur_invalid, p, lane);
+                structure_move<RNG>(r, ws.ops[cur], ws.ops[cur ^ 1], cur_invalid, p, ljump, lane);
                 pbuf = cur ^ 1;
                 need_compile = true;
                 GPR_PH(GPR_PH_STRUCT);
@@ -1431,15 +1493,14 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
             }
             if (need_cauchy) { cs = cauchy_sum_u(ws.Cs[cbuf], p, lane); GPR_PH(GPR_PH_CAUCHY); }
             if (structural) backward = df_make(-p.logcount[count], 0.0f);
-            build_eval_program(ws.prog[pbuf], ws.Cs[cbuf], ninstr, ws.eprog, lane);
             __syncwarp();
-            GPR_PH(GPR_PH_EPROG);
           }
           df S = df_make(0.0f, 0.0f);
           int pts = 0;
           if (balanced) {
             if (lane == 0) {
-                s_prog[warp] = ws.eprog;
+                s_pp[warp] = ws.prog[pbuf];
+                s_pc[warp] = ws.Cs[cbuf];
                 s_cost[warp] = active ? ninstr : -1;
                 s_count[warp] = count;
                 s_bad[warp] = 0;
@@ -1467,11 +1528,13 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                 if (lane == 0) t = atomicAdd(&s_next, 1);
                 t = __shfl_sync(FULLMASK, t, 0);
                 if (t >= ntasks) break;
-                const int q = t / npass, pass = t - q * npass;
+                /* task t: pass t mod npass of the chain of rank t / npass (exact for t < 2^16) */
+                const int q = (int)__fmul_rz(__int2float_rn(t) + 0.5f, inv_npass), pass = t - q * npass;
                 const int w = __ffs(__ballot_sync(FULLMASK, my_rank == q)) - 1;
                 if (s_bad[w]) continue;
                 float csum[K / 4];
-                const bool anybad = eval_pass_chunks<K, ONEPASS, ROLLED, NV, STREAM>(s_prog[w], ws.stk, ws.scr, ld,
+                const PCProg prog = {s_pp[w], s_pc[w]};
+                const bool anybad = eval_pass_chunks<K, ONEPASS, ROLLED, NV, STREAM>(prog, ws.stk, ws.scr, ld,
                                                                                    dv, p, lane, pass, csum);
                 const int np = ONEPASS ? dv.nd : min(32 * K, dv.nd - pass * 32 * K);
                 pts += np;
@@ -1496,7 +1559,8 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
             }
             GPR_PH(GPR_PH_COMBINE);
           } else if (active) {
-            S = eval_loglik_S<K, ONEPASS, ROLLED, NV, STREAM>(ws.eprog, ws.stk, ws.scr, ld, dv, p, lane, pts);
+            const PCProg prog = {ws.prog[pbuf], ws.Cs[cbuf]};
+            S = eval_loglik_S<K, ONEPASS, ROLLED, NV, STREAM>(prog, ws.stk, ws.scr, ld, dv, p, lane, pts);
             st_np += (unsigned long long)(count + 4) * (unsigned)pts;
             GPR_PH_COUNT(GPR_PH_NPASSES, npass);
             GPR_PH_COUNT(GPR_PH_NINSTR, (unsigned long long)ninstr * npass);

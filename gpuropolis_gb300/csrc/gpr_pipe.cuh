@@ -273,7 +273,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_pipe_kernel(const __grid
                             /* ---- structure move (main.cu:699-742) ---- */
                             fw = df_make(-p.logcount[cur_count], 0.0f);
                             const bool cur_invalid = !(isfinite(cur_prior.hi) && isfinite(cur_S.hi));
-                            structure_move<RNG>(r, wg.ops[cur], wg.ops[cur ^ 1], cur_invalid, p, lane);
+                            structure_move<RNG>(r, wg.ops[cur], wg.ops[cur ^ 1], cur_invalid, p, ljump, lane);
                             pbuf = cur ^ 1; cbuf = ccur;
                             need_compile = true;
                             GPR_PH(GPR_PH_STRUCT);
