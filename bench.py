@@ -11,9 +11,18 @@ blocks.  One bench "step" = one block (1000 MH steps of every chain).
 value     : chain-steps/s of the device-resident block loop (kernel time from
             CUDA events on the library's stream, L2 flushed between blocks).
 e2e       : the same through the C ABI with host buffers: each block uploads
-            the state from pinned memory, runs, downloads state and scores,
-            and re-draws chains on the host (the reference's loop,
-            main.cu:1156-1239).
+            the state from pinned memory, runs, re-draws the chains below the
+            MAP-delta cutoff on the device, and downloads state and scores
+            (the reference's loop, main.cu:1156-1239, as the CLI runs it with
+            --device-resample).
+roofline  : the MH kernel against FP32 issue: (reachable nodes + 4) FP32
+            ops per point evaluated over the kernel's time, against 152 SMs x
+            128 lanes x the SM clock; roofline_hbm the same work's 12 bytes
+            per point-eval against the measured HBM copy rate.
+batched / streamed : short runs of the batched uneven workload (256 datasets)
+            and of the large streamed three-variable workload (65,536
+            points, random-walk and Hamiltonian constant moves, batched
+            path), reported beside the headline.
 cpu_baseline / --impl reference : the reference's own per-chain code
             (main.cu:679-813) compiled for the host cores, OpenMP over chains,
             on a bounded sample of the same chains.
@@ -71,6 +80,30 @@ METRIC = "MH chain-steps/s & point-evals/s (1 GB300); ESS/s gradient vs random-w
 # from an ncu capture of that launch (dram__bytes_read.sum + dram__bytes_write.sum), not measured
 # in this run: the chain state read and written once; the dataset lives in shared memory.
 MH_LAUNCH_DRAM_BYTES = 113.43e6
+MH_LAUNCH_DRAM_SOURCE = "ncu capture of one launch (dram__bytes_read.sum + dram__bytes_write.sum), not this run"
+
+
+def config_of(args, w):
+    """The workload keys both arms report (the GPU arm adds its layout elsewhere)."""
+    return {"workload": args.workload, **{k: w[k] for k in ("N", "PL", "nd", "mh_steps", "map_delta")},
+            "ops": w["ops"], "const_proposal": "rw:%g" % w["rw_sd"], "rng": "lcg",
+            "l2": "GPU arm: flushed between blocks (256 MB write); the CPU arm has no GPU cache"}
+
+
+def fp32_roofline(node_points, seconds, nsm, peaks, sm_mhz=None):
+    """Algorithmic FP32 ops ((reachable nodes + 4) per point-eval, a
+    transcendental counting as one) per second against FP32 issue:
+    SMs x 128 lanes x the maximum SM clock (nominal: no measured FP32 peak)."""
+    peak = nsm * 128 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+    achieved = node_points / seconds / 1e12
+    out = {"bound": "fp32-issue", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+           "frac": achieved / peak,
+           "peak_source": "nominal: SMs x 128 FP32 lanes x max SM clock (MEASURED_PEAKS.json has no FP32 figure)",
+           "note": "algorithmic ops = (reachable non-pass-through nodes + 4) per point evaluated; exp, log, pow "
+                   "and division count as one op but cost 10-70 FP32 instructions each"}
+    if sm_mhz:
+        out["frac_at_measured_clock"] = achieved / (nsm * 128 * sm_mhz * 1e6 / 1e12)
+    return out
 
 
 def dataset(w):
@@ -245,12 +278,31 @@ def ess_comparison(g, stream, dev):
         res[name] = arm(s, steps, 3, state, {"leapfrog_steps": L, "eps_median": float(np.median(sc)),
                                              "target": tgt})
         s.close()
-    best = max(res["hmc_L8"]["ess_per_s"], res["hmc_L32"]["ess_per_s"], res["mala"]["ess_per_s"])
+    # the configured move as the workload states it: step 0.01, 8 leapfrog steps, not adapted
+    s = sampler("hmc", eps=0.01, L=8)
+    s.set_state(*state)
+    s.autotune(steps=20, seed=77)
+    dt, _ = timed(s, 20, 5, state)
+    steps = max(30, int(t_rw / (dt / 20)))
+    res["hmc_L8_eps0.01"] = arm(s, steps, 3, state, {"leapfrog_steps": 8, "eps": 0.01, "adapted": False})
+    s.close()
+    arms = ("hmc_L8", "hmc_L32", "mala")
+    best_arm = max(arms, key=lambda a: res[a]["ess_per_s"])
+    rw_ad = res["rw_adapted"]["ess_per_s"]
     return {"workload": "rational-65k", "N": N, "PL": PL, "nd": w["nd"], "constants": 5,
-            "moves": "constants only (no structure moves)", "traced_chains": NT, **res,
-            "ratio_gradient_vs_rw_sd_0.1": best / max(res["rw_sd_0.1"]["ess_per_s"], 1e-300),
-            "ratio_gradient_vs_rw_adapted": best / res["rw_adapted"]["ess_per_s"],
-            "method": "Geyer initial monotone sequence ESS, min over the five constants per chain"}
+            "moves": "constants only (no structure moves)", "traced_chains": NT,
+            "ratio_of_record": {"gradient_vs_adapted_rw": res[best_arm]["ess_per_s"] / rw_ad, "best_arm": best_arm,
+                                "hmc_L8_adapted_vs_adapted_rw": res["hmc_L8"]["ess_per_s"] / rw_ad,
+                                "hmc_L8_configured_vs_adapted_rw": res["hmc_L8_eps0.01"]["ess_per_s"] / rw_ad,
+                                "target": 3.0,
+                                "met": bool(res[best_arm]["ess_per_s"] / rw_ad >= 3.0)},
+            **res,
+            "footnote": {"gradient_vs_rw_sd_0.1": res[best_arm]["ess_per_s"] / max(res["rw_sd_0.1"]["ess_per_s"],
+                                                                                   1e-300),
+                         "note": "the configured sd 0.1 random walk accepts almost no proposal on this posterior; "
+                                 "it is not a baseline worth beating"},
+            "method": "Geyer initial monotone sequence ESS, min over the five constants per chain; every arm "
+                      "runs the adapted random walk's wall time from the same burned-in state"}
 
 
 def run_hmc_profile(args):
@@ -314,14 +366,17 @@ def cpu_runner(w):
         return _PortRunner(w), "port"
 
 
-def run_streamed(args, w):
+def streamed_measure(args, w, steps_timed, warmup):
     """Large streamed data: 16384 chains, PROGRAM_LENGTH 127, 65536 points of
     three input variables (x1, x2, x3 ~ N(0, 1), y = sin(x1) x2 + exp(-x3^2)
     + N(0, 0.05)), op set {+,-,*,/,sin,cos,exp,x1,x2,x3,const}; the dataset is
-    read from device memory in every pass (it cannot be staged per CTA).
-    Random-walk constants (sd 0.1) with the reference's structure moves, then
-    the same chains with Hamiltonian constant moves (8 leapfrog steps).
-    Data bytes per point-eval: 20 (x1, x2, x3, y, w)."""
+    read from device memory (L2) in every pass (it cannot be staged per CTA).
+    Two legs: random-walk constants (sd 0.1) with the reference's structure
+    moves, on a single-dataset handle; then, as the workload specifies, the
+    same chains on the batched path (the dataset behind gpr_set_batched_data,
+    blocks replayed from a captured graph) with Hamiltonian constant moves (8
+    leapfrog steps) beside the structure moves.  Data bytes per point-eval:
+    20 (x1, x2, x3, y, w)."""
     import torch
     import gpuropolis_gb300 as g
     dev = torch.device("cuda", 0)
@@ -330,65 +385,81 @@ def run_streamed(args, w):
     N, PL, nd, steps = w["N"], w["PL"], w["nd"], w["mh_steps"]
     x1, x2, x3, y, sd = H.multivar_data(nd, seed=2024)
     P, C = g.host_init_chains(N, PL, 99, ops=H.OPSET_MULTI)
+    peaks = measured_peaks()
+    nsm = torch.cuda.get_device_properties(dev).multi_processor_count
 
-    def timed(s, seed0):
-        for i in range(args.warmup):
-            s.run_block(steps, seed0 + i)
+    def timed(run, seed0, st_handle):
+        for i in range(warmup):
+            run(seed0 + i)
         torch.cuda.synchronize()
-        s.reset_stats()
+        st_handle.reset_stats()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        for i in range(args.steps):
-            s.run_block(steps, seed0 + 100 + i)
+        for i in range(steps_timed):
+            run(seed0 + 100 + i)
         e1.record(stream)
         torch.cuda.synchronize()
-        return e0.elapsed_time(e1) / 1e3, s.stats()
+        return e0.elapsed_time(e1) / 1e3, st_handle.stats()
+
+    def leg(sec, st, geo):
+        pe = st["eval_points"] / sec
+        return {"chain_steps_per_s": N * steps * steps_timed / sec, "point_evals_per_s": pe,
+                "data_read_gbs": pe * 20 / 1e9,
+                "roofline": fp32_roofline(st["eval_node_points"], sec, nsm, peaks),
+                "roofline_hbm": hbm_roofline(st["eval_points"], sec, peaks, None, nbytes=20),
+                "acceptance": {"structure": st["struct_accepted"] / max(1, st["struct_proposed"]),
+                               "constant": st["const_accepted"] / max(1, st["const_proposed"])},
+                "launch": geo}
 
     s = g.Sampler(N, program_length=PL, ops=H.OPSET_MULTI, n_vars=3, const_proposal=g.CONST_RANDOM_WALK,
                   rw_sd=0.1, stream=stream.cuda_stream)
-    s.set_data3(x1, x2, x3, y, sd)
-    s.set_state(P, C)
-    sec, st = timed(s, 1)
-    geo = s.launch_geometry()
-    Pw, Cw, _, _ = s.get_state()
-    s.close()
-    value = N * steps * args.steps / sec
-    pe = st["eval_points"] / sec
-    peaks = measured_peaks()
-    hbm = peaks.get("hbm_gbs")
+    try:
+        s.set_data3(x1, x2, x3, y, sd)
+        s.set_state(P, C)
+        sec, st = timed(lambda sd_: s.run_block(steps, sd_), 1, s)
+        rw = leg(sec, st, s.launch_geometry())
+        Pw, Cw, _, _ = s.get_state()
+    finally:
+        s.close()
     h = g.Sampler(N, program_length=PL, ops=H.OPSET_MULTI, n_vars=3, const_proposal=g.CONST_HMC,
                   stream=stream.cuda_stream)
-    h.set_data3(x1, x2, x3, y, sd)
-    h.set_moves(5, 0.001, 8)
-    h.set_state(Pw, Cw)
-    hsec, hst = timed(h, 7)
-    h.close()
-    print(json.dumps({
-        "metric": "MH chain-steps/s, large streamed multivariate data", "value": value, "unit": "chain-steps/s",
-        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "dtype": "f32",
-        "data": "synthetic (seeded)", "point_evals_per_s": pe,
-        "data_read_gbs": pe * 20 / 1e9,
-        "vs_hbm_peak": (pe * 20 / 1e9) / hbm if hbm else None,
-        "note": "the 1.3 MB dataset stays in L2: data bandwidth is served on chip, so it can exceed the HBM peak",
-        "acceptance": {"structure": st["struct_accepted"] / max(1, st["struct_proposed"]),
-                       "constant": st["const_accepted"] / max(1, st["const_proposed"])},
-        "hmc": {"chain_steps_per_s": N * steps * args.steps / hsec,
-                "likelihood_gradients_per_s": hst["evals"] / hsec,
-                "point_evals_per_s": hst["eval_points"] / hsec},
-        "config": {"workload": args.workload, "N": N, "PL": PL, "nd": nd, "n_vars": 3, "mh_steps": steps,
-                   "ops": "{+,-,*,/,sin,cos,exp,x1,x2,x3,const}", "launch": geo}}))
+    try:
+        h.set_batched_data([(x1, x2, x3, y, sd)])
+        h.set_moves(5, 0.001, 8)
+        h.set_state(Pw, Cw)
+        h.capture_blocks(1, steps)
+        hsec, hst = timed(lambda sd_: h.run_captured([sd_]), 7, h)
+        hmc = leg(hsec, hst, h.launch_geometry())
+        hmc["likelihood_gradients_per_s"] = hst["evals"] / hsec
+        hmc["path"] = "batched (gpr_set_batched_data, one dataset), captured graph of blocks"
+    finally:
+        h.close()
+    return {"metric": "MH chain-steps/s, large streamed multivariate data", "unit": "chain-steps/s",
+            "value": rw["chain_steps_per_s"], "steps": steps_timed, "warmup": warmup,
+            "rw": rw, "hmc_batched": hmc,
+            "note": "the 1.3 MB dataset stays in L2: data bandwidth is served on chip and can exceed the HBM peak",
+            "config": {"workload": "streamed-3var-16k", "N": N, "PL": PL, "nd": nd, "n_vars": 3,
+                       "mh_steps": steps, "ops": "{+,-,*,/,sin,cos,exp,x1,x2,x3,const}",
+                       "hmc": {"leapfrog_steps": 8, "eps": 0.001, "struct_every": 5}}}
 
 
-def hbm_roofline(point_evals, seconds, peaks, traffic):
+def run_streamed(args, w):
+    out = streamed_measure(args, w, args.steps, args.warmup)
+    out.update({"higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded)"})
+    print(json.dumps(out))
+
+
+def hbm_roofline(point_evals, seconds, peaks, traffic, nbytes=12):
     """The MH kernel against the HBM roof: algorithmic bytes = 12 per
-    point-eval (x, y and the weight of one point), over the timed launches.
-    The kernel reads them from shared memory or registers, not HBM (its DRAM
-    traffic per launch is `traffic`, the chain state); what bounds it is the
-    interpreter's instruction latency (roofline_fp32_issue, profiles/)."""
+    point-eval (x, y and the weight of one point; 20 with three input
+    variables), over the timed launches.  The kernel reads them from shared
+    memory, registers or L2, not HBM (its DRAM traffic per launch is
+    `traffic`, the chain state); the bound is FP32 issue (roofline)."""
     peak = peaks.get("hbm_gbs")
-    achieved = point_evals * 12 / seconds / 1e9
+    achieved = point_evals * nbytes / seconds / 1e9
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak if peak else None, "traffic": traffic,
+            "traffic_source": MH_LAUNCH_DRAM_SOURCE if traffic else None,
             "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if peak else None,
             "note": "12 algorithmic bytes per point-eval, served from shared memory (staged layout) or "
                     "L1/L2 (streamed layout), not HBM; DRAM traffic per launch (traffic) is the chain state. "
@@ -433,7 +504,7 @@ def batched_datasets(g, nds, seed=2024):
     return out, gens
 
 
-def run_batched(args, w):
+def batched_measure(args, w, steps_timed, warmup, compare=True):
     """Batched uneven workload: 256 independent datasets (sizes log-uniform in
     [8, 4096] points), 512 chains each (131072 chains), PROGRAM_LENGTH 47, op
     set {+,-,*,/,exp,log,pow,x,const}, random-walk constants (sd 0.1) with the
@@ -460,7 +531,7 @@ def run_batched(args, w):
         s.set_streaming(True)
     s.set_state(P0, C0)
     default_geo = s.launch_geometry()
-    for i in range(args.warmup):
+    for i in range(warmup):
         s.run_block(steps, 11 + i)
     tuned = None if args.no_autotune else s.autotune(steps=50, seed=4242)
     geo = s.launch_geometry()
@@ -473,7 +544,7 @@ def run_batched(args, w):
     evs = []
     clk = ClockSampler(os.path.join(CLOCKS_DIR, "clocks_batched.csv"))
     with clk:
-        for i in range(args.steps):
+        for i in range(steps_timed):
             flush.zero_()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
@@ -485,7 +556,7 @@ def run_batched(args, w):
     ms = float(sum(a.elapsed_time(b) for a, b in evs))
     st = s.stats()
     launches = s.launch_count() - launches0
-    value = N * steps * nb * args.steps / (ms / 1e3)
+    value = N * steps * nb * steps_timed / (ms / 1e3)
 
     # end to end through the C ABI: pinned host state in, replay, state out
     Ph = torch.empty((PL, N), dtype=torch.int32, pin_memory=True).numpy()
@@ -497,7 +568,7 @@ def run_batched(args, w):
     seeds = np.arange(nb, dtype=np.int32) + 77
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    e2e_steps = max(1, min(args.steps, 2))
+    e2e_steps = max(1, min(steps_timed, 2))
     for i in range(e2e_steps):
         lib.gpr_set_state(s.h, ptr(Ph), ptr(Ch))
         lib.gpr_run_captured(s.h, ptr(seeds + i))
@@ -511,7 +582,7 @@ def run_batched(args, w):
     hs = []
     sep = float("nan")
     try:
-        for d in range(nds if w.get("compare", True) else 0):
+        for d in range(nds if (compare and w.get("compare", True)) else 0):
             h = g.Sampler(cpd, program_length=PL, ops=H.OPSET_BASIC, rng=g.RNG_LCG,
                           const_proposal=g.CONST_RANDOM_WALK, rw_sd=w["rw_sd"], stream=stream.cuda_stream)
             h.set_data(*sets[d])
@@ -534,11 +605,9 @@ def run_batched(args, w):
 
     peaks = measured_peaks()
     props = torch.cuda.get_device_properties(dev)
-    peak_tops = props.multi_processor_count * 128 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
-    achieved = st["eval_node_points"] / (ms / 1e3) / 1e12
-    print(json.dumps({
+    return {
         "metric": "MH chain-steps/s, batched uneven datasets", "value": value, "unit": "chain-steps/s",
-        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "n_gpus": 1, "steps": steps_timed, "warmup": warmup, "ms_per_step": ms / steps_timed,
         "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded)",
         "point_evals_per_s": st["eval_points"] / (ms / 1e3),
         "separate_handles": {"chain_steps_per_s": sep, "launches_per_block": nds,
@@ -546,9 +615,8 @@ def run_batched(args, w):
         "e2e": {"value": e2e, "unit": "chain-steps/s", "h2d_bytes_per_step": Ph.nbytes + Ch.nbytes,
                 "d2h_bytes_per_step": Ph.nbytes + Ch.nbytes + prh.nbytes + lih.nbytes, "steps": e2e_steps},
         "gpu_launches": launches,
-        "roofline": hbm_roofline(st["eval_points"], ms / 1e3, peaks, None),
-        "roofline_fp32_issue": {"bound": "fp32-issue", "achieved": achieved, "peak": peak_tops,
-                                "unit": "T-ops/s", "frac": achieved / peak_tops},
+        "roofline": fp32_roofline(st["eval_node_points"], ms / 1e3, props.multi_processor_count, peaks),
+        "roofline_hbm": hbm_roofline(st["eval_points"], ms / 1e3, peaks, None),
         "acceptance": {"structure": st["struct_accepted"] / max(1, st["struct_proposed"]),
                        "constant": st["const_accepted"] / max(1, st["const_proposed"])},
         "clocks": clk.summary(0),
@@ -559,7 +627,11 @@ def run_batched(args, w):
                    "mh_steps_per_block": steps, "blocks_per_replay": nb, "rng": "lcg",
                    "resample": "per dataset, map-delta 20, on the device after each replay",
                    "const_proposal": "rw:%g" % w["rw_sd"], "l2": "flushed between replays (256 MB write)",
-                   "launch_default": default_geo, "launch": geo, "autotuned": tuned}}))
+                   "launch_default": default_geo, "launch": geo, "autotuned": tuned}}
+
+
+def run_batched(args, w):
+    print(json.dumps(batched_measure(args, w, args.steps, args.warmup)))
 
 
 def cpu_reference_rate(w, P, C, x, y, sd, target_s=12.0, threads=0, chains=None):
@@ -602,7 +674,7 @@ def run_reference(args, w):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded)",
         "point_evals_per_s": value * w["nd"],
-        "config": {"workload": args.workload, **{k: w[k] for k in ("N", "PL", "nd", "mh_steps")}},
+        "config": config_of(args, w),
         "cpu_baseline": {"value": value, "unit": "chain-steps/s", "cores": ncores, "kind": kind,
                          "sample": "%d chains x %d MH steps per step, from the seeded initial state"
                                    % (chains, w["mh_steps"])},
@@ -718,54 +790,81 @@ def run_gpu(args, w):
         return
     peaks = measured_peaks()
     clocks = clk.summary(local)
-    sm_mhz = (clocks or {}).get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
-    # FP32 issue roofline: 152 SMs x 128 FP32 lanes per clock, one op per lane
     props = torch.cuda.get_device_properties(dev)
     nsm = props.multi_processor_count
-    peak_tops = nsm * 128 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
-    alg_ops = st["eval_node_points"]
-    achieved_tops = alg_ops / (kernel_ms / 1e3) / 1e12
     geo = s.launch_geometry()
 
     ess = None if args.no_ess else ess_comparison(g, stream, dev)
     cpu = None
+    err = None
     if not args.no_cpu_baseline:
-        Pw, Cw, _, _ = s.get_state()
+        Pw, Cw, prw, liw = s.get_state()
         rate, cores, chains, dt, kind = cpu_reference_rate(w, Pw, Cw, x, y, sd)
         cpu = {"value": rate, "unit": "chain-steps/s", "cores": cores, "kind": kind,
                "sample": "%d chains x %d MH steps of the warmed-up state (%.1f s)"
                          % (chains, w["mh_steps"], dt)}
+        err = loglik_error_vs_fp64(Pw, Cw, liw, x, y, sd)
+    side = {}
+    if not args.no_side:
+        side["batched"] = batched_measure(args, WORKLOADS["batched-256ds-131k"], 2, 1, compare=False)
+        side["streamed"] = streamed_measure(args, WORKLOADS["streamed-3var-16k"], 2, 1)
     line = {
         "metric": METRIC, "value": value, "unit": "chain-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": kernel_ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded)",
         "point_evals_per_s": value * w["nd"],
-        "config": {"workload": args.workload, **{k: w[k] for k in ("N", "PL", "nd", "mh_steps", "map_delta")},
-                   "ops": w["ops"], "const_proposal": "rw:%g" % w["rw_sd"], "rng": "lcg",
-                   "l2": "flushed between blocks (256 MB write)",
-                   "parallelism": "one population over %d GPUs (resampling cutoff exchanged per block, "
-                                  "outside the timed region)" % world if world > 1 else "1 GPU",
-                   "launch": geo, "autotuned": tuned},
+        "config": config_of(args, w),
+        "parallelism": "one population over %d GPUs (resampling cutoff exchanged per block, outside the "
+                       "timed region)" % world if world > 1 else "1 GPU",
+        "layout": {"launch": geo, "autotuned": tuned},
         "e2e": {"value": e2e_value, "unit": "chain-steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "blocks": e2e_blocks,
                 "loop": "gpr_set_state (pinned host), gpr_run_block, gpr_resample (device, map-delta), "
                         "gpr_get_state (pinned host)"},
         "gpu_launches": launches,
-        "roofline": hbm_roofline(st["eval_points"], kernel_ms / 1e3, peaks,
-                                 MH_LAUNCH_DRAM_BYTES if args.workload == "plain-mh-131k" else None),
-        "roofline_fp32_issue": {"bound": "fp32-issue", "achieved": achieved_tops, "peak": peak_tops,
-                                "unit": "T-ops/s", "frac": achieved_tops / peak_tops,
-                                "note": "algorithmic FP32 ops = (node count + 4) per point evaluated; peak = "
-                                        "SMs x 128 lanes x max SM clock (nominal, no measured FP32 peak)"},
+        "roofline": fp32_roofline(st["eval_node_points"], kernel_ms / 1e3, nsm, peaks,
+                                  (clocks or {}).get("sm_mhz")),
+        "roofline_hbm": hbm_roofline(st["eval_points"], kernel_ms / 1e3, peaks,
+                                     MH_LAUNCH_DRAM_BYTES if args.workload == "plain-mh-131k" else None),
+        "loglik_err_vs_fp64": err,
+        "precision": {"evaluation": "FP32",
+                      "likelihood": "FP32 sums of 128-point chunks (<= 9 roundings), double-float across "
+                                    "chunks; <= 10 u = 6.0e-7 relative to the exact sum of the FP32 terms",
+                      "acceptance_ratio": "double-float from the prior difference and the difference of the "
+                                          "likelihood sums (the normalising sum cancels); carries the two "
+                                          "likelihoods' 10 u each",
+                      "range": "weights scaled by 2^-e chosen from the data: no overflow, no posterior floor",
+                      "fp64": "only when a block writes its scores"},
         "stats": st,
         "acceptance": {"structure": st["struct_accepted"] / max(1, st["struct_proposed"]),
                        "constant": st["const_accepted"] / max(1, st["const_proposed"])},
         "clocks": clocks,
         "cpu_baseline": cpu,
         "ess": ess,
+        **side,
     }
     print(json.dumps(line))
+
+
+def loglik_error_vs_fp64(P, C, lik, x, y, sd, n=2048):
+    """The device log-likelihoods of n chains spread over the final state
+    against the oracle's FP64 evaluation of the same programs (checker only),
+    on the chains whose FP32 evaluation is determined to 1e-6 (the oracle's
+    FP32 restatement within 1e-6 of its FP64 one)."""
+    from oracle import port
+    idx = np.linspace(0, P.shape[1] - 1, n).astype(int)
+    f64 = np.array([port.likelihood(P, C, int(i), x, y, sd, f64=True) for i in idx])
+    f32 = np.array([port.likelihood(P, C, int(i), x, y, sd, f64=False) for i in idx])
+    with np.errstate(all="ignore"):
+        cond = np.abs(f32 - f64) / np.maximum(np.abs(f64), 1.0)
+        e = np.abs(lik[idx] - f64) / np.maximum(np.abs(f64), 1.0)
+    ok = np.isfinite(f64) & np.isfinite(lik[idx]) & (cond <= 1e-6)
+    if not ok.any():
+        return None
+    return {"median": float(np.median(e[ok])), "max": float(e[ok].max()), "n": int(ok.sum()),
+            "sampled": int(n), "invalid_agree": bool(np.all(np.isfinite(f64) | ~np.isfinite(lik[idx]) |
+                                                           (cond > 1e-6)))}
 
 
 def main():
@@ -779,6 +878,8 @@ def main():
     ap.add_argument("--no-ess", action="store_true", help="skip the constants-mixing (ESS/s) comparison")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default layout (fixed launch sequence, for profilers)")
+    ap.add_argument("--no-side", action="store_true",
+                    help="skip the short batched and streamed workloads reported beside the headline")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     if args.workload == "hmc-rational-8k-profile":

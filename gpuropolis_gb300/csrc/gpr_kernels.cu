@@ -10,7 +10,7 @@ namespace gpr {
 /* ------------------------------------------------------------------------ */
 size_t mh_smem_bytes(const KParams& p, int K, int warps_per_cta, int stream) {
     return 16 + (stream ? 0 : align16((size_t)data_arrays(p) * p.nd_pad * 4)) +
-           (size_t)warps_per_cta * warp_smem_bytes(p.PL, p.max_instr, p.levels, K, false);
+           (size_t)warps_per_cta * warp_smem_bytes(p.PL, p.max_instr, p.levels, K);
 }
 
 size_t pipe_smem_bytes(const KParams& p, int K, int warps_per_cta, int stream) {

@@ -1346,8 +1346,8 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
         wbase += align16((size_t)data_arrays(p) * p.nd_pad * 4);
         if (!batched) stage_dataset(fx, bar, p, dv);
     }
-    const size_t wbytes = warp_smem_bytes(p.PL, p.max_instr, p.levels, K, false);
-    const WarpSmem ws = carve_warp<K>(wbase + (size_t)warp * wbytes, p.PL, p.max_instr, p.levels, false);
+    const size_t wbytes = warp_smem_bytes(p.PL, p.max_instr, p.levels, K);
+    const WarpSmem ws = carve_warp<K>(wbase + (size_t)warp * wbytes, p.PL, p.max_instr, p.levels);
 
     LaneData<K> ld;
     if (ONEPASS) {
@@ -1368,8 +1368,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
     /* CTA-balanced evaluation (lockstep == 1): each warp publishes its chain's
      * program; all warps then pull (chain, pass) tasks, longest programs
      * first, and leave the chunk sums of each pass here. */
-    __shared__ const uint32_t* s_pp[8];   /* the published program ...   */
-    __shared__ const float* s_pc[8];      /* ... and its constants       */
+    __shared__ const uint2* s_prog[8];    /* the published evaluation program */
     __shared__ int s_cost[8];
     __shared__ int s_count[8];
     __shared__ int s_bad[8];
@@ -1493,14 +1492,15 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
             }
             if (need_cauchy) { cs = cauchy_sum_u(ws.Cs[cbuf], p, lane); GPR_PH(GPR_PH_CAUCHY); }
             if (structural) backward = df_make(-p.logcount[count], 0.0f);
+            build_eval_program(ws.prog[pbuf], ws.Cs[cbuf], ninstr, ws.eprog, lane);
             __syncwarp();
+            GPR_PH(GPR_PH_EPROG);
           }
           df S = df_make(0.0f, 0.0f);
           int pts = 0;
           if (balanced) {
             if (lane == 0) {
-                s_pp[warp] = ws.prog[pbuf];
-                s_pc[warp] = ws.Cs[cbuf];
+                s_prog[warp] = ws.eprog;
                 s_cost[warp] = active ? ninstr : -1;
                 s_count[warp] = count;
                 s_bad[warp] = 0;
@@ -1533,8 +1533,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                 const int w = __ffs(__ballot_sync(FULLMASK, my_rank == q)) - 1;
                 if (s_bad[w]) continue;
                 float csum[K / 4];
-                const PCProg prog = {s_pp[w], s_pc[w]};
-                const bool anybad = eval_pass_chunks<K, ONEPASS, ROLLED, NV, STREAM>(prog, ws.stk, ws.scr, ld,
+                const bool anybad = eval_pass_chunks<K, ONEPASS, ROLLED, NV, STREAM>(s_prog[w], ws.stk, ws.scr, ld,
                                                                                    dv, p, lane, pass, csum);
                 const int np = ONEPASS ? dv.nd : min(32 * K, dv.nd - pass * 32 * K);
                 pts += np;
@@ -1559,8 +1558,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
             }
             GPR_PH(GPR_PH_COMBINE);
           } else if (active) {
-            const PCProg prog = {ws.prog[pbuf], ws.Cs[cbuf]};
-            S = eval_loglik_S<K, ONEPASS, ROLLED, NV, STREAM>(prog, ws.stk, ws.scr, ld, dv, p, lane, pts);
+            S = eval_loglik_S<K, ONEPASS, ROLLED, NV, STREAM>(ws.eprog, ws.stk, ws.scr, ld, dv, p, lane, pts);
             st_np += (unsigned long long)(count + 4) * (unsigned)pts;
             GPR_PH_COUNT(GPR_PH_NPASSES, npass);
             GPR_PH_COUNT(GPR_PH_NINSTR, (unsigned long long)ninstr * npass);
