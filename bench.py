@@ -798,7 +798,10 @@ def run_gpu(args, w):
     cpu = None
     err = None
     if not args.no_cpu_baseline:
-        Pw, Cw, prw, liw = s.get_state()
+        # scores of the final state (after the e2e loop's device resampling, the
+        # re-drawn chains' scores are the next block's to compute: evaluate them)
+        prw, liw = s.evaluate()
+        Pw, Cw, _, _ = s.get_state()
         rate, cores, chains, dt, kind = cpu_reference_rate(w, Pw, Cw, x, y, sd)
         cpu = {"value": rate, "unit": "chain-steps/s", "cores": cores, "kind": kind,
                "sample": "%d chains x %d MH steps of the warmed-up state (%.1f s)"
