@@ -807,6 +807,18 @@ def run_gpu(args, w):
                "sample": "%d chains x %d MH steps of the warmed-up state (%.1f s)"
                          % (chains, w["mh_steps"], dt)}
         err = loglik_error_vs_fp64(Pw, Cw, liw, x, y, sd)
+    phases = None
+    if args.phase_profile:
+        # one block of the same layout through its phase-timed build (untimed; same chains)
+        ph = s.phase_profile(w["mh_steps"], 4711)
+        cs = w["N"] * w["mh_steps"]
+        tot = sum(ph["cycles"].values())
+        phases = {"cycles_per_chain_step": {k: round(v / cs, 1) for k, v in ph["cycles"].items()},
+                  "share": {k: round(v / tot, 4) for k, v in ph["cycles"].items()},
+                  "passes_per_chain_step": ph["passes"] / cs,
+                  "instructions_per_pass": ph["instructions"] / max(1, ph["passes"]),
+                  "layout": s.launch_geometry(),
+                  "note": "clock64 cycles of each warp between phase boundaries, summed over warps, per chain-step"}
     side = {}
     if not args.no_side:
         side["batched"] = batched_measure(args, WORKLOADS["batched-256ds-131k"], 2, 1, compare=False)
@@ -845,6 +857,7 @@ def run_gpu(args, w):
         "clocks": clocks,
         "cpu_baseline": cpu,
         "ess": ess,
+        "phases": phases,
         **side,
     }
     print(json.dumps(line))
@@ -881,6 +894,8 @@ def main():
     ap.add_argument("--no-ess", action="store_true", help="skip the constants-mixing (ESS/s) comparison")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default layout (fixed launch sequence, for profilers)")
+    ap.add_argument("--phase-profile", action="store_true",
+                    help="add a per-phase cycle table of one more block, from the kernel's phase-timed build")
     ap.add_argument("--no-side", action="store_true",
                     help="skip the short batched and streamed workloads reported beside the headline")
     args = ap.parse_args()

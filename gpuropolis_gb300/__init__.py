@@ -86,6 +86,7 @@ def library():
     lib.gpr_stream.restype = vp
     lib.gpr_debug_math.argtypes = [vp, ip, vp, vp, vp, ip]
     lib.gpr_debug_phase_profile.argtypes = [vp, ip, ip, vp, ip]
+    lib.gpr_debug_stage_wait.argtypes = [vp, ip]
     lib.gpr_autotune.argtypes = [vp, ip, ip, vp, vp, vp, vp]
     lib.gpr_set_layout.argtypes = [vp, ip, ip, ip]
     lib.gpr_layout_rolled.argtypes = [vp]
@@ -285,6 +286,10 @@ class Sampler:
         self._check(self.lib.gpr_debug_phase_profile(self.h, int(steps), int(seed), _ptr(out), len(out)))
         d = {n: int(v) for n, v in zip(self.PHASE_NAMES, out)}
         return {"cycles": d, "passes": int(out[-2]), "instructions": int(out[-1])}
+
+    def set_stage_wait(self, polls):
+        """Polls of the staging barrier before a kernel gives up (testing)."""
+        self._check(self.lib.gpr_debug_stage_wait(self.h, int(polls)))
 
     def autotune(self, steps=50, seed=1):
         """Pick the fastest evaluation layout on the current state and data."""

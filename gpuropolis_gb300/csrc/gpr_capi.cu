@@ -22,6 +22,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/gpuropolis.h"
 #include "gpr_common.h"
 #include "gpr_kernels.cuh"
@@ -80,6 +82,14 @@ struct gpr_handle {
     std::string err;
 };
 
+/* An NVTX range over a C-ABI call, so that blocks, resampling and state
+ * transfers show as named spans in Nsight timelines (almost free when no
+ * tool is attached). */
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+};
+
 /* Failures with no handle to hold them (gpr_create, gpr_run_block_noalloc):
  * one message per host thread, so that calls failing at once on different
  * threads do not race on it. */
@@ -111,6 +121,9 @@ static gpr::Magic magic_for(uint32_t d) {
     r.s = (uint32_t)(31 + l);
     return r;
 }
+
+/* Polls of the dataset staging barrier before a kernel reports a timeout. */
+#define GPR_STAGE_WAIT_DEFAULT (1 << 22)
 
 /* divisor of random_int(n), main.cu:220 */
 static uint32_t divisor_for(int n) { return (uint32_t)(2147483647 / (n + 1)); }
@@ -308,6 +321,7 @@ int gpr_create(const gpr_config* cfg, int n_chains, gpr_handle** out) {
     kp.err = h->dcounter + 1;
     kp.stats = h->dstats;
     kp.lockstep = 1;
+    kp.stage_wait_iters = GPR_STAGE_WAIT_DEFAULT;
     kp.struct_every = 5;                                           /* main.cu:699 */
     kp.hmc_eps = 0.01f;
     kp.hmc_L = 8;
@@ -730,6 +744,7 @@ int gpr_capture_blocks(gpr_handle* h, int n_blocks, int steps) {
 
 int gpr_run_captured(gpr_handle* h, const int* seeds) {
     if (!h || !seeds) return GPR_ERR_ARG;
+    NvtxRange r("gpr_run_captured: MH blocks");
     if (!h->graph) return fail(h, GPR_ERR_STATE, "no captured block sequence (gpr_capture_blocks)");
     CUDA_TRY(h, cudaSetDevice(h->device));
     /* the seeds go into the kernel nodes' parameters: the update applies to
@@ -756,6 +771,7 @@ int gpr_set_data3(gpr_handle* h, const float* x1, const float* x2, const float* 
 
 int gpr_set_state(gpr_handle* h, const int32_t* P, const float* C) {
     if (!h) return GPR_ERR_ARG;
+    NvtxRange r("gpr_set_state: state in");
     if (!P || !C) return fail(h, GPR_ERR_ARG, "P and C must be non-NULL");
     const size_t cnt = (size_t)h->N * h->PL;
     for (size_t i = 0; i < cnt; ++i) {
@@ -783,6 +799,7 @@ int gpr_set_scores(gpr_handle* h, const double* prior, const double* likelihood)
 
 int gpr_get_state(gpr_handle* h, int32_t* P, float* C, double* prior, double* likelihood) {
     if (!h) return GPR_ERR_ARG;
+    NvtxRange r("gpr_get_state: state out");
     CUDA_TRY(h, cudaSetDevice(h->device));
     const size_t cnt = (size_t)h->N * h->PL;
     if (P) CUDA_TRY(h, cudaMemcpyAsync(P, h->dP, cnt * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
@@ -807,6 +824,7 @@ static int run(gpr_handle* h, int steps, int seed) {
 
 int gpr_run_block(gpr_handle* h, int steps, int random_seed) {
     if (!h) return GPR_ERR_ARG;
+    NvtxRange r("gpr_run_block: MH block");
     if (steps < 0) return fail(h, GPR_ERR_ARG, "steps must be >= 0 (got %d)", steps);
     return run(h, steps, random_seed);
 }
@@ -884,6 +902,14 @@ int gpr_debug_math(gpr_handle* h, int op, const float* a, const float* b, float*
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     cudaFree(d);
     if (e != cudaSuccess) return fail(h, GPR_ERR_CUDA, "gpr_debug_math: %s", cudaGetErrorString(e));
+    return GPR_OK;
+}
+
+int gpr_debug_stage_wait(gpr_handle* h, int polls) {
+    if (!h) return GPR_ERR_ARG;
+    if (polls < 0) return fail(h, GPR_ERR_ARG, "polls must be >= 0 (got %d)", polls);
+    drop_graph(h);
+    h->kp.stage_wait_iters = polls;
     return GPR_OK;
 }
 
@@ -1279,6 +1305,7 @@ static int select_rank(gpr_handle* h, int rank, unsigned long long* key) {
 int gpr_resample_datasets(gpr_handle* h, int mode, double param, uint32_t seed, int* n_redrawn,
                           double* cutoffs) {
     if (!h) return GPR_ERR_ARG;
+    NvtxRange r("gpr_resample: re-draw below the cutoff");
     if (mode != 0 && mode != 1) return fail(h, GPR_ERR_ARG, "unknown resample mode %d", mode);
     if (h->cfg.n_ops < 2)
         return fail(h, GPR_ERR_ARG, "re-drawing ops needs at least 2 ops (random_int(n_ops - 1))");
@@ -1328,6 +1355,7 @@ int gpr_resample(gpr_handle* h, int mode, double param, uint32_t seed, int* n_re
 
 int gpr_resample_below(gpr_handle* h, double cutoff, uint32_t seed, int chain_offset, int* n_redrawn) {
     if (!h) return GPR_ERR_ARG;
+    NvtxRange r("gpr_resample_below: re-draw below a given cutoff");
     if (h->cfg.n_ops < 2)
         return fail(h, GPR_ERR_ARG, "re-drawing ops needs at least 2 ops (random_int(n_ops - 1))");
     if (chain_offset < 0) return fail(h, GPR_ERR_ARG, "chain_offset must be >= 0 (got %d)", chain_offset);
@@ -1353,6 +1381,7 @@ int gpr_resample_below(gpr_handle* h, double cutoff, uint32_t seed, int chain_of
 
 int gpr_top_chains(gpr_handle* h, int k, double margin, int* chains, int capacity, int* n, double* threshold) {
     if (!h) return GPR_ERR_ARG;
+    NvtxRange r("gpr_top_chains: tops candidates");
     if (k < 1 || k > h->N) return fail(h, GPR_ERR_ARG, "k = %d is not in [1, %d]", k, h->N);
     if (!(margin >= 0.0)) return fail(h, GPR_ERR_ARG, "margin %g is not >= 0", margin);
     if (capacity < 0 || (capacity > 0 && !chains) || !n) return fail(h, GPR_ERR_ARG, "bad output arguments");
@@ -1502,6 +1531,7 @@ static void noalloc_params(gpr::KParams& kp, const gpr_config* cfg, int n_chains
     kp.geom_logr = gpr_rng_logf(R);
     set_prior_constants(kp, cfg->n_ops, PL);
     kp.lockstep = 1;
+    kp.stage_wait_iters = GPR_STAGE_WAIT_DEFAULT;
     kp.struct_every = 5;
     kp.hmc_eps = 0.01f;
     kp.hmc_L = 8;

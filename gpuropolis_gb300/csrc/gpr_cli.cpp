@@ -29,6 +29,7 @@
  * and --resume=FILE (continue from such a file, appending to samples.txt:
  * the continued run writes what the uninterrupted one would have).
  */
+#include <nvtx3/nvToolsExt.h>
 #include <getopt.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -395,6 +396,7 @@ int main(int argc, char** argv) {
             return 1;
         }
         if (write) {
+            nvtxRangePushA("samples.txt: format and write");
             char* buf = nullptr;
             int64_t n = gpr_format_samples(P.data(), C.data(), prior.data(), lik.data(), N, PL, o,
                                            SHOW_CONSTANTS, threads, &buf);
@@ -414,6 +416,7 @@ int main(int argc, char** argv) {
                 }
             }
             gpr_free(buf);
+            nvtxRangePop();
         }
         if (device_resample) {
             /* keyed by the block seed: the re-draw streams (seed, chain | 2^31)

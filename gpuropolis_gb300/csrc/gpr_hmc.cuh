@@ -396,13 +396,14 @@ __device__ __forceinline__ float hmc_momentum(uint32_t seed, uint32_t chain, uin
 /* d loglik / d C for every chain's current state (gpr_loglik_grad): one warp
  * per chain, grad[i*N + chain] (double, unscaled) and lik[chain]. */
 /* The dataset: staged into this CTA's shared memory, or (STREAM) read from
- * device memory.  Returns where the per-warp regions start. */
+ * device memory.  Returns where the per-warp regions start, or nullptr (the
+ * same in every thread) when the staging copy timed out. */
 template <bool STREAM>
 __device__ __forceinline__ uint8_t* grad_dataset(uint8_t* smem, const KParams& p, DataView& dv) {
     float* fx = (float*)(smem + GPR_STAGED_OFFSET);
     dv = data_view(p, fx, STREAM);
     if (STREAM) return smem + GPR_STAGED_OFFSET;
-    stage_dataset(fx, (uint64_t*)smem, p, dv);
+    if (!stage_dataset(fx, (uint64_t*)smem, p, dv)) return nullptr;
     return smem + GPR_STAGED_OFFSET + align16((size_t)data_arrays(p) * p.nd_pad * 4);
 }
 
@@ -414,6 +415,7 @@ __global__ void __launch_bounds__(128) loglik_grad_kernel(const __grid_constant_
     const int warp = threadIdx.x >> 5;
     DataView dv;
     uint8_t* wbase = grad_dataset<STREAM>(smem, p, dv);
+    if (!wbase) return;   /* the staging copy timed out: the error flag is set */
     const GradSmem ws = carve_grad(wbase + (size_t)warp * grad_warp_bytes(p.PL, p.max_instr), p.PL, p.max_instr);
     const int chain = blockIdx.x * (blockDim.x >> 5) + warp;
     if (chain >= p.N) return;
@@ -446,6 +448,7 @@ __global__ void __launch_bounds__(128) mh_hmc_kernel(const __grid_constant__ KPa
     const int warp = threadIdx.x >> 5;
     DataView dv;
     uint8_t* wbase = grad_dataset<STREAM>(smem, p, dv);
+    if (!wbase) return;   /* the staging copy timed out: the error flag is set */
     const GradSmem ws = carve_grad(wbase + (size_t)warp * grad_warp_bytes(p.PL, p.max_instr), p.PL, p.max_instr);
     const int PL = p.PL;
     const bool adapt = p.chain_scale && p.adapt_target > 0.0f;

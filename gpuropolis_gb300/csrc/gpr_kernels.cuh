@@ -96,6 +96,8 @@ struct KParams {
     int* err;          /* device error flags                                    */
     unsigned long long* stats;  /* GPR_STAT_* counters, accumulated per launch  */
     int lockstep;      /* >0: the warps of a CTA realign every `lockstep` steps  */
+    int stage_wait_iters;  /* polls of the dataset staging barrier before the kernel
+                            * gives up with error flag 1 (default 2^22)          */
     int levels;        /* value-stack slots per lane                            */
     int max_instr;     /* instruction buffer length per program                 */
 

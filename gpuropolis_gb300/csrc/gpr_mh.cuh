@@ -1130,6 +1130,10 @@ __device__ __forceinline__ DataView data_view(const KParams& p, const float* dst
     return dv;
 }
 
+/* Iterations of the staging wait after a timed-out one: the drain of the
+ * copy still in flight. */
+#define GPR_STAGE_DRAIN_ITERS (1 << 22)
+
 /* Stage the dataset into dst with one bulk TMA copy per array; bounded wait.
  * dv: the view it is staged for (its nd_pad); d: the dataset (-1: the single
  * one).  Re-staging for another dataset (reinit) invalidates and
@@ -1156,15 +1160,24 @@ static __device__ bool stage_dataset(float* dst, uint64_t* bar, const KParams& p
                          : "memory");
     }
     __syncthreads();
-    uint32_t b = smem_u32(bar);
-    uint32_t done = 0;
-    for (int it = 0; it < (1 << 22) && !done; ++it) {
-        asm volatile("{\n\t.reg .pred P1;\n\t"
-                     "mbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\n\t"
-                     "selp.b32 %0, 1, 0, P1;\n\t}"
-                     : "=r"(done) : "r"(b), "r"(0u) : "memory");
+    const uint32_t b = smem_u32(bar);
+    auto wait = [&](int limit) {
+        uint32_t done = 0;
+        for (int it = 0; it < limit && !done; ++it) {
+            asm volatile("{\n\t.reg .pred P1;\n\t"
+                         "mbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\n\t"
+                         "selp.b32 %0, 1, 0, P1;\n\t}"
+                         : "=r"(done) : "r"(b), "r"(0u) : "memory");
+        }
+        return done;
+    };
+    uint32_t done = wait(p.stage_wait_iters);
+    if (!done) {
+        /* report, then wait (bounded again) for this CTA's own copy, so that
+         * none is in flight into shared memory when the CTA gives up */
+        atomicOr(p.err, 1);
+        (void)wait(GPR_STAGE_DRAIN_ITERS);
     }
-    if (!done) atomicOr(p.err, 1);
     return !__syncthreads_or(!done);
 }
 
@@ -1344,7 +1357,8 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
     uint8_t* wbase = smem + GPR_STAGED_OFFSET;
     if (!STREAM) {
         wbase += align16((size_t)data_arrays(p) * p.nd_pad * 4);
-        if (!batched) stage_dataset(fx, bar, p, dv);
+        /* a copy that did not arrive in time: the error flag is set, the CTA leaves */
+        if (!batched && !stage_dataset(fx, bar, p, dv)) return;
     }
     const size_t wbytes = warp_smem_bytes(p.PL, p.max_instr, p.levels, K);
     const WarpSmem ws = carve_warp<K>(wbase + (size_t)warp * wbytes, p.PL, p.max_instr, p.levels);

@@ -103,7 +103,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_pipe_kernel(const __grid
     uint8_t* wbase = smem + GPR_STAGED_OFFSET;
     if (!STREAM) {
         wbase += align16((size_t)data_arrays(p) * p.nd_pad * 4);
-        if (!BATCHED) stage_dataset(fx, bar, p, dv);
+        if (!BATCHED && !stage_dataset(fx, bar, p, dv)) return;   /* timed out: flag set, the CTA leaves */
     }
     const int PL = p.PL;
     uint8_t* const mybase = wbase + (size_t)warp * pipe_warp_bytes(PL, p.max_instr, p.levels, K);

@@ -173,6 +173,14 @@ int gpr_debug_math(gpr_handle* h, int op, const float* a, const float* b, float*
  * instrumented; others return GPR_ERR_ARG. */
 int gpr_debug_phase_profile(gpr_handle* h, int steps, int random_seed, uint64_t* out, int n);
 
+/* How many times the kernels poll the barrier of the bulk copy that stages
+ * the dataset into a CTA's shared memory before giving up (default 2^22).  A
+ * CTA that gives up sets error flag 1, waits (bounded) for its own copy to
+ * land, and leaves: gpr_sync then returns GPR_ERR_DEVICE and the handle stays
+ * usable.  0 makes every staged launch give up at once -- for testing that
+ * path without a faulty GPU. */
+int gpr_debug_stage_wait(gpr_handle* h, int polls);
+
 /* Layout autotuner (no reference counterpart): times one block of `steps`
  * MH steps under each valid evaluation layout -- the pipelined kernel (two
  * chains per warp) or the lockstep one (one chain per warp), K = 4 or 8
