@@ -498,12 +498,16 @@ static int configure_launch(gpr_handle* h, int K, int onepass, int rolled, int l
     return GPR_OK;
 }
 
-/* Default layout before any autotuning: the pipelined kernel, K = 4 points
- * per lane, one pass when the data fit, heavy ops unrolled; three input
- * variables and batched data take K = 4 in passes (gpr_autotune re-checks
- * per dataset). */
+/* Default layout before any autotuning: K = 4 points per lane, one pass when
+ * the data fit, heavy ops unrolled; the lockstep kernel while a CTA can
+ * balance its chains' passes over its warps (up to GPR_MAX_PASSES passes: on
+ * the 250-point workload it measured 10% faster), the pipelined kernel beyond
+ * (which splits any number of passes over the warps: 20% faster on the
+ * 65,536-point workload than free-running warps).  Three input variables and
+ * batched data take K = 4 in passes (gpr_autotune re-checks per dataset). */
 static int choose_launch(gpr_handle* h) {
-    return configure_launch(h, 4, (h->kp.nd <= 128 && h->kp.nv != 3 && h->kp.nds == 0) ? 1 : 0, 0, 1, 8, 1);
+    const int pipe = (h->kp.nd + 127) / 128 > GPR_MAX_PASSES ? 1 : 0;
+    return configure_launch(h, 4, (h->kp.nd <= 128 && h->kp.nv != 3 && h->kp.nds == 0) ? 1 : 0, 0, 1, 8, pipe);
 }
 
 /* Device layout of a dataset: x1 | y | w | sd | x2 | x3, nd_pad floats each

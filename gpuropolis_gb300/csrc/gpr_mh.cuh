@@ -378,6 +378,35 @@ static __device__ CompileOut compile_parallel(const uint8_t* ops, int PL, uint32
     return out;
 }
 
+/* An estimate of a compiled program's evaluation time per pass, in issued
+ * instructions at four points per lane: the interpreter's dispatch plus the
+ * operation (pow, log, exp and division are tens of instructions each, an
+ * add one per point).  It orders a CTA's evaluation tasks longest first. */
+__device__ __forceinline__ int instr_cost(uint32_t ins) {
+    const uint32_t code = ins & 0xffu;
+    int body;
+    if (code >= I_BIN0) {
+        const uint32_t bop = GPR_BIN_BOP(code);
+        body = bop == BOP_POW ? 280 : bop == BOP_DIV ? 36 : 4;
+    } else {
+        switch (code) {
+            case I_END: return 0;
+            case U_EXP: body = 60; break;
+            case U_LOG: body = 100; break;
+            case U_SQRT: case U_INV: body = 36; break;
+            case U_SIN: case U_ASIN: case U_COS: case U_ACOS: case U_TAN: case U_ATAN: body = 160; break;
+            default: body = 4; break;
+        }
+    }
+    return 25 + body;
+}
+__device__ __forceinline__ int program_cost(const uint32_t* prog, int ninstr, int lane) {
+    int c = 0;
+#pragma unroll 1
+    for (int i = lane; i < ninstr; i += 32) c += instr_cost(prog[i]);
+    return (int)__reduce_add_sync(FULLMASK, (unsigned)c);
+}
+
 /* The program the evaluator runs: each instruction word paired with the
  * constant it reads (NaN for the invalid-op marker), so one 64-bit shared
  * load fetches both.  Rebuilt for every proposal, lanes in parallel. */
@@ -1383,7 +1412,8 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
      * program; all warps then pull (chain, pass) tasks, longest programs
      * first, and leave the chunk sums of each pass here. */
     __shared__ const uint2* s_prog[8];    /* the published evaluation program */
-    __shared__ int s_cost[8];
+    __shared__ int s_cost[8];             /* its estimated cost (-1: none)     */
+    __shared__ int s_ninstr[8];           /* its length                       */
     __shared__ int s_count[8];
     __shared__ int s_bad[8];
     __shared__ int s_next;
@@ -1446,6 +1476,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
         int ccur = 0;          /* constants buffer of the current state */
         float cur_len = 0.0f;
         int cur_count = 0;
+        int cur_cost = 0;      /* program_cost of the current program */
         /* the current state's prior, likelihood sum S (scale 2^-e) and Cauchy
          * sum; the forward/backward terms (main.cu:702,723,761-775) */
         df cur_prior = df_make(0.f, 0.f), cur_S = df_make(0.f, 0.f), cur_cs = df_make(0.f, 0.f);
@@ -1473,7 +1504,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
           const bool structural = !init && p.struct_every > 0 && (step % p.struct_every == 0);
           int pbuf = cur, cbuf = ccur;
           float len = cur_len;
-          int count = cur_count, ninstr = cur_ninstr;
+          int count = cur_count, ninstr = cur_ninstr, cost = cur_cost;
           df cs = cur_cs;
           if (active) {
             bool need_compile = init, need_cauchy = init;
@@ -1502,6 +1533,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                 count = co.count;
                 ninstr = co.ninstr;
                 __syncwarp();
+                cost = program_cost(ws.prog[pbuf], ninstr, lane);
                 GPR_PH(GPR_PH_COMPILE);
             }
             if (need_cauchy) { cs = cauchy_sum_u(ws.Cs[cbuf], p, lane); GPR_PH(GPR_PH_CAUCHY); }
@@ -1515,7 +1547,8 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
           if (balanced) {
             if (lane == 0) {
                 s_prog[warp] = ws.eprog;
-                s_cost[warp] = active ? ninstr : -1;
+                s_cost[warp] = active ? cost : -1;
+                s_ninstr[warp] = ninstr;
                 s_count[warp] = count;
                 s_bad[warp] = 0;
             }
@@ -1558,7 +1591,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                 }
                 st_np += (unsigned long long)(s_count[w] + 4) * (unsigned)np;
                 GPR_PH_COUNT(GPR_PH_NPASSES, 1);
-                GPR_PH_COUNT(GPR_PH_NINSTR, s_cost[w]);
+                GPR_PH_COUNT(GPR_PH_NINSTR, s_ninstr[w]);
             }
             GPR_PH(GPR_PH_EVAL);
             __syncthreads();
@@ -1594,7 +1627,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
             }
             if (accept) {
                 cur = pbuf; ccur = cbuf;
-                cur_len = len; cur_count = count; cur_ninstr = ninstr; cur_cs = cs;
+                cur_len = len; cur_count = count; cur_ninstr = ninstr; cur_cost = cost; cur_cs = cs;
                 cur_prior = prior; cur_S = S;
             }
             __syncwarp();
