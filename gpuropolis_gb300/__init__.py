@@ -87,6 +87,7 @@ def library():
     lib.gpr_debug_math.argtypes = [vp, ip, vp, vp, vp, ip]
     lib.gpr_debug_phase_profile.argtypes = [vp, ip, ip, vp, ip]
     lib.gpr_debug_stage_wait.argtypes = [vp, ip]
+    lib.gpr_debug_fp_issue.argtypes = [ip, ip, vp, vp, vp]
     lib.gpr_autotune.argtypes = [vp, ip, ip, vp, vp, vp, vp]
     lib.gpr_set_layout.argtypes = [vp, ip, ip, ip]
     lib.gpr_layout_rolled.argtypes = [vp]
@@ -141,6 +142,17 @@ def library():
 
 def _ptr(a):
     return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def fp_issue_times(device=0, iters=4096):
+    """(ms FP64 adds on all lanes, ms FP64 adds on one lane per warp, ms FP32
+    adds on all lanes) of the same work on the device."""
+    lib = library()
+    v = [ctypes.c_float() for _ in range(3)]
+    rc = lib.gpr_debug_fp_issue(device, iters, *[ctypes.byref(a) for a in v])
+    if rc != GPR_OK:
+        raise GprError(rc, lib.gpr_last_error(None).decode())
+    return tuple(a.value for a in v)
 
 
 def make_config(program_length=31, ops=None, rng=RNG_LCG, const_proposal=CONST_REFERENCE,

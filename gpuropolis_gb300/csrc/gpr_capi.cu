@@ -909,6 +909,14 @@ int gpr_debug_math(gpr_handle* h, int op, const float* a, const float* b, float*
     return GPR_OK;
 }
 
+int gpr_debug_fp_issue(int device, int iters, float* ms_dadd32, float* ms_dadd1, float* ms_fadd32) {
+    if (iters < 1 || !ms_dadd32 || !ms_dadd1 || !ms_fadd32) return fail(nullptr, GPR_ERR_ARG, "bad arguments");
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = gpr::time_fp_adds(iters, ms_dadd32, ms_dadd1, ms_fadd32);
+    if (e != cudaSuccess) return fail(nullptr, GPR_ERR_CUDA, "gpr_debug_fp_issue: %s", cudaGetErrorString(e));
+    return GPR_OK;
+}
+
 int gpr_debug_stage_wait(gpr_handle* h, int polls) {
     if (!h) return GPR_ERR_ARG;
     if (polls < 0) return fail(h, GPR_ERR_ARG, "polls must be >= 0 (got %d)", polls);

@@ -133,6 +133,48 @@ __global__ void math_kernel(int op, const float* a, const float* b, float* out, 
     out[i] = r;
 }
 
+/* Diagnostics: four independent chains of adds per thread, FP64 (on every
+ * lane, or on lane 0 of each warp only) or FP32, to time the issue cost of
+ * FP64 arithmetic against FP32 on the device. */
+template <typename T>
+__global__ void fp_add_kernel(T* out, int iters, int lane0_only) {
+    T a = (T)(threadIdx.x & 31) * (T)1e-3, b = a + (T)1, c = a + (T)2, d = a + (T)3;
+    if (!lane0_only || (threadIdx.x & 31) == 0) {
+#pragma unroll 4
+        for (int i = 0; i < iters; ++i) {
+            a = a + (T)1.000001; b = b + (T)1.000002; c = c + (T)1.000003; d = d + (T)1.000004;
+        }
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = a + b + c + d;
+}
+
+cudaError_t time_fp_adds(int iters, float* ms_d32, float* ms_d1, float* ms_f32) {
+    int dev = 0, nsm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    const int blocks = nsm * 8, threads = 256;
+    double* d = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if ((e = cudaMalloc(&d, (size_t)blocks * threads * sizeof(double))) != cudaSuccess) return e;
+    if ((e = cudaEventCreate(&e0)) == cudaSuccess) e = cudaEventCreate(&e1);
+    float* outs[3] = {ms_d32, ms_d1, ms_f32};
+    for (int rep = 0; rep < 2 && e == cudaSuccess; ++rep)      /* the first round warms up */
+        for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
+            e = cudaEventRecord(e0);
+            if (k < 2) fp_add_kernel<double><<<blocks, threads>>>(d, iters, k);
+            else fp_add_kernel<float><<<blocks, threads>>>((float*)d, iters, 0);
+            if (e == cudaSuccess) e = cudaGetLastError();
+            if (e == cudaSuccess) e = cudaEventRecord(e1);
+            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+            if (e == cudaSuccess) e = cudaEventElapsedTime(outs[k], e0, e1);
+        }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(d);
+    return e;
+}
+
 cudaError_t launch_math(int op, const float* a, const float* b, float* out, int n, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     math_kernel<<<(n + 255) / 256, 256, 0, st>>>(op, a, b, out, n);

@@ -171,6 +171,9 @@ cudaError_t launch_eval_values(const KParams& p, const float* xs, int nx, float*
                                float* length, int* count, cudaStream_t st);
 
 cudaError_t launch_math(int op, const float* a, const float* b, float* out, int n, cudaStream_t st);
+/* Times (ms) of the same adds on the current device: FP64 on all lanes, FP64
+ * on one lane per warp, FP32 on all lanes. */
+cudaError_t time_fp_adds(int iters, float* ms_d32, float* ms_d1, float* ms_f32);
 
 /* Gradient of the log-likelihood and the MH kernel with Hamiltonian constant
  * moves (gpr_hmc.cu).  grad_smem_bytes: dynamic shared memory of either for

@@ -173,6 +173,12 @@ int gpr_debug_math(gpr_handle* h, int op, const float* a, const float* b, float*
  * instrumented; others return GPR_ERR_ARG. */
 int gpr_debug_phase_profile(gpr_handle* h, int steps, int random_seed, uint64_t* out, int n);
 
+/* The issue cost of FP64 against FP32 arithmetic on `device`: the times (ms)
+ * of the same independent adds as FP64 on every lane, as FP64 on one lane per
+ * warp, and as FP32 on every lane (8 CTAs of 256 threads per SM, iters x 4
+ * adds per thread).  It is why the kernels keep FP64 out of their step loops. */
+int gpr_debug_fp_issue(int device, int iters, float* ms_dadd32, float* ms_dadd1, float* ms_fadd32);
+
 /* How many times the kernels poll the barrier of the bulk copy that stages
  * the dataset into a CTA's shared memory before giving up (default 2^22).  A
  * CTA that gives up sets error flag 1, waits (bounded) for its own copy to

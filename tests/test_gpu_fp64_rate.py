@@ -1,6 +1,9 @@
-"""The reason the kernel issues no FP64 arithmetic in its step loop: on GB300,
-FP64 throughput is a small fraction of FP32.  Measured with cuBLAS GEMMs
-(DGEMM vs SGEMM without TF32); the test prints both rates."""
+"""The reason the kernels issue no FP64 arithmetic in their step loops: on
+GB300, FP64 throughput is a small fraction of FP32.  Measured with cuBLAS
+GEMMs (DGEMM vs SGEMM without TF32), and with the library's own add kernels,
+which also show that an FP64 add issued by a single lane of a warp costs what
+a full warp's costs (so confining FP64 work to one lane saves nothing).  The
+tests print the figures."""
 import time
 
 import pytest
@@ -33,3 +36,14 @@ def test_fp64_rate_is_a_small_fraction_of_fp32():
         torch.backends.cuda.matmul.allow_tf32 = old
     print("SGEMM %.2f TFLOP/s, DGEMM %.2f TFLOP/s, ratio %.1f" % (f32, f64, f32 / f64))
     assert f32 / f64 > 8
+
+
+def test_fp64_add_issue_cost():
+    g = pytest.importorskip("gpuropolis_gb300")
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    d32, d1, f32 = g.fp_issue_times(0, 4096)
+    print("FP64 adds, 32 lanes: %.3f ms; FP64 adds, 1 lane per warp: %.3f ms; FP32 adds, 32 lanes: %.3f ms; "
+          "FP64/FP32 %.0fx" % (d32, d1, f32, d32 / f32))
+    assert d32 > 8 * f32          # FP64 is a small fraction of FP32
+    assert d1 > 0.5 * d32         # one active lane costs (almost) a whole warp
