@@ -262,9 +262,10 @@ def ess_comparison(g, stream, dev):
     res["rw_adapted"] = arm(s, w["rw_steps"], 2, state, {"sd_median": float(np.median(sc)), "target": 0.234})
     t_rw = res["rw_adapted"]["seconds"]
     s.close()
-    # HMC with the workload's 8 leapfrog steps, with 32 (longer trajectories cross the
+    # HMC with the workload's 8 leapfrog steps, with 32 and 64 (longer trajectories cross the
     # correlated posterior of the rational model's coefficients in fewer MH steps), and MALA
-    for name, L, tgt, adapt_steps in (("hmc_L8", 8, 0.8, 150), ("hmc_L32", 32, 0.65, 40), ("mala", 1, 0.574, 600)):
+    for name, L, tgt, adapt_steps in (("hmc_L8", 8, 0.8, 150), ("hmc_L32", 32, 0.65, 40), ("hmc_L64", 64, 0.65, 20),
+                                      ("mala", 1, 0.574, 600)):
         s = sampler("hmc", eps=0.0005, L=L)
         s.set_state(*state)
         s.autotune(steps=20, seed=77)          # CTA shape against L1 for the gradient tapes
@@ -286,7 +287,7 @@ def ess_comparison(g, stream, dev):
     steps = max(30, int(t_rw / (dt / 20)))
     res["hmc_L8_eps0.01"] = arm(s, steps, 3, state, {"leapfrog_steps": 8, "eps": 0.01, "adapted": False})
     s.close()
-    arms = ("hmc_L8", "hmc_L32", "mala")
+    arms = ("hmc_L8", "hmc_L32", "hmc_L64", "mala")
     best_arm = max(arms, key=lambda a: res[a]["ess_per_s"])
     rw_ad = res["rw_adapted"]["ess_per_s"]
     return {"workload": "rational-65k", "N": N, "PL": PL, "nd": w["nd"], "constants": 5,
