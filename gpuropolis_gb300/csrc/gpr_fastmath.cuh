@@ -47,40 +47,45 @@ __device__ __forceinline__ float gx_scale2(float r, float n) {
     return (r * __int_as_float((n1 + 127) << 23)) * __int_as_float((n2 + 127) << 23);
 }
 
+/* The routines below are branch-free: each computes its general case on a
+ * sanitised argument and selects the special values afterwards, so the
+ * interpreter's unrolled lanes never diverge on them. */
+
 /* 2^t for t = th + tl (double-float), |tl| <= ulp(th) */
 __device__ __forceinline__ float gx_exp2_df(float th, float tl) {
-    if (!(th > -200.0f)) return (th != th) ? th : 0.0f;
-    if (!(th < 200.0f)) return (th != th) ? th : INFINITY;
-    const float n = rintf(th);
-    const float f = (th - n) + tl;        /* th - n is exact */
-    return gx_scale2(gx_ex2_approx(f), n);
+    const float thc = fminf(fmaxf(th, -200.0f), 200.0f);   /* NaN -> -200; the result is replaced */
+    const float n = rintf(thc);
+    const float f = (thc - n) + tl;       /* thc - n is exact */
+    const float r = gx_scale2(gx_ex2_approx(f), n);
+    return (th != th) ? th : (th > -200.0f ? (th < 200.0f ? r : INFINITY) : 0.0f);
 }
 
 __device__ __forceinline__ float gx_exp(float x) {
     const float L2E_HI = 1.44269502162933349609375f;      /* float(log2 e) */
     const float L2E_LO = 1.925963033500011079e-08f;       /* log2 e - L2E_HI */
-    if (x != x) return x;
     const float th = x * L2E_HI;
     const float tl = fmaf(x, L2E_HI, -th) + x * L2E_LO;    /* exact product error + low part */
-    return gx_exp2_df(th, tl);
+    const float r = gx_exp2_df(th, tl);
+    return (x != x) ? x : r;
 }
 
 /* Split x > 0 (finite) into 2^e * m, m in [sqrt(1/2), sqrt(2)). */
 __device__ __forceinline__ float gx_frexp_sqrt2(float x, int& e) {
-    uint32_t b = __float_as_uint(x);
-    e = 0;
-    if (b < 0x00800000u) { x *= 8388608.0f; b = __float_as_uint(x); e = -23; }
-    e += (int)((b >> 23) & 0xffu) - 127;
+    const bool sub = __float_as_uint(x) < 0x00800000u;      /* subnormal: scale by 2^23 (exact) */
+    const uint32_t b = __float_as_uint(sub ? x * 8388608.0f : x);
+    e = (int)((b >> 23) & 0xffu) - 127 - (sub ? 23 : 0);
     float m = __uint_as_float((b & 0x007fffffu) | 0x3f800000u);
-    if (m > 1.41421356f) { m *= 0.5f; e += 1; }
+    const bool hi = m > 1.41421356f;
+    m = hi ? m * 0.5f : m;
+    e += hi ? 1 : 0;
     return m;
 }
 
 __device__ __forceinline__ float gx_log(float x) {
-    if (!(x > 0.0f)) return (x == 0.0f) ? -INFINITY : __int_as_float(0x7fc00000);
-    if (x == INFINITY) return x;
+    const bool ok = x > 0.0f && x < INFINITY;
+    const float xs = ok ? x : 1.0f;
     int e;
-    const float m = gx_frexp_sqrt2(x, e);
+    const float m = gx_frexp_sqrt2(xs, e);
     const float num = m - 1.0f;                       /* exact */
     const float den = m + 1.0f;
     float q = num * gx_rcp_approx(den);
@@ -92,7 +97,8 @@ __device__ __forceinline__ float gx_log(float x) {
     const float tq = 2.0f * q;
     const float lm = fmaf(tq * s2, p, tq);
     const float fe = (float)e;
-    return fmaf(fe, 0.693145751953125f, fmaf(fe, 1.42860682030941723212e-6f, lm));
+    const float r = fmaf(fe, 0.693145751953125f, fmaf(fe, 1.42860682030941723212e-6f, lm));
+    return ok ? r : (x > 0.0f ? x : (x == 0.0f ? -INFINITY : __int_as_float(0x7fc00000)));
 }
 
 /* log2(x) for finite x > 0 as a double-float (hi, lo). */
@@ -138,30 +144,25 @@ __device__ __forceinline__ void gx_log2_df(float x, float& hi, float& lo) {
 }
 
 __device__ __forceinline__ float gx_pow(float a, float b) {
-    if (b == 0.0f || a == 1.0f) return 1.0f;
-    if (a != a || b != b) return a + b;               /* NaN */
     const float fa = fabsf(a);
     const bool b_int = (truncf(b) == b);
     const bool b_odd = b_int && fabsf(b) < 16777216.0f && (((int)b) & 1);
-    if (isinf(b)) {
-        if (fa == 1.0f) return 1.0f;
-        return ((fa < 1.0f) == (b < 0.0f)) ? INFINITY : 0.0f;
-    }
-    float r;
-    if (fa == 0.0f) {
-        r = (b < 0.0f) ? INFINITY : 0.0f;
-    } else if (fa == INFINITY) {
-        r = (b < 0.0f) ? 0.0f : INFINITY;
-    } else if (a < 0.0f && !b_int) {
-        return __int_as_float(0x7fc00000);
-    } else {
-        float lh, ll;
-        gx_log2_df(fa, lh, ll);
-        const float th = b * lh;
-        const float tl = fmaf(b, lh, -th) + b * ll;
-        r = gx_exp2_df(th, tl);
-    }
-    return (a < 0.0f || (a == 0.0f && __float_as_uint(a) != 0u)) && b_odd ? -r : r;
+    /* the general case, 2^(b log2|a|), on a finite nonzero |a| and a finite b */
+    const bool gen = fa > 0.0f && fa < INFINITY;
+    const float fs = gen ? fa : 1.0f;
+    const float bs = isfinite(b) ? b : 0.0f;
+    float lh, ll;
+    gx_log2_df(fs, lh, ll);
+    const float th = bs * lh;
+    const float tl = fmaf(bs, lh, -th) + bs * ll;
+    float r = gx_exp2_df(th, tl);
+    /* C99 Annex F special values, in order of precedence (the last select wins) */
+    r = (fa == 0.0f) ? ((b < 0.0f) ? INFINITY : 0.0f) : (fa == INFINITY ? ((b < 0.0f) ? 0.0f : INFINITY) : r);
+    r = ((a < 0.0f || (a == 0.0f && __float_as_uint(a) != 0u)) && b_odd) ? -r : r;
+    r = (gen && a < 0.0f && !b_int) ? __int_as_float(0x7fc00000) : r;
+    r = isinf(b) ? (fa == 1.0f ? 1.0f : (((fa < 1.0f) == (b < 0.0f)) ? INFINITY : 0.0f)) : r;
+    r = (a != a || b != b) ? a + b : r;                /* NaN */
+    return (b == 0.0f || a == 1.0f) ? 1.0f : r;
 }
 
 }  // namespace gpr
