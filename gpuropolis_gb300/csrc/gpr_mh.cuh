@@ -56,16 +56,14 @@ struct df {
 
 __device__ __forceinline__ df df_make(float hi, float lo) { df r; r.hi = hi; r.lo = lo; return r; }
 __device__ __forceinline__ df df_neg(df a) { return df_make(-a.hi, -a.lo); }
-/* Branch-free: a non-finite sum of the high parts is the result, with a
- * zero low part (the error terms are then NaN and are discarded). */
 __device__ __forceinline__ df df_add(df a, df b) {
     const float s = __fadd_rn(a.hi, b.hi);
+    if (!isfinite(s)) return df_make(s, 0.0f);
     const float v = __fsub_rn(s, a.hi);
     float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, v)), __fsub_rn(b.hi, v));
     e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
     const float h = __fadd_rn(s, e);
-    const bool fin = isfinite(s);
-    return df_make(fin ? h : s, fin ? __fsub_rn(e, __fsub_rn(h, s)) : 0.0f);
+    return df_make(h, __fsub_rn(e, __fsub_rn(h, s)));
 }
 __device__ __forceinline__ df df_sub(df a, df b) { return df_add(a, df_neg(b)); }
 __device__ __forceinline__ bool df_invalid(df a) { return !isfinite(a.hi); }
@@ -824,6 +822,27 @@ __device__ __forceinline__ bool eval_pass_chunks(const PR prog, float* stk, floa
 /* S of an invalid likelihood (-inf, main.cu:459,462). */
 __device__ __forceinline__ df lik_invalid() { return df_make(INFINITY, 0.0f); }
 
+/* S of one program evaluated by one warp: the double-float sum of its chunk
+ * sums in chunk order, or +inf when any point is invalid. */
+template <int K, bool ONEPASS, bool ROLLED, int NV, bool STREAM, class PR>
+__device__ __forceinline__ df eval_loglik_S(const PR prog, float* stk, float* scr, const LaneData<K>& ld,
+                                            const DataView& dv, const KParams& p, int lane, int& pts) {
+    const int npass = ONEPASS ? 1 : (dv.nd + 32 * K - 1) / (32 * K);
+    const int nch = chunk_count(dv.nd);
+    df S = df_make(0.0f, 0.0f);
+#pragma unroll 1
+    for (int pass = 0; pass < npass; ++pass) {
+        float cs[K / 4];
+        const bool bad = eval_pass_chunks<K, ONEPASS, ROLLED, NV, STREAM>(prog, stk, scr, ld, dv, p, lane, pass, cs);
+        pts += ONEPASS ? dv.nd : min(32 * K, dv.nd - pass * 32 * K);
+        if (bad) return lik_invalid();
+#pragma unroll
+        for (int j = 0; j < K / 4; ++j)
+            if (pass * (K / 4) + j < nch) S = df_add(S, df_make(cs[j], 0.0f));
+    }
+    return S;
+}
+
 /* The log-likelihood (main.cu:454-468) of a chain with sum S, in FP64, for
  * the scores a block writes: -S 2^e - the normalising sum. */
 __device__ __forceinline__ double lik_of(df S, const DataView& dv, const KParams& p) {
@@ -1525,10 +1544,6 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
           }
           df S = df_make(0.0f, 0.0f);
           int pts = 0;
-          /* Evaluation tasks: balanced, the CTA's (chain, pass) pool, most
-           * expensive programs first; otherwise this warp's own passes in
-           * order.  One loop, so the kernel holds one copy of the interpreter. */
-          int my_rank = 64, ntasks = 0;
           if (balanced) {
             if (lane == 0) {
                 s_prog[warp] = ws.eprog;
@@ -1540,8 +1555,8 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
             if (threadIdx.x == 0) s_next = 0;
             __syncthreads();
             GPR_PH(GPR_PH_BAR1);
-            /* rank of this lane's chain (lane < nwarps) by estimated cost, most expensive first */
-            int nact = 0;
+            /* rank of this lane's chain (lane < nwarps) by program length, longest first */
+            int my_rank = 64, nact = 0;
             {
                 const int cl = lane < nwarps ? s_cost[lane] : -1;
                 int rk = 0;
@@ -1552,53 +1567,33 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                 }
                 if (cl >= 0) my_rank = rk;
             }
-            ntasks = nact * npass;
+            const int ntasks = nact * npass;
             GPR_PH(GPR_PH_RANK);
-          } else {
-            ntasks = active ? npass : 0;
-          }
-          bool own_bad = false;
 #pragma unroll 1
-          for (int tn = 0;; ++tn) {
-                int t = tn;
-                if (balanced) {
-                    if (lane == 0) t = atomicAdd(&s_next, 1);
-                    t = __shfl_sync(FULLMASK, t, 0);
-                }
+            for (;;) {
+                int t = 0;
+                if (lane == 0) t = atomicAdd(&s_next, 1);
+                t = __shfl_sync(FULLMASK, t, 0);
                 if (t >= ntasks) break;
-                int w = warp, pass = t;
-                const uint2* prog = ws.eprog;
-                if (balanced) {
-                    /* task t: pass t mod npass of the chain of rank t / npass (exact for t < 2^16) */
-                    const int q = (int)__fmul_rz(__int2float_rn(t) + 0.5f, inv_npass);
-                    pass = t - q * npass;
-                    w = __ffs(__ballot_sync(FULLMASK, my_rank == q)) - 1;
-                    if (s_bad[w]) continue;
-                    prog = s_prog[w];
-                }
+                /* task t: pass t mod npass of the chain of rank t / npass (exact for t < 2^16) */
+                const int q = (int)__fmul_rz(__int2float_rn(t) + 0.5f, inv_npass), pass = t - q * npass;
+                const int w = __ffs(__ballot_sync(FULLMASK, my_rank == q)) - 1;
+                if (s_bad[w]) continue;
                 float csum[K / 4];
-                const bool anybad = eval_pass_chunks<K, ONEPASS, ROLLED, NV, STREAM>(prog, ws.stk, ws.scr, ld,
+                const bool anybad = eval_pass_chunks<K, ONEPASS, ROLLED, NV, STREAM>(s_prog[w], ws.stk, ws.scr, ld,
                                                                                    dv, p, lane, pass, csum);
                 const int np = ONEPASS ? dv.nd : min(32 * K, dv.nd - pass * 32 * K);
                 pts += np;
-                st_np += (unsigned long long)((balanced ? s_count[w] : count) + 4) * (unsigned)np;
-                GPR_PH_COUNT(GPR_PH_NPASSES, 1);
-                GPR_PH_COUNT(GPR_PH_NINSTR, balanced ? s_ninstr[w] : ninstr);
-                if (balanced) {
-                    if (lane == 0) {
+                if (lane == 0) {
 #pragma unroll
-                        for (int j = 0; j < K / 4; ++j) s_part[w][pass * (K / 4) + j] = csum[j];
-                        if (anybad) s_bad[w] = 1;
-                    }
-                } else {
-                    if (anybad) { own_bad = true; break; }
-#pragma unroll
-                    for (int j = 0; j < K / 4; ++j)
-                        if (pass * (K / 4) + j < nch) S = df_add(S, df_make(csum[j], 0.0f));
+                    for (int j = 0; j < K / 4; ++j) s_part[w][pass * (K / 4) + j] = csum[j];
+                    if (anybad) s_bad[w] = 1;
                 }
-          }
-          GPR_PH(GPR_PH_EVAL);
-          if (balanced) {
+                st_np += (unsigned long long)(s_count[w] + 4) * (unsigned)np;
+                GPR_PH_COUNT(GPR_PH_NPASSES, 1);
+                GPR_PH_COUNT(GPR_PH_NINSTR, s_ninstr[w]);
+            }
+            GPR_PH(GPR_PH_EVAL);
             __syncthreads();
             GPR_PH(GPR_PH_BAR2);
             if (active) {
@@ -1609,8 +1604,12 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                 }
             }
             GPR_PH(GPR_PH_COMBINE);
-          } else if (own_bad) {
-            S = lik_invalid();
+          } else if (active) {
+            S = eval_loglik_S<K, ONEPASS, ROLLED, NV, STREAM>(ws.eprog, ws.stk, ws.scr, ld, dv, p, lane, pts);
+            st_np += (unsigned long long)(count + 4) * (unsigned)pts;
+            GPR_PH_COUNT(GPR_PH_NPASSES, npass);
+            GPR_PH_COUNT(GPR_PH_NINSTR, (unsigned long long)ninstr * npass);
+            GPR_PH(GPR_PH_EVAL);
           }
           st_pts += (unsigned)pts;
           if (active) {
