@@ -1044,6 +1044,7 @@ __device__ void constant_move(Rng& r, const WarpSmem& w, const float* Cold, floa
     /* the LCG state after the last constant's draws: the stream's state once
      * the offsets have converged */
     uint32_t endst = 0u;
+    bool all_nominal = true;   /* this lane's constants drew exactly `nominal` each */
     {
         uint32_t st = (lj.a * r.s + lj.c) & 0x7fffffffu;
 #pragma unroll 1
@@ -1056,12 +1057,21 @@ __device__ void constant_move(Rng& r, const WarpSmem& w, const float* Cold, floa
             propose_constant<RNG>(rc, Cold[c], nc, dfw, dbw, p, rw_sd);
             Cnew[c] = nc; w.fw[c] = dfw; w.bw[c] = dbw; w.ndr[c] = (int)rc.drawn;
             w.off[c] = nominal * c;
+            all_nominal = all_nominal && rc.drawn == (uint32_t)nominal;
             if (c == PL - 1) endst = rc.s;
             st = (lj.sa * st + lj.sc) & 0x7fffffffu;
         }
     }
     __syncwarp();
     bool converged = false;
+    /* The usual case (random_int rejects a draw with probability about 1e-6):
+     * every constant drew its nominal count, so the nominal offsets are the
+     * true ones and the stream continues after the last constant's draws. */
+    if (__all_sync(FULLMASK, all_nominal)) {
+        if (RNG == 0) r.s = __shfl_sync(FULLMASK, endst, (PL - 1) & 31);
+        else rng_jump<RNG>(r, (uint32_t)(nominal * PL), p);
+        converged = true;
+    }
 #pragma unroll 1
     for (int iter = 0; iter <= PL && !converged; ++iter) {
         /* redo the constants whose offset moved (marked ndr < 0) */
@@ -1324,14 +1334,36 @@ __device__ __forceinline__ void structure_move(Rng& r, const uint8_t* oc, uint8_
 #define GPR_MIN_CTAS 3
 #endif
 
+/* The SM clock, read by an asm statement with a memory clobber: the compiler
+ * keeps it in program order with the barriers and the shared-memory accesses
+ * around it, so a mark after a __syncthreads() counts the barrier's wait. */
+__device__ __forceinline__ long long ph_clock() {
+    long long t;
+    asm volatile("mov.u64 %0, %%clock64;" : "=l"(t) :: "memory");
+    return t;
+}
+
 /* Phase timing of the instrumented builds (PROF): lane 0 of each warp adds
- * the clock64 cycles since the last mark to the warp's counter `i`. */
+ * the clock cycles since the last mark to the warp's counter `i`. */
 #define GPR_PH(i)                                                                     \
     do {                                                                              \
         if constexpr (PROF) {                                                         \
-            const long long t_ = clock64();                                           \
+            const long long t_ = ph_clock();                                          \
             if (lane == 0) s_ph[warp][(i)] += (unsigned long long)(t_ - ph_t);         \
             ph_t = t_;                                                                \
+        }                                                                             \
+    } while (0)
+/* A CTA barrier followed by a mark; the instrumented builds read the clock in
+ * the same asm statement as the barrier, right after it. */
+#define GPR_SYNC_PH(i)                                                                \
+    do {                                                                              \
+        if constexpr (PROF) {                                                         \
+            long long t_;                                                             \
+            asm volatile("bar.sync 0;\n\tmov.u64 %0, %%clock64;" : "=l"(t_) :: "memory"); \
+            if (lane == 0) s_ph[warp][(i)] += (unsigned long long)(t_ - ph_t);         \
+            ph_t = t_;                                                                \
+        } else {                                                                      \
+            __syncthreads();                                                          \
         }                                                                             \
     } while (0)
 #define GPR_PH_COUNT(i, v)                                                            \
@@ -1372,7 +1404,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
     if constexpr (PROF) {
         for (int i = threadIdx.x; i < 8 * GPR_PH_SLOTS; i += blockDim.x) (&s_ph[0][0])[i] = 0ull;
         __syncthreads();
-        ph_t = clock64();
+        ph_t = ph_clock();
     }
 
     /* CTA-shared dataset (or the device arrays when streamed); with batched
@@ -1562,8 +1594,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                 s_bad[warp] = 0;
             }
             if (threadIdx.x == 0) s_next = 0;
-            __syncthreads();
-            GPR_PH(GPR_PH_BAR1);
+            GPR_SYNC_PH(GPR_PH_BAR1);
             /* rank of this lane's chain (lane < nwarps) by program length, longest first */
             int my_rank = 64, nact = 0;
             {
@@ -1603,8 +1634,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                 GPR_PH_COUNT(GPR_PH_NINSTR, s_ninstr[w]);
             }
             GPR_PH(GPR_PH_EVAL);
-            __syncthreads();
-            GPR_PH(GPR_PH_BAR2);
+            GPR_SYNC_PH(GPR_PH_BAR2);
             if (active) {
                 if (s_bad[warp]) {
                     S = lik_invalid();

@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_pipe_kernel(const __grid
     if constexpr (PROF) {
         for (int i = threadIdx.x; i < 8 * GPR_PH_SLOTS; i += blockDim.x) (&s_ph[0][0])[i] = 0ull;
         __syncthreads();
-        ph_t = clock64();
+        ph_t = ph_clock();
     }
 
     uint64_t* bar = (uint64_t*)smem;
@@ -392,8 +392,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_pipe_kernel(const __grid
                 }
                 GPR_PH(GPR_PH_EVAL);
             }
-            __syncthreads();
-            GPR_PH(GPR_PH_BAR1);
+            GPR_SYNC_PH(GPR_PH_BAR1);
         }
     }
     if (lane == 0 && p.stats) {
