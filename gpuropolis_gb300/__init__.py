@@ -99,6 +99,8 @@ def library():
     lib.gpr_reset_stats.argtypes = [vp]
     lib.gpr_set_scores.argtypes = [vp, vp, vp]
     lib.gpr_set_moves.argtypes = [vp, ip, fp, ip]
+    lib.gpr_set_hmc_jitter.argtypes = [vp, fp, fp]
+    lib.gpr_run_block_traced_first.argtypes = [vp, ip, ip, ip, ip, vp]
     lib.gpr_set_hmc_layout.argtypes = [vp, ip, ip]
     lib.gpr_set_streaming.argtypes = [vp, ip]
     lib.gpr_layout_streamed.argtypes = [vp]
@@ -340,6 +342,12 @@ class Sampler:
     def set_moves(self, struct_every=5, hmc_eps=0.01, hmc_steps=8):
         self._check(self.lib.gpr_set_moves(self.h, int(struct_every), float(hmc_eps), int(hmc_steps)))
 
+    def set_hmc_jitter(self, eps_frac=0.0, len_frac=0.0):
+        """Per-move jitter of the Hamiltonian trajectories: step x U(1 -
+        eps_frac, 1 + eps_frac), leapfrog count uniform in [L(1 - len_frac),
+        L(1 + len_frac)]."""
+        self._check(self.lib.gpr_set_hmc_jitter(self.h, float(eps_frac), float(len_frac)))
+
     def set_streaming(self, always=True):
         self._check(self.lib.gpr_set_streaming(self.h, int(bool(always))))
 
@@ -361,11 +369,13 @@ class Sampler:
         self._check(self.lib.gpr_loglik_grad(self.h, _ptr(grad), _ptr(lik)))
         return grad, lik
 
-    def run_block_traced(self, steps, seed, trace_n):
+    def run_block_traced(self, steps, seed, trace_n, chains=None):
         """run_block, returning the first trace_n constants after every step:
-        an array (N, steps, trace_n)."""
-        tr = np.empty((self.N, steps, trace_n), np.float32)
-        self._check(self.lib.gpr_run_block_traced(self.h, int(steps), int(seed), int(trace_n), _ptr(tr)))
+        an array (chains, steps, trace_n) of the first `chains` chains (all
+        N by default; every chain steps either way)."""
+        n = self.N if chains is None else int(chains)
+        tr = np.empty((n, steps, trace_n), np.float32)
+        self._check(self.lib.gpr_run_block_traced_first(self.h, int(steps), int(seed), int(trace_n), n, _ptr(tr)))
         return tr
 
     def set_scores(self, prior, lik):

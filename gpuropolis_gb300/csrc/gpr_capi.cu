@@ -325,6 +325,8 @@ int gpr_create(const gpr_config* cfg, int n_chains, gpr_handle** out) {
     kp.struct_every = 5;                                           /* main.cu:699 */
     kp.hmc_eps = 0.01f;
     kp.hmc_L = 8;
+    kp.hmc_jit_eps = 0.0f;
+    kp.hmc_jit_len = 0.0f;
     kp.max_instr = GPR_MAX_INSTR(PL);
     /* Value-stack depth: a push happens at a binary node whose children are
      * both subtrees, so at a node j <= PL/2; pending pushes lie on one
@@ -1187,6 +1189,18 @@ int gpr_set_moves(gpr_handle* h, int struct_every, float hmc_eps, int hmc_steps)
     return GPR_OK;
 }
 
+int gpr_set_hmc_jitter(gpr_handle* h, float eps_frac, float len_frac) {
+    if (!h) return GPR_ERR_ARG;
+    if (!(eps_frac >= 0.0f && eps_frac < 1.0f))
+        return fail(h, GPR_ERR_ARG, "eps_frac must be in [0, 1) (got %g)", (double)eps_frac);
+    if (!(len_frac >= 0.0f && len_frac <= 1.0f))
+        return fail(h, GPR_ERR_ARG, "len_frac must be in [0, 1] (got %g)", (double)len_frac);
+    drop_graph(h);
+    h->kp.hmc_jit_eps = eps_frac;
+    h->kp.hmc_jit_len = len_frac;
+    return GPR_OK;
+}
+
 int gpr_adapt_scales(gpr_handle* h, float target_accept) {
     if (!h) return GPR_ERR_ARG;
     if (!(target_accept >= 0.0f && target_accept < 1.0f))
@@ -1259,20 +1273,25 @@ int gpr_loglik_grad(gpr_handle* h, double* grad, double* likelihood) {
     return gpr_sync(h);
 }
 
-int gpr_run_block_traced(gpr_handle* h, int steps, int random_seed, int trace_n, float* trace) {
+int gpr_run_block_traced_first(gpr_handle* h, int steps, int random_seed, int trace_n, int n_chains,
+                               float* trace) {
     if (!h) return GPR_ERR_ARG;
     if (steps < 1) return fail(h, GPR_ERR_ARG, "steps must be >= 1 (got %d)", steps);
     if (trace_n < 1 || trace_n > 32 || trace_n > h->PL || !trace)
         return fail(h, GPR_ERR_ARG, "trace_n must be in [1, min(32, program_length)] with a buffer");
+    if (n_chains < 1 || n_chains > h->N)
+        return fail(h, GPR_ERR_ARG, "n_chains must be in [1, %d] (got %d)", h->N, n_chains);
     CUDA_TRY(h, cudaSetDevice(h->device));
-    const size_t cnt = (size_t)h->N * (size_t)steps * (size_t)trace_n;
+    const size_t cnt = (size_t)n_chains * (size_t)steps * (size_t)trace_n;
     float* dt = nullptr;
     CUDA_TRY(h, cudaMalloc(&dt, cnt * sizeof(float)));
     h->kp.trace = dt;
     h->kp.trace_n = trace_n;
+    h->kp.trace_chains = n_chains;
     int rc = run(h, steps, random_seed);
     h->kp.trace = nullptr;
     h->kp.trace_n = 0;
+    h->kp.trace_chains = 0;
     cudaError_t e = cudaSuccess;
     if (rc == GPR_OK) e = cudaMemcpyAsync(trace, dt, cnt * sizeof(float), cudaMemcpyDeviceToHost, h->stream);
     if (rc == GPR_OK && e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
@@ -1280,6 +1299,11 @@ int gpr_run_block_traced(gpr_handle* h, int steps, int random_seed, int trace_n,
     if (rc != GPR_OK) return rc;
     if (e != cudaSuccess) return fail(h, GPR_ERR_CUDA, "gpr_run_block_traced: %s", cudaGetErrorString(e));
     return gpr_sync(h);
+}
+
+int gpr_run_block_traced(gpr_handle* h, int steps, int random_seed, int trace_n, float* trace) {
+    if (!h) return GPR_ERR_ARG;
+    return gpr_run_block_traced_first(h, steps, random_seed, trace_n, h->N, trace);
 }
 
 /* ---- selection over posteriors (gpr_resample.cu) ---- */
@@ -1547,6 +1571,8 @@ static void noalloc_params(gpr::KParams& kp, const gpr_config* cfg, int n_chains
     kp.struct_every = 5;
     kp.hmc_eps = 0.01f;
     kp.hmc_L = 8;
+    kp.hmc_jit_eps = 0.0f;
+    kp.hmc_jit_len = 0.0f;
     kp.max_instr = GPR_MAX_INSTR(PL);
     int lev = 1;
     while ((1 << lev) <= PL / 2) ++lev;

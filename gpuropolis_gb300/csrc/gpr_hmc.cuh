@@ -392,6 +392,15 @@ __device__ __forceinline__ float hmc_momentum(uint32_t seed, uint32_t chain, uin
     return __fmul_rn(a, gpr_rng_sinf(gpr_rng_twopi_times(u2)));
 }
 
+/* Two uniforms in [0, 1) for move t of a chain's trajectory jitter, from the
+ * momentum's Philox stream at a counter the momenta never use. */
+__device__ __forceinline__ void hmc_jitter_uniforms(uint32_t seed, uint32_t chain, uint32_t t, float& u1, float& u2) {
+    uint32_t c[4] = {t, 0xffffffffu, 0x4a4954u, 0u};
+    gpr_philox4x32_10(c, seed ^ 0x484d43u, chain);
+    u1 = __fmul_rn((float)(c[0] >> 8), 5.9604644775390625e-08f);
+    u2 = __fmul_rn((float)(c[1] >> 8), 5.9604644775390625e-08f);
+}
+
 /* ------------------------------------------------------------------------ */
 /* d loglik / d C for every chain's current state (gpr_loglik_grad): one warp
  * per chain, grad[i*N + chain] (double, unscaled) and lik[chain]. */
@@ -535,7 +544,21 @@ __global__ void __launch_bounds__(128) mh_hmc_kernel(const __grid_constant__ KPa
                 /* ---- Hamiltonian constant move ---- */
                 st_cp++;
                 if (!df_invalid(cur_post)) {
-                    const float eps = expf(log_eps), heps = __fmul_rn(0.5f, eps);
+                    float eps = expf(log_eps);
+                    int nleap = p.hmc_L;
+                    if (p.hmc_jit_eps > 0.0f || p.hmc_jit_len > 0.0f) {
+                        /* this move's trajectory: jittered step and leapfrog count */
+                        float ue, ul;
+                        hmc_jitter_uniforms(seed, (uint32_t)chain, (uint32_t)step, ue, ul);
+                        eps = __fmul_rn(eps, __fadd_rn(1.0f, __fmul_rn(p.hmc_jit_eps, __fsub_rn(__fmul_rn(2.0f, ue), 1.0f))));
+                        if (p.hmc_jit_len > 0.0f) {
+                            const float L = (float)p.hmc_L;
+                            const int lo = max(1, __float2int_rn(__fmul_rn(L, __fsub_rn(1.0f, p.hmc_jit_len))));
+                            const int hi = max(lo, __float2int_rn(__fmul_rn(L, __fadd_rn(1.0f, p.hmc_jit_len))));
+                            nleap = lo + min((int)__fmul_rn(ul, (float)(hi - lo + 1)), hi - lo);
+                        }
+                    }
+                    const float heps = __fmul_rn(0.5f, eps);
                     /* the last structure step may have left match[] for a
                      * rejected proposal: rebuild it for the current program */
                     pop_match(ws.prog[cur], cur_ninstr, ws.match, lane);
@@ -552,7 +575,7 @@ __global__ void __launch_bounds__(128) mh_hmc_kernel(const __grid_constant__ KPa
                     df lik = df_make(-INFINITY, 0.0f);
                     bool ok = true;
 #pragma unroll 1
-                    for (int l = 1; l <= p.hmc_L && ok; ++l) {
+                    for (int l = 1; l <= nleap && ok; ++l) {
                         bool fin = true;
                         for (int i = lane; i < PL; i += 32) {
                             q[i] = __fadd_rn(q[i], __fmul_rn(eps, ws.mom[i]));
@@ -569,7 +592,7 @@ __global__ void __launch_bounds__(128) mh_hmc_kernel(const __grid_constant__ KPa
                         st_evals++; st_nodes += (unsigned)cur_count;
                         st_np += (unsigned long long)(cur_count + 4) * (unsigned)pe;
                         if (df_invalid(lik)) { ok = false; break; }
-                        const float f = l < p.hmc_L ? eps : heps;
+                        const float f = l < nleap ? eps : heps;
                         for (int i = lane; i < PL; i += 32) {
                             const float gt = __fadd_rn(__fmul_rn(ws.gnew[i], unscale), dcauchy(q[i]));
                             ws.gnew[i] = gt;
@@ -610,7 +633,7 @@ __global__ void __launch_bounds__(128) mh_hmc_kernel(const __grid_constant__ KPa
                     __syncwarp();
                 }
             }
-            if (p.trace && !init && lane < p.trace_n)
+            if (p.trace && !init && lane < p.trace_n && chain < p.trace_chains)
                 p.trace[((size_t)chain * p.steps + step) * p.trace_n + lane] = ws.Cs[ccur][lane];
         }
 

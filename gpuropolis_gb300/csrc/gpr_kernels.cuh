@@ -105,9 +105,13 @@ struct KParams {
     int struct_every;  /* a structure move every this many steps (main.cu:699: 5); 0 = never */
     float hmc_eps;     /* leapfrog step of the gradient constant moves          */
     int hmc_L;         /* leapfrog steps (1 = MALA)                             */
+    float hmc_jit_eps; /* each move's step: hmc step x U(1 - j, 1 + j); 0 = fixed */
+    float hmc_jit_len; /* each move's leapfrog count: uniform integer in
+                        * [L(1 - j), L(1 + j)] (rounded, >= 1); 0 = fixed     */
     float* trace;      /* optional: C[0..trace_n) of each chain after each step,
                         * trace[(chain * steps + step) * trace_n + i]             */
     int trace_n;       /* <= 32 */
+    int trace_chains;  /* only chains below this are traced                     */
     float* chain_scale;   /* optional: per-chain random-walk sd (const_mode 1) or
                            * leapfrog step (Hamiltonian moves), else rw_sd / hmc_eps */
     float adapt_target;   /* > 0: adapt chain_scale toward this acceptance rate

@@ -1671,7 +1671,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                 cur_prior = prior; cur_S = S;
             }
             __syncwarp();
-            if (p.trace && !init && lane < p.trace_n)
+            if (p.trace && !init && lane < p.trace_n && chain < p.trace_chains)
                 p.trace[((size_t)chain * p.steps + step) * p.trace_n + lane] = ws.Cs[ccur][lane];
           }
           GPR_PH(GPR_PH_ACCEPT);

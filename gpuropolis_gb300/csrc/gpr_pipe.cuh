@@ -243,7 +243,7 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_pipe_kernel(const __grid
                             cur_len = len; cur_count = count; cur_ninstr = ninstr; cur_cs = cs;
                             cur_prior = prior; cur_S = S;
                         }
-                        if (p.trace && !init && lane < p.trace_n)
+                        if (p.trace && !init && lane < p.trace_n && chain < p.trace_chains)
                             p.trace[((size_t)chain * p.steps + (step - 1)) * p.trace_n + lane] = wg.Cs[ccur][lane];
                         GPR_PH(GPR_PH_ACCEPT);
                     }

@@ -258,6 +258,15 @@ int gpr_reset_stats(gpr_handle* h);
  * constant proposals.  Defaults: 5, 0.01, 8. */
 int gpr_set_moves(gpr_handle* h, int struct_every, float hmc_eps, int hmc_steps);
 
+/* Trajectory jitter of the Hamiltonian constant moves: each move draws its
+ * leapfrog step as (the chain's) step x U(1 - eps_frac, 1 + eps_frac) and its
+ * leapfrog count uniformly from the integers in [L(1 - len_frac), L(1 +
+ * len_frac)] (rounded; at least 1), from a counter-based stream keyed by
+ * (seed, chain, step).  Randomising the trajectory keeps detailed balance
+ * and breaks the periodic orbits a fixed step x count can fall into on
+ * strongly correlated posteriors.  Defaults: 0, 0 (fixed trajectories). */
+int gpr_set_hmc_jitter(gpr_handle* h, float eps_frac, float len_frac);
+
 /* Per-chain proposal scales: with target_accept in (0, 1), the following
  * blocks adapt each chain's own random-walk sd (GPR_CONST_RANDOM_WALK:
  * Robbins-Monro on log sd) or leapfrog step (GPR_CONST_HMC: dual averaging,
@@ -280,6 +289,11 @@ int gpr_loglik_grad(gpr_handle* h, double* grad, double* likelihood);
  * constants of every chain: trace[(chain*steps + step)*trace_n + i] (host,
  * N*steps*trace_n floats).  For mixing measurements. */
 int gpr_run_block_traced(gpr_handle* h, int steps, int random_seed, int trace_n, float* trace);
+
+/* The same, recording only chains 0..n_chains-1 (all chains still step):
+ * trace[(chain*steps + step)*trace_n + i], n_chains*steps*trace_n floats. */
+int gpr_run_block_traced_first(gpr_handle* h, int steps, int random_seed, int trace_n, int n_chains,
+                               float* trace);
 
 /* ---- selection over the chains' posteriors, on the device ---- */
 

@@ -256,6 +256,27 @@ def test_ess_geyer_on_ar1():
     assert ess_geyer(np.ones((2, 100)))[0] == 0
 
 
+def test_population_ess_on_short_ar1_runs():
+    """Populations of stationary AR(1) chains (tau = (1 + a) / (1 - a)) whose
+    runs are 1.5 to 20 autocorrelation times long: the population estimator
+    stays within 12% of T / tau, where the per-chain estimator overestimates
+    the short runs by more than 2x."""
+    from gpuropolis_gb300.diagnostics import ess_geyer, ess_population
+    r = np.random.default_rng(1)
+    for a, T, m in ((0.9, 800, 200), (0.99, 3000, 400), (0.995, 1000, 800), (0.999, 3000, 1000)):
+        e = r.normal(size=(m, T))
+        x = np.empty_like(e)
+        x[:, 0] = e[:, 0] / np.sqrt(1 - a * a)
+        for t in range(1, T):
+            x[:, t] = a * x[:, t - 1] + e[:, t]
+        want = T * (1 - a) / (1 + a)
+        got = ess_population(x)
+        assert abs(got / want - 1) < 0.12, (a, T, got, want)
+        if T < 3 * (1 + a) / (1 - a):
+            assert np.median(ess_geyer(x)) > 2 * want
+    assert ess_population(np.ones((3, 50))) == 0.0
+
+
 def test_variable_leaves_need_three_variables():
     """x2/x3 leaf ops are refused for a univariate handle, before any device
     work; the op-code string prints the variable leaves as X, Y, Z."""
