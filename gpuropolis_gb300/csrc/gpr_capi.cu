@@ -849,7 +849,8 @@ int gpr_sync(gpr_handle* h) {
     if (flags) {
         cudaMemset(h->dcounter + 1, 0, sizeof(int));
         return fail(h, GPR_ERR_DEVICE, "kernel error flags 0x%x (1: dataset staging timed out, "
-                    "2: constant-proposal offsets did not converge)", flags);
+                    "2: constant-proposal offsets did not converge, 4: a consistency check of the phase-timed build "
+                    "failed)", flags);
     }
     return GPR_OK;
 }

@@ -1335,8 +1335,9 @@ __device__ __forceinline__ void structure_move(Rng& r, const uint8_t* oc, uint8_
 #endif
 
 /* The SM clock, read by an asm statement with a memory clobber: the compiler
- * keeps it in program order with the barriers and the shared-memory accesses
- * around it, so a mark after a __syncthreads() counts the barrier's wait. */
+ * keeps it in program order with the shared-memory accesses around it.  The
+ * hardware need not: a mark right after a __syncthreads() can be read before
+ * the warp stalls on the barrier, and that wait then counts in the next phase. */
 __device__ __forceinline__ long long ph_clock() {
     long long t;
     asm volatile("mov.u64 %0, %%clock64;" : "=l"(t) :: "memory");
@@ -1351,19 +1352,6 @@ __device__ __forceinline__ long long ph_clock() {
             const long long t_ = ph_clock();                                          \
             if (lane == 0) s_ph[warp][(i)] += (unsigned long long)(t_ - ph_t);         \
             ph_t = t_;                                                                \
-        }                                                                             \
-    } while (0)
-/* A CTA barrier followed by a mark; the instrumented builds read the clock in
- * the same asm statement as the barrier, right after it. */
-#define GPR_SYNC_PH(i)                                                                \
-    do {                                                                              \
-        if constexpr (PROF) {                                                         \
-            long long t_;                                                             \
-            asm volatile("bar.sync 0;\n\tmov.u64 %0, %%clock64;" : "=l"(t_) :: "memory"); \
-            if (lane == 0) s_ph[warp][(i)] += (unsigned long long)(t_ - ph_t);         \
-            ph_t = t_;                                                                \
-        } else {                                                                      \
-            __syncthreads();                                                          \
         }                                                                             \
     } while (0)
 #define GPR_PH_COUNT(i, v)                                                            \
@@ -1551,7 +1539,12 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
             bool need_compile = init, need_cauchy = init;
             if (structural) {
                 /* ---- structure move (main.cu:699-742) ---- */
-                forward = df_make(-p.logcount[cur_count], 0.0f);
+                int cc = cur_count;
+                if constexpr (PROF) {
+                    /* and that the chain's node count is in range */
+                    if ((unsigned)cc > (unsigned)PL) { if (lane == 0) atomicOr(p.err, 4); cc = 0; }
+                }
+                forward = df_make(-p.logcount[cc], 0.0f);
                 const bool cur_invalid = !(isfinite(cur_prior.hi) && isfinite(cur_S.hi));
                 structure_move<RNG>(r, ws.ops[cur], ws.ops[cur ^ 1], cur_invalid, p, s_lj[lane], lane);
                 pbuf = cur ^ 1;
@@ -1594,7 +1587,8 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                 s_bad[warp] = 0;
             }
             if (threadIdx.x == 0) s_next = 0;
-            GPR_SYNC_PH(GPR_PH_BAR1);
+            __syncthreads();
+            GPR_PH(GPR_PH_BAR1);
             /* rank of this lane's chain (lane < nwarps) by program length, longest first */
             int my_rank = 64, nact = 0;
             {
@@ -1618,6 +1612,10 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                 /* task t: pass t mod npass of the chain of rank t / npass (exact for t < 2^16) */
                 const int q = (int)__fmul_rz(__int2float_rn(t) + 0.5f, inv_npass), pass = t - q * npass;
                 const int w = __ffs(__ballot_sync(FULLMASK, my_rank == q)) - 1;
+                if constexpr (PROF) {
+                    /* the instrumented build checks that the task has a chain */
+                    if (w < 0) { if (lane == 0) atomicOr(p.err, 4); break; }
+                }
                 if (s_bad[w]) continue;
                 float csum[K / 4];
                 const bool anybad = eval_pass_chunks<K, ONEPASS, ROLLED, NV, STREAM>(s_prog[w], ws.stk, ws.scr, ld,
@@ -1634,7 +1632,8 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_block_kernel(const __gri
                 GPR_PH_COUNT(GPR_PH_NINSTR, s_ninstr[w]);
             }
             GPR_PH(GPR_PH_EVAL);
-            GPR_SYNC_PH(GPR_PH_BAR2);
+            __syncthreads();
+            GPR_PH(GPR_PH_BAR2);
             if (active) {
                 if (s_bad[warp]) {
                     S = lik_invalid();

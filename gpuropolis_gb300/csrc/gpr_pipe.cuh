@@ -392,7 +392,8 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_pipe_kernel(const __grid
                 }
                 GPR_PH(GPR_PH_EVAL);
             }
-            GPR_SYNC_PH(GPR_PH_BAR1);
+            __syncthreads();
+            GPR_PH(GPR_PH_BAR1);
         }
     }
     if (lane == 0 && p.stats) {

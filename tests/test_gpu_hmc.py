@@ -37,8 +37,11 @@ def _const_model(N, seed):
     return x, y, sd, P, C, grid, cdf
 
 
-@pytest.mark.parametrize("mode,eps,L", [("hmc", 0.03, 8), ("mala", 0.05, 1), ("rw", 0.1, 0)])
+@pytest.mark.parametrize("mode,eps,L", [("hmc", 0.03, 8), ("hmc_jitter", 0.03, 8), ("mala", 0.05, 1),
+                                        ("rw", 0.1, 0)])
 def test_constant_moves_keep_the_posterior(mode, eps, L):
+    """hmc_jitter draws each move's step from 0.03 x U(0.7, 1.3) and its
+    leapfrog count from [1, 16]."""
     N, steps = 8192, 60
     x, y, sd, P, C, grid, cdf = _const_model(N, seed=3)
     if mode == "rw":
@@ -47,6 +50,8 @@ def test_constant_moves_keep_the_posterior(mode, eps, L):
     else:
         s = g.Sampler(N, program_length=PL, const_proposal=g.CONST_HMC)
         s.set_moves(0, eps, L)
+        if mode == "hmc_jitter":
+            s.set_hmc_jitter(0.3, 1.0)
     try:
         s.set_data(x, y, sd)
         s.set_state(P, C)
@@ -106,3 +111,28 @@ def test_adapted_scales_reach_the_target_acceptance(mode, target):
     assert np.all(np.isfinite(sc)) and np.all(sc > 0)
     ks = stats.kstest(C1[0].astype(np.float64), lambda v: np.interp(v, grid, cdf))
     assert ks.pvalue > 1e-3, (mode, ks)
+
+
+def test_traced_first_chains_match_the_full_trace():
+    """gpr_run_block_traced_first records the first chains' constants exactly
+    as the full trace does, and every chain still steps."""
+    N, steps = 512, 12
+    x, y, sd, P, C, grid, cdf = _const_model(N, seed=4)
+    s = g.Sampler(N, program_length=PL, const_proposal=g.CONST_HMC)
+    try:
+        s.set_moves(0, 0.03, 4)
+        s.set_hmc_jitter(0.2, 0.5)
+        s.set_data(x, y, sd)
+        s.set_state(P, C)
+        full = s.run_block_traced(steps, 77, 3)
+        Cf = s.get_state()[1]
+        s.set_state(P, C)
+        part = s.run_block_traced(steps, 77, 3, chains=100)
+        Cp = s.get_state()[1]
+        with pytest.raises(g.GprError):
+            s.run_block_traced(steps, 77, 3, chains=N + 1)
+    finally:
+        s.close()
+    assert part.shape == (100, steps, 3)
+    assert np.array_equal(part.view(np.uint32), full[:100].view(np.uint32))
+    assert np.array_equal(Cp.view(np.uint32), Cf.view(np.uint32))
