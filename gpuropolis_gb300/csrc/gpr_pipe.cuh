@@ -122,7 +122,16 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_pipe_kernel(const __grid
             ld.valid |= (v ? 1u : 0u) << k;
         }
     }
-    const LaneJump ljump = make_lane_jump(p, lane);
+    /* Each lane's LCG jump maps (the same in every warp), read around each
+     * proposal instead of held in registers. */
+    __shared__ LaneJump s_lj[32];
+    if (warp == 0) s_lj[lane] = make_lane_jump(p, lane);
+    /* The block's counters (GPR_STAT_*), per warp in shared memory, added to
+     * p.stats once when the warp leaves (the first claim's barrier orders
+     * these stores before any use). */
+    __shared__ unsigned long long s_st[8][GPR_NSTATS];
+    for (int i = lane; i < GPR_NSTATS; i += 32) s_st[warp][i] = 0ull;
+#define ST_ADD(i, v) do { if (lane == 0) s_st[warp][(i)] += (unsigned long long)(v); } while (0)
 
     __shared__ PipeSlot s_slot[2][8];
     __shared__ const uint32_t* s_pp[2][8];   /* published program ...          */
@@ -154,8 +163,6 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_pipe_kernel(const __grid
         return &s_part[g][w][0];
     };
 
-    unsigned long long st_nodes = 0, st_np = 0, st_pts = 0;
-    int st_evals = 0, st_sp = 0, st_sa = 0, st_cp = 0, st_ca = 0;
     GPR_PH(GPR_PH_CLAIM);
 
 #pragma unroll 1
@@ -235,9 +242,10 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_pipe_kernel(const __grid
                                 log_sd = rm_update(log_sd, prob, p.adapt_target, n_cmoves++);
                                 rw_sd = expf(log_sd);
                             }
-                            if (structural) { st_sp++; st_sa += accept; } else { st_cp++; st_ca += accept; }
+                            if (structural) { ST_ADD(GPR_STAT_STRUCT_PROPOSED, 1); ST_ADD(GPR_STAT_STRUCT_ACCEPTED, accept); }
+                            else { ST_ADD(GPR_STAT_CONST_PROPOSED, 1); ST_ADD(GPR_STAT_CONST_ACCEPTED, accept); }
                         }
-                        st_evals++; st_nodes += (unsigned)count;
+                        ST_ADD(GPR_STAT_EVALS, 1); ST_ADD(GPR_STAT_EVAL_NODES, count);
                         if (accept) {
                             cur = pbuf; ccur = cbuf;
                             cur_len = len; cur_count = count; cur_ninstr = ninstr; cur_cs = cs;
@@ -273,14 +281,14 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_pipe_kernel(const __grid
                             /* ---- structure move (main.cu:699-742) ---- */
                             fw = df_make(-p.logcount[cur_count], 0.0f);
                             const bool cur_invalid = !(isfinite(cur_prior.hi) && isfinite(cur_S.hi));
-                            structure_move<RNG>(r, wg.ops[cur], wg.ops[cur ^ 1], cur_invalid, p, ljump, lane);
+                            structure_move<RNG>(r, wg.ops[cur], wg.ops[cur ^ 1], cur_invalid, p, s_lj[lane], lane);
                             pbuf = cur ^ 1; cbuf = ccur;
                             need_compile = true;
                             GPR_PH(GPR_PH_STRUCT);
                         } else if (!init) {
                             /* ---- constant move (main.cu:743-806) ---- */
                             df fws, bws;
-                            constant_move<RNG>(r, wg, wg.Cs[ccur], wg.Cs[ccur ^ 1], fws, bws, p, ljump, lane, rw_sd);
+                            constant_move<RNG>(r, wg, wg.Cs[ccur], wg.Cs[ccur ^ 1], fws, bws, p, s_lj[lane], lane, rw_sd);
                             if (p.const_mode == 0) { fw = df_add(fw, fws); bw = df_add(bw, bws); }
                             pbuf = cur; cbuf = ccur ^ 1;
                             len = cur_len; count = cur_count; ninstr = cur_ninstr;
@@ -387,8 +395,8 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_pipe_kernel(const __grid
                         GPR_PH_COUNT(GPR_PH_NINSTR, s_cost[e][w]);
                         if (bad) break;
                     }
-                    st_pts += (unsigned)np;
-                    st_np += (unsigned long long)(s_cnt[e][w] + 4) * (unsigned)np;
+                    ST_ADD(GPR_STAT_EVAL_POINTS, np);
+                    ST_ADD(GPR_STAT_EVAL_NODE_POINTS, (unsigned long long)(s_cnt[e][w] + 4) * (unsigned)np);
                 }
                 GPR_PH(GPR_PH_EVAL);
             }
@@ -396,16 +404,9 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_pipe_kernel(const __grid
             GPR_PH(GPR_PH_BAR1);
         }
     }
-    if (lane == 0 && p.stats) {
-        atomicAdd(&p.stats[GPR_STAT_EVALS], (unsigned long long)st_evals);
-        atomicAdd(&p.stats[GPR_STAT_EVAL_NODES], st_nodes);
-        atomicAdd(&p.stats[GPR_STAT_EVAL_POINTS], st_pts);
-        atomicAdd(&p.stats[GPR_STAT_EVAL_NODE_POINTS], st_np);
-        atomicAdd(&p.stats[GPR_STAT_STRUCT_PROPOSED], (unsigned long long)st_sp);
-        atomicAdd(&p.stats[GPR_STAT_STRUCT_ACCEPTED], (unsigned long long)st_sa);
-        atomicAdd(&p.stats[GPR_STAT_CONST_PROPOSED], (unsigned long long)st_cp);
-        atomicAdd(&p.stats[GPR_STAT_CONST_ACCEPTED], (unsigned long long)st_ca);
-    }
+    if (lane == 0 && p.stats)
+        for (int i = 0; i < GPR_NSTATS; ++i) atomicAdd(&p.stats[i], s_st[warp][i]);
+#undef ST_ADD
     if constexpr (PROF) {
         if (lane == 0 && p.phase)
             for (int i = 0; i < GPR_PH_SLOTS; ++i) atomicAdd(&p.phase[i], s_ph[warp][i]);

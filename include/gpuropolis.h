@@ -379,9 +379,9 @@ int gpr_map_chain(gpr_handle* h, int* chain, double* posterior);
  * that stream to finish the block before returning, and reports kernel error
  * flags as gpr_sync does.  Every call looks up the scratch array's device
  * address with cudaGetSymbolAddress (which allocates nothing), so a context
- * reset between calls is harmless; the first call on each device also loads
- * the library's device code there: make that first call before any stream
- * capture.  cfg->n_vars must be 0 or 1 (one input variable).  Failures are
+ * reset between calls is harmless.  Because every call synchronises its
+ * stream, no call can be made while a stream is being captured into a graph.
+ * cfg->n_vars must be 0 or 1 (one input variable).  Failures are
  * described by gpr_last_error(NULL), per host thread. */
 int gpr_run_block_noalloc(const gpr_config* cfg, int n_chains, int32_t* P, float* C,
                           double* prior, double* likelihood, const float* x, const float* y,

@@ -92,3 +92,50 @@ def test_all_layouts_give_the_same_chains(case):
     # the block did something: some chains moved, some scores are finite
     assert np.isfinite(ref[1][3]).mean() > 0.2
     assert not np.array_equal(ref[1][1], C)
+
+
+PROF_LAYOUTS = [
+    dict(K=4, onepass=0, rolled=0, pipe=0),
+    dict(K=4, onepass=0, rolled=0, pipe=0, stream=True),
+    dict(K=8, onepass=1, rolled=0, pipe=0),
+    dict(K=4, onepass=0, rolled=0, pipe=1),
+    dict(K=4, onepass=0, rolled=0, pipe=1, stream=True),
+    dict(K=8, onepass=1, rolled=0, pipe=1),
+]
+
+
+@pytest.mark.parametrize("layout", PROF_LAYOUTS, ids=lambda l: "-".join("%s%s" % kv for kv in sorted(l.items())))
+def test_phase_timed_build_gives_the_same_chains(layout):
+    """gpr_debug_phase_profile runs the layout's phase-timed build: the same
+    chains as run_block, bit for bit (1001 chains, so the last chain group is
+    partly empty), its own consistency checks quiet, and counters that add up
+    (every phase's cycles counted, the passes of every evaluation)."""
+    kw, make, N, steps = CASES["expdecay250-rw-lcg"]
+    data = make()
+    P, C = g.host_init_chains(N, kw["program_length"], 77, ops=kw["ops"])
+    want = _run(kw, data, N, steps, layout, P, C)
+    s = g.Sampler(N, **kw)
+    try:
+        s.set_data(*data)
+        lay = dict(layout)
+        if lay.pop("stream", False):
+            s.set_streaming(True)
+        s.set_layout(lay["K"], lay["onepass"], lay["rolled"], 1, 8, lay["pipe"])
+        s.set_state(P, C)
+        s.reset_stats()
+        ph = s.phase_profile(steps, 12345)
+        got = s.get_state()
+        st = s.stats()
+    finally:
+        s.close()
+    assert np.array_equal(got[0], want[0])
+    assert np.array_equal(got[1].view(np.uint32), want[1].view(np.uint32))
+    np.testing.assert_array_equal(got[2], want[2])
+    np.testing.assert_array_equal(got[3], want[3])
+    cyc = ph["cycles"]
+    assert cyc["evaluation"] > 0 and cyc["constant_proposal"] > 0 and cyc["compile"] > 0
+    # at most ceil(250 / (32 K)) passes per evaluation (one in the one-pass
+    # layouts); an evaluation that meets an invalid value may skip the rest
+    npass = 1 if layout["onepass"] else -(-250 // (32 * layout["K"]))
+    assert st["evals"] >= N * steps
+    assert 0.5 * st["evals"] * npass < ph["passes"] <= st["evals"] * npass, (ph["passes"], st["evals"], npass)
