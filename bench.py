@@ -236,7 +236,7 @@ class EssRig:
         the CTA shape autotuned and per-chain steps adapted toward target."""
         s = self.sampler("hmc", eps=0.0005, L=L)
         s.set_state(*self.state)
-        s.autotune(steps=20, seed=77)          # CTA shape against L1 for the gradient tapes
+        s.autotune(steps=10, seed=77)          # CTA shape against L1 for the gradient tapes
         s.set_hmc_jitter(0.0, len_jit)
         s.adapt_scales(target)
         for i in range(2):
@@ -322,7 +322,7 @@ def ess_comparison(g, stream, dev):
     # the configured move as the workload states it: step 0.01, 8 leapfrog steps, not adapted
     s = rig.sampler("hmc", eps=0.01, L=8)
     s.set_state(*rig.state)
-    s.autotune(steps=20, seed=77)
+    s.autotune(steps=10, seed=77)
     dt, _ = rig.timed(s, 20, 5)
     steps = max(30, int(t_rw / (dt / 20)))
     res["hmc_L8_eps0.01"] = arm(s, steps, 3, {"leapfrog_steps": 8, "eps": 0.01, "adapted": False})

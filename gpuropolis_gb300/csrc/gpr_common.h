@@ -83,11 +83,12 @@ GPR_HDI int gpr_op_class(int o) {
 }
 
 /* ---- compiled program: a reachable-only postfix form of the heap tree ----
- * One 32-bit word per instruction: bits 0-7 code, bits 8-15 heap node (the
- * constant C[node] an instruction reads).  The evaluator keeps the running
+ * One 16-bit word per instruction (gpr_word): bits 0-7 code, bits 8-15 heap
+ * node (the constant C[node] an instruction reads).  The evaluator keeps the running
  * value in an accumulator; leaf operands (x1..x3, 1, a constant) are folded into
  * the instruction that consumes them, so the value stack is touched only
  * where both children of a binary node are subtrees. */
+typedef uint16_t gpr_word;
 enum gpr_icode {
     I_END = 0,
     I_LDX = 1, I_LDC = 2, I_LD1 = 3, I_PUSH = 4, I_LDNAN = 5, I_LDX2 = 6, I_LDX3 = 7,

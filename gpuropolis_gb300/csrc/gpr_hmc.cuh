@@ -47,7 +47,7 @@ struct alignas(K == 4 ? 16 : (K == 2 ? 8 : 4)) Row {
 struct GradSmem {
     uint8_t* ops[2];
     float* Cs[2];       /* [0], [1]: current and proposed constants            */
-    uint32_t* prog[2];
+    gpr_word* prog[2];
     uint2* eprog;
     int16_t* match;     /* POP instruction -> index of its PUSH                 */
     float* gacc;        /* [PL][GPR_GACC_STRIDE]: per-lane gradient sums; also
@@ -68,7 +68,7 @@ __host__ __device__ __forceinline__ size_t grad_warp_bytes(int PL, int max_instr
     size_t b = 0;
     b += 2 * plp;                                              /* ops */
     b += align16(2 * plp * 4);                                 /* Cs */
-    b += align16(2 * (size_t)max_instr * 4);                   /* prog */
+    b += align16(2 * (size_t)max_instr * sizeof(gpr_word));    /* prog */
     b += align16((size_t)max_instr * 8);                       /* eprog */
     b += align16((size_t)max_instr * 2);                       /* match */
     b += grad_rows_bytes(PL);                                  /* gradient rows | compiler scratch */
@@ -82,7 +82,7 @@ __device__ __forceinline__ GradSmem carve_grad(uint8_t* base, int PL, int max_in
     uint8_t* p = base;
     w.ops[0] = p; w.ops[1] = p + plp; p += 2 * plp;
     w.Cs[0] = (float*)p; w.Cs[1] = (float*)p + plp; p += align16(2 * plp * 4);
-    w.prog[0] = (uint32_t*)p; w.prog[1] = (uint32_t*)p + max_instr; p += align16(2 * (size_t)max_instr * 4);
+    w.prog[0] = (gpr_word*)p; w.prog[1] = (gpr_word*)p + max_instr; p += align16(2 * (size_t)max_instr * sizeof(gpr_word));
     w.eprog = (uint2*)p; p += align16((size_t)max_instr * 8);
     w.match = (int16_t*)p; p += align16((size_t)max_instr * 2);
     w.gacc = (float*)p; p += grad_rows_bytes(PL);
@@ -94,7 +94,7 @@ __device__ __forceinline__ GradSmem carve_grad(uint8_t* base, int PL, int max_in
 
 /* For each POP instruction of the program, the index of the PUSH whose value
  * it pops (the stack discipline is a property of the program alone). */
-__device__ __forceinline__ void pop_match(const uint32_t* prog, int ninstr, int16_t* match, int lane) {
+__device__ __forceinline__ void pop_match(const gpr_word* prog, int ninstr, int16_t* match, int lane) {
     if (lane == 0) {
         int16_t st[32];
         int sp = 0;

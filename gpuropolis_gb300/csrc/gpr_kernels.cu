@@ -13,14 +13,15 @@ size_t mh_smem_bytes(const KParams& p, int K, int warps_per_cta, int stream) {
            (size_t)warps_per_cta * warp_smem_bytes(p.PL, p.max_instr, p.levels, K);
 }
 
-size_t pipe_smem_bytes(const KParams& p, int K, int warps_per_cta, int stream) {
-    return 16 + (stream ? 0 : align16((size_t)data_arrays(p) * p.nd_pad * 4)) +
-           (size_t)warps_per_cta * pipe_warp_bytes(p.PL, p.max_instr, p.levels, K);
-}
-
 int pipe_part_stride(int nd) {
     const int nch = (nd + GPR_CHUNK_POINTS - 1) / GPR_CHUNK_POINTS;
     return nch <= GPR_PIPE_CHUNKS ? 0 : nch;
+}
+
+size_t pipe_smem_bytes(const KParams& p, int K, int warps_per_cta, int stream) {
+    return 16 + (stream ? 0 : align16((size_t)data_arrays(p) * p.nd_pad * 4)) +
+           (size_t)warps_per_cta * pipe_warp_bytes(p.PL, p.max_instr, p.levels, K) +
+           (pipe_part_stride(p.nd) == 0 ? pipe_board_bytes() : 0);
 }
 
 static const void* pick_pipe(int K, int onepass, int rng, int rolled, int stream, int nv, int batched) {

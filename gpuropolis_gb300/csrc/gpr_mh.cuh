@@ -274,7 +274,7 @@ __device__ __forceinline__ float leaf_len(int r) { return r == PL_NAN ? __int_as
 __device__ __forceinline__ int leaf_cnt(int r) { return r == PL_X ? 0 : 1; }
 
 template <int NV>
-static __device__ CompileOut compile_parallel(const uint8_t* ops, int PL, uint32_t* prog, const CompileScratch& cs,
+static __device__ CompileOut compile_parallel(const uint8_t* ops, int PL, gpr_word* prog, const CompileScratch& cs,
                                        int lane) {
     int D = 0;
     while ((2 << D) <= PL) ++D;     /* deepest heap level */
@@ -400,7 +400,7 @@ __device__ __forceinline__ int instr_cost(uint32_t ins) {
     }
     return 25 + body;
 }
-__device__ __forceinline__ int program_cost(const uint32_t* prog, int ninstr, int lane) {
+__device__ __forceinline__ int program_cost(const gpr_word* prog, int ninstr, int lane) {
     int c = 0;
 #pragma unroll 1
     for (int i = lane; i < ninstr; i += 32) c += instr_cost(prog[i]);
@@ -410,7 +410,7 @@ __device__ __forceinline__ int program_cost(const uint32_t* prog, int ninstr, in
 /* The program the evaluator runs: each instruction word paired with the
  * constant it reads (NaN for the invalid-op marker), so one 64-bit shared
  * load fetches both.  Rebuilt for every proposal, lanes in parallel. */
-__device__ __forceinline__ void build_eval_program(const uint32_t* prog, const float* Cs, int ninstr,
+__device__ __forceinline__ void build_eval_program(const gpr_word* prog, const float* Cs, int ninstr,
                                                    uint2* eprog, int lane) {
 #pragma unroll 1
     for (int i = lane; i < ninstr; i += 32) {
@@ -489,7 +489,7 @@ __device__ __forceinline__ void heavy_staged(float (&acc)[K], const float (&w)[K
  * compiled program and the chain's constants array, the constant of heap node
  * n being cs[n] (NaN for the invalid-op marker 255). */
 struct PCProg {
-    const uint32_t* p;
+    const gpr_word* p;
     const float* cs;
 };
 __device__ __forceinline__ uint2 prog_at(const uint2* e, int i) { return e[i]; }
@@ -648,7 +648,7 @@ __device__ __forceinline__ float warp_sum(float v) {
 struct WarpSmem {
     uint8_t* ops[2];
     float* Cs[2];
-    uint32_t* prog[2];
+    gpr_word* prog[2];
     uint2* eprog;    /* evaluation program: (instruction, constant) pairs */
     int* off;        /* per constant: offset of its first draw   */
     int* ndr;        /* per constant: draws used                 */
@@ -676,7 +676,7 @@ __host__ __device__ __forceinline__ size_t warp_smem_bytes(int PL, int max_instr
     size_t b = 0;
     b += 2 * plp;                                /* ops */
     b += align16(2 * plp * 4);                   /* Cs */
-    b += align16(2 * (size_t)max_instr * 4);     /* prog */
+    b += align16(2 * (size_t)max_instr * sizeof(gpr_word));     /* prog */
     if (eprog) b += align16((size_t)max_instr * 8);   /* eprog */
     b += shared_region_bytes(PL, levels, K);     /* stack + scratch | constant-move records */
     return align16(b);
@@ -689,7 +689,7 @@ __device__ __forceinline__ WarpSmem carve_warp(uint8_t* base, int PL, int max_in
     uint8_t* p = base;
     w.ops[0] = p; w.ops[1] = p + plp; p += 2 * plp;
     w.Cs[0] = (float*)p; w.Cs[1] = (float*)p + plp; p += align16(2 * plp * 4);
-    w.prog[0] = (uint32_t*)p; w.prog[1] = (uint32_t*)p + max_instr; p += align16(2 * (size_t)max_instr * 4);
+    w.prog[0] = (gpr_word*)p; w.prog[1] = (gpr_word*)p + max_instr; p += align16(2 * (size_t)max_instr * sizeof(gpr_word));
     w.eprog = nullptr;
     if (eprog) { w.eprog = (uint2*)p; p += align16((size_t)max_instr * 8); }
     w.stk = (float*)p;

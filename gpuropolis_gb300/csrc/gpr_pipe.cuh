@@ -54,11 +54,17 @@ struct PipeSlot {
  * constant-move records | compiler scratch). */
 __host__ __device__ __forceinline__ size_t pipe_slot_bytes(int PL, int max_instr) {
     const size_t plp = align16((size_t)PL);
-    return 2 * plp + align16(2 * plp * 4) + align16(2 * (size_t)max_instr * 4);
+    return 2 * plp + align16(2 * plp * 4) + align16(2 * (size_t)max_instr * sizeof(gpr_word));
 }
 __host__ __device__ __forceinline__ size_t pipe_warp_bytes(int PL, int max_instr, int levels, int K) {
     return 2 * pipe_slot_bytes(PL, max_instr) + shared_region_bytes(PL, levels, K);
 }
+
+/* The CTA's chunk-sum board, [2 groups][8 warps][GPR_PIPE_CHUNKS] floats, in
+ * dynamic shared memory after the warps' regions.  It exists only when every
+ * chain's chunks fit on it; larger datasets keep their chunk sums in p.part
+ * (p.part_stride > 0) and leave that shared memory to more resident CTAs. */
+__host__ __device__ __forceinline__ size_t pipe_board_bytes() { return (size_t)2 * 8 * GPR_PIPE_CHUNKS * 4; }
 
 /* The WarpSmem view of slot g of a warp's region (no evaluation program:
  * the pipelined kernel interprets program and constants in place). */
@@ -69,7 +75,7 @@ __device__ __forceinline__ WarpSmem carve_pipe(uint8_t* base, int PL, int max_in
     uint8_t* p = base + (size_t)g * pipe_slot_bytes(PL, max_instr);
     w.ops[0] = p; w.ops[1] = p + plp; p += 2 * plp;
     w.Cs[0] = (float*)p; w.Cs[1] = (float*)p + plp; p += align16(2 * plp * 4);
-    w.prog[0] = (uint32_t*)p; w.prog[1] = (uint32_t*)p + max_instr;
+    w.prog[0] = (gpr_word*)p; w.prog[1] = (gpr_word*)p + max_instr;
     w.eprog = nullptr;
     uint8_t* r = base + 2 * pipe_slot_bytes(PL, max_instr);
     w.stk = (float*)r;
@@ -134,14 +140,13 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_pipe_kernel(const __grid
 #define ST_ADD(i, v) do { if (lane == 0) s_st[warp][(i)] += (unsigned long long)(v); } while (0)
 
     __shared__ PipeSlot s_slot[2][8];
-    __shared__ const uint32_t* s_pp[2][8];   /* published program ...          */
+    __shared__ const gpr_word* s_pp[2][8];   /* published program ...          */
     __shared__ const float* s_pc[2][8];      /* ... and its constants          */
     __shared__ int s_cost[2][8];             /* its length (-1: none)          */
     __shared__ int s_cnt[2][8];              /* its node count                 */
     __shared__ int s_bad[2][8];              /* a point was invalid            */
     __shared__ int s_next[2];                /* next task of each pool         */
     __shared__ int s_group_base;
-    __shared__ float s_part[2][8][GPR_PIPE_CHUNKS];
 
     /* the dataset's passes, chunks and task split */
     int npass = 0, nch = 0, ppt = 1, tpc = 1;
@@ -158,9 +163,10 @@ __global__ void __launch_bounds__(256, GPR_MIN_CTAS) mh_pipe_kernel(const __grid
     };
     split(dv);
     /* chunk sums of (group, warp): the board, or this CTA's rows of p.part */
+    float* const board = (float*)(wbase + (size_t)nwarps * pipe_warp_bytes(PL, p.max_instr, p.levels, K));
     auto part_row = [&](int g, int w) -> float* {
         if (p.part_stride > 0) return p.part + ((size_t)(blockIdx.x * 2 + g) * 8 + w) * p.part_stride;
-        return &s_part[g][w][0];
+        return board + ((size_t)g * 8 + w) * GPR_PIPE_CHUNKS;
     };
 
     GPR_PH(GPR_PH_CLAIM);
