@@ -24,7 +24,9 @@
  * --vars=3 (data lines "x1 x2 x3 y sd"; the op set then also holds the leaves
  * x1, x2, x3, op codes 27-29, unless --ops gives one), --adapt=T (random-walk
  * and gradient moves: each chain's own scale adapted toward acceptance T
- * during the blocks not written out, 0..burn, then kept), --checkpoint=FILE
+ * during the blocks not written out, 0..burn, then kept), --hmc-jitter=A:B
+ * (gradient moves: each move's leapfrog step drawn from EPS x U(1-A, 1+A) and
+ * its count from [L(1-B), L(1+B)]), --checkpoint=FILE
  * (after every block: the chains, the seed and the host stream's position)
  * and --resume=FILE (continue from such a file, appending to samples.txt:
  * the continued run writes what the uninterrupted one would have).
@@ -55,11 +57,12 @@ static double resample_param = 0.5;
 static int device_resample = 0, tops_k = 0;
 static int n_vars = 1, ops_given = 0;
 static float adapt_target = 0.0f;
+static float jit_eps = 0.0f, jit_len = 0.0f;
 static std::string ckpt_path, resume_path;
 static std::vector<int> ops;
 
 enum { OPT_PL = 1000, OPT_MAXLEN, OPT_OPS, OPT_RNG, OPT_CONST, OPT_RESAMPLE, OPT_THREADS, OPT_DEVRES, OPT_TOPS, OPT_STRUCT,
-       OPT_VARS, OPT_ADAPT, OPT_CKPT, OPT_RESUME };
+       OPT_VARS, OPT_ADAPT, OPT_CKPT, OPT_RESUME, OPT_JITTER };
 
 static struct option long_options[] = {
     {"in", required_argument, NULL, 'd'},
@@ -91,6 +94,7 @@ static struct option long_options[] = {
     {"adapt", required_argument, NULL, OPT_ADAPT},
     {"checkpoint", required_argument, NULL, OPT_CKPT},
     {"resume", required_argument, NULL, OPT_RESUME},
+    {"hmc-jitter", required_argument, NULL, OPT_JITTER},
     {NULL, 0, 0, 0}};
 
 static int parse_ops(const char* s) {
@@ -166,6 +170,10 @@ static int process_arguments(int argc, char** argv) {
             case OPT_DEVRES: device_resample = 1; break;
             case OPT_TOPS: tops_k = atoi(optarg); if (tops_k < 1) return 1; break;
             case OPT_STRUCT: struct_every = atoi(optarg); if (struct_every < 0) return 1; break;
+            case OPT_JITTER:
+                if (sscanf(optarg, "%f:%f", &jit_eps, &jit_len) != 2) return 1;
+                if (!(jit_eps >= 0.0f && jit_eps < 1.0f && jit_len >= 0.0f && jit_len <= 1.0f)) return 1;
+                break;
             default: return 1;
         }
     return 0;
@@ -261,6 +269,8 @@ int main(int argc, char** argv) {
         FAIL("--checkpoint / --resume do not keep the adaptation's state; run --adapt without them");
     if (adapt_target > 0.0f && const_mode == GPR_CONST_REFERENCE)
         FAIL("--adapt needs --const-proposal=rw:SD, hmc:EPS:L or mala:EPS (the reference's proposals have no scale)");
+    if ((jit_eps > 0.0f || jit_len > 0.0f) && const_mode != GPR_CONST_HMC)
+        FAIL("--hmc-jitter needs --const-proposal=hmc:EPS:L or mala:EPS");
 
     if (n_vars == 3 && !ops_given)
         for (int o = 27; o <= 29; ++o) ops.push_back(o);   /* the reference's ops and x1, x2, x3 */
@@ -282,7 +292,8 @@ int main(int argc, char** argv) {
             fprintf(stderr, "Invalid GPU device %d\n", WHICH_GPU);   /* main.cu:1045 */
         return 1;
     }
-    if (gpr_set_moves(h, struct_every, hmc_eps, hmc_steps) != GPR_OK) {
+    if (gpr_set_moves(h, struct_every, hmc_eps, hmc_steps) != GPR_OK ||
+        (const_mode == GPR_CONST_HMC && gpr_set_hmc_jitter(h, jit_eps, jit_len) != GPR_OK)) {
         fprintf(stderr, "%s\n", gpr_last_error(h));
         gpr_destroy(h);
         return 1;
@@ -344,6 +355,8 @@ int main(int argc, char** argv) {
                 const_mode == GPR_CONST_RANDOM_WALK ? "rw:" : const_mode == GPR_CONST_HMC ? "hmc:" : "reference");
         if (const_mode == GPR_CONST_RANDOM_WALK) fprintf(lg, "%g", rw_sd);
         if (const_mode == GPR_CONST_HMC) fprintf(lg, "%g:%d", hmc_eps, hmc_steps);
+        if (const_mode == GPR_CONST_HMC && (jit_eps > 0.0f || jit_len > 0.0f))
+            fprintf(lg, " (jitter %g:%g)", jit_eps, jit_len);
         fprintf(lg, "\n# \tStructure move every: %d steps", struct_every);
         if (adapt_target > 0.0f) fprintf(lg, "\n# \tAdapt: per-chain scales toward acceptance %g in blocks 0..%d", adapt_target, burn);
         fprintf(lg, "\n# \tResample: %s:%g%s\n# \tOps:", resample_mode == GPR_RESAMPLE_MAP_DELTA ? "map-delta" : "quantile",

@@ -34,6 +34,9 @@ def _cli(args):
     (["--resample=map-delta:-1"], "--resample"),
     (["--adapt=0.3"], "--adapt needs"),
     (["--adapt=0.3", "--const-proposal=rw:0.1", "--checkpoint=/tmp/x"], "do not keep the adaptation"),
+    (["--hmc-jitter=0.2"], "Invalid command line arguments"),
+    (["--hmc-jitter=1.5:0"], "Invalid command line arguments"),
+    (["--hmc-jitter=0.2:0.5"], "--hmc-jitter needs"),
 ])
 def test_cli_rejects(args, message):
     r = _cli(args)
