@@ -90,14 +90,16 @@ def config_of(args, w):
             "l2": "GPU arm: flushed between blocks (256 MB write); the CPU arm has no GPU cache"}
 
 
-def fp32_roofline(node_points, seconds, nsm, peaks, sm_mhz=None):
+def fp32_roofline(node_points, seconds, nsm, peaks, sm_mhz=None, traffic=None):
     """Algorithmic FP32 ops ((reachable nodes + 4) per point-eval, a
     transcendental counting as one) per second against FP32 issue:
-    SMs x 128 lanes x the maximum SM clock (nominal: no measured FP32 peak)."""
+    SMs x 128 lanes x the maximum SM clock (nominal: no measured FP32 peak).
+    traffic: DRAM bytes of one launch from an ncu capture, when there is one."""
     peak = nsm * 128 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
     achieved = node_points / seconds / 1e12
     out = {"bound": "fp32-issue", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-           "frac": achieved / peak,
+           "frac": achieved / peak, "traffic": traffic,
+           "traffic_source": MH_LAUNCH_DRAM_SOURCE if traffic else None,
            "peak_source": "nominal: SMs x 128 FP32 lanes x max SM clock (MEASURED_PEAKS.json has no FP32 figure)",
            "note": "algorithmic ops = (reachable non-pass-through nodes + 4) per point evaluated; exp, log, pow "
                    "and division count as one op but cost 10-70 FP32 instructions each"}
@@ -917,7 +919,8 @@ def run_gpu(args, w):
                         "gpr_get_state (pinned host)"},
         "gpu_launches": launches,
         "roofline": fp32_roofline(st["eval_node_points"], kernel_ms / 1e3, nsm, peaks,
-                                  (clocks or {}).get("sm_mhz")),
+                                  (clocks or {}).get("sm_mhz"),
+                                  MH_LAUNCH_DRAM_BYTES if args.workload == "plain-mh-131k" else None),
         "roofline_hbm": hbm_roofline(st["eval_points"], kernel_ms / 1e3, peaks,
                                      MH_LAUNCH_DRAM_BYTES if args.workload == "plain-mh-131k" else None),
         "loglik_err_vs_fp64": err,
