@@ -34,7 +34,6 @@
 namespace gpr {
 
 #define GPR_HMC_K 4          /* points per lane of the adjoint and Hamiltonian kernels */
-#define GPR_GACC_STRIDE 33   /* per-constant gradient rows, padded against bank conflicts */
 #define GPR_ASTK_MAX 8       /* adjoint-stack rows: value-stack depth for PROGRAM_LENGTH <= 255 */
 
 /* One tape row: an instruction's result at this lane's K points. */
@@ -50,15 +49,15 @@ struct GradSmem {
     gpr_word* prog[2];
     uint2* eprog;
     int16_t* match;     /* POP instruction -> index of its PUSH                 */
-    float* gacc;        /* [PL][GPR_GACC_STRIDE]: per-lane gradient sums; also
-                         * the compiler's scratch                               */
+    float* gacc;        /* [PL]: the gradient sums (lane 0 adds each warp-summed
+                         * share); also the compiler's scratch                   */
     float* gcur;        /* gradient of the log-posterior at the current state   */
     float* gnew;        /* ... at the trajectory's position                     */
     float* mom;         /* momentum                                             */
 };
 
 __host__ __device__ __forceinline__ size_t grad_rows_bytes(int PL) {
-    const size_t gacc = (size_t)PL * GPR_GACC_STRIDE * 4;
+    const size_t gacc = (size_t)PL * 4;
     const size_t comp = 5 * align16((size_t)PL + 1) * 4;
     return align16(gacc > comp ? gacc : comp);
 }
@@ -276,12 +275,18 @@ __device__ __forceinline__ void backward_tape(const uint2* __restrict__ prog, in
                 share = __fadd_rn(share, av);
             }
             if (src == SRC_POP) astk[sp++] = spill;
-            else if (src == SRC_C && (int)node < PL) gacc[node * GPR_GACC_STRIDE + lane] += share;
+            else if (src == SRC_C && (int)node < PL) {
+                const float tot = warp_sum(share);
+                if (lane == 0) gacc[node] += tot;
+            }
         } else if (code == I_LDC) {
             float share = 0.0f;
 #pragma unroll
             for (int k = 0; k < K; ++k) { share = __fadd_rn(share, adj[k]); adj[k] = 0.0f; }
-            if ((int)node < PL) gacc[node * GPR_GACC_STRIDE + lane] += share;
+            if ((int)node < PL) {
+                const float tot = warp_sum(share);
+                if (lane == 0) gacc[node] += tot;
+            }
         } else if (code == I_LDX || code == I_LD1 || code == I_LDNAN || code == I_LDX2 || code == I_LDX3) {
 #pragma unroll
             for (int k = 0; k < K; ++k) adj[k] = 0.0f;
@@ -327,7 +332,7 @@ __device__ df eval_loglik_grad(const uint2* prog, int ninstr, const GradSmem& ws
     Row<K> tape[MAXI];             /* thread-local: results of every instruction */
     Row<K> astk[GPR_ASTK_MAX];     /* adjoints of pushed values                  */
 #pragma unroll 1
-    for (int j = lane; j < PL * GPR_GACC_STRIDE; j += 32) ws.gacc[j] = 0.0f;
+    for (int j = lane; j < PL; j += 32) ws.gacc[j] = 0.0f;
     __syncwarp();
     float s = 0.0f;
     bool bad = false;
@@ -360,13 +365,7 @@ __device__ df eval_loglik_grad(const uint2* prog, int ninstr, const GradSmem& ws
     }
     __syncwarp();
 #pragma unroll 1
-    for (int c = lane; c < PL; c += 32) {
-        float t = 0.0f;
-        const float* row = ws.gacc + c * GPR_GACC_STRIDE;
-#pragma unroll 8
-        for (int j = 0; j < 32; ++j) t = __fadd_rn(t, row[j]);
-        g[c] = t;
-    }
+    for (int c = lane; c < PL; c += 32) g[c] = ws.gacc[c];
     __syncwarp();
     if (bad) return df_make(-INFINITY, 0.0f);
     df S = warp_sum_df(df_make(s, 0.0f));
