@@ -388,7 +388,7 @@ static int batched_wpc(const gpr::KParams& kp, int wpc, int pipe = 0) {
  * caps the shared-memory carveout, which leaves the rest of the SM's L1 to
  * the thread-local gradient tapes. */
 static int configure_hmc(gpr_handle* h, int wpc0 = 4, int ctas_per_sm = 0, int stream_mode = -1) {
-    if (wpc0 < 1 || wpc0 > 4) wpc0 = 4;   /* the kernel is built for CTAs of at most 128 threads */
+    if (wpc0 < 1 || wpc0 > 8) wpc0 = 4;
     drop_graph(h);
     gpr::KParams& kp = h->kp;
     if (!gpr::grad_supported(kp))
@@ -1009,10 +1009,10 @@ int gpr_autotune(gpr_handle* h, int steps, int seed, int* K, int* onepass, int* 
     if (hmc) {
         /* CTA size and residency cap, each with the data staged (unless the
          * handle always streams) and streamed */
-        const int shapes[6][2] = {{4, 0}, {4, 7}, {4, 5}, {4, 4}, {2, 0}, {1, 0}};
-        for (int i = 0; i < 12; ++i) {
-            const int want_stream = i >= 6;
-            if (configure_hmc(h, shapes[i % 6][0], shapes[i % 6][1], want_stream) != GPR_OK) continue;
+        const int shapes[8][2] = {{4, 0}, {4, 7}, {4, 5}, {4, 4}, {2, 0}, {1, 0}, {8, 0}, {8, 3}};
+        for (int i = 0; i < 16; ++i) {
+            const int want_stream = i >= 8;
+            if (configure_hmc(h, shapes[i % 8][0], shapes[i % 8][1], want_stream) != GPR_OK) continue;
             if (h->lc.stream != want_stream) continue;   /* forced one way: tried once */
             for (int rep = 0; rep < 2; ++rep) {
                 AT_TRY(cudaMemcpyAsync(h->dP, sP, cnt * sizeof(int32_t), cudaMemcpyDeviceToDevice, h->stream));
@@ -1104,7 +1104,7 @@ done:
 int gpr_set_hmc_layout(gpr_handle* h, int warps_per_cta, int ctas_per_sm) {
     if (!h) return GPR_ERR_ARG;
     if (h->kp.const_mode != GPR_CONST_HMC) return fail(h, GPR_ERR_ARG, "not a GPR_CONST_HMC handle");
-    if ((warps_per_cta != 1 && warps_per_cta != 2 && warps_per_cta != 4) || ctas_per_sm < 0)
+    if ((warps_per_cta != 1 && warps_per_cta != 2 && warps_per_cta != 4 && warps_per_cta != 8) || ctas_per_sm < 0)
         return fail(h, GPR_ERR_ARG, "invalid layout: %d warps per CTA, %d CTAs per SM", warps_per_cta, ctas_per_sm);
     CUDA_TRY(h, cudaSetDevice(h->device));
     return configure_hmc(h, warps_per_cta, ctas_per_sm);

@@ -450,7 +450,7 @@ __global__ void __launch_bounds__(128) loglik_grad_kernel(const __grid_constant_
  * claimed from the global counter; evaluation with the adjoint on K points
  * per lane. */
 template <int K, int MAXI, int RNG, bool STREAM, int NV>
-__global__ void __launch_bounds__(128) mh_hmc_kernel(const __grid_constant__ KParams p) {
+__global__ void __launch_bounds__(256) mh_hmc_kernel(const __grid_constant__ KParams p) {
     extern __shared__ __align__(128) uint8_t smem[];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;

@@ -217,8 +217,8 @@ int gpr_set_layout3(gpr_handle* h, int K, int onepass, int rolled, int lockstep,
 int gpr_set_streaming(gpr_handle* h, int always);
 int gpr_layout_streamed(gpr_handle* h);
 
-/* Layout of a GPR_CONST_HMC handle's kernel: warps (chains) per CTA (1, 2 or
- * 4) and at most ctas_per_sm resident CTAs per SM (0: as many as fit).
+/* Layout of a GPR_CONST_HMC handle's kernel: warps (chains) per CTA (1, 2, 4
+ * or 8) and at most ctas_per_sm resident CTAs per SM (0: as many as fit).
  * Fewer CTAs leave more of each SM's L1 to the gradient tapes; gpr_autotune
  * times a set of these for GPR_CONST_HMC handles. */
 int gpr_set_hmc_layout(gpr_handle* h, int warps_per_cta, int ctas_per_sm);
